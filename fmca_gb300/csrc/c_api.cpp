@@ -1,0 +1,292 @@
+// extern "C" boundary of fmca_gb300 (declared in include/fmca_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "../../include/fmca_gb300.h"
+#include "h2_gpu.h"
+#include "h2_plan.h"
+
+struct fmca_plan {
+  fmca::Plan plan;
+  fmca::gpu::DevPlan* dev = nullptr;
+  // device staging for fmca_matvec_host
+  void* hx = nullptr;
+  void* hy = nullptr;
+  size_t hx_bytes = 0, hy_bytes = 0;
+  int64_t min_leaf = 0;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+fmca_status fail(fmca_status s, const std::string& msg) {
+  g_last_error = msg;
+  return s;
+}
+fmca_status ok() { return FMCA_OK; }
+
+fmca_status check_kernel(const fmca_kernel_desc* k) {
+  if (!k) return fail(FMCA_ERR_INVALID_ARGUMENT, "kernel descriptor is NULL");
+  if (k->type < 0 || k->type >= fmca::K_NUM_KERNELS)
+    return fail(FMCA_ERR_INVALID_ARGUMENT,
+                "unknown kernel type " + std::to_string(k->type));
+  if (!(k->l > 0) || !std::isfinite(k->l))
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "kernel length scale must be > 0");
+  if (!std::isfinite(k->sigma2) || !std::isfinite(k->c))
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "kernel parameters must be finite");
+  return FMCA_OK;
+}
+
+fmca::gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
+  fmca::gpu::KernelDesc d;
+  d.type = k->type;
+  d.l = k->l;
+  d.c = k->c;
+  d.nu = k->nu;
+  d.sigma2 = k->sigma2;
+  return d;
+}
+
+fmca_status check_gpu_plan(const fmca_plan* p, int precision) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  if (precision != FMCA_PREC_FP64 && precision != FMCA_PREC_MIXED)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown precision mode");
+  if (p->plan.interp.dim > 3)
+    return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports dim <= 3");
+  if (p->plan.interp.deg > 7)
+    return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports degree <= 7");
+  return FMCA_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char* fmca_last_error(void) { return g_last_error.c_str(); }
+const char* fmca_version(void) { return "fmca_gb300 0.1.0"; }
+
+fmca_status fmca_kernel_type_from_name(const char* name, int* type) {
+  if (!name || !type) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  const int t = fmca::kernel_type_from_name(name);
+  if (t < 0)
+    return fail(FMCA_ERR_UNSUPPORTED, std::string("kernel not implemented: ") + name);
+  *type = t;
+  return ok();
+}
+
+fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
+                             const double* P_cols, int64_t n_cols, int degree,
+                             double eta, int64_t min_leaf, fmca_plan** out) {
+  if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!P_rows) return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows is NULL");
+  if (dim < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "dim must be >= 1");
+  if (n_rows < 1 || n_rows > (int64_t)0xFFFFFFFEll)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "n_rows out of range");
+  const bool same = (P_cols == nullptr || P_cols == P_rows);
+  if (same) n_cols = n_rows;
+  if (n_cols < 1 || n_cols > (int64_t)0xFFFFFFFEll)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "n_cols out of range");
+  if (degree < 0 || degree > 16)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "degree out of range");
+  if (!(eta >= 0) || !std::isfinite(eta))
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "eta must be finite and >= 0");
+  if (min_leaf < 0 || min_leaf > (int64_t)0x7FFFFFFF)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "min_leaf out of range");
+  for (int64_t i = 0; i < (int64_t)dim * n_rows; ++i)
+    if (!std::isfinite(P_rows[i]))
+      return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows holds a non-finite value");
+  if (!same)
+    for (int64_t i = 0; i < (int64_t)dim * n_cols; ++i)
+      if (!std::isfinite(P_cols[i]))
+        return fail(FMCA_ERR_INVALID_ARGUMENT, "P_cols holds a non-finite value");
+  try {
+    fmca_plan* p = new fmca_plan();
+    p->min_leaf = min_leaf;
+    p->plan.build(P_rows, (uint32_t)n_rows, same ? P_rows : P_cols,
+                  (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same);
+    *out = p;
+  } catch (const std::bad_alloc&) {
+    return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
+  } catch (const std::exception& e) {
+    return fail(FMCA_ERR_INTERNAL, e.what());
+  }
+  return ok();
+}
+
+fmca_status fmca_plan_destroy(fmca_plan* plan) {
+  if (!plan) return ok();
+  fmca::gpu::destroy(plan->dev);
+  if (plan->hx) cudaFree(plan->hx);
+  if (plan->hy) cudaFree(plan->hy);
+  delete plan;
+  return ok();
+}
+
+fmca_status fmca_plan_info(const fmca_plan* p, int64_t out[FMCA_INFO_COUNT]) {
+  if (!p || !out) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  for (int i = 0; i < FMCA_INFO_COUNT; ++i) out[i] = 0;
+  const fmca::Plan& P = p->plan;
+  out[FMCA_INFO_N_ROWS] = P.rows.n;
+  out[FMCA_INFO_N_COLS] = P.cols.n;
+  out[FMCA_INFO_DIM] = P.interp.dim;
+  out[FMCA_INFO_DEGREE] = P.interp.deg;
+  out[FMCA_INFO_Q] = P.interp.q;
+  out[FMCA_INFO_ROW_CLUSTERS] = P.rows.nclusters();
+  out[FMCA_INFO_COL_CLUSTERS] = P.cols.nclusters();
+  out[FMCA_INFO_FAR_BLOCKS] = (int64_t)P.pat.far_row.size();
+  out[FMCA_INFO_NEAR_BLOCKS] = (int64_t)P.pat.near_row.size();
+  out[FMCA_INFO_NEAR_PAIRS] = (int64_t)P.pat.near_pairs;
+  out[FMCA_INFO_ROW_LEVELS] = P.rows.nlevels();
+  out[FMCA_INFO_COL_LEVELS] = P.cols.nlevels();
+  out[FMCA_INFO_ROW_LEAVES] = (int64_t)P.row_leaves.size();
+  out[FMCA_INFO_COL_LEAVES] = (int64_t)P.col_leaves.size();
+  out[FMCA_INFO_MIN_LEAF] =
+      p->min_leaf > P.interp.q ? p->min_leaf : (int64_t)P.interp.q;
+  return ok();
+}
+
+fmca_status fmca_plan_statistics(const fmca_plan* p, double out[6]) {
+  if (!p || !out) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  p->plan.statistics(out);
+  return ok();
+}
+
+fmca_status fmca_plan_permutation(const fmca_plan* p, int side, uint32_t* perm) {
+  if (!p || !perm) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (side != 0 && side != 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "side must be 0 or 1");
+  const fmca::Tree& t = side == 0 ? p->plan.rows : p->plan.cols;
+  std::memcpy(perm, t.perm.data(), sizeof(uint32_t) * t.n);
+  return ok();
+}
+
+fmca_status fmca_plan_clusters(const fmca_plan* p, int side, int32_t* meta,
+                               double* bb) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  if (side != 0 && side != 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "side must be 0 or 1");
+  const fmca::Tree& t = side == 0 ? p->plan.rows : p->plan.cols;
+  const int C = t.nclusters(), dim = t.dim;
+  for (int c = 0; c < C; ++c) {
+    if (meta) {
+      meta[4 * c + 0] = (int32_t)t.begin[c];
+      meta[4 * c + 1] = (int32_t)t.size[c];
+      meta[4 * c + 2] = t.level[c];
+      meta[4 * c + 3] = t.parent[c];
+    }
+    if (bb)
+      for (int d = 0; d < dim; ++d) {
+        bb[(size_t)c * 3 * dim + d] = t.bbmin[(size_t)c * dim + d];
+        bb[(size_t)c * 3 * dim + dim + d] = t.bbmax[(size_t)c * dim + d];
+        bb[(size_t)c * 3 * dim + 2 * dim + d] = t.bbext[(size_t)c * dim + d];
+      }
+  }
+  return ok();
+}
+
+fmca_status fmca_plan_blocks(const fmca_plan* p, int kind, int32_t* rows,
+                             int32_t* cols) {
+  if (!p || !rows || !cols) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (kind != 0 && kind != 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "kind must be 0 or 1");
+  const auto& r = kind == 0 ? p->plan.pat.far_row : p->plan.pat.near_row;
+  const auto& c = kind == 0 ? p->plan.pat.far_col : p->plan.pat.near_col;
+  std::memcpy(rows, r.data(), sizeof(int32_t) * r.size());
+  std::memcpy(cols, c.data(), sizeof(int32_t) * c.size());
+  return ok();
+}
+
+fmca_status fmca_matvec_workspace_size(const fmca_plan* p, int precision,
+                                       int nrhs, size_t* bytes) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  if (!bytes || nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "bad nrhs or NULL bytes");
+  *bytes = fmca::gpu::workspace_bytes(p->plan, precision, nrhs);
+  return ok();
+}
+
+fmca_status fmca_matvec(fmca_plan* p, const fmca_kernel_desc* kernel,
+                        int precision, int dtype, int order, int nrhs,
+                        const void* x, int64_t x_stride_i, int64_t x_stride_r,
+                        void* y, int64_t y_stride_i, int64_t y_stride_r,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  s = check_kernel(kernel);
+  if (s != FMCA_OK) return s;
+  if (dtype != FMCA_DTYPE_F64 && dtype != FMCA_DTYPE_F32)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown dtype");
+  if (order != FMCA_ORDER_NATURAL && order != FMCA_ORDER_CLUSTER)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown order");
+  if (nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "nrhs must be >= 1");
+  if (!x || !y) return fail(FMCA_ERR_INVALID_ARGUMENT, "x or y is NULL");
+  std::string err;
+  int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  st = fmca::gpu::matvec(p->plan, p->dev, to_desc(kernel), precision, dtype, order,
+                         nrhs, x, x_stride_i, x_stride_r, y, y_stride_i, y_stride_r,
+                         workspace, workspace_bytes, (cudaStream_t)stream, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_matvec_host(fmca_plan* p, const fmca_kernel_desc* kernel,
+                             int precision, int order, int nrhs, const double* x,
+                             double* y) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  if (!x || !y || nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "bad x, y or nrhs");
+  const size_t bx = sizeof(double) * (size_t)p->plan.cols.n * nrhs;
+  const size_t by = sizeof(double) * (size_t)p->plan.rows.n * nrhs;
+  cudaError_t e;
+  if (p->hx_bytes < bx) {
+    if (p->hx) cudaFree(p->hx);
+    p->hx = nullptr;
+    p->hx_bytes = 0;
+    if ((e = cudaMalloc(&p->hx, bx)) != cudaSuccess)
+      return fail(FMCA_ERR_OUT_OF_MEMORY, cudaGetErrorString(e));
+    p->hx_bytes = bx;
+  }
+  if (p->hy_bytes < by) {
+    if (p->hy) cudaFree(p->hy);
+    p->hy = nullptr;
+    p->hy_bytes = 0;
+    if ((e = cudaMalloc(&p->hy, by)) != cudaSuccess)
+      return fail(FMCA_ERR_OUT_OF_MEMORY, cudaGetErrorString(e));
+    p->hy_bytes = by;
+  }
+  if ((e = cudaMemcpy(p->hx, x, bx, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return fail(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  s = fmca_matvec(p, kernel, precision, FMCA_DTYPE_F64, order, nrhs, p->hx, 1,
+                  (int64_t)p->plan.cols.n, p->hy, 1, (int64_t)p->plan.rows.n, nullptr,
+                  0, nullptr);
+  if (s != FMCA_OK) return s;
+  if ((e = cudaMemcpy(y, p->hy, by, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return fail(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  return fmca_plan_check_device_error(p);
+}
+
+fmca_status fmca_plan_check_device_error(fmca_plan* p) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  std::string err;
+  int st = fmca::gpu::check_device_error(p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_kernel_eval(const fmca_kernel_desc* kernel, int dim,
+                             const double* PR, int64_t n_r, const double* PC,
+                             int64_t n_c, double* out) {
+  fmca_status s = check_kernel(kernel);
+  if (s != FMCA_OK) return s;
+  if (!PR || !PC || !out || dim < 1 || n_r < 1 || n_c < 1)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "bad arguments");
+  std::string err;
+  int st = fmca::gpu::dense_eval(to_desc(kernel), dim, PR, n_r, PC, n_c, out, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,37 @@
+// GPU side of the H2 matvec: device copy of a Plan and the matvec driver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "h2_plan.h"
+
+namespace fmca {
+namespace gpu {
+
+struct DevPlan;
+
+struct KernelDesc {
+  int type;
+  double l, c, nu, sigma2;
+};
+
+// status codes are the fmca_status values of include/fmca_gb300.h
+int upload(const Plan& plan, int precision, DevPlan** dev, std::string* err);
+void destroy(DevPlan* dev);
+size_t workspace_bytes(const Plan& plan, int precision, int nrhs);
+int matvec(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision,
+           int dtype, int order, int nrhs, const void* x, int64_t sxi,
+           int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
+           size_t ws_bytes, cudaStream_t stream, std::string* err);
+int check_device_error(DevPlan* dev, std::string* err);
+int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
+               const double* PC, int64_t nc, double* out, std::string* err);
+// device the plan lives on (-1 if not uploaded)
+int device_of(const DevPlan* dev);
+
+}  // namespace gpu
+}  // namespace fmca

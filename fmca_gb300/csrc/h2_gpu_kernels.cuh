@@ -1,0 +1,722 @@
+// Device code of the H2 matvec (sm_103a).
+//
+// Stages of one product y = K_H2 x (FMCA/src/H2Matrix/H2MatrixBase.h:113-152):
+//   gather      x (natural order, any strides) -> xc (cluster order, ld = ldv)
+//   leafmom     t_tau = V_tau xc_tau for column leaves, V generated from the
+//               points on the fly (forward_transform_impl.h:31-33,
+//               NystromMoments.h:24-34)
+//   m2m         t_dad = sum_sons E_son t_son, one launch per level, bottom-up
+//               (forward_transform_impl.h:24-30)
+//   ksum far    s_tau = sum_sigma K(xi_tau, xi_sigma) t_sigma over the
+//               admissible list of every row cluster (NystromEvaluator.h:
+//               40-56 + H2MatrixBase.h:140-142)
+//   l2l         s_son += E_son^T s_dad, one launch per level, top-down
+//               (backward_transform_impl.h:21-28)
+//   leafgather  yfar_tau = V_tau^T s_tau for row leaves
+//               (backward_transform_impl.h:29-31)
+//   ksum near   ynear_tau = sum K(X_tau, X_sigma) xc_sigma over the dense
+//               list of every row leaf (NystromEvaluator.h:61-71 +
+//               H2MatrixBase.h:143-146)
+//   scatter     y = sigma2 * (ynear + yfar), combined in FP64, natural order
+//
+// ksum is the hot kernel: one CTA owns a group of targets (points of a row
+// leaf, or interpolation nodes of a row cluster) and streams the group's
+// source intervals through shared memory with cp.async.bulk copies completed
+// on mbarriers (3-stage ring).  Each thread keeps TPT targets x RB
+// right-hand sides in registers; every source costs one broadcast load of
+// its coordinates and RB/4 broadcast vector loads of its values.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fmca {
+namespace gpu {
+
+constexpr double kDblEps = 2.220446049250313080847263336181640625e-16;
+
+template <typename T>
+struct alignas(4 * sizeof(T)) Pt4 {
+  T x, y, z, w;
+};
+
+// target group of ksum: targets [tbegin, tbegin + tcount) of the target
+// array, sources = union of intervals ivl[2*ivl_begin .. 2*ivl_end)
+struct KGroup {
+  uint32_t tbegin, tcount;
+  int32_t ivl_begin, ivl_end;
+};
+
+template <typename T>
+struct KParams {
+  int type;
+  T l, c;
+  T a;   // sqrt(3)/l, sqrt(5)/l, ... (per type)
+  T e2;  // scale of the exponent in base 2 (FP32 path)
+};
+
+template <typename T>
+struct InterpDev {
+  int dim, p1, q;
+  T xi[8], w[8];
+};
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src,
+                                         uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+      "%2;\n selp.u32 %0, 1, 0, p;\n}" : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for a phase of an mbarrier for at most limit_ns; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_timer_ns() - t0 > limit_ns) return false;
+  }
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait
+
+// ---------------------------------------------------------------------------
+// radial kernels, evaluated from the squared distance.
+// KT >= 0: compile-time kernel type; KT < 0: runtime switch on kp.type.
+// FP64: operation order of FMCA/src/CovarianceKernel/CovarianceKernel.h.
+__device__ __forceinline__ double keval_ref(int type, double r2,
+                                           const KParams<double>& kp) {
+  const double r = sqrt(r2);
+  const double l = kp.l;
+  switch (type) {
+    case 0:
+      return exp(-r / l);
+    case 1:
+      return (1. + kp.a * r) * exp(-1.7320508075688772 * r / l);
+    case 2:
+      return (1. + kp.a * r + 5 * r * r / (3 * l * l)) *
+             exp(-2.23606797749979 * r / l);
+    case 3:
+      return exp(-0.5 * r * r / (l * l));
+    case 4: {
+      const double t = r / l;
+      return (1. + kp.a * r + 14. / 5 * (t * t) +
+              7. * 2.6457513110645907 / 15. * (t * t * t)) *
+             exp(-2.6457513110645907 * r / l);
+    }
+    case 5: {
+      const double t = r / l;
+      return (1. + 3. / l * r + 27. / 7. * (t * t) + 18. / 7. * (t * t * t) +
+              27. / 35. * (t * t * t * t)) *
+             exp(-3 * r / l);
+    }
+    case 6:
+      return 1. / sqrt((r / l) * (r / l) + kp.c * kp.c);
+    case 7:
+      return sqrt((r / l) * (r / l) + kp.c * kp.c);
+    case 8:
+      return r / l;
+    case 9:
+      return (r / l) * (r / l) * (r / l);
+  }
+  return 0.;
+}
+
+// FP32: approximate sqrt / exp2 on the SFU, FP32 FMA elsewhere.
+__device__ __forceinline__ float keval_fast(int type, float r2,
+                                            const KParams<float>& kp) {
+  switch (type) {
+    case 0: {  // exp(-r/l)
+      const float r = sqrt_approx(r2);
+      return ex2_approx(r * kp.e2);
+    }
+    case 1: {  // (1 + a r) exp(-a r)
+      const float r = sqrt_approx(r2);
+      const float e = ex2_approx(r * kp.e2);
+      return fmaf(kp.a * r, e, e);
+    }
+    case 2: {  // (1 + a r + (a r)^2 / 3) exp(-a r)
+      const float r = sqrt_approx(r2);
+      const float t = kp.a * r;
+      const float e = ex2_approx(r * kp.e2);
+      return fmaf(fmaf(t, 0.333333343f, 1.f), t, 1.f) * e;
+    }
+    case 3:  // exp(-r^2 / (2 l^2))
+      return ex2_approx(r2 * kp.e2);
+    case 4: {
+      const float r = sqrt_approx(r2);
+      const float t = r / kp.l;
+      const float e = ex2_approx(r * kp.e2);
+      const float p = fmaf(fmaf(fmaf(t, 1.2346839451789856f, 2.8f), t,
+                                2.6457513110645907f),
+                           t, 1.f);
+      return p * e;
+    }
+    case 5: {
+      const float r = sqrt_approx(r2);
+      const float t = r / kp.l;
+      const float e = ex2_approx(r * kp.e2);
+      const float p =
+          fmaf(fmaf(fmaf(fmaf(t, 0.77142857f, 2.5714285f), t, 3.857142857f), t,
+                    3.f),
+               t, 1.f);
+      return p * e;
+    }
+    case 6: {
+      const float t2 = r2 / (kp.l * kp.l);
+      return rsqrt_approx(t2 + kp.c * kp.c);
+    }
+    case 7: {
+      const float t2 = r2 / (kp.l * kp.l);
+      return sqrt_approx(t2 + kp.c * kp.c);
+    }
+    case 8:
+      return sqrt_approx(r2) / kp.l;
+    case 9: {
+      const float t = sqrt_approx(r2) / kp.l;
+      return t * t * t;
+    }
+  }
+  return 0.f;
+}
+
+template <typename T, int KT>
+__device__ __forceinline__ T keval(T r2, const KParams<T>& kp);
+template <>
+__device__ __forceinline__ double keval<double, -1>(double r2,
+                                                    const KParams<double>& kp) {
+  return keval_ref(kp.type, r2, kp);
+}
+template <>
+__device__ __forceinline__ double keval<double, 0>(double r2,
+                                                   const KParams<double>& kp) {
+  return keval_ref(0, r2, kp);
+}
+template <>
+__device__ __forceinline__ double keval<double, 1>(double r2,
+                                                   const KParams<double>& kp) {
+  return keval_ref(1, r2, kp);
+}
+template <>
+__device__ __forceinline__ double keval<double, 2>(double r2,
+                                                   const KParams<double>& kp) {
+  return keval_ref(2, r2, kp);
+}
+template <>
+__device__ __forceinline__ double keval<double, 3>(double r2,
+                                                   const KParams<double>& kp) {
+  return keval_ref(3, r2, kp);
+}
+template <>
+__device__ __forceinline__ float keval<float, -1>(float r2,
+                                                  const KParams<float>& kp) {
+  return keval_fast(kp.type, r2, kp);
+}
+template <>
+__device__ __forceinline__ float keval<float, 0>(float r2,
+                                                 const KParams<float>& kp) {
+  return keval_fast(0, r2, kp);
+}
+template <>
+__device__ __forceinline__ float keval<float, 1>(float r2,
+                                                 const KParams<float>& kp) {
+  return keval_fast(1, r2, kp);
+}
+template <>
+__device__ __forceinline__ float keval<float, 2>(float r2,
+                                                 const KParams<float>& kp) {
+  return keval_fast(2, r2, kp);
+}
+template <>
+__device__ __forceinline__ float keval<float, 3>(float r2,
+                                                 const KParams<float>& kp) {
+  return keval_fast(3, r2, kp);
+}
+
+// ---------------------------------------------------------------------------
+// ksum: out[t][rofs + r] (+)= sum_s k(|tgt_t - src_s|) * sval[s][rofs + r]
+// Shared memory: [bars | counts] (128 B), then STAGES tiles of TS source
+// coordinates, then STAGES tiles of TS x ldv source values.
+template <typename T, int KT, int TPT, int RB, int TS, int STAGES>
+__global__ void ksum_kernel(const KGroup* __restrict__ groups,
+                            const uint32_t* __restrict__ ivl,
+                            const Pt4<T>* __restrict__ tgt,
+                            const Pt4<T>* __restrict__ src,
+                            const T* __restrict__ sval, int ldv,
+                            T* __restrict__ out, int rofs, int rcount,
+                            KParams<T> kp, int accumulate, int* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+  int* scnt = reinterpret_cast<int*>(smem_raw + 8 * STAGES);
+  Pt4<T>* spts = reinterpret_cast<Pt4<T>*>(smem_raw + 128);
+  T* svals = reinterpret_cast<T*>(smem_raw + 128 + STAGES * TS * sizeof(Pt4<T>));
+
+  const KGroup g = groups[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+
+  T tx[TPT], ty[TPT], tz[TPT];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const uint32_t i = tid + t * nthr;
+    if (i < g.tcount) {
+      const Pt4<T> p = tgt[g.tbegin + i];
+      tx[t] = p.x;
+      ty[t] = p.y;
+      tz[t] = p.z;
+    } else {
+      tx[t] = ty[t] = tz[t] = T(0);
+    }
+  }
+  T acc[TPT][RB];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t)
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[t][r] = T(0);
+
+  int ntiles = 0;
+  for (int i = g.ivl_begin; i < g.ivl_end; ++i)
+    ntiles += (int)((ivl[2 * i + 1] - ivl[2 * i] + TS - 1) / TS);
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // producer cursor (thread 0 only)
+  int pi = g.ivl_begin;
+  uint32_t poff = 0;
+  int issued = 0;
+  auto issue = [&](int stage) {
+    const uint32_t b = ivl[2 * pi], e = ivl[2 * pi + 1];
+    const uint32_t s0 = b + poff;
+    const uint32_t cnt = (e - s0) < (uint32_t)TS ? (e - s0) : (uint32_t)TS;
+    scnt[stage] = (int)cnt;
+    const uint32_t bp = cnt * (uint32_t)sizeof(Pt4<T>);
+    const uint32_t bv = cnt * (uint32_t)ldv * (uint32_t)sizeof(T);
+    mbar_expect_tx(&bars[stage], bp + bv);
+    bulk_g2s(spts + stage * TS, src + s0, bp, &bars[stage]);
+    bulk_g2s(svals + (size_t)stage * TS * ldv, sval + (size_t)s0 * ldv, bv,
+             &bars[stage]);
+    poff += cnt;
+    if (b + poff >= e) {
+      ++pi;
+      poff = 0;
+    }
+    ++issued;
+  };
+  if (tid == 0)
+    for (int s = 0; s < STAGES && s < ntiles; ++s) issue(s);
+
+  bool aborted = false;
+  for (int k = 0; k < ntiles; ++k) {
+    const int stage = k % STAGES;
+    const uint32_t parity = (uint32_t)((k / STAGES) & 1);
+    const bool ok = mbar_wait_bounded(&bars[stage], parity, kWaitLimitNs);
+    if (ok) {
+      const int cnt = scnt[stage];
+      const Pt4<T>* P = spts + stage * TS;
+      const T* V = svals + (size_t)stage * TS * ldv + rofs;
+#pragma unroll 2
+      for (int j = 0; j < cnt; ++j) {
+        const Pt4<T> s = P[j];
+        T kv[TPT];
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+          const T dx = tx[t] - s.x, dy = ty[t] - s.y, dz = tz[t] - s.z;
+          kv[t] = keval<T, KT>(dx * dx + dy * dy + dz * dz, kp);
+        }
+        const T* v = V + (size_t)j * ldv;
+        if constexpr (RB % 4 == 0 && sizeof(T) == 4) {
+#pragma unroll
+          for (int r = 0; r < RB; r += 4) {
+            const float4 vv = *reinterpret_cast<const float4*>(v + r);
+#pragma unroll
+            for (int t = 0; t < TPT; ++t) {
+              acc[t][r + 0] = fmaf(kv[t], vv.x, acc[t][r + 0]);
+              acc[t][r + 1] = fmaf(kv[t], vv.y, acc[t][r + 1]);
+              acc[t][r + 2] = fmaf(kv[t], vv.z, acc[t][r + 2]);
+              acc[t][r + 3] = fmaf(kv[t], vv.w, acc[t][r + 3]);
+            }
+          }
+        } else if constexpr (RB % 2 == 0 && sizeof(T) == 8) {
+#pragma unroll
+          for (int r = 0; r < RB; r += 2) {
+            const double2 vv = *reinterpret_cast<const double2*>(v + r);
+#pragma unroll
+            for (int t = 0; t < TPT; ++t) {
+              acc[t][r + 0] = fma(kv[t], vv.x, acc[t][r + 0]);
+              acc[t][r + 1] = fma(kv[t], vv.y, acc[t][r + 1]);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            const T vv = v[r];
+#pragma unroll
+            for (int t = 0; t < TPT; ++t) acc[t][r] += kv[t] * vv;
+          }
+        }
+      }
+    }
+    if (__syncthreads_or(ok ? 0 : 1)) {
+      aborted = true;
+      break;
+    }
+    if (tid == 0 && k + STAGES < ntiles) issue(stage);
+  }
+  if (aborted) {
+    if (tid == 0) {
+      atomicExch(err, 1);
+      // drain the copies this CTA still has in flight, again bounded
+      const int consumed_max = issued;
+      for (int k = 0; k < consumed_max; ++k)
+        mbar_wait_bounded(&bars[k % STAGES], (uint32_t)((k / STAGES) & 1),
+                          kWaitLimitNs / 4);
+    }
+    return;
+  }
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const uint32_t i = tid + t * nthr;
+    if (i < g.tcount) {
+      T* o = out + (size_t)(g.tbegin + i) * ldv + rofs;
+#pragma unroll
+      for (int r = 0; r < RB; ++r)
+        if (r < rcount) o[r] = accumulate ? o[r] + acc[t][r] : acc[t][r];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 1-D barycentric Lagrange factors, same guard and operation order as the
+// host (TensorProductInterpolator.h:65-81)
+template <typename T>
+__device__ __forceinline__ void lagrange1d(const InterpDev<T>& ip, T x, T* f) {
+  T weight = T(0);
+  for (int k = 0; k < ip.p1; ++k) weight += ip.w[k] / (x - ip.xi[k]);
+  for (int a = 0; a < ip.p1; ++a) {
+    const T dxa = x - ip.xi[a];
+    f[a] = (fabs(dxa) > T(kDblEps)) ? ip.w[a] / dxa / weight : T(1);
+  }
+}
+
+// leaf moments: t[c][k][r] = sum_i V_c[k][i] x[i][r]
+// blockDim 128; shared: midx q*3 ints, F[64][3][8], X[64][RB]
+template <typename T, int RB>
+__global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
+                               const uint32_t* __restrict__ cbegin,
+                               const uint32_t* __restrict__ csize,
+                               const T* __restrict__ bbmin,
+                               const T* __restrict__ bbext,
+                               const Pt4<T>* __restrict__ pts,
+                               const T* __restrict__ xc, int ldv, int rofs,
+                               int rcount, const int* __restrict__ midx_g,
+                               InterpDev<T> ip, T* __restrict__ tout) {
+  constexpr int CH = 64;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* F = reinterpret_cast<T*>(smem_raw);  // CH x 3 x 8
+  T* X = F + CH * 24;                     // CH x RB
+  int* midx = reinterpret_cast<int*>(X + CH * RB);
+  const int c = leaves[blockIdx.x];
+  const uint32_t b = cbegin[c], n = csize[c];
+  const int q = ip.q, tid = threadIdx.x;
+  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  T lo[3], ex[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = d < ip.dim ? bbmin[c * 3 + d] : T(0);
+    ex[d] = d < ip.dim ? bbext[c * 3 + d] : T(1);
+  }
+  __syncthreads();
+  for (int kc = 0; kc < q; kc += blockDim.x) {
+    const int k = kc + tid;
+    const bool valid = k < q;
+    const int m0 = valid ? midx[k * 3 + 0] : 0;
+    const int m1 = valid ? midx[k * 3 + 1] : 0;
+    const int m2 = valid ? midx[k * 3 + 2] : 0;
+    T acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = T(0);
+    for (uint32_t i0 = 0; i0 < n; i0 += CH) {
+      const int cnt = (int)((n - i0) < (uint32_t)CH ? (n - i0) : CH);
+      if (tid < cnt) {
+        const Pt4<T> p = pts[b + i0 + tid];
+        const T pc[3] = {p.x, p.y, p.z};
+        for (int d = 0; d < 3; ++d) {
+          T* f = F + (tid * 3 + d) * 8;
+          if (d < ip.dim)
+            lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f);
+          else
+            f[0] = T(1);
+        }
+      }
+      for (int e = tid; e < cnt * RB; e += blockDim.x) {
+        const int i = e / RB, r = e % RB;
+        X[e] = (r < rcount) ? xc[(size_t)(b + i0 + i) * ldv + rofs + r] : T(0);
+      }
+      __syncthreads();
+      if (valid) {
+        for (int i = 0; i < cnt; ++i) {
+          const T v = F[(i * 3 + 0) * 8 + m0] * F[(i * 3 + 1) * 8 + m1] *
+                      F[(i * 3 + 2) * 8 + m2];
+#pragma unroll
+          for (int r = 0; r < RB; ++r) acc[r] += v * X[i * RB + r];
+        }
+      }
+      __syncthreads();
+    }
+    if (valid) {
+      T* o = tout + ((size_t)c * q + k) * ldv + rofs;
+      for (int r = 0; r < rcount; ++r) o[r] = acc[r];
+    }
+  }
+}
+
+// one transfer level.  up == true (M2M): for each cluster c in list,
+//   t[c][k] = sum_sons sum_j E_son[k][j] t[son][j]
+// up == false (L2L): for each cluster c in list (level >= 1),
+//   s[c][j] += sum_k E_c[k][j] s[parent][k]
+// E_c[k][j] = e_c[0][k0][j0] * e_c[1][k1][j1] * e_c[2][k2][j2]
+// shared: midx q*3, e[3][8][8], S[64][RB]
+template <typename T, int RB, bool UP>
+__global__ void transfer_kernel(const int32_t* __restrict__ clist,
+                                const int32_t* __restrict__ son0,
+                                const int32_t* __restrict__ nsons,
+                                const int32_t* __restrict__ parent,
+                                const T* __restrict__ E,
+                                const int* __restrict__ midx_g, InterpDev<T> ip,
+                                T* __restrict__ buf, int ldv, int rofs,
+                                int rcount) {
+  constexpr int JC = 64;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* e = reinterpret_cast<T*>(smem_raw);  // 3 x 8 x 8
+  T* S = e + 192;                         // JC x RB
+  int* midx = reinterpret_cast<int*>(S + JC * RB);
+  const int c = clist[blockIdx.x];
+  const int q = ip.q, p1 = ip.p1, tid = threadIdx.x;
+  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  const int nsrc = UP ? nsons[c] : 1;
+  for (int kc = 0; kc < q; kc += blockDim.x) {
+    const int k = kc + tid;  // output index
+    const bool valid = k < q;
+    T acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = T(0);
+    for (int si = 0; si < nsrc; ++si) {
+      const int ec = UP ? son0[c] + si : c;       // cluster whose E is used
+      const int sc = UP ? son0[c] + si : parent[c];  // source moments
+      __syncthreads();
+      for (int i = tid; i < 192; i += blockDim.x) {
+        const int d = i / 64, a = (i / 8) % 8, bb = i % 8;
+        e[i] = (d < ip.dim && a < p1 && bb < p1)
+                   ? E[(((size_t)ec * ip.dim + d) * p1 + a) * p1 + bb]
+                   : ((a == 0 && bb == 0) ? T(1) : T(0));
+      }
+      for (int j0 = 0; j0 < q; j0 += JC) {
+        const int cnt = (q - j0) < JC ? (q - j0) : JC;
+        __syncthreads();
+        for (int i = tid; i < cnt * RB; i += blockDim.x) {
+          const int j = i / RB, r = i % RB;
+          S[i] = (r < rcount) ? buf[((size_t)sc * q + j0 + j) * ldv + rofs + r]
+                              : T(0);
+        }
+        __syncthreads();
+        if (valid) {
+          const int k0 = midx[k * 3], k1 = midx[k * 3 + 1], k2 = midx[k * 3 + 2];
+          for (int j = 0; j < cnt; ++j) {
+            const int jj = j0 + j;
+            const int j0_ = midx[jj * 3], j1_ = midx[jj * 3 + 1],
+                      j2_ = midx[jj * 3 + 2];
+            // UP: E_son[k][jj]; DOWN: E_c[jj][k] (transpose)
+            const T ev = UP ? e[0 * 64 + k0 * 8 + j0_] * e[1 * 64 + k1 * 8 + j1_] *
+                                  e[2 * 64 + k2 * 8 + j2_]
+                            : e[0 * 64 + j0_ * 8 + k0] * e[1 * 64 + j1_ * 8 + k1] *
+                                  e[2 * 64 + j2_ * 8 + k2];
+#pragma unroll
+            for (int r = 0; r < RB; ++r) acc[r] += ev * S[j * RB + r];
+          }
+        }
+      }
+    }
+    if (valid) {
+      T* o = buf + ((size_t)c * q + k) * ldv + rofs;
+      for (int r = 0; r < rcount; ++r) o[r] = UP ? acc[r] : o[r] + acc[r];
+    }
+  }
+}
+
+// leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves
+// shared: F[blockDim][3][8], S[64][RB], midx q*3
+template <typename T, int RB>
+__global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
+                                  const uint32_t* __restrict__ cbegin,
+                                  const uint32_t* __restrict__ csize,
+                                  const T* __restrict__ bbmin,
+                                  const T* __restrict__ bbext,
+                                  const Pt4<T>* __restrict__ pts,
+                                  const T* __restrict__ s, int ldv, int rofs,
+                                  int rcount, const int* __restrict__ midx_g,
+                                  InterpDev<T> ip, T* __restrict__ yout) {
+  constexpr int KC = 64;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* F = reinterpret_cast<T*>(smem_raw);   // blockDim x 24
+  T* S = F + blockDim.x * 24;              // KC x RB
+  int* midx = reinterpret_cast<int*>(S + KC * RB);
+  const int c = leaves[blockIdx.x];
+  const uint32_t b = cbegin[c], n = csize[c];
+  const int q = ip.q, tid = threadIdx.x;
+  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  T lo[3], ex[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = d < ip.dim ? bbmin[c * 3 + d] : T(0);
+    ex[d] = d < ip.dim ? bbext[c * 3 + d] : T(1);
+  }
+  T* f = F + tid * 24;
+  for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+    const bool valid = i0 + tid < n;
+    if (valid) {
+      const Pt4<T> p = pts[b + i0 + tid];
+      const T pc[3] = {p.x, p.y, p.z};
+      for (int d = 0; d < 3; ++d) {
+        if (d < ip.dim)
+          lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8);
+        else
+          f[d * 8] = T(1);
+      }
+    }
+    T acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = T(0);
+    for (int k0 = 0; k0 < q; k0 += KC) {
+      const int cnt = (q - k0) < KC ? (q - k0) : KC;
+      __syncthreads();
+      for (int i = tid; i < cnt * RB; i += blockDim.x) {
+        const int k = i / RB, r = i % RB;
+        S[i] = (r < rcount) ? s[((size_t)c * q + k0 + k) * ldv + rofs + r] : T(0);
+      }
+      __syncthreads();
+      if (valid) {
+        for (int k = 0; k < cnt; ++k) {
+          const int kk = k0 + k;
+          const T v = f[midx[kk * 3]] * f[8 + midx[kk * 3 + 1]] *
+                      f[16 + midx[kk * 3 + 2]];
+#pragma unroll
+          for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
+        }
+      }
+    }
+    if (valid) {
+      T* o = yout + (size_t)(b + i0 + tid) * ldv + rofs;
+      for (int r = 0; r < rcount; ++r) o[r] = acc[r];
+    }
+    __syncthreads();
+  }
+}
+
+// x (natural order, strides) -> xc (cluster order, ld ldv, zero padded)
+template <typename TI, typename T>
+__global__ void gather_kernel(const uint32_t* __restrict__ perm, int64_t n,
+                              int R, const TI* __restrict__ x, int64_t sxi,
+                              int64_t sxr, T* __restrict__ xc, int ldv) {
+  const int64_t total = n * (int64_t)ldv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / ldv;
+    const int r = (int)(e % ldv);
+    const int64_t src = perm ? (int64_t)perm[i] : i;
+    xc[e] = r < R ? (T)x[src * sxi + (int64_t)r * sxr] : T(0);
+  }
+}
+
+// y (natural order) = sigma2 * (ynear + yfar), combined in FP64
+template <typename T, typename TO>
+__global__ void scatter_kernel(const uint32_t* __restrict__ perm, int64_t n,
+                               int R, const T* __restrict__ ynear,
+                               const T* __restrict__ yfar, int ldv,
+                               double sigma2, TO* __restrict__ y, int64_t syi,
+                               int64_t syr) {
+  const int64_t total = n * (int64_t)R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e % R);
+    const int64_t dst = perm ? (int64_t)perm[i] : i;
+    const double v =
+        (double)ynear[i * ldv + r] + (double)yfar[i * ldv + r];
+    y[dst * syi + (int64_t)r * syr] = (TO)(sigma2 * v);
+  }
+}
+
+// dense FP64 kernel matrix (CovarianceKernel::eval), column-major n_r x n_c
+__global__ void dense_eval_kernel(int dim, const double* __restrict__ PR,
+                                  int64_t nr, const double* __restrict__ PC,
+                                  int64_t nc, KParams<double> kp, double sigma2,
+                                  double* __restrict__ out) {
+  const int64_t total = nr * nc;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % nr, j = e / nr;
+    double r2 = 0;
+    for (int d = 0; d < dim; ++d) {
+      const double dd = PR[i * dim + d] - PC[j * dim + d];
+      r2 = d == 0 ? dd * dd : r2 + dd * dd;
+    }
+    out[e] = sigma2 * keval_ref(kp.type, r2, kp);
+  }
+}
+
+}  // namespace gpu
+}  // namespace fmca

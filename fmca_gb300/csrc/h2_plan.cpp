@@ -1,0 +1,510 @@
+// Host-side H2 plan construction.  Compile with -ffp-contract=off.
+#include "h2_plan.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <stdexcept>
+
+namespace fmca {
+
+namespace {
+constexpr double kEps = std::numeric_limits<double>::epsilon();
+constexpr double kInf = std::numeric_limits<double>::infinity();
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// kernels
+int kernel_type_from_name(const std::string& name) {
+  std::string s(name);
+  for (auto& ch : s) ch = (char)std::toupper((unsigned char)ch);
+  static const char* names[] = {"EXPONENTIAL",     "MATERN32",     "MATERN52",
+                                "GAUSSIAN",        "MATERN72",     "MATERN92",
+                                "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D",
+                                "TRIHARMONIC3D"};
+  for (int i = 0; i < K_NUM_KERNELS; ++i)
+    if (s == names[i]) return i;
+  return -1;
+}
+
+const char* kernel_type_name(int type) {
+  static const char* names[] = {"EXPONENTIAL",     "MATERN32",     "MATERN52",
+                                "GAUSSIAN",        "MATERN72",     "MATERN92",
+                                "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D",
+                                "TRIHARMONIC3D"};
+  return (type >= 0 && type < K_NUM_KERNELS) ? names[type] : "UNKNOWN";
+}
+
+// Expression order follows FMCA/src/CovarianceKernel/CovarianceKernel.h:56-116.
+double kernel_eval_host(int type, double l, double c, double r) {
+  switch (type) {
+    case K_EXPONENTIAL:
+      return std::exp(-r / l);
+    case K_MATERN32:
+      return (1. + std::sqrt(3.) / l * r) * std::exp(-std::sqrt(3.) * r / l);
+    case K_MATERN52:
+      return (1. + std::sqrt(5.) / l * r + 5 * r * r / (3 * l * l)) *
+             std::exp(-std::sqrt(5.) * r / l);
+    case K_GAUSSIAN:
+      return std::exp(-0.5 * r * r / (l * l));
+    case K_MATERN72:
+      return (1. + std::sqrt(7.) / l * r + 14. / 5 * std::pow(r / l, 2.) +
+              7. * std::sqrt(7.) / 15. * std::pow(r / l, 3.)) *
+             std::exp(-std::sqrt(7.) * r / l);
+    case K_MATERN92:
+      return (1. + 3. / l * r + 27. / 7. * std::pow(r / l, 2.) +
+              18. / 7. * std::pow(r / l, 3.) + 27. / 35. * std::pow(r / l, 4.)) *
+             std::exp(-3 * r / l);
+    case K_INVMULTIQUADRIC:
+      return 1. / std::sqrt((r / l) * (r / l) + c * c);
+    case K_MULTIQUADRIC:
+      return std::sqrt((r / l) * (r / l) + c * c);
+    case K_BIHARMONIC3D:
+      return r / l;
+    case K_TRIHARMONIC3D:
+      return (r / l) * (r / l) * (r / l);
+  }
+  return std::numeric_limits<double>::quiet_NaN();
+}
+
+// ---------------------------------------------------------------------------
+// interpolation (TensorProductInterpolator.h:39-61, MultiIndexSet.h:87-100)
+void Interp::init(int dim_, int deg_) {
+  dim = dim_;
+  deg = deg_;
+  const double weight = 2. * M_PI / (2. * double(deg) + 2.);
+  xi.assign(deg + 1, 0.);
+  w.assign(deg + 1, 0.);
+  for (int k = 0; k <= deg; ++k) {
+    xi[k] = std::cos(weight * (double(k) + 0.5));
+    xi[k] = 0.5 * (xi[k] + 1);
+    w[k] = std::sin(weight * (double(k) + 0.5));
+    if (k % 2 == 1) w[k] *= -1.;
+  }
+  // all multi-indices with entries <= deg, ordered by 1-norm, then lex
+  q = 1;
+  for (int i = 0; i < dim; ++i) q *= (deg + 1);
+  std::vector<std::vector<int>> set(q, std::vector<int>(dim));
+  for (int k = 0; k < q; ++k) {
+    int r = k;
+    for (int i = dim - 1; i >= 0; --i) {
+      set[k][i] = r % (deg + 1);
+      r /= (deg + 1);
+    }
+  }
+  std::sort(set.begin(), set.end(),
+            [](const std::vector<int>& a, const std::vector<int>& b) {
+              int na = 0, nb = 0;
+              for (int v : a) na += v;
+              for (int v : b) nb += v;
+              if (na != nb) return na < nb;
+              return std::lexicographical_compare(a.begin(), a.end(), b.begin(),
+                                                  b.end());
+            });
+  midx.assign((size_t)q * dim, 0);
+  Xi.assign((size_t)q * dim, 0.);
+  for (int k = 0; k < q; ++k)
+    for (int i = 0; i < dim; ++i) {
+      midx[(size_t)k * dim + i] = set[k][i];
+      Xi[(size_t)k * dim + i] = xi[set[k][i]];
+    }
+}
+
+// Barycentric Lagrange basis in one variable (TensorProductInterpolator.h:65-81).
+// The multivariate basis value of multi-index k is the product over the
+// dimensions, taken in dimension order starting from 1.
+void Interp::lagrange1d(double x, double* f) const {
+  double weight = 0;
+  for (int k = 0; k <= deg; ++k) weight += w[k] / (x - xi[k]);
+  for (int a = 0; a <= deg; ++a)
+    f[a] = (std::abs(x - xi[a]) > kEps) ? w[a] / (x - xi[a]) / weight : 1.;
+}
+
+// ---------------------------------------------------------------------------
+// cluster tree
+namespace {
+struct TmpNode {
+  uint32_t begin, size;
+  int level;
+  int sons[2];
+  int nsons;
+  std::vector<double> bb;  // min[dim], max[dim], ext[dim]
+};
+
+struct TreeBuilder {
+  const double* P;
+  int dim;
+  uint32_t split_threshold;
+  std::vector<uint32_t>* idx;
+  std::vector<TmpNode> nodes;
+
+  double coord(uint32_t i, int d) const { return P[(size_t)i * dim + d]; }
+
+  // ClusterTreeInitializer<ClusterTree>::init_ClusterTree_impl + the
+  // CardinalityBisection splitter
+  void refine(int me) {
+    if (nodes[me].size <= split_threshold) return;
+    TmpNode s0 = nodes[me], s1 = nodes[me];
+    s0.level = s1.level = nodes[me].level + 1;
+    s0.nsons = s1.nsons = 0;
+    // longest edge of the (propagated) father box, first maximum
+    int longest = 0;
+    for (int d = 1; d < dim; ++d)
+      if (s0.bb[2 * dim + d] > s0.bb[2 * dim + longest]) longest = d;
+    uint32_t* ids = idx->data();
+    const double* Pl = P;
+    const int D = dim;
+    const int L = longest;
+    std::sort(ids + s0.begin, ids + s0.begin + s0.size,
+              [Pl, D, L](uint32_t i, uint32_t j) {
+                return Pl[(size_t)i * D + L] < Pl[(size_t)j * D + L];
+              });
+    s0.size /= 2;
+    s1.size -= s0.size;
+    s1.begin += s0.size;
+    s0.bb[dim + longest] = coord(ids[s0.begin + s0.size - 1], longest);
+    s0.bb[2 * dim + longest] = s0.bb[dim + longest] - s0.bb[longest];
+    s1.bb[longest] = coord(ids[s1.begin], longest);
+    s1.bb[2 * dim + longest] = s1.bb[dim + longest] - s1.bb[longest];
+    const int i0 = (int)nodes.size();
+    nodes.push_back(std::move(s0));
+    nodes.push_back(std::move(s1));
+    nodes[me].sons[0] = i0;
+    nodes[me].sons[1] = i0 + 1;
+    nodes[me].nsons = 2;
+    refine(i0);
+    refine(i0 + 1);
+  }
+
+  // shrinkToFit_impl (ClusterTreeInitializer_ClusterTree.h:88-132)
+  void shrink(int me) {
+    std::vector<double> bb(3 * dim);
+    TmpNode& nd = nodes[me];
+    if (nd.size) {
+      const uint32_t* ids = idx->data();
+      for (int d = 0; d < dim; ++d) bb[d] = bb[dim + d] = coord(ids[nd.begin], d);
+      if (nd.nsons) {
+        for (int s = 0; s < nd.nsons; ++s) {
+          shrink(nodes[me].sons[s]);
+          const TmpNode& sn = nodes[nodes[me].sons[s]];
+          if (sn.size)
+            for (int d = 0; d < dim; ++d) {
+              bb[d] = std::min(bb[d], sn.bb[d]);
+              bb[dim + d] = std::max(bb[dim + d], sn.bb[dim + d]);
+            }
+        }
+      } else {
+        for (uint32_t i = 0; i < nd.size; ++i)
+          for (int d = 0; d < dim; ++d) {
+            const double v = coord(ids[nd.begin + i], d);
+            bb[d] = std::min(v, bb[d]);
+            bb[dim + d] = std::max(v, bb[dim + d]);
+          }
+      }
+    } else {
+      for (int d = 0; d < dim; ++d) {
+        bb[d] = kInf;
+        bb[dim + d] = -kInf;
+      }
+    }
+    for (int d = 0; d < dim; ++d) bb[2 * dim + d] = bb[dim + d] - bb[d];
+    for (int d = 0; d < dim; ++d)
+      if (bb[dim + d] - bb[d] < 2e2 * kEps) {
+        bb[dim + d] += 1e2 * kEps;
+        bb[d] -= 1e2 * kEps;
+        bb[2 * dim + d] = bb[dim + d] - bb[d];
+      }
+    nodes[me].bb = std::move(bb);
+  }
+};
+}  // namespace
+
+void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize) {
+  dim = dim_;
+  n = n_;
+  perm.resize(n);
+  std::iota(perm.begin(), perm.end(), 0u);
+  TreeBuilder tb;
+  tb.P = P;
+  tb.dim = dim;
+  tb.split_threshold = min_csize >= 1 ? (2 * min_csize - 1) : 1;
+  tb.idx = &perm;
+  TmpNode root;
+  root.begin = 0;
+  root.size = n;
+  root.level = 0;
+  root.nsons = 0;
+  root.bb.assign(3 * dim, 0.);
+  // init_BoundingBox_impl: box of all points, inflated by an epsilon layer
+  for (int d = 0; d < dim; ++d) {
+    double lo = n ? P[d] : 0., hi = n ? P[d] : 0.;
+    for (uint32_t i = 1; i < n; ++i) {
+      lo = std::min(lo, P[(size_t)i * dim + d]);
+      hi = std::max(hi, P[(size_t)i * dim + d]);
+    }
+    lo -= kEps * std::abs(lo);
+    hi += kEps * std::abs(hi);
+    root.bb[d] = lo;
+    root.bb[dim + d] = hi;
+    root.bb[2 * dim + d] = hi - lo;
+  }
+  tb.nodes.reserve(2 * (n / std::max<uint32_t>(1, min_csize)) + 8);
+  tb.nodes.push_back(std::move(root));
+  tb.refine(0);
+  tb.shrink(0);
+  // level-order numbering (IDDFSForwardIterator): breadth first, sons in order
+  const int C = (int)tb.nodes.size();
+  std::vector<int> order;
+  order.reserve(C);
+  order.push_back(0);
+  for (size_t h = 0; h < order.size(); ++h)
+    for (int s = 0; s < tb.nodes[order[h]].nsons; ++s)
+      order.push_back(tb.nodes[order[h]].sons[s]);
+  std::vector<int> newid(C);
+  for (int i = 0; i < C; ++i) newid[order[i]] = i;
+  begin.resize(C);
+  size.resize(C);
+  level.resize(C);
+  parent.assign(C, -1);
+  son0.assign(C, -1);
+  nsons.assign(C, 0);
+  bbmin.resize((size_t)C * dim);
+  bbmax.resize((size_t)C * dim);
+  bbext.resize((size_t)C * dim);
+  int maxlev = 0;
+  for (int i = 0; i < C; ++i) {
+    const TmpNode& nd = tb.nodes[order[i]];
+    begin[i] = nd.begin;
+    size[i] = nd.size;
+    level[i] = nd.level;
+    maxlev = std::max(maxlev, nd.level);
+    nsons[i] = nd.nsons;
+    if (nd.nsons) {
+      son0[i] = newid[nd.sons[0]];
+      for (int s = 0; s < nd.nsons; ++s) parent[newid[nd.sons[s]]] = i;
+    }
+    for (int d = 0; d < dim; ++d) {
+      bbmin[(size_t)i * dim + d] = nd.bb[d];
+      bbmax[(size_t)i * dim + d] = nd.bb[dim + d];
+      bbext[(size_t)i * dim + d] = nd.bb[2 * dim + d];
+    }
+  }
+  level_ptr.assign(maxlev + 2, 0);
+  for (int i = 0; i < C; ++i) level_ptr[level[i] + 1] = i + 1;
+  for (int l = 1; l <= maxlev + 1; ++l)
+    level_ptr[l] = std::max(level_ptr[l], level_ptr[l - 1]);
+}
+
+// ---------------------------------------------------------------------------
+// cluster bases
+void compute_transfer_factors(const Tree& t, const Interp& ip,
+                              std::vector<double>* E) {
+  const int C = t.nclusters(), dim = t.dim, p1 = ip.deg + 1;
+  const size_t per = (size_t)dim * p1 * p1;
+  E->assign((size_t)C * per, 0.);
+  std::vector<double> f(p1);
+  for (int c = 1; c < C; ++c) {
+    const int fa = t.parent[c];
+    if (fa < 0 || t.size[c] == 0) continue;  // E stays zero for empty sons
+    double* e = E->data() + (size_t)c * per;
+    for (int d = 0; d < dim; ++d) {
+      const double sc = t.bbext[(size_t)c * dim + d];
+      const double sf = t.bbext[(size_t)fa * dim + d];
+      const double mc = t.bbmin[(size_t)c * dim + d];
+      const double mf = t.bbmin[(size_t)fa * dim + d];
+      for (int b = 0; b < p1; ++b) {
+        // compute_cluster_bases_impl.h:134-139
+        const double u = ip.xi[b] * sc / sf + (mc - mf) / sf;
+        ip.lagrange1d(u, f.data());
+        for (int a = 0; a < p1; ++a) e[((size_t)d * p1 + a) * p1 + b] = f[a];
+      }
+    }
+  }
+}
+
+// interpolation nodes of a cluster: Xi .* ext + min (NystromEvaluator.h:44-49)
+void compute_node_coords(const Tree& t, const Interp& ip,
+                         std::vector<double>* nodes) {
+  const int C = t.nclusters(), dim = t.dim, q = ip.q;
+  nodes->assign((size_t)C * q * dim, 0.);
+  for (int c = 0; c < C; ++c)
+    for (int k = 0; k < q; ++k)
+      for (int d = 0; d < dim; ++d)
+        (*nodes)[((size_t)c * q + k) * dim + d] =
+            ip.Xi[(size_t)k * dim + d] * t.bbext[(size_t)c * dim + d] +
+            t.bbmin[(size_t)c * dim + d];
+}
+
+// ---------------------------------------------------------------------------
+// admissibility (Admissibility.h:19-29, 95-115)
+namespace {
+enum Adm { kRefine = 0, kLowRank = 1, kDense = 2 };
+
+inline double norm_seq(const double* v, int dim) {
+  double s = v[0] * v[0];
+  for (int d = 1; d < dim; ++d) s += v[d] * v[d];
+  return std::sqrt(s);
+}
+
+Adm compare(const Tree& r, int i, const Tree& c, int j, double eta) {
+  const int dim = r.dim;
+  double tmp[16];
+  std::vector<double> big;
+  double* v = tmp;
+  if (dim > 16) {
+    big.resize(dim);
+    v = big.data();
+  }
+  const double radius1 = 0.5 * norm_seq(r.bbext.data() + (size_t)i * dim, dim);
+  const double radius2 = 0.5 * norm_seq(c.bbext.data() + (size_t)j * dim, dim);
+  for (int d = 0; d < dim; ++d)
+    v[d] = 0.5 * (r.bbmin[(size_t)i * dim + d] - c.bbmin[(size_t)j * dim + d] +
+                  r.bbmax[(size_t)i * dim + d] - c.bbmax[(size_t)j * dim + d]);
+  double dist = norm_seq(v, dim) - radius1 - radius2;
+  dist = dist > 0 ? dist : 0;
+  const double radius = radius1 > radius2 ? radius1 : radius2;
+  if (radius > eta * dist) {
+    if (!r.nsons[i] || !c.nsons[j]) return kDense;
+    return kRefine;
+  }
+  return kLowRank;
+}
+}  // namespace
+
+void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
+                 int dim, int deg, double eta_, uint32_t min_leaf, bool same) {
+  interp.init(dim, deg);
+  eta = eta_;
+  points_r.assign(Pr, Pr + (size_t)dim * nr);
+  if (same)
+    points_c = points_r;
+  else
+    points_c.assign(Pc, Pc + (size_t)dim * nc);
+  same_tree = same;
+  const uint32_t mincsize =
+      min_leaf > (uint32_t)interp.q ? min_leaf : (uint32_t)interp.q;
+  rows.build(Pr, dim, nr, mincsize);
+  if (same)
+    cols = rows;
+  else
+    cols.build(Pc, dim, nc, mincsize);
+  compute_transfer_factors(rows, interp, &row_E);
+  compute_node_coords(rows, interp, &row_nodes);
+  if (same) {
+    col_E = row_E;
+    col_nodes = row_nodes;
+  } else {
+    compute_transfer_factors(cols, interp, &col_E);
+    compute_node_coords(cols, interp, &col_nodes);
+  }
+  // leaves in cluster (point) order
+  auto leaves_of = [](const Tree& t, std::vector<int32_t>* out) {
+    out->clear();
+    for (int c = 0; c < t.nclusters(); ++c)
+      if (!t.nsons[c]) out->push_back(c);
+    std::sort(out->begin(), out->end(), [&t](int a, int b) {
+      return t.begin[a] != t.begin[b] ? t.begin[a] < t.begin[b] : a < b;
+    });
+  };
+  leaves_of(rows, &row_leaves);
+  leaves_of(cols, &col_leaves);
+
+  // pattern: depth-first stack over cluster pairs (H2MatrixBase.h:160-191)
+  Pattern& P = pat;
+  P = Pattern();
+  const uint32_t qq = (uint32_t)interp.q * (uint32_t)interp.q;  // Index arithmetic
+  std::vector<std::pair<int32_t, int32_t>> stack;
+  stack.emplace_back(0, 0);
+  while (!stack.empty()) {
+    const auto blk = stack.back();
+    stack.pop_back();
+    const int i = blk.first, j = blk.second;
+    const Adm adm = compare(rows, i, cols, j, eta);
+    if (adm == kLowRank) {
+      // only low-rank if cheaper than the dense block; 32-bit unsigned
+      // products exactly like the reference's Index type
+      const uint32_t dense = rows.size[i] * cols.size[j];
+      if (qq < dense) {
+        P.far_row.push_back(i);
+        P.far_col.push_back(j);
+      } else {
+        P.near_row.push_back(i);
+        P.near_col.push_back(j);
+      }
+    } else if (adm == kRefine) {
+      for (int b = 0; b < cols.nsons[j]; ++b)
+        for (int a = 0; a < rows.nsons[i]; ++a)
+          stack.emplace_back(rows.son0[i] + a, cols.son0[j] + b);
+    } else {
+      P.near_row.push_back(i);
+      P.near_col.push_back(j);
+    }
+  }
+  // far field CSR by row cluster, column clusters ascending
+  const int Cr = rows.nclusters();
+  P.far_ptr.assign(Cr + 1, 0);
+  for (int32_t r : P.far_row) P.far_ptr[r + 1]++;
+  for (int c = 0; c < Cr; ++c) P.far_ptr[c + 1] += P.far_ptr[c];
+  P.far_idx.assign(P.far_row.size(), 0);
+  {
+    std::vector<int32_t> fill(P.far_ptr.begin(), P.far_ptr.end() - 1);
+    for (size_t b = 0; b < P.far_row.size(); ++b)
+      P.far_idx[fill[P.far_row[b]]++] = P.far_col[b];
+    for (int c = 0; c < Cr; ++c)
+      std::sort(P.far_idx.begin() + P.far_ptr[c], P.far_idx.begin() + P.far_ptr[c + 1]);
+  }
+  // near field: split dense blocks onto row leaves, merge column intervals
+  const int nleaf = (int)row_leaves.size();
+  std::vector<uint32_t> leaf_begin(nleaf);
+  for (int l = 0; l < nleaf; ++l) leaf_begin[l] = rows.begin[row_leaves[l]];
+  std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per_leaf(nleaf);
+  P.near_pairs = 0;
+  for (size_t b = 0; b < P.near_row.size(); ++b) {
+    const int i = P.near_row[b], j = P.near_col[b];
+    P.near_pairs += (uint64_t)rows.size[i] * cols.size[j];
+    if (rows.size[i] == 0 || cols.size[j] == 0) continue;
+    const uint32_t lo = rows.begin[i], hi = rows.begin[i] + rows.size[i];
+    int l = (int)(std::lower_bound(leaf_begin.begin(), leaf_begin.end(), lo) -
+                  leaf_begin.begin());
+    for (; l < nleaf && leaf_begin[l] < hi; ++l) {
+      if (rows.size[row_leaves[l]] == 0) continue;
+      per_leaf[l].emplace_back(cols.begin[j], cols.begin[j] + cols.size[j]);
+    }
+  }
+  P.near_ptr.assign(nleaf + 1, 0);
+  P.near_ivl.clear();
+  for (int l = 0; l < nleaf; ++l) {
+    auto& v = per_leaf[l];
+    std::sort(v.begin(), v.end());
+    size_t start = P.near_ivl.size();
+    for (const auto& iv : v) {
+      if (P.near_ivl.size() > start && P.near_ivl.back() == iv.first)
+        P.near_ivl.back() = iv.second;
+      else {
+        P.near_ivl.push_back(iv.first);
+        P.near_ivl.push_back(iv.second);
+      }
+    }
+    P.near_ptr[l + 1] = (int32_t)(P.near_ivl.size() / 2);
+    std::vector<std::pair<uint32_t, uint32_t>>().swap(v);
+  }
+}
+
+void Plan::statistics(double out[6]) const {
+  size_t mem = 0;
+  const uint32_t qq = (uint32_t)interp.q * (uint32_t)interp.q;
+  for (size_t b = 0; b < pat.far_row.size(); ++b) mem += qq;
+  for (size_t b = 0; b < pat.near_row.size(); ++b)
+    mem += (uint32_t)(rows.size[pat.near_row[b]] * cols.size[pat.near_col[b]]);
+  out[0] = rows.n;
+  out[1] = cols.n;
+  out[2] = (double)pat.far_row.size();
+  out[3] = (double)pat.near_row.size();
+  out[4] = std::round(double(mem) / rows.n);
+  out[5] = double(mem * sizeof(double)) / 1e9;
+}
+
+}  // namespace fmca

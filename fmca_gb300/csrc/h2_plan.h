@@ -1,0 +1,133 @@
+// Host-side H2 plan for the matrix-free H2 kernel matvec.
+//
+// The plan holds everything that depends only on the point clouds, the
+// interpolation degree and the admissibility parameter:
+//   * two cluster trees (rows, columns) built exactly like FMCA's
+//     ClusterTree with CardinalityBisection
+//     (FMCA/src/Clustering/ClusterTreeInitializer_ClusterTree.h:24-132,
+//      FMCA/src/Clustering/ClusterTreeSplitter.h:198-219),
+//     clusters numbered in level order like FMCA's IDDFS iterator
+//     (FMCA/src/util/IDDFSForwardIterator.h:37-63);
+//   * the Chebyshev tensor-product interpolation tables
+//     (FMCA/src/Interpolator/TensorProductInterpolator.h:39-81,
+//      FMCA/src/util/MultiIndexSet.h:87-187);
+//   * per-cluster 1-D transfer factors: the tensor-product transfer matrix of
+//     FMCA (FMCA/src/H2Matrix/compute_cluster_bases_impl.h:37-50) is the
+//     Kronecker product of d small (p+1)x(p+1) factors, which is what the GPU
+//     applies;
+//   * the admissible (far) and inadmissible (near) block lists of
+//     H2MatrixBase::computePattern (FMCA/src/H2Matrix/H2MatrixBase.h:160-191)
+//     with CompareCluster (FMCA/src/Clustering/Admissibility.h:19-29,95-115),
+//     re-organised as row-owned CSR lists for the GPU.
+//
+// Every floating-point expression that feeds a discrete decision (bounding
+// boxes, split dimension, admissibility) is evaluated in the same operation
+// order as the reference, and this file must be compiled with
+// -ffp-contract=off so that no multiply-add is fused.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace fmca {
+
+// Radial kernels of FMCA's CovarianceKernel (FMCA/src/CovarianceKernel/
+// CovarianceKernel.h:56-116).  The numeric codes are part of the C ABI.
+enum KernelType : int {
+  K_EXPONENTIAL = 0,
+  K_MATERN32 = 1,
+  K_MATERN52 = 2,
+  K_GAUSSIAN = 3,
+  K_MATERN72 = 4,
+  K_MATERN92 = 5,
+  K_INVMULTIQUADRIC = 6,
+  K_MULTIQUADRIC = 7,
+  K_BIHARMONIC3D = 8,
+  K_TRIHARMONIC3D = 9,
+  K_NUM_KERNELS = 10
+};
+
+// Parses an FMCA kernel name (case-insensitive, like CovarianceKernel.h:54).
+// Returns -1 for names that are not supported.
+int kernel_type_from_name(const std::string& name);
+const char* kernel_type_name(int type);
+// Scalar FP64 evaluation of the radial function k(r) with the reference's
+// expression order; used by the host (statistics, tests) only.
+double kernel_eval_host(int type, double l, double c, double r);
+
+// Chebyshev tensor-product interpolator on [0,1]^d.
+struct Interp {
+  int dim = 0;
+  int deg = 0;
+  int q = 0;                 // (deg+1)^dim
+  std::vector<double> xi;    // deg+1 univariate nodes
+  std::vector<double> w;     // deg+1 barycentric weights
+  std::vector<int> midx;     // q x dim multi-indices, graded-lex order
+  std::vector<double> Xi;    // dim x q node coordinates (column-major)
+  void init(int dim, int deg);
+  // 1-D Lagrange factors f[a] = l_a(x), a = 0..deg, with the reference's
+  // coincident-node guard (TensorProductInterpolator.h:70-79).
+  void lagrange1d(double x, double* f) const;
+};
+
+// Cluster tree in level order.  Cluster c owns cluster-ordered points
+// [begin[c], begin[c] + size[c]); perm maps cluster order to natural order
+// (ClusterTreeBase::indices()).
+struct Tree {
+  int dim = 0;
+  uint32_t n = 0;
+  std::vector<uint32_t> perm;
+  std::vector<uint32_t> begin, size;
+  std::vector<int32_t> level, parent, son0, nsons;
+  std::vector<double> bbmin, bbmax, bbext;  // C x dim, row-major per cluster
+  std::vector<int32_t> level_ptr;           // clusters of level l
+  int nclusters() const { return (int)begin.size(); }
+  int nlevels() const { return (int)level_ptr.size() - 1; }
+  // Builds the tree: min_csize is the effective minimum leaf size
+  // (H2ClusterTree.h:68-70 passes max(min_cluster_size, q)).
+  void build(const double* P, int dim, uint32_t n, uint32_t min_csize);
+};
+
+// Row-owned block lists.
+struct Pattern {
+  // raw block lists as produced by the pattern recursion (row, col ids)
+  std::vector<int32_t> far_row, far_col;    // low-rank leaves
+  std::vector<int32_t> near_row, near_col;  // dense leaves
+  // far field: CSR over row clusters; each entry a column cluster, ascending
+  std::vector<int32_t> far_ptr, far_idx;
+  // near field: CSR over row leaves (leaf index into Plan::row_leaves);
+  // entries are merged half-open intervals of column points (cluster order)
+  std::vector<int32_t> near_ptr;
+  std::vector<uint32_t> near_ivl;  // pairs (begin, end)
+  uint64_t near_pairs = 0;         // sum |tau| |sigma| over dense leaves
+};
+
+struct Plan {
+  Interp interp;
+  Tree rows, cols;
+  std::vector<double> points_r, points_c;  // dim x n, natural order
+  bool same_tree = false;  // rows and cols built from the same cloud
+  double eta = 0.8;
+  Pattern pat;
+  std::vector<int32_t> row_leaves, col_leaves;  // cluster ids of leaves
+  // per-cluster transfer factors e[c][dd][a][b] (dim x (p+1) x (p+1)):
+  // E_c (son c -> its father) = kron over dd of e[c][dd]
+  std::vector<double> row_E, col_E;
+  // interpolation node coordinates per cluster: C x q x dim
+  std::vector<double> row_nodes, col_nodes;
+
+  void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
+             int dim, int deg, double eta, uint32_t min_leaf, bool same);
+  // (m, n, #low-rank blocks, #dense blocks, nz per row, GB)
+  // exactly like H2MatrixBase::statistics (H2MatrixBase.h:70-105)
+  void statistics(double out[6]) const;
+};
+
+// Recomputes the transfer factors of one tree for an interpolator.
+void compute_transfer_factors(const Tree& t, const Interp& ip,
+                              std::vector<double>* E);
+void compute_node_coords(const Tree& t, const Interp& ip,
+                         std::vector<double>* nodes);
+
+}  // namespace fmca

@@ -1,0 +1,248 @@
+"""Host-side mirror of FMCA's Python H2 interface on top of the C ABI.
+
+``CovarianceKernel`` and ``H2Matrix`` keep the names, argument meaning and
+defaults of the reference's pybind module (py/FMCA.cpp:209-250, 448-468):
+
+    cov = CovarianceKernel("MATERN32", 0.5)
+    H = H2Matrix(cov, P, P, 4, 0.8)      # P: dim x n, float64
+    y = H.action(x)                      # x: n x R, natural order
+    H.statistics()                       # (6, 1): m, n, #LR, #dense, nz/row, GB
+
+Differences, all additive: the interpolation is the Chebyshev tensor-product
+interpolator (the reference's pybind module instantiates the total-degree
+one); ``min_leaf`` and ``precision`` keyword arguments; ``CovarianceKernel``
+accepts a variance ``sigma2``; ``action`` also takes torch tensors (CPU or
+CUDA) and returns the same kind of tensor.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import KernelDesc, check
+
+_PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class CovarianceKernel:
+    """Radial covariance kernel, like FMCA's CovarianceKernel(type, l, c, nu)."""
+
+    def __init__(self, ktype: str = "EXPONENTIAL", l: float = 1.0, c: float = 1.0,
+                 nu: float = 1.0, sigma2: float = 1.0):
+        lib = _lib.load()
+        t = C.c_int(0)
+        check(lib.fmca_kernel_type_from_name(str(ktype).encode(), C.byref(t)))
+        self._type = t.value
+        self._name = str(ktype).upper()
+        self.l = float(l)
+        self.c = float(c)
+        self.nu = float(nu)
+        self.sigma2 = float(sigma2)
+
+    def kernelType(self) -> str:  # noqa: N802 (reference name)
+        return self._name
+
+    @property
+    def type_code(self) -> int:
+        return self._type
+
+    def desc(self) -> KernelDesc:
+        return KernelDesc(self._type, self.l, self.c, self.nu, self.sigma2)
+
+    def eval(self, PR, PC) -> np.ndarray:
+        """Dense K(PR, PC): PR dim x n_r, PC dim x n_c; FP64 on the GPU."""
+        PR = np.asfortranarray(PR, dtype=np.float64)
+        PC = np.asfortranarray(PC, dtype=np.float64)
+        if PR.ndim != 2 or PC.ndim != 2 or PR.shape[0] != PC.shape[0]:
+            raise ValueError("PR and PC must be dim x n arrays of the same dim")
+        out = np.empty((PR.shape[1], PC.shape[1]), dtype=np.float64, order="F")
+        d = self.desc()
+        check(_lib.load().fmca_kernel_eval(C.byref(d), PR.shape[0], _dptr(PR), PR.shape[1],
+                                           _dptr(PC), PC.shape[1], _dptr(out)))
+        return out
+
+
+class H2Matrix:
+    """Matrix-free H2 approximation of K(Pr, Pc) with a GPU matvec.
+
+    Mirrors pyH2Matrix(ker, Pr, Pc, p=3, eta=0.8) (py/FMCA.cpp:209-220).
+    """
+
+    def __init__(self, cov: CovarianceKernel, Pr, Pc=None, p: int = 3,
+                 eta: float = 0.8, min_leaf: int = 0, precision: str = "mixed"):
+        lib = _lib.load()
+        self.cov = cov
+        self.p = int(p)
+        self.eta = float(eta)
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+        Pr = np.asfortranarray(Pr, dtype=np.float64)
+        if Pr.ndim != 2:
+            raise ValueError("Pr must be a dim x n array")
+        same = Pc is None or Pc is Pr
+        if not same:
+            Pc = np.asfortranarray(Pc, dtype=np.float64)
+            if Pc.ndim != 2 or Pc.shape[0] != Pr.shape[0]:
+                raise ValueError("Pc must be a dim x n array with the dim of Pr")
+            same = Pc.shape == Pr.shape and np.array_equal(Pc, Pr)
+        self.dim = Pr.shape[0]
+        handle = C.c_void_p()
+        Pcp = None if same else _dptr(Pc)
+        nc = Pr.shape[1] if same else Pc.shape[1]
+        check(lib.fmca_plan_create(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc, self.p,
+                                   self.eta, int(min_leaf), C.byref(handle)))
+        self._h = handle
+        info = (C.c_int64 * _lib.INFO_COUNT)()
+        check(lib.fmca_plan_info(self._h, info))
+        self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
+        self._ws = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().fmca_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def rows(self) -> int:
+        return self.info["n_rows"]
+
+    def cols(self) -> int:
+        return self.info["n_cols"]
+
+    # -- reference methods -------------------------------------------------
+    def statistics(self, verbose: bool = True) -> np.ndarray:
+        out = np.zeros(6, dtype=np.float64)
+        check(_lib.load().fmca_plan_statistics(self._h, _dptr(out)))
+        if verbose:
+            print(f"matrix size:                  {int(out[0])} x {int(out[1])}")
+            print(f"number of low rank blocks:    {int(out[2])}")
+            print(f"number of full blocks:        {int(out[3])}")
+            print(f"nz per row:                   {out[4]:g}")
+            print(f"storage size:                 {out[5]:g}GB")
+        return out.reshape(6, 1)
+
+    def _perm(self, side: int) -> np.ndarray:
+        n = self.info["n_rows"] if side == 0 else self.info["n_cols"]
+        out = np.empty(n, dtype=np.uint32)
+        check(_lib.load().fmca_plan_permutation(
+            self._h, side, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out
+
+    def rindices(self) -> np.ndarray:
+        return self._perm(0)
+
+    def cindices(self) -> np.ndarray:
+        return self._perm(1)
+
+    def clusters(self, side: int = 0):
+        """(meta, bb): meta[c] = (begin, size, level, parent); bb[c] = (min, max, ext)."""
+        C_ = self.info["row_clusters"] if side == 0 else self.info["col_clusters"]
+        meta = np.empty((C_, 4), dtype=np.int32)
+        bb = np.empty((C_, 3, self.dim), dtype=np.float64)
+        check(_lib.load().fmca_plan_clusters(self._h, side,
+                                             meta.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             _dptr(bb)))
+        return meta, bb
+
+    def blocks(self, kind: int):
+        """(rows, cols) cluster ids of the low-rank (0) or dense (1) blocks."""
+        n = self.info["far_blocks"] if kind == 0 else self.info["near_blocks"]
+        r = np.empty(n, dtype=np.int32)
+        c = np.empty(n, dtype=np.int32)
+        check(_lib.load().fmca_plan_blocks(self._h, kind,
+                                           r.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           c.ctypes.data_as(C.POINTER(C.c_int32))))
+        return r, c
+
+    def action(self, rhs, precision: Optional[str] = None):
+        """y = K_H2 rhs in natural order (pyH2Matrix::action)."""
+        prec = _PREC[precision or self.precision]
+        try:
+            import torch
+        except ImportError:  # pragma: no cover
+            torch = None
+        if torch is not None and isinstance(rhs, torch.Tensor):
+            if rhs.is_cuda:
+                return self.matvec(rhs, precision=precision)
+            dev = torch.device("cuda", torch.cuda.current_device())
+            y = self.matvec(rhs.to(dev, non_blocking=True), precision=precision)
+            return y.to("cpu")
+        x = np.asfortranarray(rhs, dtype=np.float64)
+        vec = x.ndim == 1
+        if vec:
+            x = x.reshape(-1, 1, order="F")
+        if x.ndim != 2 or x.shape[0] != self.cols():
+            raise ValueError(f"rhs must have {self.cols()} rows")
+        y = np.empty((self.rows(), x.shape[1]), dtype=np.float64, order="F")
+        d = self.cov.desc()
+        check(_lib.load().fmca_matvec_host(self._h, C.byref(d), prec, _lib.ORDER_NATURAL,
+                                           x.shape[1], _dptr(x), _dptr(y)))
+        return y[:, 0] if vec else y
+
+    # -- device API --------------------------------------------------------
+    def workspace_bytes(self, nrhs: int, precision: Optional[str] = None) -> int:
+        n = C.c_size_t(0)
+        check(_lib.load().fmca_matvec_workspace_size(
+            self._h, _PREC[precision or self.precision], int(nrhs), C.byref(n)))
+        return int(n.value)
+
+    def matvec(self, x, y=None, precision: Optional[str] = None, order: str = "natural",
+               stream=None, workspace=None):
+        """Device matvec on torch CUDA tensors (n_cols x R, any strides).
+
+        Runs asynchronously on ``stream`` (default: torch's current stream).
+        """
+        import torch
+        prec = _PREC[precision or self.precision]
+        if x.dim() == 1:
+            return self.matvec(x.unsqueeze(1), None if y is None else y.unsqueeze(1),
+                               precision, order, stream, workspace).squeeze(1)
+        if x.dtype not in (torch.float64, torch.float32):
+            raise TypeError("x must be float64 or float32")
+        if x.shape[0] != self.cols():
+            raise ValueError(f"x must have {self.cols()} rows")
+        R = x.shape[1]
+        dev = x.device
+        if y is None:
+            y = torch.empty((self.rows(), R), dtype=x.dtype, device=dev)
+        if y.dtype != x.dtype or y.shape != (self.rows(), R) or y.device != dev:
+            raise ValueError("y must match x in dtype and device and be n_rows x R")
+        dt = _lib.DTYPE_F64 if x.dtype == torch.float64 else _lib.DTYPE_F32
+        with torch.cuda.device(dev):
+            if stream is None:
+                stream = torch.cuda.current_stream(dev)
+            if workspace is None:
+                key = (prec, R, dev.index)
+                need = self.workspace_bytes(R, precision)
+                ws = self._ws.get(key)
+                if ws is None or ws.numel() < need:
+                    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+                    self._ws[key] = ws
+                workspace = ws
+            d = self.cov.desc()
+            check(_lib.load().fmca_matvec(
+                self._h, C.byref(d), prec, dt,
+                _lib.ORDER_NATURAL if order == "natural" else _lib.ORDER_CLUSTER, R,
+                C.c_void_p(x.data_ptr()), x.stride(0), x.stride(1),
+                C.c_void_p(y.data_ptr()), y.stride(0), y.stride(1),
+                C.c_void_p(workspace.data_ptr()), workspace.numel(),
+                C.c_void_p(stream.cuda_stream)))
+        return y
+
+    def check_device_error(self) -> None:
+        check(_lib.load().fmca_plan_check_device_error(self._h))

@@ -1,0 +1,187 @@
+/*
+ * fmca_gb300 — C ABI of the GB300 H2-matrix kernel matvec.
+ *
+ * This is the drop-in boundary for FMCA's matrix-free H2 product.  Every
+ * entry point takes plain pointers and sizes, returns an fmca_status and
+ * never aborts; a message for the last failure of the calling thread is
+ * available from fmca_last_error().
+ *
+ * Reference interfaces replaced (paths inside muchip/fmca):
+ *   fmca_plan_create      H2ClusterTree(mom, min_csize, P) for rows and
+ *                         columns + H2Matrix::computePattern(rct, cct, eta):
+ *                         FMCA/src/H2Matrix/H2ClusterTree.h:60-74,
+ *                         FMCA/src/H2Matrix/H2MatrixBase.h:160-191;
+ *                         the Python constructor pyH2Matrix(ker, Pr, Pc, p,
+ *                         eta): py/FMCA.cpp:210-220.
+ *   fmca_plan_statistics  H2MatrixBase::statistics(): H2MatrixBase.h:70-105,
+ *                         py/FMCA.cpp:222.
+ *   fmca_plan_permutation ClusterTreeBase::indices(), pyH2Matrix::rindices /
+ *                         cindices: FMCA/src/Clustering/ClusterTreeBase.h:63-65,
+ *                         py/FMCA.cpp:224-229.
+ *   fmca_plan_clusters    per-cluster bounding boxes and index ranges of the
+ *                         two trees (ClusterTreeBase::bb/indices_begin/
+ *                         block_size): ClusterTreeBase.h:61-71.
+ *   fmca_plan_blocks      the leaves of the block tree built by
+ *                         computePattern (low-rank / dense): H2MatrixBase.h:
+ *                         160-191.
+ *   fmca_matvec           H2MatrixBase::action(mat_eval, rhs) with the
+ *                         (unsymmetric)NystromEvaluator + CovarianceKernel:
+ *                         H2MatrixBase.h:113-152, NystromEvaluator.h:40-71,
+ *                         unsymmetricNystromEvaluator.h:42-73,
+ *                         CovarianceKernel.h:50-151; in natural order it is
+ *                         pyH2Matrix::action: py/FMCA.cpp:230-240.
+ *   fmca_matvec_host      the same as fmca_matvec with host buffers (the
+ *                         call made by the Python binding's .action).
+ *   fmca_kernel_eval      CovarianceKernel::eval(PR, PC): CovarianceKernel.h:
+ *                         145-151 (FP64, host buffers, GPU evaluation).
+ */
+#ifndef FMCA_GB300_H_
+#define FMCA_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FMCA_OK = 0,
+  FMCA_ERR_INVALID_ARGUMENT = 1,
+  FMCA_ERR_UNSUPPORTED = 2,
+  FMCA_ERR_CUDA = 3,
+  FMCA_ERR_OUT_OF_MEMORY = 4,
+  FMCA_ERR_TIMEOUT = 5,
+  FMCA_ERR_INTERNAL = 6
+} fmca_status;
+
+/* Kernel codes; names as accepted by FMCA's CovarianceKernel. */
+enum {
+  FMCA_KERNEL_EXPONENTIAL = 0,
+  FMCA_KERNEL_MATERN32 = 1,
+  FMCA_KERNEL_MATERN52 = 2,
+  FMCA_KERNEL_GAUSSIAN = 3,
+  FMCA_KERNEL_MATERN72 = 4,
+  FMCA_KERNEL_MATERN92 = 5,
+  FMCA_KERNEL_INVMULTIQUADRIC = 6,
+  FMCA_KERNEL_MULTIQUADRIC = 7,
+  FMCA_KERNEL_BIHARMONIC3D = 8,
+  FMCA_KERNEL_TRIHARMONIC3D = 9
+};
+
+/* Arithmetic of the matvec. */
+enum {
+  /* every stage in FP64 on CUDA cores: the plain FP64 GPU H2 product */
+  FMCA_PREC_FP64 = 0,
+  /* FP32 near field and FP32 coupling on CUDA cores, FP32 accumulation,
+     final near + far combination in FP64 */
+  FMCA_PREC_MIXED = 1
+};
+
+enum { FMCA_DTYPE_F64 = 0, FMCA_DTYPE_F32 = 1 };
+/* FMCA_ORDER_NATURAL: x and y are indexed like the input point clouds
+   (pyH2Matrix::action).  FMCA_ORDER_CLUSTER: both are in cluster order
+   (H2MatrixBase::action). */
+enum { FMCA_ORDER_NATURAL = 0, FMCA_ORDER_CLUSTER = 1 };
+
+typedef struct {
+  int type;      /* FMCA_KERNEL_* */
+  double l;      /* length scale (CovarianceKernel l) */
+  double c;      /* shift of the (inverse) multiquadric (CovarianceKernel c) */
+  double nu;     /* accepted for signature parity; unused */
+  double sigma2; /* variance: K = sigma2 * k(r); 1.0 reproduces FMCA */
+} fmca_kernel_desc;
+
+typedef struct fmca_plan fmca_plan;
+
+/* Plan information, indices of fmca_plan_info's output array. */
+enum {
+  FMCA_INFO_N_ROWS = 0,
+  FMCA_INFO_N_COLS = 1,
+  FMCA_INFO_DIM = 2,
+  FMCA_INFO_DEGREE = 3,
+  FMCA_INFO_Q = 4,
+  FMCA_INFO_ROW_CLUSTERS = 5,
+  FMCA_INFO_COL_CLUSTERS = 6,
+  FMCA_INFO_FAR_BLOCKS = 7,
+  FMCA_INFO_NEAR_BLOCKS = 8,
+  FMCA_INFO_NEAR_PAIRS = 9,
+  FMCA_INFO_ROW_LEVELS = 10,
+  FMCA_INFO_COL_LEVELS = 11,
+  FMCA_INFO_ROW_LEAVES = 12,
+  FMCA_INFO_COL_LEAVES = 13,
+  FMCA_INFO_MIN_LEAF = 14,
+  FMCA_INFO_COUNT = 16
+};
+
+/* Message of the last failure on this thread (empty if none). */
+const char* fmca_last_error(void);
+/* Library version string. */
+const char* fmca_version(void);
+
+/* Maps an FMCA kernel name ("MATERN32", case-insensitive) to its code. */
+fmca_status fmca_kernel_type_from_name(const char* name, int* type);
+
+/* Builds the plan on the host.  P_rows: dim x n_rows, column-major FP64
+   (one point per column, like FMCA's Matrix P).  P_cols may be NULL or equal
+   to P_rows for the symmetric case.  degree: interpolation degree p.
+   min_leaf: minimum leaf size (the effective value is max(min_leaf,
+   (p+1)^dim) like H2ClusterTree::init).  Device data is uploaded lazily on
+   the first matvec to the current CUDA device. */
+fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
+                             const double* P_cols, int64_t n_cols, int degree,
+                             double eta, int64_t min_leaf, fmca_plan** out);
+fmca_status fmca_plan_destroy(fmca_plan* plan);
+fmca_status fmca_plan_info(const fmca_plan* plan, int64_t out[FMCA_INFO_COUNT]);
+/* (rows, cols, #low-rank blocks, #dense blocks, nz per row, storage GB) */
+fmca_status fmca_plan_statistics(const fmca_plan* plan, double out[6]);
+/* side 0: rows, 1: columns.  perm[i] = natural index of cluster-order i. */
+fmca_status fmca_plan_permutation(const fmca_plan* plan, int side,
+                                  uint32_t* perm);
+/* Per cluster in level order: meta[4c+0..3] = (begin, size, level, parent),
+   bb[3*dim*c + ...] = (min[dim], max[dim], extent[dim]).  Either pointer may
+   be NULL. */
+fmca_status fmca_plan_clusters(const fmca_plan* plan, int side, int32_t* meta,
+                               double* bb);
+/* kind 0: low-rank (far) blocks, 1: dense (near) blocks; row/col cluster ids
+   in the order the pattern recursion produced them. */
+fmca_status fmca_plan_blocks(const fmca_plan* plan, int kind, int32_t* rows,
+                             int32_t* cols);
+
+/* Bytes of device workspace fmca_matvec needs for nrhs right-hand sides. */
+fmca_status fmca_matvec_workspace_size(const fmca_plan* plan, int precision,
+                                       int nrhs, size_t* bytes);
+
+/* y = K_H2 x on the GPU.  x: n_cols x nrhs, y: n_rows x nrhs, both device
+   pointers of dtype; element (i, r) lives at ptr[i*stride_i + r*stride_r]
+   (column-major FMCA layout: stride_i = 1, stride_r = n).  workspace: device
+   memory of fmca_matvec_workspace_size bytes, or NULL to use a buffer owned
+   by the plan.  stream: a cudaStream_t (NULL = legacy default stream).  The
+   call is asynchronous; device-side failures (timeouts of bounded waits) are
+   reported by fmca_plan_check_device_error after a synchronisation. */
+fmca_status fmca_matvec(fmca_plan* plan, const fmca_kernel_desc* kernel,
+                        int precision, int dtype, int order, int nrhs,
+                        const void* x, int64_t x_stride_i, int64_t x_stride_r,
+                        void* y, int64_t y_stride_i, int64_t y_stride_r,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* The same product with FP64 column-major host buffers (ld = n); copies in
+   and out and synchronises. */
+fmca_status fmca_matvec_host(fmca_plan* plan, const fmca_kernel_desc* kernel,
+                             int precision, int order, int nrhs,
+                             const double* x, double* y);
+
+/* Returns FMCA_ERR_TIMEOUT if a kernel of this plan gave up a bounded wait
+   since the last call, and clears the flag.  Synchronises the device. */
+fmca_status fmca_plan_check_device_error(fmca_plan* plan);
+
+/* Dense kernel matrix K(PR, PC) (n_r x n_c, column-major FP64 host buffers),
+   evaluated on the GPU in FP64; like CovarianceKernel::eval. */
+fmca_status fmca_kernel_eval(const fmca_kernel_desc* kernel, int dim,
+                             const double* PR, int64_t n_r, const double* PC,
+                             int64_t n_c, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FMCA_GB300_H_ */

@@ -1,0 +1,126 @@
+"""ORACLE — test infrastructure only (see h2_oracle.cpp for what it restates
+and what pins it).  Loaded by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline legs; never by the fmca_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    lib = C.CDLL(path)
+    dp, vp, i64, i32 = C.POINTER(C.c_double), C.c_void_p, C.c_int64, C.c_int
+    lib.oracle_plan_create.restype = vp
+    lib.oracle_plan_create.argtypes = [dp, i32, i64, dp, i64, i32, C.c_double, i64]
+    lib.oracle_plan_destroy.argtypes = [vp]
+    lib.oracle_counts.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.oracle_perm.argtypes = [vp, i32, C.POINTER(C.c_uint32)]
+    lib.oracle_clusters.argtypes = [vp, i32, C.POINTER(C.c_int32), dp]
+    lib.oracle_blocks.argtypes = [vp, i32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.oracle_statistics.argtypes = [vp, dp]
+    lib.oracle_check_transfer.restype = C.c_double
+    lib.oracle_check_transfer.argtypes = [vp]
+    lib.oracle_action.argtypes = [vp, i32, C.c_double, C.c_double, C.c_double, dp, i32, dp,
+                                  i32, i32, dp]
+    lib.oracle_dense_matvec.argtypes = [i32, C.c_double, C.c_double, C.c_double, i32, dp, i64,
+                                        dp, i64, dp, i32, dp, i32]
+    lib.oracle_kernel.restype = C.c_double
+    lib.oracle_kernel.argtypes = [i32, C.c_double, C.c_double, C.c_double]
+    _lib = lib
+    return lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OraclePlan:
+    """FP64 CPU H2 restatement over the same inputs as fmca_gb300.H2Matrix."""
+
+    def __init__(self, Pr, Pc=None, p=3, eta=0.8, min_leaf=0):
+        lib = load()
+        self.Pr = np.asfortranarray(Pr, dtype=np.float64)
+        self.same = Pc is None
+        self.Pc = self.Pr if self.same else np.asfortranarray(Pc, dtype=np.float64)
+        self.dim = self.Pr.shape[0]
+        self._h = lib.oracle_plan_create(_d(self.Pr), self.dim, self.Pr.shape[1],
+                                         None if self.same else _d(self.Pc), self.Pc.shape[1],
+                                         int(p), float(eta), int(min_leaf))
+        cnt = (C.c_int64 * 5)()
+        lib.oracle_counts(self._h, cnt)
+        self.row_clusters, self.col_clusters, self.n_far, self.n_near, self.q = list(cnt)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().oracle_plan_destroy(self._h)
+            self._h = None
+
+    def perm(self, side):
+        n = self.Pr.shape[1] if side == 0 else self.Pc.shape[1]
+        out = np.empty(n, dtype=np.uint32)
+        load().oracle_perm(self._h, side, out.ctypes.data_as(C.POINTER(C.c_uint32)))
+        return out
+
+    def clusters(self, side):
+        Cn = self.row_clusters if side == 0 else self.col_clusters
+        meta = np.empty((Cn, 4), dtype=np.int32)
+        bb = np.empty((Cn, 3, self.dim), dtype=np.float64)
+        load().oracle_clusters(self._h, side, meta.ctypes.data_as(C.POINTER(C.c_int32)), _d(bb))
+        return meta, bb
+
+    def blocks(self, kind):
+        n = self.n_far if kind == 0 else self.n_near
+        r = np.empty(n, dtype=np.int32)
+        c = np.empty(n, dtype=np.int32)
+        load().oracle_blocks(self._h, kind, r.ctypes.data_as(C.POINTER(C.c_int32)),
+                             c.ctypes.data_as(C.POINTER(C.c_int32)))
+        return r, c
+
+    def statistics(self):
+        out = np.zeros(6)
+        load().oracle_statistics(self._h, _d(out))
+        return out
+
+    def check_transfer(self):
+        return load().oracle_check_transfer(self._h)
+
+    def action(self, ktype, l, x, c=1.0, sigma2=1.0, bucket_stride=1, nthreads=0):
+        """y = sigma2 * H2(x) in natural order; returns (y, (dense_pairs, lr_pairs))."""
+        x = np.asfortranarray(x, dtype=np.float64)
+        vec = x.ndim == 1
+        if vec:
+            x = x.reshape(-1, 1, order="F")
+        y = np.empty((self.Pr.shape[1], x.shape[1]), dtype=np.float64, order="F")
+        work = np.zeros(2)
+        load().oracle_action(self._h, int(ktype), float(l), float(c), float(sigma2), _d(x),
+                             x.shape[1], _d(y), int(bucket_stride), int(nthreads), _d(work))
+        return (y[:, 0] if vec else y), tuple(work)
+
+
+def dense_matvec(ktype, l, Pr, Pc, x, c=1.0, sigma2=1.0, nthreads=0):
+    Pr = np.asfortranarray(Pr, dtype=np.float64)
+    Pc = np.asfortranarray(Pc, dtype=np.float64)
+    x = np.asfortranarray(x, dtype=np.float64)
+    vec = x.ndim == 1
+    if vec:
+        x = x.reshape(-1, 1, order="F")
+    y = np.empty((Pr.shape[1], x.shape[1]), dtype=np.float64, order="F")
+    load().oracle_dense_matvec(int(ktype), float(l), float(c), float(sigma2), Pr.shape[0], _d(Pr),
+                               Pr.shape[1], _d(Pc), Pc.shape[1], _d(x), x.shape[1], _d(y),
+                               int(nthreads))
+    return y[:, 0] if vec else y
+
+
+def kernel(ktype, l, r, c=1.0):
+    return load().oracle_kernel(int(ktype), float(l), float(c), float(r))
