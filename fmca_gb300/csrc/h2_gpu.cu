@@ -305,14 +305,20 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
   return FMCA_OK;
 }
 
-// right-hand-side blocking: RB accumulators per target, ld of all buffers
+// right-hand-side blocking: RB accumulators per target; every per-row buffer
+// is chunk-major ([R / RB][rows][ld]) so one chunk is contiguous and a source
+// tile of ksum copies only its chunk.  ld = max(RB, 16 bytes / sizeof(T))
+// keeps every row of a chunk 16-byte aligned for the bulk copies.
 int rhs_block(int nrhs) { return nrhs <= 1 ? 1 : (nrhs <= 8 ? 8 : 32); }
 template <typename T>
 int ld_for(int nrhs) {
   const int rb = rhs_block(nrhs);
-  int ld = (nrhs + rb - 1) / rb * rb;
   const int minld = 16 / (int)sizeof(T);
-  return ld < minld ? minld : ld;
+  return rb < minld ? minld : rb;
+}
+int nchunks_for(int nrhs) {
+  const int rb = rhs_block(nrhs);
+  return (nrhs + rb - 1) / rb;
 }
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -324,7 +330,7 @@ struct Workspace {
 
 template <typename T>
 size_t ws_layout(const Plan& plan, int nrhs, void* base, Workspace<T>* w) {
-  const int ld = ld_for<T>(nrhs);
+  const size_t ld = ld_for<T>(nrhs), nch = nchunks_for(nrhs);
   const size_t q = plan.interp.q;
   size_t off = 0;
   auto take = [&](size_t elems) {
@@ -333,11 +339,11 @@ size_t ws_layout(const Plan& plan, int nrhs, void* base, Workspace<T>* w) {
     return p;
   };
   Workspace<T> tmp;
-  tmp.xc = take((size_t)plan.cols.n * ld);
-  tmp.t = take((size_t)plan.cols.nclusters() * q * ld);
-  tmp.s = take((size_t)plan.rows.nclusters() * q * ld);
-  tmp.ynear = take((size_t)plan.rows.n * ld);
-  tmp.yfar = take((size_t)plan.rows.n * ld);
+  tmp.xc = take((size_t)plan.cols.n * ld * nch);
+  tmp.t = take((size_t)plan.cols.nclusters() * q * ld * nch);
+  tmp.s = take((size_t)plan.rows.nclusters() * q * ld * nch);
+  tmp.ynear = take((size_t)plan.rows.n * ld * nch);
+  tmp.yfar = take((size_t)plan.rows.n * ld * nch);
   if (w) *w = tmp;
   return off;
 }
@@ -547,24 +553,33 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
   };
   if (dtype == FMCA_DTYPE_F64)
-    gather_kernel<double, T><<<blocks((int64_t)plan.cols.n * ld), nthr, 0, st>>>(
-        pc, plan.cols.n, nrhs, static_cast<const double*>(x), sxi, sxr, w.xc, ld);
+    gather_kernel<double, T><<<blocks((int64_t)plan.cols.n * ld * nchunks_for(nrhs)), nthr, 0,
+                               st>>>(pc, plan.cols.n, nrhs, rb, ld,
+                                     static_cast<const double*>(x), sxi, sxr, w.xc);
   else
-    gather_kernel<float, T><<<blocks((int64_t)plan.cols.n * ld), nthr, 0, st>>>(
-        pc, plan.cols.n, nrhs, static_cast<const float*>(x), sxi, sxr, w.xc, ld);
+    gather_kernel<float, T><<<blocks((int64_t)plan.cols.n * ld * nchunks_for(nrhs)), nthr, 0,
+                              st>>>(pc, plan.cols.n, nrhs, rb, ld,
+                                    static_cast<const float*>(x), sxi, sxr, w.xc);
   FMCA_CK(cudaGetLastError());
-  for (int rofs = 0; rofs < nrhs; rofs += rb) {
-    const int rcount = std::min(rb, nrhs - rofs);
+  const size_t q = plan.interp.q;
+  for (int ch = 0; ch * rb < nrhs; ++ch) {
+    const int rcount = std::min(rb, nrhs - ch * rb);
+    Workspace<T> wc;
+    wc.xc = w.xc + (size_t)ch * plan.cols.n * ld;
+    wc.t = w.t + (size_t)ch * plan.cols.nclusters() * q * ld;
+    wc.s = w.s + (size_t)ch * plan.rows.nclusters() * q * ld;
+    wc.ynear = w.ynear + (size_t)ch * plan.rows.n * ld;
+    wc.yfar = w.yfar + (size_t)ch * plan.rows.n * ld;
     cudaError_t e;
     switch (rb) {
       case 1:
-        e = run_tree_stages<T, 1>(plan, dp, S, w, ld, rofs, rcount, kp, st);
+        e = run_tree_stages<T, 1>(plan, dp, S, wc, ld, 0, rcount, kp, st);
         break;
       case 8:
-        e = run_tree_stages<T, 8>(plan, dp, S, w, ld, rofs, rcount, kp, st);
+        e = run_tree_stages<T, 8>(plan, dp, S, wc, ld, 0, rcount, kp, st);
         break;
       default:
-        e = run_tree_stages<T, 32>(plan, dp, S, w, ld, rofs, rcount, kp, st);
+        e = run_tree_stages<T, 32>(plan, dp, S, wc, ld, 0, rcount, kp, st);
         break;
     }
     FMCA_CK(e);
@@ -572,11 +587,11 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_kernel<T, double><<<blocks((int64_t)plan.rows.n * nrhs), nthr, 0, st>>>(
-        pr, plan.rows.n, nrhs, w.ynear, w.yfar, ld, k.sigma2, static_cast<double*>(y),
+        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, k.sigma2, static_cast<double*>(y),
         syi, syr);
   else
     scatter_kernel<T, float><<<blocks((int64_t)plan.rows.n * nrhs), nthr, 0, st>>>(
-        pr, plan.rows.n, nrhs, w.ynear, w.yfar, ld, k.sigma2, static_cast<float*>(y),
+        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, k.sigma2, static_cast<float*>(y),
         syi, syr);
   FMCA_CK(cudaGetLastError());
   return FMCA_OK;

@@ -666,36 +666,41 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
   }
 }
 
-// x (natural order, strides) -> xc (cluster order, ld ldv, zero padded)
+// x (natural order, strides) -> xc (cluster order).  Buffers are chunk-major:
+// right-hand side r of row i lives at [(r / rb) * n + i] * ld + r % rb, with
+// ld >= rb; padding columns are zero.
 template <typename TI, typename T>
 __global__ void gather_kernel(const uint32_t* __restrict__ perm, int64_t n,
-                              int R, const TI* __restrict__ x, int64_t sxi,
-                              int64_t sxr, T* __restrict__ xc, int ldv) {
-  const int64_t total = n * (int64_t)ldv;
+                              int R, int rb, int ld, const TI* __restrict__ x,
+                              int64_t sxi, int64_t sxr, T* __restrict__ xc) {
+  const int nchunks = (R + rb - 1) / rb;
+  const int64_t per = n * (int64_t)ld;
+  const int64_t total = per * nchunks;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / ldv;
-    const int r = (int)(e % ldv);
+    const int64_t ch = e / per, rem = e % per;
+    const int64_t i = rem / ld;
+    const int rr = (int)(rem % ld);
+    const int r = (int)ch * rb + rr;
     const int64_t src = perm ? (int64_t)perm[i] : i;
-    xc[e] = r < R ? (T)x[src * sxi + (int64_t)r * sxr] : T(0);
+    xc[e] = (rr < rb && r < R) ? (T)x[src * sxi + (int64_t)r * sxr] : T(0);
   }
 }
 
 // y (natural order) = sigma2 * (ynear + yfar), combined in FP64
 template <typename T, typename TO>
 __global__ void scatter_kernel(const uint32_t* __restrict__ perm, int64_t n,
-                               int R, const T* __restrict__ ynear,
-                               const T* __restrict__ yfar, int ldv,
-                               double sigma2, TO* __restrict__ y, int64_t syi,
-                               int64_t syr) {
+                               int R, int rb, int ld, const T* __restrict__ ynear,
+                               const T* __restrict__ yfar, double sigma2,
+                               TO* __restrict__ y, int64_t syi, int64_t syr) {
   const int64_t total = n * (int64_t)R;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / R;
     const int r = (int)(e % R);
+    const int64_t k = ((int64_t)(r / rb) * n + i) * ld + r % rb;
     const int64_t dst = perm ? (int64_t)perm[i] : i;
-    const double v =
-        (double)ynear[i * ldv + r] + (double)yfar[i * ldv + r];
+    const double v = (double)ynear[k] + (double)yfar[k];
     y[dst * syi + (int64_t)r * syr] = (TO)(sigma2 * v);
   }
 }

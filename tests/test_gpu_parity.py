@@ -1,0 +1,167 @@
+"""GPU matvec against the FP64 oracle (same seeded inputs), through the C ABI.
+
+Tolerances: FMCA_PREC_FP64 must match the oracle to 1e-12 relative (2-norm
+over all right-hand sides); FMCA_PREC_MIXED (FP32 arithmetic, FP32
+accumulation, FP64 final combination) to 1e-5 relative."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err, sphere_cloud, uniform_cloud
+from fmca_gb300 import CovarianceKernel, H2Matrix
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "mixed": 1e-5}
+KNAMES = ["EXPONENTIAL", "MATERN32", "MATERN52", "GAUSSIAN", "MATERN72", "MATERN92",
+          "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D", "TRIHARMONIC3D"]
+
+
+@pytest.fixture(scope="module")
+def c1():
+    # n = 1e4 uniform [0,1]^3 (seed 0), EXPONENTIAL l=1, p=3, eta=0.8, leaf 64
+    P = uniform_cloud(10000, 3, seed=0)
+    x = np.random.default_rng(0).standard_normal(10000)
+    O = oracle.OraclePlan(P, None, 3, 0.8, 64)
+    y_ref, _ = O.action(0, 1.0, x)
+    return P, x, y_ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c1_against_oracle(cuda_device, c1, precision):
+    P, x, y_ref = c1
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, 3, 0.8, min_leaf=64,
+                 precision=precision)
+    y = H.action(x)
+    assert rel_err(y, y_ref) < TOL[precision]
+    H.check_device_error()
+
+
+def test_c1_against_dense(cuda_device, c1):
+    # the GPU product has the oracle's compression error w.r.t. dense K x
+    P, x, y_ref = c1
+    yd = oracle.dense_matvec(0, 1.0, P, P, x)
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, 3, 0.8, min_leaf=64,
+                 precision="fp64")
+    y = H.action(x)
+    e_gpu, e_ref = rel_err(y, yd), rel_err(y_ref, yd)
+    assert e_ref < 1e-4
+    assert abs(e_gpu - e_ref) < 1e-10
+
+
+@pytest.mark.parametrize("kname", KNAMES)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_all_kernels(cuda_device, kname, precision):
+    P = uniform_cloud(6000, 3, seed=11)
+    X = np.random.default_rng(11).standard_normal((6000, 3))
+    kt = KNAMES.index(kname)
+    O = oracle.OraclePlan(P, None, 3, 0.8, 32)
+    Y_ref, _ = O.action(kt, 0.7, X, c=0.9)
+    H = H2Matrix(CovarianceKernel(kname, 0.7, 0.9), P, P, 3, 0.8, min_leaf=32,
+                 precision=precision)
+    assert rel_err(H.action(X), Y_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("R", [1, 2, 7, 8, 9, 32, 33, 64])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_rhs_counts(cuda_device, R, precision):
+    P = uniform_cloud(5000, 3, seed=R)
+    X = np.random.default_rng(R).standard_normal((5000, R))
+    O = oracle.OraclePlan(P, None, 4, 0.8, 0)
+    Y_ref, _ = O.action(1, 0.5, X)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 4, 0.8, precision=precision)
+    assert rel_err(H.action(X), Y_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_unsymmetric_sphere(cuda_device, precision):
+    Pr = sphere_cloud(7000, seed=1)
+    Pc = sphere_cloud(4000, seed=2)
+    X = np.random.default_rng(2).standard_normal((4000, 5))
+    O = oracle.OraclePlan(Pr, Pc, 4, 0.8, 96)
+    Y_ref, _ = O.action(2, 0.3, X, sigma2=1.7)
+    H = H2Matrix(CovarianceKernel("MATERN52", 0.3, sigma2=1.7), Pr, Pc, 4, 0.8, min_leaf=96,
+                 precision=precision)
+    assert rel_err(H.action(X), Y_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_two_dimensional_aniso(cuda_device, precision):
+    P = uniform_cloud(20000, 2, seed=4)
+    P[0] *= 4
+    x = np.random.default_rng(4).choice([-1.0, 1.0], size=(20000, 4))
+    O = oracle.OraclePlan(P, None, 5, 0.6, 128)
+    Y_ref, _ = O.action(0, 0.1, x)
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 0.1), P, P, 5, 0.6, min_leaf=128,
+                 precision=precision)
+    assert rel_err(H.action(x), Y_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_leaves_and_one_dim(cuda_device, precision):
+    # leaves above the 256-target group size, and d = 1
+    P = uniform_cloud(6000, 3, seed=8)
+    x = np.random.default_rng(8).standard_normal(6000)
+    O = oracle.OraclePlan(P, None, 2, 0.8, 400)
+    y_ref, _ = O.action(3, 0.2, x)
+    H = H2Matrix(CovarianceKernel("GAUSSIAN", 0.2), P, P, 2, 0.8, min_leaf=400,
+                 precision=precision)
+    assert rel_err(H.action(x), y_ref) < TOL[precision]
+    P1 = uniform_cloud(3000, 1, seed=8)
+    x1 = np.random.default_rng(9).standard_normal(3000)
+    O1 = oracle.OraclePlan(P1, None, 6, 0.8, 0)
+    y1_ref, _ = O1.action(1, 0.05, x1)
+    H1 = H2Matrix(CovarianceKernel("MATERN32", 0.05), P1, P1, 6, 0.8, precision=precision)
+    assert rel_err(H1.action(x1), y1_ref) < TOL[precision]
+
+
+def test_tiny_clouds(cuda_device):
+    for n in (1, 2, 17):
+        P = uniform_cloud(n, 3, seed=n)
+        x = np.random.default_rng(n).standard_normal(n)
+        O = oracle.OraclePlan(P, None, 2, 0.8, 0)
+        y_ref, _ = O.action(0, 1.0, x)
+        for prec in ("fp64", "mixed"):
+            H = H2Matrix(CovarianceKernel("EXPONENTIAL"), P, P, 2, 0.8, precision=prec)
+            assert rel_err(H.action(x), y_ref) < TOL[prec]
+
+
+def test_torch_device_api(cuda_device):
+    import torch
+    P = uniform_cloud(8000, 3, seed=21)
+    X = np.random.default_rng(21).standard_normal((8000, 16))
+    O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+    Y_ref, _ = O.action(1, 0.4, X)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.4), P, P, 3, 0.8)
+    Xt = torch.tensor(X, device=cuda_device)
+    for prec in ("fp64", "mixed"):
+        y64 = H.matvec(Xt, precision=prec)                       # row-major (n, R)
+        assert rel_err(y64.cpu().numpy(), Y_ref) < TOL[prec]
+        Xf = Xt.t().contiguous().t()                              # column-major strides
+        y_cm = H.matvec(Xf, precision=prec)
+        assert rel_err(y_cm.cpu().numpy(), Y_ref) < TOL[prec]
+    y32 = H.matvec(Xt.float(), precision="mixed")
+    assert y32.dtype == torch.float32
+    assert rel_err(y32.double().cpu().numpy(), Y_ref) < 2e-5
+    # cluster order in and out: y_c = K_c x_c
+    pr, pc = H.rindices(), H.cindices()
+    Xc = Xt[torch.as_tensor(pc.astype(np.int64), device=cuda_device)]
+    yc = H.matvec(Xc, precision="fp64", order="cluster")
+    assert rel_err(yc.cpu().numpy(), Y_ref[pr.astype(np.int64)]) < 1e-12
+    # CPU tensors go through the device and come back
+    yt = H.action(torch.tensor(X))
+    assert yt.device.type == "cpu" and rel_err(yt.numpy(), Y_ref) < TOL["mixed"]
+    torch.cuda.synchronize()
+    H.check_device_error()
+
+
+def test_dense_kernel_eval(cuda_device):
+    rng = np.random.default_rng(0)
+    PR, PC = rng.random((3, 50)), rng.random((3, 40))
+    for kt, kname in enumerate(KNAMES):
+        K = CovarianceKernel(kname, 0.6, 0.8).eval(PR, PC)
+        r = np.linalg.norm(PR[:, :, None] - PC[:, None, :], axis=0)
+        ref = np.vectorize(lambda t: oracle.kernel(kt, 0.6, t, c=0.8))(r)
+        assert np.allclose(K, ref, rtol=1e-13, atol=1e-300)
