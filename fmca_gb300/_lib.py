@@ -25,6 +25,7 @@ STATUS_NAMES = {
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FP32 = 2
 DTYPE_F64 = 0
 DTYPE_F32 = 1
 ORDER_NATURAL = 0
@@ -44,7 +45,9 @@ EXPORTED = [
     "fmca_plan_statistics", "fmca_plan_permutation", "fmca_plan_clusters",
     "fmca_plan_blocks", "fmca_matvec_workspace_size", "fmca_matvec",
     "fmca_matvec_host", "fmca_plan_check_device_error", "fmca_kernel_eval",
+    "fmca_plan_set_profiling", "fmca_plan_profile",
 ]
+STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
 
 class FmcaError(RuntimeError):
@@ -92,6 +95,8 @@ def load() -> C.CDLL:
     lib.fmca_matvec_host.argtypes = [vp, C.POINTER(KernelDesc), i32, i32, i32, dp, dp]
     lib.fmca_plan_check_device_error.argtypes = [vp]
     lib.fmca_kernel_eval.argtypes = [C.POINTER(KernelDesc), i32, dp, i64, dp, i64, dp]
+    lib.fmca_plan_set_profiling.argtypes = [vp, i32]
+    lib.fmca_plan_profile.argtypes = [vp, dp, C.POINTER(C.c_int64)]
     for name in EXPORTED:
         if name not in ("fmca_last_error", "fmca_version"):
             getattr(lib, name).restype = C.c_int

@@ -19,6 +19,7 @@ struct fmca_plan {
   void* hy = nullptr;
   size_t hx_bytes = 0, hy_bytes = 0;
   int64_t min_leaf = 0;
+  bool profile = false;
 };
 
 namespace {
@@ -54,7 +55,8 @@ fmca::gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
 
 fmca_status check_gpu_plan(const fmca_plan* p, int precision) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
-  if (precision != FMCA_PREC_FP64 && precision != FMCA_PREC_MIXED)
+  if (precision != FMCA_PREC_FP64 && precision != FMCA_PREC_MIXED &&
+      precision != FMCA_PREC_FP32)
     return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown precision mode");
   if (p->plan.interp.dim > 3)
     return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports dim <= 3");
@@ -225,6 +227,7 @@ fmca_status fmca_matvec(fmca_plan* p, const fmca_kernel_desc* kernel,
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
+  fmca::gpu::set_profiling(p->dev, p->profile);
   st = fmca::gpu::matvec(p->plan, p->dev, to_desc(kernel), precision, dtype, order,
                          nrhs, x, x_stride_i, x_stride_r, y, y_stride_i, y_stride_r,
                          workspace, workspace_bytes, (cudaStream_t)stream, &err);
@@ -272,6 +275,22 @@ fmca_status fmca_plan_check_device_error(fmca_plan* p) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   std::string err;
   int st = fmca::gpu::check_device_error(p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_plan_set_profiling(fmca_plan* p, int enable) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->profile = enable != 0;
+  fmca::gpu::set_profiling(p->dev, p->profile);
+  return ok();
+}
+
+fmca_status fmca_plan_profile(fmca_plan* p, double* stage_ms, int64_t* launches) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  double tmp[FMCA_STAGE_COUNT];
+  std::string err;
+  int st = fmca::gpu::profile(p->dev, stage_ms ? stage_ms : tmp, launches, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
   return ok();
 }

@@ -8,6 +8,7 @@
 #include "../../include/fmca_gb300.h"
 #include "h2_gpu.h"
 #include "h2_gpu_kernels.cuh"
+#include "h2_tc_kernels.cuh"
 
 namespace fmca {
 namespace gpu {
@@ -24,7 +25,8 @@ namespace {
     }                                                                        \
   } while (0)
 
-constexpr int kGroupCap = 256;  // targets per ksum CTA (128 threads x 2)
+constexpr int kGroupCap = 256;    // targets per ksum CTA (128 threads x 2)
+constexpr int kTcGroupCap = 128;  // targets per ksum_tc CTA (4 warps x 32)
 constexpr int kStages = 3;
 template <typename T>
 struct TileSize;
@@ -79,11 +81,30 @@ struct DevPlan {
   std::vector<int> m2m_ptr;
   int32_t* l2l_list = nullptr;  // row clusters of level >= 1, by level
   std::vector<int> l2l_ptr;
-  GroupList far, near;
+  GroupList far, near;        // chunked to kGroupCap targets
+  GroupList far_tc, near_tc;  // chunked to kTcGroupCap targets
   int* err_flag = nullptr;
   void* ws = nullptr;
   size_t ws_bytes = 0;
   std::mutex mu;
+  // stage profiling: events recorded at stage boundaries of the last matvec
+  bool profile = false;
+  std::vector<cudaEvent_t> events;
+  std::vector<int> event_stage;
+  int nevents = 0;
+  int64_t launches = 0;  // kernels launched by the last matvec
+  void mark(int stage, cudaStream_t st) {
+    if (!profile) return;
+    if (nevents >= (int)events.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      events.push_back(e);
+      event_stage.push_back(0);
+    }
+    cudaEventRecord(events[nevents], st);
+    event_stage[nevents] = stage;
+    ++nevents;
+  }
 };
 
 namespace {
@@ -116,11 +137,12 @@ struct HostGroups {
   int maxcount = 0;
 };
 
-void add_target_range(HostGroups* hg, uint32_t tb, uint32_t tc, int ib, int ie) {
-  for (uint32_t o = 0; o < tc; o += kGroupCap) {
+void add_target_range(HostGroups* hg, uint32_t tb, uint32_t tc, int ib, int ie,
+                      uint32_t cap) {
+  for (uint32_t o = 0; o < tc; o += cap) {
     KGroup g;
     g.tbegin = tb + o;
-    g.tcount = std::min<uint32_t>(kGroupCap, tc - o);
+    g.tcount = std::min<uint32_t>(cap, tc - o);
     g.ivl_begin = ib;
     g.ivl_end = ie;
     hg->groups.push_back(g);
@@ -168,6 +190,7 @@ int upload_set(const Plan& plan, DevPlan* dp, DevSet<T>* s, std::string* err) {
       o.x = (T)p[0];
       o.y = dim > 1 ? (T)p[1] : T(0);
       o.z = dim > 2 ? (T)p[2] : T(0);
+      o.w = T(1);  // source weight of the tensor-core kernel sum
     }
   };
   auto make_nodes = [&](const std::vector<double>& nd, int C,
@@ -260,8 +283,11 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     FMCA_TRY(to_device(dp, lst.data(), lst.size(), &dp->l2l_list, err));
   }
   // far groups: targets = nodes of every row cluster, sources = node ranges
-  // of the admissible column clusters, consecutive clusters merged
-  {
+  // of the admissible column clusters, consecutive clusters merged.
+  // Two chunkings: kGroupCap targets (CUDA-core kernel sum) and kTcGroupCap
+  // (tensor-core kernel sum).
+  for (int pass = 0; pass < 2; ++pass) {
+    const uint32_t cap = pass == 0 ? kGroupCap : kTcGroupCap;
     HostGroups hg;
     const int q = ip.q;
     const Pattern& P = plan.pat;
@@ -276,24 +302,25 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
           hg.ivl.push_back(e);
         }
       }
-      add_target_range(&hg, (uint32_t)c * q, q, ib, (int)(hg.ivl.size() / 2));
+      add_target_range(&hg, (uint32_t)c * q, q, ib, (int)(hg.ivl.size() / 2), cap);
     }
     sort_groups(&hg);
-    FMCA_TRY(upload_groups(dp, hg, &dp->far, err));
+    FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->far : &dp->far_tc, err));
   }
   // near groups: targets = points of every row leaf, sources = merged
   // column point intervals
-  {
+  for (int pass = 0; pass < 2; ++pass) {
+    const uint32_t cap = pass == 0 ? kGroupCap : kTcGroupCap;
     HostGroups hg;
     const Pattern& P = plan.pat;
     hg.ivl = P.near_ivl;
     for (size_t l = 0; l < plan.row_leaves.size(); ++l) {
       const int c = plan.row_leaves[l];
       add_target_range(&hg, plan.rows.begin[c], plan.rows.size[c], P.near_ptr[l],
-                       P.near_ptr[l + 1]);
+                       P.near_ptr[l + 1], cap);
     }
     sort_groups(&hg);
-    FMCA_TRY(upload_groups(dp, hg, &dp->near, err));
+    FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->near : &dp->near_tc, err));
   }
   {
     void* p = nullptr;
@@ -465,6 +492,7 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
   const size_t midx_bytes = (size_t)q * 3 * sizeof(int);
   // upward pass: leaf moments
   {
+    dp->launches += dp->nleaves_c ? 1 : 0;
     auto kern = leafmom_kernel<T, RB>;
     const size_t smem = (64 * 24 + 64 * RB) * sizeof(T) + midx_bytes;
     ensure_smem(kern, smem);
@@ -472,6 +500,7 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
       kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
                                              S.bbmin_c, S.bbext_c, S.pts_c, w.xc, ld,
                                              rofs, rcount, dp->midx, S.ip, w.t);
+    dp->mark(FMCA_STAGE_LEAFMOM, st);
   }
   // M2M, bottom-up
   {
@@ -480,16 +509,21 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     ensure_smem(kern, smem);
     for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
       const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
-      if (nb)
+      if (nb) {
         kern<<<nb, 128, smem, st>>>(dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
                                     dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip,
                                     w.t, ld, rofs, rcount);
+        ++dp->launches;
+      }
     }
+    dp->mark(FMCA_STAGE_M2M, st);
   }
   // far-field coupling
   cudaError_t e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s,
                                  rofs, rcount, kp, 0, dp->err_flag, st);
   if (e != cudaSuccess) return e;
+  dp->launches += dp->far.ngroups ? 1 : 0;
+  dp->mark(FMCA_STAGE_FAR, st);
   // L2L, top-down
   {
     auto kern = transfer_kernel<T, RB, false>;
@@ -497,11 +531,14 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     ensure_smem(kern, smem);
     for (int l = 1; l < plan.rows.nlevels(); ++l) {
       const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
-      if (nb)
+      if (nb) {
         kern<<<nb, 128, smem, st>>>(dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
                                     dp->parent_r, S.E_r, dp->midx, S.ip, w.s, ld,
                                     rofs, rcount);
+        ++dp->launches;
+      }
     }
+    dp->mark(FMCA_STAGE_L2L, st);
   }
   // leaf gather
   {
@@ -512,21 +549,21 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
       kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
                                              S.bbmin_r, S.bbext_r, S.pts_r, w.s, ld,
                                              rofs, rcount, dp->midx, S.ip, w.yfar);
+    dp->launches += dp->nleaves_r ? 1 : 0;
+    dp->mark(FMCA_STAGE_LEAFGATHER, st);
   }
   // near field
-  return launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, rofs,
-                        rcount, kp, 0, dp->err_flag, st);
+  e = launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, rofs, rcount,
+                     kp, 0, dp->err_flag, st);
+  dp->launches += dp->near.ngroups ? 1 : 0;
+  dp->mark(FMCA_STAGE_NEAR, st);
+  return e;
 }
 
-template <typename T>
-int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
-             int dtype, int order, int nrhs, const void* x, int64_t sxi,
-             int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-             size_t wsb, cudaStream_t st, std::string* err) {
-  const int ld = ld_for<T>(nrhs);
-  const int rb = rhs_block(nrhs);
-  const size_t need = ws_layout<T>(plan, nrhs, nullptr, nullptr);
-  if (!ws) {
+// caller workspace if given, else the plan's own (grown on demand)
+int acquire_ws(DevPlan* dp, size_t need, void** ws, size_t wsb, cudaStream_t st,
+               std::string* err) {
+  if (!*ws) {
     if (dp->ws_bytes < need) {
       if (dp->ws) {
         FMCA_CK(cudaStreamSynchronize(st));
@@ -537,13 +574,28 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
       FMCA_CK(cudaMalloc(&dp->ws, need));
       dp->ws_bytes = need;
     }
-    ws = dp->ws;
+    *ws = dp->ws;
   } else if (wsb < need) {
     *err = "workspace too small: need " + std::to_string(need) + " bytes";
     return FMCA_ERR_INVALID_ARGUMENT;
   }
+  return FMCA_OK;
+}
+
+template <typename T>
+int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
+             int dtype, int order, int nrhs, const void* x, int64_t sxi,
+             int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
+             size_t wsb, cudaStream_t st, std::string* err) {
+  const int ld = ld_for<T>(nrhs);
+  const int rb = rhs_block(nrhs);
+  const size_t need = ws_layout<T>(plan, nrhs, nullptr, nullptr);
+  FMCA_TRY(acquire_ws(dp, need, &ws, wsb, st, err));
   Workspace<T> w;
   ws_layout<T>(plan, nrhs, ws, &w);
+  dp->nevents = 0;
+  dp->launches = 0;
+  dp->mark(-1, st);
   const KParams<T> kp = make_kparams<T>(k);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
   const uint32_t* pr = order == FMCA_ORDER_NATURAL ? dp->perm_r : nullptr;
@@ -561,6 +613,8 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
                               st>>>(pc, plan.cols.n, nrhs, rb, ld,
                                     static_cast<const float*>(x), sxi, sxr, w.xc);
   FMCA_CK(cudaGetLastError());
+  ++dp->launches;
+  dp->mark(FMCA_STAGE_GATHER, st);
   const size_t q = plan.interp.q;
   for (int ch = 0; ch * rb < nrhs; ++ch) {
     const int rcount = std::min(rb, nrhs - ch * rb);
@@ -593,7 +647,212 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     scatter_kernel<T, float><<<blocks((int64_t)plan.rows.n * nrhs), nthr, 0, st>>>(
         pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, k.sigma2, static_cast<float*>(y),
         syi, syr);
+  ++dp->launches;
+  dp->mark(FMCA_STAGE_SCATTER, st);
   FMCA_CK(cudaGetLastError());
+  return FMCA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision with tensor-core kernel sums
+struct TcWorkspace {
+  float *xc, *t, *s, *ynear, *yfar;
+  __half *xh, *xl, *th, *tl;
+  Pt4<float>* nodes_s;
+  unsigned int* cmax;
+};
+
+size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
+  const size_t nch = (nrhs + kTcRhs - 1) / kTcRhs, ld = kTcRhs;
+  const size_t q = plan.interp.q;
+  const size_t Cr = plan.rows.nclusters(), Cc = plan.cols.nclusters();
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    void* p = base ? static_cast<char*>(base) + off : nullptr;
+    off += align_up(bytes);
+    return p;
+  };
+  TcWorkspace t;
+  t.xc = (float*)take(plan.cols.n * ld * nch * 4);
+  t.xh = (__half*)take(plan.cols.n * ld * nch * 2);
+  t.xl = (__half*)take(plan.cols.n * ld * nch * 2);
+  t.t = (float*)take(Cc * q * ld * nch * 4);
+  t.th = (__half*)take(Cc * q * ld * 2);
+  t.tl = (__half*)take(Cc * q * ld * 2);
+  t.nodes_s = (Pt4<float>*)take(Cc * q * sizeof(Pt4<float>));
+  t.s = (float*)take(Cr * q * ld * nch * 4);
+  t.ynear = (float*)take(plan.rows.n * ld * nch * 4);
+  t.yfar = (float*)take(plan.rows.n * ld * nch * 4);
+  t.cmax = (unsigned int*)take((size_t)nrhs * 4);
+  if (w) *w = t;
+  return off;
+}
+
+bool tc_supported(int type, int nrhs) {
+  return type >= FMCA_KERNEL_EXPONENTIAL && type <= FMCA_KERNEL_MATERN92 && nrhs > 16;
+}
+
+template <int KT, int MT>
+cudaError_t launch_tc_t(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
+                        const __half* vh, const __half* vl, float* out, int rcount,
+                        const KParams<float>& kp, int* errf, cudaStream_t st) {
+  auto kern = ksum_tc_kernel<KT, MT>;
+  const size_t smem = 128 + (size_t)kTcStages * kTcTile * (16 + 4 * kTcRhs);
+  ensure_smem(kern, smem);
+  kern<<<gl.ngroups, 128, smem, st>>>(gl.groups, gl.ivl, tgt, src, vh, vl, out, kTcRhs,
+                                       rcount, kp, errf);
+  return cudaGetLastError();
+}
+
+// groups hold at most kTcGroupCap = 4 warps x 2 m-tiles x 16 targets
+template <int KT>
+cudaError_t launch_tc_mt(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
+                         const __half* vh, const __half* vl, float* out, int rcount,
+                         const KParams<float>& kp, int* errf, cudaStream_t st) {
+  return launch_tc_t<KT, 2>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+}
+
+cudaError_t launch_tc(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
+                      const __half* vh, const __half* vl, float* out, int rcount,
+                      const KParams<float>& kp, int* errf, cudaStream_t st) {
+  if (gl.ngroups == 0) return cudaSuccess;
+  switch (kp.type) {
+    case 0:
+      return launch_tc_mt<0>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+    case 1:
+      return launch_tc_mt<1>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+    case 2:
+      return launch_tc_mt<2>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+    case 3:
+      return launch_tc_mt<3>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+    default:
+      return launch_tc_mt<-1>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+  }
+}
+
+int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
+              int dtype, int order, int nrhs, const void* x, int64_t sxi, int64_t sxr,
+              void* y, int64_t syi, int64_t syr, void* ws, size_t wsb, cudaStream_t st,
+              std::string* err) {
+  constexpr int RB = kTcRhs;
+  const int ld = kTcRhs;
+  const size_t need = tc_ws_layout(plan, nrhs, nullptr, nullptr);
+  FMCA_TRY(acquire_ws(dp, need, &ws, wsb, st, err));
+  TcWorkspace w;
+  tc_ws_layout(plan, nrhs, ws, &w);
+  dp->nevents = 0;
+  dp->launches = 0;
+  dp->mark(-1, st);
+  const KParams<float> kp = make_kparams<float>(k);
+  const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
+  const uint32_t* pr = order == FMCA_ORDER_NATURAL ? dp->perm_r : nullptr;
+  const int nthr = 256;
+  auto blocks = [&](int64_t total) {
+    int64_t b = (total + nthr - 1) / nthr;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+  };
+  const int64_t nc = plan.cols.n, nr = plan.rows.n;
+  const int nch = (nrhs + RB - 1) / RB;
+  FMCA_CK(cudaMemsetAsync(w.cmax, 0, sizeof(unsigned int) * nrhs, st));
+  if (dtype == FMCA_DTYPE_F64) {
+    colmax_kernel<double><<<blocks(nc * nrhs), nthr, 0, st>>>(
+        nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax);
+    gather_split_kernel<double><<<blocks(nc * RB * nch), nthr, 0, st>>>(
+        pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
+  } else {
+    colmax_kernel<float><<<blocks(nc * nrhs), nthr, 0, st>>>(
+        nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax);
+    gather_split_kernel<float><<<blocks(nc * RB * nch), nthr, 0, st>>>(
+        pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
+  }
+  FMCA_CK(cudaGetLastError());
+  dp->launches += 2;
+  dp->mark(FMCA_STAGE_GATHER, st);
+  const size_t q = plan.interp.q;
+  const size_t midx_bytes = q * 3 * sizeof(int);
+  const int Cc = plan.cols.nclusters(), Cr = plan.rows.nclusters();
+  for (int ch = 0; ch < nch; ++ch) {
+    const int rcount = std::min(RB, nrhs - ch * RB);
+    float* xc = w.xc + (size_t)ch * nc * ld;
+    const __half* xh = w.xh + (size_t)ch * nc * ld;
+    const __half* xl = w.xl + (size_t)ch * nc * ld;
+    float* t = w.t + (size_t)ch * Cc * q * ld;
+    float* s = w.s + (size_t)ch * Cr * q * ld;
+    float* ynear = w.ynear + (size_t)ch * nr * ld;
+    float* yfar = w.yfar + (size_t)ch * nr * ld;
+    {
+      auto kern = leafmom_kernel<float, RB>;
+      const size_t smem = (64 * 24 + 64 * RB) * sizeof(float) + midx_bytes;
+      ensure_smem(kern, smem);
+      if (dp->nleaves_c) {
+        kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
+                                               S.bbmin_c, S.bbext_c, S.pts_c, xc, ld, 0,
+                                               rcount, dp->midx, S.ip, t);
+        ++dp->launches;
+      }
+      dp->mark(FMCA_STAGE_LEAFMOM, st);
+    }
+    {
+      auto kern = transfer_kernel<float, RB, true>;
+      const size_t smem = (192 + 64 * RB) * sizeof(float) + midx_bytes;
+      ensure_smem(kern, smem);
+      for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
+        const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
+        if (nb) {
+          kern<<<nb, 128, smem, st>>>(dp->m2m_list + dp->m2m_ptr[l], dp->son0_c, dp->nsons_c,
+                                      nullptr, S.E_c, dp->midx, S.ip, t, ld, 0, rcount);
+          ++dp->launches;
+        }
+      }
+      dp->mark(FMCA_STAGE_M2M, st);
+    }
+    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, w.th, w.tl,
+                                       w.nodes_s);
+    ++dp->launches;
+    FMCA_CK(launch_tc(dp->far_tc, S.nodes_r, w.nodes_s, w.th, w.tl, s, rcount, kp,
+                      dp->err_flag, st));
+    dp->launches += dp->far_tc.ngroups ? 1 : 0;
+    dp->mark(FMCA_STAGE_FAR, st);
+    {
+      auto kern = transfer_kernel<float, RB, false>;
+      const size_t smem = (192 + 64 * RB) * sizeof(float) + midx_bytes;
+      ensure_smem(kern, smem);
+      for (int l = 1; l < plan.rows.nlevels(); ++l) {
+        const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
+        if (nb) {
+          kern<<<nb, 128, smem, st>>>(dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
+                                      dp->parent_r, S.E_r, dp->midx, S.ip, s, ld, 0, rcount);
+          ++dp->launches;
+        }
+      }
+      dp->mark(FMCA_STAGE_L2L, st);
+    }
+    {
+      auto kern = leafgather_kernel<float, RB>;
+      const size_t smem = (128 * 24 + 64 * RB) * sizeof(float) + midx_bytes;
+      ensure_smem(kern, smem);
+      if (dp->nleaves_r) {
+        kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
+                                               S.bbmin_r, S.bbext_r, S.pts_r, s, ld, 0,
+                                               rcount, dp->midx, S.ip, yfar);
+        ++dp->launches;
+      }
+      dp->mark(FMCA_STAGE_LEAFGATHER, st);
+    }
+    FMCA_CK(launch_tc(dp->near_tc, S.pts_r, S.pts_c, xh, xl, ynear, rcount, kp,
+                      dp->err_flag, st));
+    dp->launches += dp->near_tc.ngroups ? 1 : 0;
+    dp->mark(FMCA_STAGE_NEAR, st);
+  }
+  if (dtype == FMCA_DTYPE_F64)
+    scatter_scaled_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
+        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, k.sigma2, static_cast<double*>(y), syi, syr);
+  else
+    scatter_scaled_kernel<float><<<blocks(nr * nrhs), nthr, 0, st>>>(
+        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, k.sigma2, static_cast<float*>(y), syi, syr);
+  FMCA_CK(cudaGetLastError());
+  ++dp->launches;
+  dp->mark(FMCA_STAGE_SCATTER, st);
   return FMCA_OK;
 }
 
@@ -627,14 +886,17 @@ void destroy(DevPlan* dp) {
   cudaGetDevice(&cur);
   if (dp->device >= 0 && dp->device != cur) cudaSetDevice(dp->device);
   for (void* p : dp->allocs) cudaFree(p);
+  for (cudaEvent_t e : dp->events) cudaEventDestroy(e);
   if (dp->ws) cudaFree(dp->ws);
   if (dp->device >= 0 && dp->device != cur && cur >= 0) cudaSetDevice(cur);
   delete dp;
 }
 
 size_t workspace_bytes(const Plan& plan, int precision, int nrhs) {
-  return precision == FMCA_PREC_FP64 ? ws_layout<double>(plan, nrhs, nullptr, nullptr)
-                                     : ws_layout<float>(plan, nrhs, nullptr, nullptr);
+  if (precision == FMCA_PREC_FP64) return ws_layout<double>(plan, nrhs, nullptr, nullptr);
+  const size_t f = ws_layout<float>(plan, nrhs, nullptr, nullptr);
+  if (precision == FMCA_PREC_FP32) return f;
+  return std::max(f, tc_ws_layout(plan, nrhs, nullptr, nullptr));
 }
 
 int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
@@ -645,6 +907,9 @@ int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
   if (precision == FMCA_PREC_FP64)
     return matvec_t<double>(plan, dp, dp->d, k, dtype, order, nrhs, x, sxi, sxr, y,
                             syi, syr, ws, ws_bytes, st, err);
+  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs))
+    return matvec_tc(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi, syr, ws,
+                     ws_bytes, st, err);
   return matvec_t<float>(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi,
                          syr, ws, ws_bytes, st, err);
 }
@@ -681,6 +946,24 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
 }
 
 int device_of(const DevPlan* dp) { return dp ? dp->device : -1; }
+
+void set_profiling(DevPlan* dp, bool on) {
+  if (dp) dp->profile = on;
+}
+
+int profile(DevPlan* dp, double* stage_ms, int64_t* launches, std::string* err) {
+  for (int i = 0; i < FMCA_STAGE_COUNT; ++i) stage_ms[i] = 0;
+  if (launches) *launches = dp ? dp->launches : 0;
+  if (!dp || dp->nevents < 2) return FMCA_OK;
+  FMCA_CK(cudaEventSynchronize(dp->events[dp->nevents - 1]));
+  for (int k = 1; k < dp->nevents; ++k) {
+    float ms = 0;
+    FMCA_CK(cudaEventElapsedTime(&ms, dp->events[k - 1], dp->events[k]));
+    const int sid = dp->event_stage[k];
+    if (sid >= 0 && sid < FMCA_STAGE_COUNT) stage_ms[sid] += ms;
+  }
+  return FMCA_OK;
+}
 
 }  // namespace gpu
 }  // namespace fmca

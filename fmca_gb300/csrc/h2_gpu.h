@@ -32,6 +32,8 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
                const double* PC, int64_t nc, double* out, std::string* err);
 // device the plan lives on (-1 if not uploaded)
 int device_of(const DevPlan* dev);
+void set_profiling(DevPlan* dev, bool on);
+int profile(DevPlan* dev, double* stage_ms, int64_t* launches, std::string* err);
 
 }  // namespace gpu
 }  // namespace fmca

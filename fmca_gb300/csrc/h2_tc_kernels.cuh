@@ -1,0 +1,361 @@
+// Tensor-core kernel sums of the mixed-precision matvec (sm_103a).
+//
+// ksum_tc computes out[t][0..32) = sum_s a(t, s) * v[s][0..32) for one
+// group of targets per CTA, like ksum_kernel, with the contraction on the
+// tensor cores:
+//   * a(t, s) = k(|tgt_t - src_s|) * src_s.w is evaluated in FP32 by the
+//     warp that owns the targets, directly in the register layout of the
+//     A operand of mma.m16n8k16 (no shared-memory round trip), and split
+//     into two FP16 halves a = a_hi + a_lo (22 significant bits);
+//   * the source values arrive pre-split (v = v_hi + v_lo, FP16) in shared
+//     memory through cp.async.bulk copies completed on mbarriers, and are
+//     read as B fragments with ldmatrix.trans;
+//   * three products a_hi v_hi + a_hi v_lo + a_lo v_hi accumulate in FP32.
+//     The tensor cores round the accumulation toward zero, so a long sum
+//     drifts toward zero; the MMA accumulators are therefore emptied into
+//     separate FP32 registers (round-to-nearest adds) after every tile of
+//     kTcTile sources and restart from zero.
+// Values are kept inside the FP16 range by exact power-of-two scalings:
+// every right-hand side is divided by 2^ceil(log2 max|x_r|) before the
+// product (and multiplied back at the end), and the interpolated moments of
+// each column cluster by 2^e_sigma, which is folded into a through src.w.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "h2_gpu_kernels.cuh"
+
+namespace fmca {
+namespace gpu {
+
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, "
+      "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t& r0, uint32_t& r1, uint32_t& r2,
+                                              uint32_t& r3, const void* p) {
+  asm volatile(
+      "ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+      : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+      : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) {
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// (a, b) -> hi = fp16(a, b), lo = fp16(a - hi, b - hi)
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 hf = __half22float2(h);
+  hi = h2_bits(h);
+  lo = h2_bits(__floats2half2_rn(a - hf.x, b - hf.y));
+}
+
+constexpr int kTcTile = 64;   // sources per pipeline stage
+constexpr int kTcStages = 3;
+constexpr int kTcRhs = 32;    // right-hand sides per product (4 n-tiles of 8)
+
+// Shared memory: [bars | counts] (128 B) | STAGES x TS source points |
+// STAGES x TS x 32 FP16 v_hi | STAGES x TS x 32 FP16 v_lo
+template <int KT, int MT>
+__global__ void __launch_bounds__(128)
+    ksum_tc_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
+                   const Pt4<float>* __restrict__ tgt, const Pt4<float>* __restrict__ src,
+                   const __half* __restrict__ vhi, const __half* __restrict__ vlo,
+                   float* __restrict__ out, int ldo, int rcount, KParams<float> kp,
+                   int* err) {
+  constexpr int TS = kTcTile, STAGES = kTcStages;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+  int* scnt = reinterpret_cast<int*>(smem_raw + 8 * STAGES);
+  Pt4<float>* spts = reinterpret_cast<Pt4<float>*>(smem_raw + 128);
+  __half* shi = reinterpret_cast<__half*>(smem_raw + 128 + STAGES * TS * 16);
+  __half* slo = shi + STAGES * TS * kTcRhs;
+
+  const KGroup g = groups[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gid = lane >> 2, tig = lane & 3;
+
+  // zero the value buffers once so rows past a partial tile hold finite data;
+  // the proxy fence orders these generic writes before the bulk copies
+  {
+    uint4* z = reinterpret_cast<uint4*>(shi);
+    const int n16 = STAGES * TS * kTcRhs * 2 * 2 / 16;
+    for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+
+  // targets of this thread: rows gid and gid + 8 of each of the warp's m-tiles
+  float tx[MT][2], ty[MT][2], tz[MT][2];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t i = (uint32_t)(warp * MT * 16 + m * 16 + gid + 8 * h);
+      if (i < g.tcount) {
+        const Pt4<float> p = tgt[g.tbegin + i];
+        tx[m][h] = p.x;
+        ty[m][h] = p.y;
+        tz[m][h] = p.z;
+      } else {
+        tx[m][h] = ty[m][h] = tz[m][h] = 0.f;
+      }
+    }
+  float acc[MT][4][4], tot[MT][4][4];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[m][n][c] = tot[m][n][c] = 0.f;
+
+  int ntiles = 0;
+  for (int i = g.ivl_begin; i < g.ivl_end; ++i)
+    ntiles += (int)((ivl[2 * i + 1] - ivl[2 * i] + TS - 1) / TS);
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int pi = g.ivl_begin;
+  uint32_t poff = 0;
+  int issued = 0;
+  auto issue = [&](int stage) {
+    const uint32_t b = ivl[2 * pi], e = ivl[2 * pi + 1];
+    const uint32_t s0 = b + poff;
+    const uint32_t cnt = (e - s0) < (uint32_t)TS ? (e - s0) : (uint32_t)TS;
+    scnt[stage] = (int)cnt;
+    const uint32_t bp = cnt * 16u, bv = cnt * (uint32_t)kTcRhs * 2u;
+    mbar_expect_tx(&bars[stage], bp + 2 * bv);
+    bulk_g2s(spts + stage * TS, src + s0, bp, &bars[stage]);
+    bulk_g2s(shi + (size_t)stage * TS * kTcRhs, vhi + (size_t)s0 * kTcRhs, bv, &bars[stage]);
+    bulk_g2s(slo + (size_t)stage * TS * kTcRhs, vlo + (size_t)s0 * kTcRhs, bv, &bars[stage]);
+    poff += cnt;
+    if (b + poff >= e) {
+      ++pi;
+      poff = 0;
+    }
+    ++issued;
+  };
+  if (tid == 0)
+    for (int s = 0; s < STAGES && s < ntiles; ++s) issue(s);
+
+  // ldmatrix row / column of this lane inside a 16 x 16 block
+  const int lrow = (lane & 7) + ((lane >> 3) & 1) * 8;
+  const int lcol = (lane >> 4) * 8;
+
+  bool aborted = false;
+  for (int k = 0; k < ntiles; ++k) {
+    const int stage = k % STAGES;
+    const uint32_t parity = (uint32_t)((k / STAGES) & 1);
+    const bool ok = mbar_wait_bounded(&bars[stage], parity, kWaitLimitNs);
+    if (ok) {
+      const int cnt = scnt[stage];
+      const Pt4<float>* P = spts + stage * TS;
+      const __half* H = shi + (size_t)stage * TS * kTcRhs;
+      const __half* L = slo + (size_t)stage * TS * kTcRhs;
+      for (int ks = 0; ks < cnt; ks += 16) {
+        // B fragments of the 4 n-tiles, hi and lo
+        uint32_t bh[4][2], bl[4][2];
+        const __half* hrow = H + (size_t)(ks + lrow) * kTcRhs + lcol;
+        const __half* lrowp = L + (size_t)(ks + lrow) * kTcRhs + lcol;
+        ldsm_x4_trans(bh[0][0], bh[0][1], bh[1][0], bh[1][1], hrow);
+        ldsm_x4_trans(bh[2][0], bh[2][1], bh[3][0], bh[3][1], hrow + 16);
+        ldsm_x4_trans(bl[0][0], bl[0][1], bl[1][0], bl[1][1], lrowp);
+        ldsm_x4_trans(bl[2][0], bl[2][1], bl[3][0], bl[3][1], lrowp + 16);
+        // this thread's source columns: 2 tig, 2 tig + 1, 2 tig + 8, 2 tig + 9
+        Pt4<float> sp[4];
+        bool sv[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int j = ks + 2 * tig + (c & 1) + (c >> 1) * 8;
+          sv[c] = j < cnt;
+          sp[c] = P[j];
+        }
+#pragma unroll
+        for (int m = 0; m < MT; ++m) {
+          float av[2][4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const float dx = tx[m][h] - sp[c].x, dy = ty[m][h] - sp[c].y,
+                          dz = tz[m][h] - sp[c].z;
+              const float kv = keval<float, KT>(dx * dx + dy * dy + dz * dz, kp) * sp[c].w;
+              av[h][c] = sv[c] ? kv : 0.f;
+            }
+          uint32_t ahi[4], alo[4];
+          split2(av[0][0], av[0][1], ahi[0], alo[0]);
+          split2(av[1][0], av[1][1], ahi[1], alo[1]);
+          split2(av[0][2], av[0][3], ahi[2], alo[2]);
+          split2(av[1][2], av[1][3], ahi[3], alo[3]);
+#pragma unroll
+          for (int n = 0; n < 4; ++n) {
+            mma16816(acc[m][n], ahi, bh[n][0], bh[n][1]);
+            mma16816(acc[m][n], ahi, bl[n][0], bl[n][1]);
+            mma16816(acc[m][n], alo, bh[n][0], bh[n][1]);
+          }
+        }
+      }
+      // empty the tensor-core accumulators into the FP32 totals
+#pragma unroll
+      for (int m = 0; m < MT; ++m)
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            tot[m][n][c] += acc[m][n][c];
+            acc[m][n][c] = 0.f;
+          }
+    }
+    if (__syncthreads_or(ok ? 0 : 1)) {
+      aborted = true;
+      break;
+    }
+    if (tid == 0 && k + STAGES < ntiles) issue(stage);
+  }
+  if (aborted) {
+    if (tid == 0) {
+      atomicExch(err, 1);
+      for (int k = 0; k < issued; ++k)
+        mbar_wait_bounded(&bars[k % STAGES], (uint32_t)((k / STAGES) & 1), kWaitLimitNs / 4);
+    }
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t i = (uint32_t)(warp * MT * 16 + m * 16 + gid + 8 * h);
+      if (i >= g.tcount) continue;
+      float* o = out + (size_t)(g.tbegin + i) * ldo;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const int c = n * 8 + 2 * tig;
+        if (c < rcount) o[c] = tot[m][n][2 * h];
+        if (c + 1 < rcount) o[c + 1] = tot[m][n][2 * h + 1];
+      }
+    }
+}
+
+// per-column max |x| as float bits (positive floats order like integers)
+template <typename TI>
+__global__ void colmax_kernel(int64_t n, int R, const TI* __restrict__ x, int64_t sxi,
+                              int64_t sxr, unsigned int* __restrict__ cmax) {
+  const int64_t total = n * (int64_t)R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e % R);
+    const float v = fabsf((float)x[i * sxi + (int64_t)r * sxr]);
+    if (v > 0.f) atomicMax(&cmax[r], __float_as_uint(v));
+  }
+}
+
+// power-of-two exponent that maps max |v| into (1/2, 1]; 0 for max = 0
+__device__ __forceinline__ int scale_exp(float m) {
+  if (!(m > 0.f) || !isfinite(m)) return 0;
+  int e;
+  frexpf(m, &e);  // m = f * 2^e, f in [0.5, 1)
+  return e;
+}
+
+// gather for the mixed path: x' = x * 2^-e_r (cluster order, chunk-major
+// [chunk][n][32]) in FP32 and split into FP16 hi / lo parts
+template <typename TI>
+__global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,
+                                   const TI* __restrict__ x, int64_t sxi, int64_t sxr,
+                                   const unsigned int* __restrict__ cmax,
+                                   float* __restrict__ xc, __half* __restrict__ xh,
+                                   __half* __restrict__ xl) {
+  const int nchunks = (R + kTcRhs - 1) / kTcRhs;
+  const int64_t per = n * (int64_t)kTcRhs;
+  const int64_t total = per * nchunks;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ch = e / per, rem = e % per;
+    const int64_t i = rem / kTcRhs;
+    const int r = (int)ch * kTcRhs + (int)(rem % kTcRhs);
+    float v = 0.f;
+    if (r < R) {
+      const int64_t src = perm ? (int64_t)perm[i] : i;
+      const int ex = scale_exp(__uint_as_float(cmax[r]));
+      v = ldexpf((float)x[src * sxi + (int64_t)r * sxr], -ex);
+    }
+    xc[e] = v;
+    const __half h = __float2half_rn(v);
+    xh[e] = h;
+    xl[e] = __float2half_rn(v - __half2float(h));
+  }
+}
+
+// per column cluster: e = exponent of max |t|, t'' = t * 2^-e split into
+// FP16 hi / lo, and the cluster's node coordinates with w = 2^e
+__global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict__ t,
+                              const Pt4<float>* __restrict__ nodes,
+                              __half* __restrict__ th, __half* __restrict__ tl,
+                              Pt4<float>* __restrict__ nodes_s) {
+  const int c = blockIdx.x;
+  if (c >= C) return;
+  __shared__ float red[32];
+  const size_t base = (size_t)c * q * kTcRhs;
+  float m = 0.f;
+  for (int e = threadIdx.x; e < q * kTcRhs; e += blockDim.x)
+    if ((e % kTcRhs) < rcount) m = fmaxf(m, fabsf(t[base + e]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  const float mx = red[0];
+  const int ex = scale_exp(mx);
+  const float w = mx > 0.f ? ldexpf(1.f, ex) : 0.f;
+  for (int e = threadIdx.x; e < q * kTcRhs; e += blockDim.x) {
+    const float v = (e % kTcRhs) < rcount ? ldexpf(t[base + e], -ex) : 0.f;
+    const __half h = __float2half_rn(v);
+    th[base + e] = h;
+    tl[base + e] = __float2half_rn(v - __half2float(h));
+  }
+  for (int k = threadIdx.x; k < q; k += blockDim.x) {
+    Pt4<float> p = nodes[(size_t)c * q + k];
+    p.w = w;
+    nodes_s[(size_t)c * q + k] = p;
+  }
+}
+
+// y (natural order) = sigma2 * 2^e_r * (ynear + yfar), combined in FP64
+template <typename TO>
+__global__ void scatter_scaled_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,
+                                      const float* __restrict__ ynear,
+                                      const float* __restrict__ yfar,
+                                      const unsigned int* __restrict__ cmax, double sigma2,
+                                      TO* __restrict__ y, int64_t syi, int64_t syr) {
+  const int64_t total = n * (int64_t)R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e % R);
+    const int64_t k = ((int64_t)(r / kTcRhs) * n + i) * kTcRhs + r % kTcRhs;
+    const int64_t dst = perm ? (int64_t)perm[i] : i;
+    const double v = (double)ynear[k] + (double)yfar[k];
+    const int ex = scale_exp(__uint_as_float(cmax[r]));
+    y[dst * syi + (int64_t)r * syr] = (TO)(ldexp(sigma2 * v, ex));
+  }
+}
+
+}  // namespace gpu
+}  // namespace fmca

@@ -24,7 +24,7 @@ import numpy as np
 from . import _lib
 from ._lib import KernelDesc, check
 
-_PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+_PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, "fp32": _lib.PREC_FP32}
 
 
 def _dptr(a: np.ndarray):
@@ -82,7 +82,7 @@ class H2Matrix:
         self.p = int(p)
         self.eta = float(eta)
         if precision not in _PREC:
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
         self.precision = precision
         Pr = np.asfortranarray(Pr, dtype=np.float64)
         if Pr.ndim != 2:
@@ -169,8 +169,13 @@ class H2Matrix:
                                            c.ctypes.data_as(C.POINTER(C.c_int32))))
         return r, c
 
-    def action(self, rhs, precision: Optional[str] = None):
-        """y = K_H2 rhs in natural order (pyH2Matrix::action)."""
+    def action(self, rhs, precision: Optional[str] = None, out=None):
+        """y = K_H2 rhs in natural order (pyH2Matrix::action).
+
+        numpy input: FP64 host buffers through fmca_matvec_host.  torch input:
+        CUDA tensors stay on the device; CPU tensors are copied to the current
+        device and the result copied back, into ``out`` when given (a pinned
+        ``out`` and a pinned ``rhs`` make both copies asynchronous DMA)."""
         prec = _PREC[precision or self.precision]
         try:
             import torch
@@ -178,10 +183,14 @@ class H2Matrix:
             torch = None
         if torch is not None and isinstance(rhs, torch.Tensor):
             if rhs.is_cuda:
-                return self.matvec(rhs, precision=precision)
+                return self.matvec(rhs, out, precision=precision)
             dev = torch.device("cuda", torch.cuda.current_device())
             y = self.matvec(rhs.to(dev, non_blocking=True), precision=precision)
-            return y.to("cpu")
+            if out is None:
+                return y.to("cpu")
+            out.copy_(y, non_blocking=True)
+            torch.cuda.current_stream(dev).synchronize()
+            return out
         x = np.asfortranarray(rhs, dtype=np.float64)
         vec = x.ndim == 1
         if vec:
@@ -243,6 +252,17 @@ class H2Matrix:
                 C.c_void_p(workspace.data_ptr()), workspace.numel(),
                 C.c_void_p(stream.cuda_stream)))
         return y
+
+    def set_profiling(self, enable: bool = True) -> None:
+        """CUDA-event timing of the stages of the following matvecs."""
+        check(_lib.load().fmca_plan_set_profiling(self._h, 1 if enable else 0))
+
+    def profile(self):
+        """(stage -> ms, kernel launches) of the last matvec (waits for it)."""
+        ms = np.zeros(len(_lib.STAGES), dtype=np.float64)
+        n = C.c_int64(0)
+        check(_lib.load().fmca_plan_profile(self._h, _dptr(ms), C.byref(n)))
+        return dict(zip(_lib.STAGES, ms.tolist())), int(n.value)
 
     def check_device_error(self) -> None:
         check(_lib.load().fmca_plan_check_device_error(self._h))

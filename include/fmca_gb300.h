@@ -73,9 +73,16 @@ enum {
 enum {
   /* every stage in FP64 on CUDA cores: the plain FP64 GPU H2 product */
   FMCA_PREC_FP64 = 0,
-  /* FP32 near field and FP32 coupling on CUDA cores, FP32 accumulation,
-     final near + far combination in FP64 */
-  FMCA_PREC_MIXED = 1
+  /* kernel values in FP32; near-field and far-field contractions on the
+     tensor cores with FP16 hi/lo split operands (three products, about 22
+     significant bits) and FP32 accumulation; transfers, leaf moments and the
+     leaf gather in FP32; final near + far combination in FP64.  Kernels that
+     are not bounded by 1 (MULTIQUADRIC, INVMULTIQUADRIC, BIHARMONIC3D,
+     TRIHARMONIC3D) and fewer than 17 right-hand sides use FMCA_PREC_FP32. */
+  FMCA_PREC_MIXED = 1,
+  /* every stage in FP32 on CUDA cores with FP32 accumulation, final
+     combination in FP64 */
+  FMCA_PREC_FP32 = 2
 };
 
 enum { FMCA_DTYPE_F64 = 0, FMCA_DTYPE_F32 = 1 };
@@ -174,6 +181,30 @@ fmca_status fmca_matvec_host(fmca_plan* plan, const fmca_kernel_desc* kernel,
 /* Returns FMCA_ERR_TIMEOUT if a kernel of this plan gave up a bounded wait
    since the last call, and clears the flag.  Synchronises the device. */
 fmca_status fmca_plan_check_device_error(fmca_plan* plan);
+
+/* Stages of one matvec, indices of fmca_plan_profile's output. */
+enum {
+  FMCA_STAGE_GATHER = 0,     /* natural -> cluster order */
+  FMCA_STAGE_LEAFMOM = 1,    /* leaf moments (upward pass, leaves) */
+  FMCA_STAGE_M2M = 2,        /* transfers, upward pass */
+  FMCA_STAGE_FAR = 3,        /* far-field coupling */
+  FMCA_STAGE_L2L = 4,        /* transfers, downward pass */
+  FMCA_STAGE_LEAFGATHER = 5, /* leaf gather (downward pass, leaves) */
+  FMCA_STAGE_NEAR = 6,       /* near field */
+  FMCA_STAGE_SCATTER = 7,    /* combination and cluster -> natural order */
+  FMCA_STAGE_COUNT = 8
+};
+
+/* Enables CUDA-event timing of the stages of the following matvecs on this
+   plan (adds one event record per stage; off by default).  No reference
+   counterpart: the reference times phases with Tictoc
+   (FMCA/src/util/Tictoc.h:22-42) around whole calls only. */
+fmca_status fmca_plan_set_profiling(fmca_plan* plan, int enable);
+/* Stage times in ms of the last matvec on this plan (waits for its events)
+   and the number of kernels it launched.  stage_ms has FMCA_STAGE_COUNT
+   entries; either pointer may be NULL. */
+fmca_status fmca_plan_profile(fmca_plan* plan, double* stage_ms,
+                              int64_t* launches);
 
 /* Dense kernel matrix K(PR, PC) (n_r x n_c, column-major FP64 host buffers),
    evaluated on the GPU in FP64; like CovarianceKernel::eval. */

@@ -57,9 +57,10 @@ class OraclePlan:
         self._h = lib.oracle_plan_create(_d(self.Pr), self.dim, self.Pr.shape[1],
                                          None if self.same else _d(self.Pc), self.Pc.shape[1],
                                          int(p), float(eta), int(min_leaf))
-        cnt = (C.c_int64 * 5)()
+        cnt = (C.c_int64 * 6)()
         lib.oracle_counts(self._h, cnt)
-        self.row_clusters, self.col_clusters, self.n_far, self.n_near, self.q = list(cnt)
+        (self.row_clusters, self.col_clusters, self.n_far, self.n_near, self.q,
+         self.near_pairs) = list(cnt)
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -506,16 +506,21 @@ void* oracle_plan_create(const double* Pr, int dim, int64_t nr, const double* Pc
 
 void oracle_plan_destroy(void* h) { delete static_cast<OPlan*>(h); }
 
-// counts: [row clusters, col clusters, far blocks, dense blocks, q]
+// counts: [row clusters, col clusters, far blocks, dense blocks, q,
+//          dense point pairs]
 void oracle_counts(void* h, int64_t* out) {
   OPlan* P = static_cast<OPlan*>(h);
-  int64_t nf = 0, nd = 0;
-  for (auto& b : P->blocks) (b.low_rank ? nf : nd)++;
+  int64_t nf = 0, nd = 0, pairs = 0;
+  for (auto& b : P->blocks) {
+    (b.low_rank ? nf : nd)++;
+    if (!b.low_rank) pairs += (int64_t)b.row->size * (int64_t)b.col->size;
+  }
   out[0] = (int64_t)P->rt.by_id.size();
   out[1] = (int64_t)P->ct.by_id.size();
   out[2] = nf;
   out[3] = nd;
   out[4] = P->ip.q();
+  out[5] = pairs;
 }
 
 void oracle_perm(void* h, int side, uint32_t* out) {

@@ -85,5 +85,7 @@ def test_workspace_size_grows_with_rhs():
     P = np.random.default_rng(0).random((3, 2000))
     H = H2Matrix(CovarianceKernel("EXPONENTIAL"), P, P, 3, 0.8)
     a, b = H.workspace_bytes(1, "mixed"), H.workspace_bytes(32, "mixed")
-    assert 0 < a < b
-    assert H.workspace_bytes(32, "fp64") > b
+    assert 0 < a <= b < H.workspace_bytes(64, "mixed")
+    assert H.workspace_bytes(1, "fp32") < H.workspace_bytes(32, "fp32")
+    assert H.workspace_bytes(32, "fp64") > H.workspace_bytes(32, "fp32")
+    assert b >= H.workspace_bytes(32, "fp32")

@@ -1,8 +1,11 @@
 """GPU matvec against the FP64 oracle (same seeded inputs), through the C ABI.
 
-Tolerances: FMCA_PREC_FP64 must match the oracle to 1e-12 relative (2-norm
-over all right-hand sides); FMCA_PREC_MIXED (FP32 arithmetic, FP32
-accumulation, FP64 final combination) to 1e-5 relative."""
+Tolerances (relative 2-norm over all right-hand sides): FMCA_PREC_FP64 must
+match the oracle to 1e-12; FMCA_PREC_FP32 (FP32 CUDA cores, FP32
+accumulation) and FMCA_PREC_MIXED (FP32 kernel values, tensor-core
+contractions on FP16 hi/lo splits, FP32 accumulation) to 1e-5.  The mixed
+mode runs on the tensor cores for the bounded kernels with more than 16
+right-hand sides and falls back to FP32 otherwise."""
 from __future__ import annotations
 
 import numpy as np
@@ -14,7 +17,8 @@ from fmca_gb300 import CovarianceKernel, H2Matrix
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "mixed": 1e-5}
+TOL = {"fp64": 1e-12, "fp32": 1e-5, "mixed": 1e-5}
+PRECS = ["fp64", "fp32", "mixed"]
 KNAMES = ["EXPONENTIAL", "MATERN32", "MATERN52", "GAUSSIAN", "MATERN72", "MATERN92",
           "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D", "TRIHARMONIC3D"]
 
@@ -29,7 +33,7 @@ def c1():
     return P, x, y_ref
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECS)
 def test_c1_against_oracle(cuda_device, c1, precision):
     P, x, y_ref = c1
     H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, 3, 0.8, min_leaf=64,
@@ -52,10 +56,11 @@ def test_c1_against_dense(cuda_device, c1):
 
 
 @pytest.mark.parametrize("kname", KNAMES)
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECS)
 def test_all_kernels(cuda_device, kname, precision):
+    # 20 right-hand sides: the mixed mode takes the tensor-core path
     P = uniform_cloud(6000, 3, seed=11)
-    X = np.random.default_rng(11).standard_normal((6000, 3))
+    X = np.random.default_rng(11).standard_normal((6000, 20))
     kt = KNAMES.index(kname)
     O = oracle.OraclePlan(P, None, 3, 0.8, 32)
     Y_ref, _ = O.action(kt, 0.7, X, c=0.9)
@@ -64,8 +69,8 @@ def test_all_kernels(cuda_device, kname, precision):
     assert rel_err(H.action(X), Y_ref) < TOL[precision]
 
 
-@pytest.mark.parametrize("R", [1, 2, 7, 8, 9, 32, 33, 64])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("R", [1, 2, 7, 8, 9, 16, 17, 32, 33, 64, 70])
+@pytest.mark.parametrize("precision", PRECS)
 def test_rhs_counts(cuda_device, R, precision):
     P = uniform_cloud(5000, 3, seed=R)
     X = np.random.default_rng(R).standard_normal((5000, R))
@@ -75,11 +80,11 @@ def test_rhs_counts(cuda_device, R, precision):
     assert rel_err(H.action(X), Y_ref) < TOL[precision]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECS)
 def test_unsymmetric_sphere(cuda_device, precision):
     Pr = sphere_cloud(7000, seed=1)
     Pc = sphere_cloud(4000, seed=2)
-    X = np.random.default_rng(2).standard_normal((4000, 5))
+    X = np.random.default_rng(2).standard_normal((4000, 24))
     O = oracle.OraclePlan(Pr, Pc, 4, 0.8, 96)
     Y_ref, _ = O.action(2, 0.3, X, sigma2=1.7)
     H = H2Matrix(CovarianceKernel("MATERN52", 0.3, sigma2=1.7), Pr, Pc, 4, 0.8, min_leaf=96,
@@ -87,11 +92,11 @@ def test_unsymmetric_sphere(cuda_device, precision):
     assert rel_err(H.action(X), Y_ref) < TOL[precision]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECS)
 def test_two_dimensional_aniso(cuda_device, precision):
     P = uniform_cloud(20000, 2, seed=4)
     P[0] *= 4
-    x = np.random.default_rng(4).choice([-1.0, 1.0], size=(20000, 4))
+    x = np.random.default_rng(4).choice([-1.0, 1.0], size=(20000, 64))
     O = oracle.OraclePlan(P, None, 5, 0.6, 128)
     Y_ref, _ = O.action(0, 0.1, x)
     H = H2Matrix(CovarianceKernel("EXPONENTIAL", 0.1), P, P, 5, 0.6, min_leaf=128,
@@ -99,18 +104,18 @@ def test_two_dimensional_aniso(cuda_device, precision):
     assert rel_err(H.action(x), Y_ref) < TOL[precision]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", PRECS)
 def test_large_leaves_and_one_dim(cuda_device, precision):
     # leaves above the 256-target group size, and d = 1
     P = uniform_cloud(6000, 3, seed=8)
-    x = np.random.default_rng(8).standard_normal(6000)
+    x = np.random.default_rng(8).standard_normal((6000, 20))
     O = oracle.OraclePlan(P, None, 2, 0.8, 400)
     y_ref, _ = O.action(3, 0.2, x)
     H = H2Matrix(CovarianceKernel("GAUSSIAN", 0.2), P, P, 2, 0.8, min_leaf=400,
                  precision=precision)
     assert rel_err(H.action(x), y_ref) < TOL[precision]
     P1 = uniform_cloud(3000, 1, seed=8)
-    x1 = np.random.default_rng(9).standard_normal(3000)
+    x1 = np.random.default_rng(9).standard_normal((3000, 18))
     O1 = oracle.OraclePlan(P1, None, 6, 0.8, 0)
     y1_ref, _ = O1.action(1, 0.05, x1)
     H1 = H2Matrix(CovarianceKernel("MATERN32", 0.05), P1, P1, 6, 0.8, precision=precision)
@@ -123,9 +128,12 @@ def test_tiny_clouds(cuda_device):
         x = np.random.default_rng(n).standard_normal(n)
         O = oracle.OraclePlan(P, None, 2, 0.8, 0)
         y_ref, _ = O.action(0, 1.0, x)
-        for prec in ("fp64", "mixed"):
+        for prec in PRECS:
             H = H2Matrix(CovarianceKernel("EXPONENTIAL"), P, P, 2, 0.8, precision=prec)
             assert rel_err(H.action(x), y_ref) < TOL[prec]
+            X = np.tile(x[:, None], (1, 20)) * np.arange(1, 21)
+            Y_ref = y_ref[:, None] * np.arange(1, 21)
+            assert rel_err(H.action(X), Y_ref) < TOL[prec]
 
 
 def test_torch_device_api(cuda_device):
@@ -136,7 +144,7 @@ def test_torch_device_api(cuda_device):
     Y_ref, _ = O.action(1, 0.4, X)
     H = H2Matrix(CovarianceKernel("MATERN32", 0.4), P, P, 3, 0.8)
     Xt = torch.tensor(X, device=cuda_device)
-    for prec in ("fp64", "mixed"):
+    for prec in PRECS:
         y64 = H.matvec(Xt, precision=prec)                       # row-major (n, R)
         assert rel_err(y64.cpu().numpy(), Y_ref) < TOL[prec]
         Xf = Xt.t().contiguous().t()                              # column-major strides
@@ -165,3 +173,40 @@ def test_dense_kernel_eval(cuda_device):
         r = np.linalg.norm(PR[:, :, None] - PC[:, None, :], axis=0)
         ref = np.vectorize(lambda t: oracle.kernel(kt, 0.6, t, c=0.8))(r)
         assert np.allclose(K, ref, rtol=1e-13, atol=1e-300)
+
+
+@pytest.mark.parametrize("scale", [1e-30, 1e-6, 1.0, 1e8, 1e30])
+def test_mixed_scaling_of_magnitudes(cuda_device, scale):
+    # the tensor-core path scales right-hand sides and moments by powers of
+    # two; results must not depend on the magnitude of x
+    P = uniform_cloud(8000, 3, seed=31)
+    rng = np.random.default_rng(31)
+    X = rng.standard_normal((8000, 32))
+    X[:, 3] = 1.0                 # constant column: large moments
+    X[:, 5] = 0.0                 # zero column
+    X[:100, 7] *= 1e6             # a few dominant entries
+    O = oracle.OraclePlan(P, None, 4, 0.8, 0)
+    Y_ref, _ = O.action(1, 0.3, X * scale)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.3), P, P, 4, 0.8, precision="mixed")
+    Y = H.action(X * scale)
+    assert np.all(Y[:, 5] == 0.0)
+    for r in range(32):
+        if r == 5:
+            continue
+        assert rel_err(Y[:, r], Y_ref[:, r]) < 1e-5, r
+
+
+def test_mixed_uses_tensor_core_kernel_count(cuda_device):
+    # the mixed path launches the split/scale kernels (two more launches per
+    # chunk than the FP32 path)
+    P = uniform_cloud(5000, 3, seed=2)
+    X = np.random.default_rng(2).standard_normal((5000, 32))
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.3), P, P, 3, 0.8)
+    import torch
+    H.set_profiling(True)
+    H.matvec(torch.tensor(X, device=cuda_device), precision="fp32")
+    _, n32 = H.profile()
+    H.matvec(torch.tensor(X, device=cuda_device), precision="mixed")
+    stages, nmx = H.profile()
+    assert nmx == n32 + 2
+    assert stages["near"] > 0 and stages["far"] > 0
