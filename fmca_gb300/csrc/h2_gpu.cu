@@ -754,19 +754,26 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   const int64_t nc = plan.cols.n, nr = plan.rows.n;
   const int nch = (nrhs + RB - 1) / RB;
   FMCA_CK(cudaMemsetAsync(w.cmax, 0, sizeof(unsigned int) * nrhs, st));
-  if (dtype == FMCA_DTYPE_F64) {
-    colmax_kernel<double><<<blocks(nc * nrhs), nthr, 0, st>>>(
-        nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax);
+  constexpr int kColChunk = 4096;  // columns per colmax launch (16 KB shared)
+  for (int c0 = 0; c0 < nrhs; c0 += kColChunk) {
+    const int ncol = std::min(kColChunk, nrhs - c0);
+    const size_t smem = sizeof(unsigned int) * ncol;
+    if (dtype == FMCA_DTYPE_F64)
+      colmax_kernel<double><<<152 * 4, nthr, smem, st>>>(
+          nc, c0, ncol, static_cast<const double*>(x), sxi, sxr, w.cmax);
+    else
+      colmax_kernel<float><<<152 * 4, nthr, smem, st>>>(
+          nc, c0, ncol, static_cast<const float*>(x), sxi, sxr, w.cmax);
+    ++dp->launches;
+  }
+  if (dtype == FMCA_DTYPE_F64)
     gather_split_kernel<double><<<blocks(nc * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
-  } else {
-    colmax_kernel<float><<<blocks(nc * nrhs), nthr, 0, st>>>(
-        nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax);
+  else
     gather_split_kernel<float><<<blocks(nc * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
-  }
   FMCA_CK(cudaGetLastError());
-  dp->launches += 2;
+  dp->launches += 1;
   dp->mark(FMCA_STAGE_GATHER, st);
   const size_t q = plan.interp.q;
   const size_t midx_bytes = q * 3 * sizeof(int);

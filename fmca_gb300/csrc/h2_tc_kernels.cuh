@@ -59,14 +59,39 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
   lo = h2_bits(__floats2half2_rn(a - hf.x, b - hf.y));
 }
 
-constexpr int kTcTile = 64;   // sources per pipeline stage
+constexpr int kTcTile = 128;  // sources per pipeline stage
 constexpr int kTcStages = 3;
 constexpr int kTcRhs = 32;    // right-hand sides per product (4 n-tiles of 8)
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// Radial kernel of two squared distances with packed FP32x2 arithmetic;
+// the approximate square root and exponential run per element on the SFU.
+template <int KT>
+__device__ __forceinline__ float2 keval2(float2 r2, const KParams<float>& kp) {
+  if constexpr (KT == 3) {  // GAUSSIAN: exp(-r^2 / (2 l^2))
+    const float2 u = __fmul2_rn(r2, f2(kp.e2, kp.e2));
+    return f2(ex2_approx(u.x), ex2_approx(u.y));
+  } else if constexpr (KT == 0 || KT == 1 || KT == 2) {
+    const float2 r = f2(sqrt_approx(r2.x), sqrt_approx(r2.y));
+    const float2 u = __fmul2_rn(r, f2(kp.e2, kp.e2));
+    const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+    if constexpr (KT == 0) return e;  // EXPONENTIAL
+    const float2 t = __fmul2_rn(r, f2(kp.a, kp.a));
+    if constexpr (KT == 1) return __ffma2_rn(t, e, e);  // MATERN32: (1 + t) e
+    // MATERN52: (1 + t + t^2 / 3) e
+    const float2 p = __ffma2_rn(__ffma2_rn(t, f2(0.333333343f, 0.333333343f), f2(1.f, 1.f)),
+                                t, f2(1.f, 1.f));
+    return __fmul2_rn(p, e);
+  } else {
+    return f2(keval_fast(kp.type, r2.x, kp), keval_fast(kp.type, r2.y, kp));
+  }
+}
 
 // Shared memory: [bars | counts] (128 B) | STAGES x TS source points |
 // STAGES x TS x 32 FP16 v_hi | STAGES x TS x 32 FP16 v_lo
 template <int KT, int MT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 4)
     ksum_tc_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const Pt4<float>* __restrict__ src,
                    const __half* __restrict__ vhi, const __half* __restrict__ vlo,
@@ -84,30 +109,34 @@ __global__ void __launch_bounds__(128)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gid = lane >> 2, tig = lane & 3;
 
-  // zero the value buffers once so rows past a partial tile hold finite data;
-  // the proxy fence orders these generic writes before the bulk copies
+  // zero the source buffers once, so rows past a partial tile always hold
+  // finite data (masked through a zero weight); the proxy fence orders these
+  // generic writes before the bulk copies
   {
-    uint4* z = reinterpret_cast<uint4*>(shi);
-    const int n16 = STAGES * TS * kTcRhs * 2 * 2 / 16;
+    uint4* z = reinterpret_cast<uint4*>(spts);
+    const int n16 = STAGES * TS * (16 + kTcRhs * 2 * 2) / 16;
     for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
 
-  // targets of this thread: rows gid and gid + 8 of each of the warp's m-tiles
-  float tx[MT][2], ty[MT][2], tz[MT][2];
+  // targets of this thread: rows gid and gid + 8 of each of the warp's
+  // m-tiles, duplicated into both halves of a packed pair
+  float2 tx[MT][2], ty[MT][2], tz[MT][2];
 #pragma unroll
   for (int m = 0; m < MT; ++m)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const uint32_t i = (uint32_t)(warp * MT * 16 + m * 16 + gid + 8 * h);
+      float px = 0.f, py = 0.f, pz = 0.f;
       if (i < g.tcount) {
         const Pt4<float> p = tgt[g.tbegin + i];
-        tx[m][h] = p.x;
-        ty[m][h] = p.y;
-        tz[m][h] = p.z;
-      } else {
-        tx[m][h] = ty[m][h] = tz[m][h] = 0.f;
+        px = p.x;
+        py = p.y;
+        pz = p.z;
       }
+      tx[m][h] = f2(px, px);
+      ty[m][h] = f2(py, py);
+      tz[m][h] = f2(pz, pz);
     }
   float acc[MT][4][4], tot[MT][4][4];
 #pragma unroll
@@ -173,32 +202,37 @@ __global__ void __launch_bounds__(128)
         ldsm_x4_trans(bh[2][0], bh[2][1], bh[3][0], bh[3][1], hrow + 16);
         ldsm_x4_trans(bl[0][0], bl[0][1], bl[1][0], bl[1][1], lrowp);
         ldsm_x4_trans(bl[2][0], bl[2][1], bl[3][0], bl[3][1], lrowp + 16);
-        // this thread's source columns: 2 tig, 2 tig + 1, 2 tig + 8, 2 tig + 9
-        Pt4<float> sp[4];
-        bool sv[4];
+        // this thread's source columns, as two packed pairs:
+        // pair 0 = (2 tig, 2 tig + 1), pair 1 = (2 tig + 8, 2 tig + 9)
+        float2 nsx[2], nsy[2], nsz[2], wv[2];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int j = ks + 2 * tig + (c & 1) + (c >> 1) * 8;
-          sv[c] = j < cnt;
-          sp[c] = P[j];
+        for (int pp = 0; pp < 2; ++pp) {
+          const int j = ks + 2 * tig + pp * 8;
+          const Pt4<float> a = P[j], b = P[j + 1];
+          nsx[pp] = f2(-a.x, -b.x);
+          nsy[pp] = f2(-a.y, -b.y);
+          nsz[pp] = f2(-a.z, -b.z);
+          wv[pp] = f2(j < cnt ? a.w : 0.f, j + 1 < cnt ? b.w : 0.f);
         }
 #pragma unroll
         for (int m = 0; m < MT; ++m) {
-          float av[2][4];
-#pragma unroll
-          for (int h = 0; h < 2; ++h)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              const float dx = tx[m][h] - sp[c].x, dy = ty[m][h] - sp[c].y,
-                          dz = tz[m][h] - sp[c].z;
-              const float kv = keval<float, KT>(dx * dx + dy * dy + dz * dz, kp) * sp[c].w;
-              av[h][c] = sv[c] ? kv : 0.f;
-            }
           uint32_t ahi[4], alo[4];
-          split2(av[0][0], av[0][1], ahi[0], alo[0]);
-          split2(av[1][0], av[1][1], ahi[1], alo[1]);
-          split2(av[0][2], av[0][3], ahi[2], alo[2]);
-          split2(av[1][2], av[1][3], ahi[3], alo[3]);
+#pragma unroll
+          for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const float2 dx = __fadd2_rn(tx[m][h], nsx[pp]);
+              const float2 dy = __fadd2_rn(ty[m][h], nsy[pp]);
+              const float2 dz = __fadd2_rn(tz[m][h], nsz[pp]);
+              const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+              const float2 av = __fmul2_rn(keval2<KT>(r2, kp), wv[pp]);
+              // register 2 pp + h of the A fragment: row gid + 8 h, pair pp
+              const __half2 hh = __floats2half2_rn(av.x, av.y);
+              const float2 hf = __half22float2(hh);
+              const float2 lo = __ffma2_rn(hf, f2(-1.f, -1.f), av);  // av - hf, exact
+              ahi[2 * pp + h] = h2_bits(hh);
+              alo[2 * pp + h] = h2_bits(__floats2half2_rn(lo.x, lo.y));
+            }
 #pragma unroll
           for (int n = 0; n < 4; ++n) {
             mma16816(acc[m][n], ahi, bh[n][0], bh[n][1]);
@@ -248,18 +282,37 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// per-column max |x| as float bits (positive floats order like integers)
+// per-column max |x| as float bits (positive floats order like integers).
+// Columns [c0, c0 + nc) of this launch; a block reduces into shared memory
+// first (per-thread running maxima when the grid stride is a multiple of
+// nc, so every thread stays on one column) and flushes once per column.
 template <typename TI>
-__global__ void colmax_kernel(int64_t n, int R, const TI* __restrict__ x, int64_t sxi,
-                              int64_t sxr, unsigned int* __restrict__ cmax) {
-  const int64_t total = n * (int64_t)R;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / R;
-    const int r = (int)(e % R);
-    const float v = fabsf((float)x[i * sxi + (int64_t)r * sxr]);
-    if (v > 0.f) atomicMax(&cmax[r], __float_as_uint(v));
+__global__ void colmax_kernel(int64_t n, int c0, int nc, const TI* __restrict__ x,
+                              int64_t sxi, int64_t sxr, unsigned int* __restrict__ cmax) {
+  extern __shared__ unsigned int smax[];
+  for (int r = threadIdx.x; r < nc; r += blockDim.x) smax[r] = 0u;
+  __syncthreads();
+  const int64_t total = n * (int64_t)nc;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t first = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (stride % nc == 0) {
+    unsigned int m = 0u;
+    const int r = (int)(first % nc);
+    for (int64_t e = first; e < total; e += stride) {
+      const int64_t i = e / nc;
+      m = max(m, __float_as_uint(fabsf((float)x[i * sxi + (int64_t)(c0 + r) * sxr])));
+    }
+    if (first < total) atomicMax(&smax[r], m);
+  } else {
+    for (int64_t e = first; e < total; e += stride) {
+      const int64_t i = e / nc;
+      const int r = (int)(e % nc);
+      atomicMax(&smax[r], __float_as_uint(fabsf((float)x[i * sxi + (int64_t)(c0 + r) * sxr])));
+    }
   }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nc; r += blockDim.x)
+    if (smax[r]) atomicMax(&cmax[c0 + r], smax[r]);
 }
 
 // power-of-two exponent that maps max |v| into (1/2, 1]; 0 for max = 0
