@@ -8,27 +8,25 @@
 #include <string>
 
 #include "../../include/fmca_gb300.h"
+#include "c_api_internal.h"
 #include "h2_gpu.h"
 #include "h2_plan.h"
 
-struct fmca_plan {
-  fmca::Plan plan;
-  fmca::gpu::DevPlan* dev = nullptr;
-  // device staging for fmca_matvec_host
-  void* hx = nullptr;
-  void* hy = nullptr;
-  size_t hx_bytes = 0, hy_bytes = 0;
-  int64_t min_leaf = 0;
-  bool profile = false;
-};
-
 namespace {
 thread_local std::string g_last_error;
+}  // namespace
 
+namespace fmca {
+namespace capi {
 fmca_status fail(fmca_status s, const std::string& msg) {
   g_last_error = msg;
   return s;
 }
+}  // namespace capi
+}  // namespace fmca
+
+namespace {
+using fmca::capi::fail;
 fmca_status ok() { return FMCA_OK; }
 
 fmca_status check_kernel(const fmca_kernel_desc* k) {
@@ -43,16 +41,6 @@ fmca_status check_kernel(const fmca_kernel_desc* k) {
   return FMCA_OK;
 }
 
-fmca::gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
-  fmca::gpu::KernelDesc d;
-  d.type = k->type;
-  d.l = k->l;
-  d.c = k->c;
-  d.nu = k->nu;
-  d.sigma2 = k->sigma2;
-  return d;
-}
-
 fmca_status check_gpu_plan(const fmca_plan* p, int precision) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   if (precision != FMCA_PREC_FP64 && precision != FMCA_PREC_MIXED &&
@@ -64,6 +52,40 @@ fmca_status check_gpu_plan(const fmca_plan* p, int precision) {
     return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports degree <= 7");
   return FMCA_OK;
 }
+}  // namespace
+
+namespace fmca {
+namespace capi {
+gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
+  gpu::KernelDesc d;
+  d.type = k->type;
+  d.l = k->l;
+  d.c = k->c;
+  d.nu = k->nu;
+  d.sigma2 = k->sigma2;
+  return d;
+}
+
+fmca_status check_matvec_args(const fmca_plan* p, const fmca_kernel_desc* kernel,
+                              int precision, int dtype, int order, int nrhs,
+                              const void* x, const void* y) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  s = check_kernel(kernel);
+  if (s != FMCA_OK) return s;
+  if (dtype != FMCA_DTYPE_F64 && dtype != FMCA_DTYPE_F32)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown dtype");
+  if (order != FMCA_ORDER_NATURAL && order != FMCA_ORDER_CLUSTER)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown order");
+  if (nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "nrhs must be >= 1");
+  if (!x || !y) return fail(FMCA_ERR_INVALID_ARGUMENT, "x or y is NULL");
+  return FMCA_OK;
+}
+}  // namespace capi
+}  // namespace fmca
+
+namespace {
+using fmca::capi::to_desc;
 }  // namespace
 
 extern "C" {

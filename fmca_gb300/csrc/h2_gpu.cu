@@ -958,6 +958,12 @@ void set_profiling(DevPlan* dp, bool on) {
   if (dp) dp->profile = on;
 }
 
+bool resident(const DevPlan* dp, int precision) {
+  int cur = -1;
+  if (!dp || cudaGetDevice(&cur) != cudaSuccess || cur != dp->device) return false;
+  return precision == FMCA_PREC_FP64 ? dp->d.ready : dp->f.ready;
+}
+
 int profile(DevPlan* dp, double* stage_ms, int64_t* launches, std::string* err) {
   for (int i = 0; i < FMCA_STAGE_COUNT; ++i) stage_ms[i] = 0;
   if (launches) *launches = dp ? dp->launches : 0;

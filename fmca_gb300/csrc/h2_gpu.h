@@ -33,6 +33,9 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
 // device the plan lives on (-1 if not uploaded)
 int device_of(const DevPlan* dev);
 void set_profiling(DevPlan* dev, bool on);
+// true if the plan's device data for this precision lives on the current
+// device (so a matvec needs no further device allocation besides workspace)
+bool resident(const DevPlan* dev, int precision);
 int profile(DevPlan* dev, double* stage_ms, int64_t* launches, std::string* err);
 
 }  // namespace gpu

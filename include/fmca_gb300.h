@@ -172,6 +172,32 @@ fmca_status fmca_matvec(fmca_plan* plan, const fmca_kernel_desc* kernel,
                         void* y, int64_t y_stride_i, int64_t y_stride_r,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same product as fmca_matvec, for callers that cannot allocate device
+   memory when they run it: for instance a plugin inside an application that
+   owns all GPU memory through its own allocator or budget, or a latency-bound
+   loop that cannot afford cudaMalloc / cudaFree (both can synchronise the
+   device).  This entry point allocates nothing: its scratch is a fixed
+   64 MiB device array built into the library (held on every GPU that loads
+   it until the process exits), and the caller passes x and y as for
+   fmca_matvec.  Has no counterpart in the reference.
+   - Plans whose scratch for this precision and nrhs exceeds 64 MiB (see
+     fmca_matvec_workspace_size) are rejected with FMCA_ERR_UNSUPPORTED.
+   - The plan must already be resident on the current device for this
+     precision (it becomes resident, allocating once, on its first
+     fmca_matvec / fmca_matvec_host call there); otherwise
+     FMCA_ERR_INVALID_ARGUMENT.
+   - The first call on each device looks up the array's device address; make
+     that first call before any stream capture.
+   - All calls share the one array: calls whose GPU work overlaps (other
+     streams, other threads) race and give wrong results. */
+fmca_status fmca_matvec_static_scratch(fmca_plan* plan,
+                                       const fmca_kernel_desc* kernel,
+                                       int precision, int dtype, int order,
+                                       int nrhs, const void* x,
+                                       int64_t x_stride_i, int64_t x_stride_r,
+                                       void* y, int64_t y_stride_i,
+                                       int64_t y_stride_r, void* stream);
+
 /* The same product with FP64 column-major host buffers (ld = n); copies in
    and out and synchronises. */
 fmca_status fmca_matvec_host(fmca_plan* plan, const fmca_kernel_desc* kernel,
