@@ -111,6 +111,21 @@ def gpu_smi_id(torch, dev) -> str:
     return str(dev.index or 0)
 
 
+def max_over_ranks(ms: float, dist=None, device=None) -> float:
+    """Step time of the slowest rank (the contract's max over ranks)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_replica: float, ms: float, world: int) -> float:
+    """Whole-job throughput of ``world`` independent replicas (weak scaling)."""
+    return world * units_per_replica / (ms * 1e-3)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -225,12 +240,8 @@ def main():
     barrier()
     clocks = sampler.stop()
     H.set_profiling(False)
-    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.n * args.rhs / (ms * 1e-3)
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / args.steps, dist, dev)
+    value = replica_throughput(args.n * args.rhs, ms, world)
     stage_ms = {s: v / args.steps for s, v in stage_tot.items()}
     H.check_device_error()
 
@@ -247,12 +258,8 @@ def main():
         t0 = time.perf_counter()
         yh = H.action(Xh, out=Yh)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_ms = statistics.median(e2e_t) * 1e3
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * args.n * args.rhs / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(statistics.median(e2e_t) * 1e3, dist, dev)
+    e2e_value = replica_throughput(args.n * args.rhs, e2e_ms, world)
     assert yh.shape == (args.n, args.rhs)
 
     # accuracy against the plain FP64 GPU H2 product (the 5x denominator)
