@@ -46,6 +46,7 @@ EXPORTED = [
     "fmca_plan_blocks", "fmca_matvec_workspace_size", "fmca_matvec",
     "fmca_matvec_host", "fmca_plan_check_device_error", "fmca_kernel_eval",
     "fmca_plan_set_profiling", "fmca_plan_profile", "fmca_matvec_static_scratch",
+    "fmca_matvec_adjoint_workspace_size", "fmca_matvec_adjoint", "fmca_plan_update_points",
 ]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
@@ -97,6 +98,11 @@ def load() -> C.CDLL:
     lib.fmca_kernel_eval.argtypes = [C.POINTER(KernelDesc), i32, dp, i64, dp, i64, dp]
     lib.fmca_matvec_static_scratch.argtypes = [vp, C.POINTER(KernelDesc), i32, i32, i32,
                                                i32, vp, i64, i64, vp, i64, i64, vp]
+    lib.fmca_matvec_adjoint_workspace_size.argtypes = [vp, i32, i32, C.POINTER(C.c_size_t)]
+    lib.fmca_matvec_adjoint.argtypes = [vp, C.POINTER(KernelDesc), i32, i32, i32, vp, i64, i64,
+                                        vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, C.c_size_t,
+                                        vp]
+    lib.fmca_plan_update_points.argtypes = [vp, dp, dp]
     lib.fmca_plan_set_profiling.argtypes = [vp, i32]
     lib.fmca_plan_profile.argtypes = [vp, dp, C.POINTER(C.c_int64)]
     for name in EXPORTED:

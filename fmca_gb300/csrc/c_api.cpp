@@ -301,6 +301,62 @@ fmca_status fmca_plan_check_device_error(fmca_plan* p) {
   return ok();
 }
 
+fmca_status fmca_matvec_adjoint_workspace_size(const fmca_plan* p, int precision, int nrhs,
+                                               size_t* bytes) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  if (!bytes || nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "bad nrhs or NULL bytes");
+  *bytes = fmca::gpu::adjoint_workspace_bytes(p->plan, precision, nrhs);
+  return ok();
+}
+
+fmca_status fmca_matvec_adjoint(fmca_plan* p, const fmca_kernel_desc* kernel, int precision,
+                                int dtype, int nrhs, const void* x, int64_t x_stride_i,
+                                int64_t x_stride_r, const void* y, int64_t y_stride_i,
+                                int64_t y_stride_r, double* values, void* dX,
+                                int64_t dX_stride_i, int64_t dX_stride_d, void* Kx, void* Ky,
+                                void* workspace, size_t workspace_bytes, void* stream) {
+  fmca_status s =
+      fmca::capi::check_matvec_args(p, kernel, precision, dtype, FMCA_ORDER_NATURAL, nrhs,
+                                    x, y);
+  if (s != FMCA_OK) return s;
+  std::string err;
+  int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  fmca::gpu::set_profiling(p->dev, p->profile);
+  st = fmca::gpu::adjoint(p->plan, p->dev, to_desc(kernel), precision, dtype, nrhs, x,
+                          x_stride_i, x_stride_r, y, y_stride_i, y_stride_r, values, dX,
+                          dX_stride_i, dX_stride_d, Kx, Ky, workspace, workspace_bytes,
+                          (cudaStream_t)stream, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_plan_update_points(fmca_plan* p, const double* P_rows, const double* P_cols) {
+  if (!p || !P_rows) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  fmca::Plan& P = p->plan;
+  const size_t dim = P.interp.dim;
+  const bool same = P.same_tree && (P_cols == nullptr || P_cols == P_rows);
+  if (!same && !P_cols)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "P_cols is required for two point clouds");
+  for (size_t i = 0; i < dim * P.rows.n; ++i)
+    if (!std::isfinite(P_rows[i]))
+      return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows holds a non-finite value");
+  if (!same)
+    for (size_t i = 0; i < dim * P.cols.n; ++i)
+      if (!std::isfinite(P_cols[i]))
+        return fail(FMCA_ERR_INVALID_ARGUMENT, "P_cols holds a non-finite value");
+  P.points_r.assign(P_rows, P_rows + dim * P.rows.n);
+  if (same)
+    P.points_c = P.points_r;
+  else
+    P.points_c.assign(P_cols, P_cols + dim * P.cols.n);
+  std::string err;
+  int st = fmca::gpu::update_points(P, p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
 fmca_status fmca_plan_set_profiling(fmca_plan* p, int enable) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   p->profile = enable != 0;

@@ -7,6 +7,7 @@
 
 #include "../../include/fmca_gb300.h"
 #include "h2_gpu.h"
+#include "h2_adjoint_kernels.cuh"
 #include "h2_gpu_kernels.cuh"
 #include "h2_tc_kernels.cuh"
 
@@ -380,7 +381,9 @@ KParams<T> make_kparams(const KernelDesc& k) {
   KParams<T> kp;
   const double l = k.l, log2e = 1.4426950408889634;
   double a = 0, e2 = 0;
-  switch (k.type) {
+  // the length-scale derivative kernels share the constants of their kernel
+  const int base = k.type >= K_DL_EXPONENTIAL ? k.type - K_DL_EXPONENTIAL : k.type;
+  switch (base) {
     case FMCA_KERNEL_EXPONENTIAL:
       e2 = -log2e / l;
       break;
@@ -410,7 +413,14 @@ KParams<T> make_kparams(const KernelDesc& k) {
   kp.c = (T)k.c;
   kp.a = (T)a;
   kp.e2 = (T)e2;
+  kp.il = (T)(1. / l);
   return kp;
+}
+
+// scale applied to the assembled product: sigma2, divided by l for the
+// length-scale derivative kernels (their device values are l * dk/dl)
+double output_scale(const KernelDesc& k) {
+  return k.type >= K_DL_EXPONENTIAL ? k.sigma2 / k.l : k.sigma2;
 }
 
 template <typename K>
@@ -582,17 +592,37 @@ int acquire_ws(DevPlan* dp, size_t need, void** ws, size_t wsb, cudaStream_t st,
   return FMCA_OK;
 }
 
+// Where a finished matvec left its cluster-ordered input and leaf expansions
+// (used by the adjoint).  All buffers are chunk-major [nch][rows][ld].
+struct MatvecState {
+  const void* xc = nullptr;        // input in cluster order (T)
+  const void* s = nullptr;         // downward-pass expansions per row cluster (T)
+  const unsigned int* cmax = nullptr;  // column maxima of the scaled path, or null
+  int ld = 0, rb = 0, nch = 0;
+  bool fp64 = false;
+};
+
 template <typename T>
 int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
              int dtype, int order, int nrhs, const void* x, int64_t sxi,
              int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-             size_t wsb, cudaStream_t st, std::string* err) {
+             size_t wsb, cudaStream_t st, std::string* err,
+             MatvecState* state = nullptr) {
   const int ld = ld_for<T>(nrhs);
   const int rb = rhs_block(nrhs);
   const size_t need = ws_layout<T>(plan, nrhs, nullptr, nullptr);
   FMCA_TRY(acquire_ws(dp, need, &ws, wsb, st, err));
   Workspace<T> w;
   ws_layout<T>(plan, nrhs, ws, &w);
+  if (state) {
+    state->xc = w.xc;
+    state->s = w.s;
+    state->cmax = nullptr;
+    state->ld = ld;
+    state->rb = rb;
+    state->nch = nchunks_for(nrhs);
+    state->fp64 = sizeof(T) == 8;
+  }
   dp->nevents = 0;
   dp->launches = 0;
   dp->mark(-1, st);
@@ -641,11 +671,11 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_kernel<T, double><<<blocks((int64_t)plan.rows.n * nrhs), nthr, 0, st>>>(
-        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, k.sigma2, static_cast<double*>(y),
+        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, output_scale(k), static_cast<double*>(y),
         syi, syr);
   else
     scatter_kernel<T, float><<<blocks((int64_t)plan.rows.n * nrhs), nthr, 0, st>>>(
-        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, k.sigma2, static_cast<float*>(y),
+        pr, plan.rows.n, nrhs, rb, ld, w.ynear, w.yfar, output_scale(k), static_cast<float*>(y),
         syi, syr);
   ++dp->launches;
   dp->mark(FMCA_STAGE_SCATTER, st);
@@ -688,8 +718,12 @@ size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
   return off;
 }
 
+// kernels whose values lie in [0, 1] (the FP16 split needs a bounded range):
+// the six covariance kernels and l * dk/dl of the first four
 bool tc_supported(int type, int nrhs) {
-  return type >= FMCA_KERNEL_EXPONENTIAL && type <= FMCA_KERNEL_MATERN92 && nrhs > 16;
+  const bool bounded = (type >= FMCA_KERNEL_EXPONENTIAL && type <= FMCA_KERNEL_MATERN92) ||
+                       (type >= K_DL_EXPONENTIAL && type <= K_DL_GAUSSIAN);
+  return bounded && nrhs > 16;
 }
 
 template <int KT, int MT>
@@ -733,13 +767,22 @@ cudaError_t launch_tc(const GroupList& gl, const Pt4<float>* tgt, const Pt4<floa
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
               int dtype, int order, int nrhs, const void* x, int64_t sxi, int64_t sxr,
               void* y, int64_t syi, int64_t syr, void* ws, size_t wsb, cudaStream_t st,
-              std::string* err) {
+              std::string* err, MatvecState* state = nullptr) {
   constexpr int RB = kTcRhs;
   const int ld = kTcRhs;
   const size_t need = tc_ws_layout(plan, nrhs, nullptr, nullptr);
   FMCA_TRY(acquire_ws(dp, need, &ws, wsb, st, err));
   TcWorkspace w;
   tc_ws_layout(plan, nrhs, ws, &w);
+  if (state) {
+    state->xc = w.xc;
+    state->s = w.s;
+    state->cmax = w.cmax;
+    state->ld = ld;
+    state->rb = RB;
+    state->nch = (nrhs + RB - 1) / RB;
+    state->fp64 = false;
+  }
   dp->nevents = 0;
   dp->launches = 0;
   dp->mark(-1, st);
@@ -853,10 +896,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_scaled_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
-        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, k.sigma2, static_cast<double*>(y), syi, syr);
+        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, output_scale(k), static_cast<double*>(y), syi, syr);
   else
     scatter_scaled_kernel<float><<<blocks(nr * nrhs), nthr, 0, st>>>(
-        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, k.sigma2, static_cast<float*>(y), syi, syr);
+        pr, nr, nrhs, w.ynear, w.yfar, w.cmax, output_scale(k), static_cast<float*>(y), syi, syr);
   FMCA_CK(cudaGetLastError());
   ++dp->launches;
   dp->mark(FMCA_STAGE_SCATTER, st);
@@ -921,6 +964,293 @@ int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
                          syr, ws, ws_bytes, st, err);
 }
 
+// ---------------------------------------------------------------------------
+// adjoint
+namespace {
+
+constexpr int kDotBlocks = 152 * 4;
+
+// z (contiguous n_r x R column-major, dtype of x) = K x
+int matvec_state(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
+                 int dtype, int nrhs, const void* x, int64_t sxi, int64_t sxr, void* z,
+                 void* ws, size_t wsb, cudaStream_t st, std::string* err, MatvecState* state) {
+  const int64_t nr = plan.rows.n;
+  if (precision == FMCA_PREC_FP64)
+    return matvec_t<double>(plan, dp, dp->d, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr,
+                            z, 1, nr, ws, wsb, st, err, state);
+  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs))
+    return matvec_tc(plan, dp, dp->f, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr, z, 1, nr,
+                     ws, wsb, st, err, state);
+  return matvec_t<float>(plan, dp, dp->f, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr, z,
+                         1, nr, ws, wsb, st, err, state);
+}
+
+// out[idx] = scale * sum_{i,r} a[i, r] b[i, r]; a strided, b contiguous
+// (n x R column-major); both of dtype
+cudaError_t launch_dot(int dtype, int64_t n, int R, const void* a, int64_t sai, int64_t sar,
+                       const void* b, double* partial, double scale, double* out, int idx,
+                       cudaStream_t st) {
+  if (dtype == FMCA_DTYPE_F64)
+    dot_partial_kernel<double, double><<<kDotBlocks, 256, 0, st>>>(
+        n, R, static_cast<const double*>(a), sai, sar, static_cast<const double*>(b), 1, n,
+        partial);
+  else
+    dot_partial_kernel<float, float><<<kDotBlocks, 256, 0, st>>>(
+        n, R, static_cast<const float*>(a), sai, sar, static_cast<const float*>(b), 1, n,
+        partial);
+  dot_final_kernel<<<1, 256, 0, st>>>(partial, kDotBlocks, scale, out, idx);
+  return cudaGetLastError();
+}
+
+__global__ void set_scalar_kernel(double* out, int idx, double v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) out[idx] = v;
+}
+
+template <typename T, int RB>
+cudaError_t launch_near_grad(const GroupList& gl, const Pt4<T>* tgt, const Pt4<T>* src,
+                             const T* tval, const T* sval, int ld, const double* cs,
+                             int rcount, const KParams<T>& kp, double scale, double* G,
+                             int* errf, cudaStream_t st) {
+  if (gl.ngroups == 0) return cudaSuccess;
+  constexpr int TS = TileSize<T>::value;
+  auto kern = near_grad_kernel<T, RB, TS, kStages>;
+  const size_t smem = 128 + (size_t)kStages * TS * (sizeof(Pt4<T>) + (size_t)ld * sizeof(T));
+  ensure_smem(kern, smem);
+  const int threads = std::max(32, (gl.maxcount + 31) / 32 * 32);
+  kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
+                                          rcount, kp, scale, G, errf);
+  return cudaGetLastError();
+}
+
+template <typename T, int RB>
+cudaError_t launch_far_grad(const Plan& plan, DevPlan* dp, DevSet<T>& S, const T* U,
+                            const T* tval, int ld, const double* cs, int rcount,
+                            double scale, double* G, cudaStream_t st) {
+  if (!dp->nleaves_r) return cudaSuccess;
+  auto kern = far_grad_kernel<T, RB>;
+  const size_t smem =
+      (128 * 48 + 64 * RB) * sizeof(T) + (size_t)plan.interp.q * 3 * sizeof(int);
+  ensure_smem(kern, smem);
+  kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r, S.bbmin_r,
+                                         S.bbext_r, S.pts_r, U, tval, ld, cs, rcount,
+                                         dp->midx, S.ip, scale, G);
+  return cudaGetLastError();
+}
+
+template <typename T>
+int grad_terms(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
+               const MatvecState& A, const MatvecState& B, int nrhs, const double* cs,
+               double scale, double* G, cudaStream_t st, std::string* err) {
+  const KParams<T> kp = make_kparams<T>(k);
+  const size_t q = plan.interp.q;
+  const int64_t nr = plan.rows.n, nc = plan.cols.n;
+  const size_t Cr = plan.rows.nclusters();
+  const int ld = A.ld, rb = A.rb;
+  for (int ch = 0; ch < A.nch; ++ch) {
+    const int rcount = std::min(rb, nrhs - ch * rb);
+    const T* xa = static_cast<const T*>(A.xc) + (size_t)ch * nc * ld;
+    const T* yb = static_cast<const T*>(B.xc) + (size_t)ch * nr * ld;
+    const T* ua = static_cast<const T*>(A.s) + (size_t)ch * Cr * q * ld;
+    const T* ub = static_cast<const T*>(B.s) + (size_t)ch * Cr * q * ld;
+    const double* csc = cs + ch * rb;
+    cudaError_t e = cudaSuccess;
+    switch (rb) {
+      case 1:
+        e = launch_near_grad<T, 1>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
+                                   scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_near_grad<T, 1>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
+                                     scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 1>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 1>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+        break;
+      case 8:
+        e = launch_near_grad<T, 8>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
+                                   scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_near_grad<T, 8>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
+                                     scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 8>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 8>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+        break;
+      default:
+        e = launch_near_grad<T, 32>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
+                                    scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_near_grad<T, 32>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
+                                      scale, G, dp->err_flag, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 32>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
+        if (e == cudaSuccess)
+          e = launch_far_grad<T, 32>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+        break;
+    }
+    FMCA_CK(e);
+  }
+  return FMCA_OK;
+}
+
+struct AdjointWorkspace {
+  void *wsA, *wsB;
+  size_t mv;
+  void* z;  // dtype of the inputs
+  double *G, *partial, *colscale, *scal;
+};
+
+size_t adjoint_layout(const Plan& plan, int precision, int nrhs, void* base,
+                      AdjointWorkspace* w) {
+  const size_t mv = align_up(workspace_bytes(plan, precision, nrhs));
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    void* p = base ? static_cast<char*>(base) + off : nullptr;
+    off += align_up(bytes);
+    return p;
+  };
+  AdjointWorkspace t;
+  t.mv = mv;
+  t.wsA = take(mv);
+  t.wsB = take(mv);
+  t.z = take(sizeof(double) * std::max<size_t>(plan.rows.n, plan.cols.n) * nrhs);
+  t.G = (double*)take(sizeof(double) * 4 * std::max<size_t>(plan.rows.n, plan.cols.n));
+  t.partial = (double*)take(sizeof(double) * kDotBlocks);
+  t.colscale = (double*)take(sizeof(double) * nrhs);
+  t.scal = (double*)take(sizeof(double) * 8);
+  if (w) *w = t;
+  return off;
+}
+
+}  // namespace
+
+size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs) {
+  return adjoint_layout(plan, precision, nrhs, nullptr, nullptr);
+}
+
+int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int dtype,
+            int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
+            int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx, void* Ky,
+            void* ws, size_t wsb, cudaStream_t st, std::string* err) {
+  std::lock_guard<std::mutex> lock(dp->mu);
+  const bool base_kernel = k.type >= FMCA_KERNEL_EXPONENTIAL && k.type <= FMCA_KERNEL_GAUSSIAN;
+  if ((dX || Ky) && !plan.same_tree) {
+    *err = "gradients w.r.t. the points and K^T y need one point cloud (Pr == Pc)";
+    return FMCA_ERR_UNSUPPORTED;
+  }
+  if (dX && !base_kernel) {
+    *err = "point gradients are implemented for EXPONENTIAL, MATERN32, MATERN52, GAUSSIAN";
+    return FMCA_ERR_UNSUPPORTED;
+  }
+  const size_t need = adjoint_layout(plan, precision, nrhs, nullptr, nullptr);
+  FMCA_TRY(acquire_ws(dp, need, &ws, wsb, st, err));
+  AdjointWorkspace w;
+  adjoint_layout(plan, precision, nrhs, ws, &w);
+  KernelDesc k1 = k;
+  k1.sigma2 = 1.0;
+  const int64_t nr = plan.rows.n, nc = plan.cols.n;
+  const int nthr = 256;
+  auto blocks = [&](int64_t total) {
+    int64_t b = (total + nthr - 1) / nthr;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+  };
+  MatvecState A, B;
+  // z = K x with unit variance; f = sigma2 * y . z, df/dsigma2 = y . z
+  FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, nrhs, x, sxi, sxr, w.z, w.wsA, w.mv,
+                        st, err, &A));
+  FMCA_CK(launch_dot(dtype, nr, nrhs, y, syi, syr, w.z, w.partial, 1.0, w.scal, 0, st));
+  if (values) {
+    scalar_axpy_kernel<<<1, 32, 0, st>>>(w.scal, 0, k.sigma2, values, 0);
+    scalar_axpy_kernel<<<1, 32, 0, st>>>(w.scal, 0, 1.0, values, 2);
+  }
+  if (Kx) {
+    if (dtype == FMCA_DTYPE_F64)
+      scale_copy_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
+          nr, nrhs, static_cast<const double*>(w.z), k.sigma2, static_cast<double*>(Kx), syi,
+          syr);
+    else
+      scale_copy_kernel<float><<<blocks(nr * nrhs), nthr, 0, st>>>(
+          nr, nrhs, static_cast<const float*>(w.z), k.sigma2, static_cast<float*>(Kx), syi,
+          syr);
+  }
+  // df/dl = sigma2 * y . H2[dk/dl] x
+  if (values) {
+    if (base_kernel) {
+      KernelDesc kd = k1;
+      kd.type = k.type + K_DL_EXPONENTIAL;
+      FMCA_TRY(matvec_state(plan, dp, kd, precision, dtype, nrhs, x, sxi, sxr, w.z, w.wsB,
+                            w.mv, st, err, nullptr));
+      FMCA_CK(launch_dot(dtype, nr, nrhs, y, syi, syr, w.z, w.partial, k.sigma2, values, 1,
+                         st));
+    } else {
+      set_scalar_kernel<<<1, 32, 0, st>>>(values, 1, std::nan(""));
+    }
+  }
+  if (dX || Ky) {
+    // the y-side product (K is symmetric for one point cloud)
+    FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, nrhs, y, syi, syr, w.z, w.wsB, w.mv,
+                          st, err, &B));
+    if (Ky) {
+      if (dtype == FMCA_DTYPE_F64)
+        scale_copy_kernel<double><<<blocks(nc * nrhs), nthr, 0, st>>>(
+            nc, nrhs, static_cast<const double*>(w.z), k.sigma2, static_cast<double*>(Ky),
+            sxi, sxr);
+      else
+        scale_copy_kernel<float><<<blocks(nc * nrhs), nthr, 0, st>>>(
+            nc, nrhs, static_cast<const float*>(w.z), k.sigma2, static_cast<float*>(Ky), sxi,
+            sxr);
+    }
+  }
+  if (dX) {
+    FMCA_CK(cudaMemsetAsync(w.G, 0, sizeof(double) * 4 * nr, st));
+    colscale_kernel<<<1, 256, 0, st>>>(nrhs, A.cmax, B.cmax, w.colscale);
+    if (A.fp64)
+      FMCA_TRY(grad_terms<double>(plan, dp, dp->d, k1, A, B, nrhs, w.colscale, k.sigma2, w.G,
+                                  st, err));
+    else
+      FMCA_TRY(grad_terms<float>(plan, dp, dp->f, k1, A, B, nrhs, w.colscale, k.sigma2, w.G,
+                                 st, err));
+    if (dtype == FMCA_DTYPE_F64)
+      grad_scatter_kernel<double><<<blocks(nr * plan.interp.dim), nthr, 0, st>>>(
+          dp->perm_r, nr, plan.interp.dim, w.G, static_cast<double*>(dX), sdi, sdd);
+    else
+      grad_scatter_kernel<float><<<blocks(nr * plan.interp.dim), nthr, 0, st>>>(
+          dp->perm_r, nr, plan.interp.dim, w.G, static_cast<float*>(dX), sdi, sdd);
+  }
+  FMCA_CK(cudaGetLastError());
+  return FMCA_OK;
+}
+
+int update_points(const Plan& plan, DevPlan* dp, std::string* err) {
+  if (!dp) return FMCA_OK;
+  auto refresh = [&](auto& S) -> int {
+    using T = std::remove_reference_t<decltype(S.ip.xi[0])>;
+    if (!S.ready) return FMCA_OK;
+    const int dim = plan.interp.dim;
+    for (int side = 0; side < 2; ++side) {
+      const Tree& t = side == 0 ? plan.rows : plan.cols;
+      const std::vector<double>& Pn = side == 0 ? plan.points_r : plan.points_c;
+      std::vector<Pt4<T>> hp(t.n);
+      for (uint32_t i = 0; i < t.n; ++i) {
+        const double* p = Pn.data() + (size_t)t.perm[i] * dim;
+        hp[i] = Pt4<T>{(T)p[0], dim > 1 ? (T)p[1] : T(0), dim > 2 ? (T)p[2] : T(0), T(1)};
+      }
+      FMCA_CK(cudaMemcpy(side == 0 ? S.pts_r : S.pts_c, hp.data(), sizeof(Pt4<T>) * t.n,
+                         cudaMemcpyHostToDevice));
+    }
+    return FMCA_OK;
+  };
+  std::lock_guard<std::mutex> lock(dp->mu);
+  int cur = -1;
+  FMCA_CK(cudaGetDevice(&cur));
+  if (cur != dp->device) FMCA_CK(cudaSetDevice(dp->device));
+  int s = refresh(dp->d);
+  if (s == FMCA_OK) s = refresh(dp->f);
+  if (cur != dp->device) cudaSetDevice(cur);
+  return s;
+}
+
 int check_device_error(DevPlan* dp, std::string* err) {
   if (!dp || !dp->err_flag) return FMCA_OK;
   FMCA_CK(cudaDeviceSynchronize());
@@ -943,7 +1273,7 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
   FMCA_CK(cudaMemcpy(dr, PR, sizeof(double) * dim * nr, cudaMemcpyHostToDevice));
   FMCA_CK(cudaMemcpy(dc, PC, sizeof(double) * dim * nc, cudaMemcpyHostToDevice));
   const KParams<double> kp = make_kparams<double>(k);
-  dense_eval_kernel<<<152 * 16, 256>>>(dim, dr, nr, dc, nc, kp, k.sigma2, dout);
+  dense_eval_kernel<<<152 * 16, 256>>>(dim, dr, nr, dc, nc, kp, output_scale(k), dout);
   FMCA_CK(cudaGetLastError());
   FMCA_CK(cudaMemcpy(out, dout, sizeof(double) * nr * nc, cudaMemcpyDeviceToHost));
   cudaFree(dr);

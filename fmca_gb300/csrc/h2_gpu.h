@@ -33,6 +33,16 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
 // device the plan lives on (-1 if not uploaded)
 int device_of(const DevPlan* dev);
 void set_profiling(DevPlan* dev, bool on);
+size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs);
+// values (device, 3 doubles): f, df/dl, df/dsigma2; dX (device, natural
+// order); Kx (strides of y) = K x, Ky (strides of x) = K y.  Any output may
+// be null.
+int adjoint(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision, int dtype,
+            int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
+            int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx,
+            void* Ky, void* ws, size_t ws_bytes, cudaStream_t stream, std::string* err);
+// re-uploads the point coordinates held by the plan (tree and boxes fixed)
+int update_points(const Plan& plan, DevPlan* dev, std::string* err);
 // true if the plan's device data for this precision lives on the current
 // device (so a matvec needs no further device allocation besides workspace)
 bool resident(const DevPlan* dev, int precision);

@@ -53,6 +53,7 @@ struct KParams {
   T l, c;
   T a;   // sqrt(3)/l, sqrt(5)/l, ... (per type)
   T e2;  // scale of the exponent in base 2 (FP32 path)
+  T il;  // 1 / l
 };
 
 template <typename T>
@@ -170,6 +171,24 @@ __device__ __forceinline__ double keval_ref(int type, double r2,
       return r / l;
     case 9:
       return (r / l) * (r / l) * (r / l);
+    // length-scale derivatives, returned as l * dk/dl (dimensionless; the
+    // driver divides the result by l)
+    case 10: {
+      const double t = r / l;
+      return t * exp(-t);
+    }
+    case 11: {
+      const double u = kp.a * r;
+      return u * u * exp(-u);
+    }
+    case 12: {
+      const double u = kp.a * r;
+      return u * u / 3. * (1. + u) * exp(-u);
+    }
+    case 13: {
+      const double t2 = r2 / (l * l);
+      return t2 * exp(-0.5 * t2);
+    }
   }
   return 0.;
 }
@@ -228,6 +247,23 @@ __device__ __forceinline__ float keval_fast(int type, float r2,
       const float t = sqrt_approx(r2) / kp.l;
       return t * t * t;
     }
+    // l * dk/dl of kernels 0..3 (bounded by 1)
+    case 10: {
+      const float r = sqrt_approx(r2);
+      return r * kp.il * ex2_approx(r * kp.e2);
+    }
+    case 11: {
+      const float r = sqrt_approx(r2);
+      const float u = kp.a * r;
+      return u * u * ex2_approx(r * kp.e2);
+    }
+    case 12: {
+      const float r = sqrt_approx(r2);
+      const float u = kp.a * r;
+      return u * u * 0.333333343f * (1.f + u) * ex2_approx(r * kp.e2);
+    }
+    case 13:
+      return r2 * kp.il * kp.il * ex2_approx(r2 * kp.e2);
   }
   return 0.f;
 }
@@ -467,7 +503,7 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
                                int rcount, const int* __restrict__ midx_g,
                                InterpDev<T> ip, T* __restrict__ tout) {
   constexpr int CH = 64;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   T* F = reinterpret_cast<T*>(smem_raw);  // CH x 3 x 8
   T* X = F + CH * 24;                     // CH x RB
   int* midx = reinterpret_cast<int*>(X + CH * RB);
@@ -541,7 +577,7 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
                                 T* __restrict__ buf, int ldv, int rofs,
                                 int rcount) {
   constexpr int JC = 64;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   T* e = reinterpret_cast<T*>(smem_raw);  // 3 x 8 x 8
   T* S = e + 192;                         // JC x RB
   int* midx = reinterpret_cast<int*>(S + JC * RB);
@@ -611,7 +647,7 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
                                   int rcount, const int* __restrict__ midx_g,
                                   InterpDev<T> ip, T* __restrict__ yout) {
   constexpr int KC = 64;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   T* F = reinterpret_cast<T*>(smem_raw);   // blockDim x 24
   T* S = F + blockDim.x * 24;              // KC x RB
   int* midx = reinterpret_cast<int*>(S + KC * RB);

@@ -21,20 +21,22 @@ constexpr double kInf = std::numeric_limits<double>::infinity();
 int kernel_type_from_name(const std::string& name) {
   std::string s(name);
   for (auto& ch : s) ch = (char)std::toupper((unsigned char)ch);
-  static const char* names[] = {"EXPONENTIAL",     "MATERN32",     "MATERN52",
-                                "GAUSSIAN",        "MATERN72",     "MATERN92",
-                                "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D",
-                                "TRIHARMONIC3D"};
+  static const char* names[] = {"EXPONENTIAL",     "MATERN32",       "MATERN52",
+                                "GAUSSIAN",        "MATERN72",       "MATERN92",
+                                "INVMULTIQUADRIC", "MULTIQUADRIC",   "BIHARMONIC3D",
+                                "TRIHARMONIC3D",   "DL_EXPONENTIAL", "DL_MATERN32",
+                                "DL_MATERN52",     "DL_GAUSSIAN"};
   for (int i = 0; i < K_NUM_KERNELS; ++i)
     if (s == names[i]) return i;
   return -1;
 }
 
 const char* kernel_type_name(int type) {
-  static const char* names[] = {"EXPONENTIAL",     "MATERN32",     "MATERN52",
-                                "GAUSSIAN",        "MATERN72",     "MATERN92",
-                                "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D",
-                                "TRIHARMONIC3D"};
+  static const char* names[] = {"EXPONENTIAL",     "MATERN32",       "MATERN52",
+                                "GAUSSIAN",        "MATERN72",       "MATERN92",
+                                "INVMULTIQUADRIC", "MULTIQUADRIC",   "BIHARMONIC3D",
+                                "TRIHARMONIC3D",   "DL_EXPONENTIAL", "DL_MATERN32",
+                                "DL_MATERN52",     "DL_GAUSSIAN"};
   return (type >= 0 && type < K_NUM_KERNELS) ? names[type] : "UNKNOWN";
 }
 
@@ -66,6 +68,18 @@ double kernel_eval_host(int type, double l, double c, double r) {
       return r / l;
     case K_TRIHARMONIC3D:
       return (r / l) * (r / l) * (r / l);
+    case K_DL_EXPONENTIAL:  // d/dl exp(-r/l) = (r/l^2) exp(-r/l)
+      return r / (l * l) * std::exp(-r / l);
+    case K_DL_MATERN32: {  // (3 r^2 / l^3) exp(-sqrt(3) r / l)
+      const double a = std::sqrt(3.) / l;
+      return a * a * r * r / l * std::exp(-a * r);
+    }
+    case K_DL_MATERN52: {  // (a^2 r^2 / (3 l)) (1 + a r) exp(-a r), a = sqrt(5)/l
+      const double a = std::sqrt(5.) / l;
+      return a * a * r * r / (3. * l) * (1. + a * r) * std::exp(-a * r);
+    }
+    case K_DL_GAUSSIAN:  // (r^2 / l^3) exp(-r^2 / (2 l^2))
+      return r * r / (l * l * l) * std::exp(-0.5 * r * r / (l * l));
   }
   return std::numeric_limits<double>::quiet_NaN();
 }

@@ -45,7 +45,13 @@ enum KernelType : int {
   K_MULTIQUADRIC = 7,
   K_BIHARMONIC3D = 8,
   K_TRIHARMONIC3D = 9,
-  K_NUM_KERNELS = 10
+  // derivatives dk/dl of the four covariance kernels with respect to the
+  // length scale (the far field of H2[dk/dl] is dS/dl at the fixed nodes)
+  K_DL_EXPONENTIAL = 10,
+  K_DL_MATERN32 = 11,
+  K_DL_MATERN52 = 12,
+  K_DL_GAUSSIAN = 13,
+  K_NUM_KERNELS = 14
 };
 
 // Parses an FMCA kernel name (case-insensitive, like CovarianceKernel.h:54).

@@ -253,6 +253,69 @@ class H2Matrix:
                 C.c_void_p(stream.cuda_stream)))
         return y
 
+    def update_points(self, Pr, Pc=None) -> None:
+        """Moves the points, keeping the tree, boxes, nodes and block lists."""
+        Pr = np.asfortranarray(Pr, dtype=np.float64)
+        if Pr.shape != (self.dim, self.rows()):
+            raise ValueError("Pr must have the shape of the plan's row points")
+        Pcp = None
+        if Pc is not None:
+            Pc = np.asfortranarray(Pc, dtype=np.float64)
+            if Pc.shape != (self.dim, self.cols()):
+                raise ValueError("Pc must have the shape of the plan's column points")
+            Pcp = _dptr(Pc)
+        check(_lib.load().fmca_plan_update_points(self._h, _dptr(Pr), Pcp))
+
+    def adjoint(self, x, y, precision: Optional[str] = None, want_dX: bool = True,
+                want_Kx: bool = False, want_Ky: bool = False, stream=None):
+        """Gradients of f = sum_r y_r^T K x_r on CUDA tensors.
+
+        Returns a dict with ``values`` (f, df/dl, df/dsigma2 as a float64
+        CUDA tensor), and when asked ``dX`` (n x dim, natural order),
+        ``Kx`` = K x and ``Ky`` = K y.  The tree and boxes stay fixed."""
+        import torch
+        prec = _PREC[precision or self.precision]
+        if x.dim() == 1:
+            x = x.unsqueeze(1)
+        if y.dim() == 1:
+            y = y.unsqueeze(1)
+        if x.dtype != y.dtype or x.device != y.device or x.shape[1] != y.shape[1]:
+            raise ValueError("x and y must share dtype, device and number of columns")
+        if x.shape[0] != self.cols() or y.shape[0] != self.rows():
+            raise ValueError("x must have n_cols rows and y n_rows rows")
+        dev = x.device
+        R = x.shape[1]
+        dt = _lib.DTYPE_F64 if x.dtype == torch.float64 else _lib.DTYPE_F32
+        out = {"values": torch.zeros(3, dtype=torch.float64, device=dev)}
+        dX = torch.empty((self.rows(), self.dim), dtype=x.dtype, device=dev) if want_dX else None
+        Kx = torch.empty_like(y) if want_Kx else None
+        Ky = torch.empty_like(x) if want_Ky else None
+        with torch.cuda.device(dev):
+            if stream is None:
+                stream = torch.cuda.current_stream(dev)
+            nb = C.c_size_t(0)
+            check(_lib.load().fmca_matvec_adjoint_workspace_size(self._h, prec, R, C.byref(nb)))
+            key = ("adj", prec, R, dev.index)
+            ws = self._ws.get(key)
+            if ws is None or ws.numel() < nb.value:
+                ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+                self._ws[key] = ws
+            d = self.cov.desc()
+            ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+            check(_lib.load().fmca_matvec_adjoint(
+                self._h, C.byref(d), prec, dt, R,
+                ptr(x), x.stride(0), x.stride(1), ptr(y), y.stride(0), y.stride(1),
+                ptr(out["values"]), ptr(dX), dX.stride(0) if dX is not None else 0,
+                dX.stride(1) if dX is not None else 0, ptr(Kx), ptr(Ky),
+                ptr(ws), ws.numel(), C.c_void_p(stream.cuda_stream)))
+        if dX is not None:
+            out["dX"] = dX
+        if Kx is not None:
+            out["Kx"] = Kx
+        if Ky is not None:
+            out["Ky"] = Ky
+        return out
+
     def set_profiling(self, enable: bool = True) -> None:
         """CUDA-event timing of the stages of the following matvecs."""
         check(_lib.load().fmca_plan_set_profiling(self._h, 1 if enable else 0))

@@ -66,7 +66,14 @@ enum {
   FMCA_KERNEL_INVMULTIQUADRIC = 6,
   FMCA_KERNEL_MULTIQUADRIC = 7,
   FMCA_KERNEL_BIHARMONIC3D = 8,
-  FMCA_KERNEL_TRIHARMONIC3D = 9
+  FMCA_KERNEL_TRIHARMONIC3D = 9,
+  /* dk/dl of EXPONENTIAL, MATERN32, MATERN52, GAUSSIAN (names "DL_..."):
+     fmca_matvec with these gives sigma2 * H2[dk/dl] x, the derivative of the
+     H2 product with respect to the length scale at fixed nodes */
+  FMCA_KERNEL_DL_EXPONENTIAL = 10,
+  FMCA_KERNEL_DL_MATERN32 = 11,
+  FMCA_KERNEL_DL_MATERN52 = 12,
+  FMCA_KERNEL_DL_GAUSSIAN = 13
 };
 
 /* Arithmetic of the matvec. */
@@ -203,6 +210,39 @@ fmca_status fmca_matvec_static_scratch(fmca_plan* plan,
 fmca_status fmca_matvec_host(fmca_plan* plan, const fmca_kernel_desc* kernel,
                              int precision, int order, int nrhs,
                              const double* x, double* y);
+
+/* Adjoint of the H2 product (no counterpart in the reference, which has no
+   derivatives).  For f = sum_r y_r^T K x_r with K = sigma2 * H2[k] (cluster
+   tree, boxes and interpolation nodes held fixed), it computes on the device:
+     values[0..2] = f, df/dl, df/dsigma2   (FP64; NaN for df/dl of kernels
+                                            without a DL_ counterpart)
+     dX           = df/dX, n x dim in natural order (strides), dtype of x;
+                    needs one point cloud (P_cols NULL) and one of
+                    EXPONENTIAL, MATERN32, MATERN52, GAUSSIAN
+     Kx           = K x  (n_rows x nrhs, strides of y), optional
+     Ky           = K y  (n_cols x nrhs, strides of x; one point cloud)
+   Any output pointer may be NULL.  x: n_cols x nrhs, y: n_rows x nrhs, both
+   device buffers of dtype.  workspace: fmca_matvec_adjoint_workspace_size
+   bytes or NULL (plan-owned).  Asynchronous on stream. */
+fmca_status fmca_matvec_adjoint_workspace_size(const fmca_plan* plan,
+                                               int precision, int nrhs,
+                                               size_t* bytes);
+fmca_status fmca_matvec_adjoint(fmca_plan* plan, const fmca_kernel_desc* kernel,
+                                int precision, int dtype, int nrhs,
+                                const void* x, int64_t x_stride_i,
+                                int64_t x_stride_r, const void* y,
+                                int64_t y_stride_i, int64_t y_stride_r,
+                                double* values, void* dX, int64_t dX_stride_i,
+                                int64_t dX_stride_d, void* Kx, void* Ky,
+                                void* workspace, size_t workspace_bytes,
+                                void* stream);
+/* Replaces the point coordinates (dim x n, column-major FP64, host) while
+   keeping the cluster tree, boxes, interpolation nodes and block lists: the
+   H2 matrix of moved points with a frozen structure, as differentiated by
+   fmca_matvec_adjoint.  P_cols may be NULL for one point cloud.  Synchronous.
+   No counterpart in the reference (which rebuilds the tree). */
+fmca_status fmca_plan_update_points(fmca_plan* plan, const double* P_rows,
+                                    const double* P_cols);
 
 /* Returns FMCA_ERR_TIMEOUT if a kernel of this plan gave up a bounded wait
    since the last call, and clears the flag.  Synchronises the device. */

@@ -35,6 +35,8 @@ def load() -> C.CDLL:
                                   i32, i32, dp]
     lib.oracle_dense_matvec.argtypes = [i32, C.c_double, C.c_double, C.c_double, i32, dp, i64,
                                         dp, i64, dp, i32, dp, i32]
+    lib.oracle_adjoint.argtypes = [vp, i32, C.c_double, C.c_double, dp, dp, i32, dp, dp, i32]
+    lib.oracle_update_points.argtypes = [vp, dp]
     lib.oracle_kernel.restype = C.c_double
     lib.oracle_kernel.argtypes = [i32, C.c_double, C.c_double, C.c_double]
     _lib = lib
@@ -93,6 +95,13 @@ class OraclePlan:
         load().oracle_statistics(self._h, _d(out))
         return out
 
+    def update_points(self, P):
+        """Moves the points of a one-cloud plan, keeping its structure."""
+        assert self.same
+        P = np.asfortranarray(P, dtype=np.float64)
+        assert P.shape == self.Pr.shape
+        load().oracle_update_points(self._h, _d(P))
+
     def check_transfer(self):
         return load().oracle_check_transfer(self._h)
 
@@ -107,6 +116,21 @@ class OraclePlan:
         load().oracle_action(self._h, int(ktype), float(l), float(c), float(sigma2), _d(x),
                              x.shape[1], _d(y), int(bucket_stride), int(nthreads), _d(work))
         return (y[:, 0] if vec else y), tuple(work)
+
+
+def adjoint(O: "OraclePlan", ktype, l, x, y, sigma2=1.0, nthreads=0):
+    """(f, df/dl, df/dsigma2), dX (n x dim) of f = sum_r y_r^T K x_r for the
+    oracle's one-cloud plan, tree and boxes fixed."""
+    x = np.asfortranarray(x, dtype=np.float64)
+    y = np.asfortranarray(y, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1, order="F")
+        y = y.reshape(-1, 1, order="F")
+    vals = np.zeros(3)
+    dX = np.zeros((O.Pr.shape[1], O.dim))
+    load().oracle_adjoint(O._h, int(ktype), float(l), float(sigma2), _d(x), _d(y), x.shape[1],
+                          _d(vals), _d(dX), int(nthreads))
+    return vals, dX
 
 
 def dense_matvec(ktype, l, Pr, Pc, x, c=1.0, sigma2=1.0, nthreads=0):

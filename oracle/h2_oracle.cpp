@@ -353,6 +353,19 @@ KernelFn make_kernel(int type, Scalar l, Scalar c) {
     case 7: return [l, c](Scalar r) { return std::sqrt((r / l) * (r / l) + c * c); };
     case 8: return [l](Scalar r) { return r / l; };
     case 9: return [l](Scalar r) { return (r / l) * (r / l) * (r / l); };
+    // length-scale derivatives dk/dl of kernels 0..3
+    case 10: return [l](Scalar r) { return r / (l * l) * std::exp(-r / l); };
+    case 11:
+      return [l](Scalar r) {
+        const Scalar a = std::sqrt(3.) / l;
+        return a * a * r * r / l * std::exp(-a * r);
+      };
+    case 12:
+      return [l](Scalar r) {
+        const Scalar a = std::sqrt(5.) / l;
+        return a * a * r * r / (3. * l) * (1. + a * r) * std::exp(-a * r);
+      };
+    case 13: return [l](Scalar r) { return r * r / (l * l * l) * std::exp(-0.5 * r * r / (l * l)); };
   }
   return [](Scalar) { return std::numeric_limits<Scalar>::quiet_NaN(); };
 }
@@ -595,15 +608,29 @@ double oracle_check_transfer(void* h) {
 // bucket_stride > 1 processes only every bucket_stride-th column bucket
 // (a bounded sample for timing); work[0..1] receive the dense pairs and the
 // interpolated pairs (q^2 per low-rank block) processed.
+static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
+                        const double* x, int R, double* y, int bucket_stride, double* work,
+                        std::vector<Mat>* leaf_expansions);
+
 void oracle_action(void* h, int ktype, double l, double c, double sigma2,
                    const double* x, int R, double* y, int bucket_stride,
                    int nthreads, double* work) {
-  OPlan* P = static_cast<OPlan*>(h);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
   (void)nthreads;
 #endif
+  action_impl(static_cast<OPlan*>(h), ktype, l, c, sigma2, x, R, y, bucket_stride, work,
+              nullptr);
+}
+
+}  // extern "C"
+
+// the action; optionally returns the row-cluster expansions after the
+// downward pass (at the leaves: what V^T multiplies)
+static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
+                        const double* x, int R, double* y, int bucket_stride, double* work,
+                        std::vector<Mat>* leaf_expansions) {
   const KernelFn kern = make_kernel(ktype, l, c);
   const Index dim = P->dim;
   const int nr = (int)P->rt.root.size, nc = (int)P->ct.root.size;
@@ -666,6 +693,135 @@ void oracle_action(void* h, int ktype, double l, double c, double sigma2,
     work[0] = dense_pairs;
     work[1] = lr_pairs;
   }
+  if (leaf_expansions) *leaf_expansions = std::move(tlhs);
+}
+
+namespace {
+// Lagrange basis of the nodes xi in product form and its derivative:
+// l_a(x) = prod_{b != a} (x - xi_b) / (xi_a - xi_b),
+// l_a'(x) = sum_{m != a} 1 / (xi_a - xi_m) prod_{b != a, m} (x - xi_b) / (xi_a - xi_b)
+void lagrange_product(const std::vector<Scalar>& xi, Scalar x, Scalar* f, Scalar* df) {
+  const int n = (int)xi.size();
+  for (int a = 0; a < n; ++a) {
+    Scalar v = 1, dv = 0;
+    for (int b = 0; b < n; ++b)
+      if (b != a) v *= (x - xi[b]) / (xi[a] - xi[b]);
+    for (int m = 0; m < n; ++m) {
+      if (m == a) continue;
+      Scalar t = 1. / (xi[a] - xi[m]);
+      for (int b = 0; b < n; ++b)
+        if (b != a && b != m) t *= (x - xi[b]) / (xi[a] - xi[b]);
+      dv += t;
+    }
+    f[a] = v;
+    df[a] = dv;
+  }
+}
+
+// k'(r) / r of kernels 0..3
+Scalar kernel_grad_over_r(int ktype, Scalar l, Scalar r) {
+  if (r <= 0) return 0;
+  switch (ktype) {
+    case 0: return -std::exp(-r / l) / (l * r);
+    case 1: {
+      const Scalar a = std::sqrt(3.) / l;
+      return -a * a * std::exp(-a * r);
+    }
+    case 2: {
+      const Scalar a = std::sqrt(5.) / l;
+      return -(a * a / 3.) * (1. + a * r) * std::exp(-a * r);
+    }
+    case 3: return -std::exp(-0.5 * r * r / (l * l)) / (l * l);
+  }
+  return std::numeric_limits<Scalar>::quiet_NaN();
+}
+}  // namespace
+
+extern "C" {
+
+// Gradients of f = sum_r y_r^T K x_r, K = sigma2 H2[k], tree and boxes fixed,
+// for one point cloud: values = (f, df/dl, df/dsigma2), dX (n x dim,
+// row-major, natural order).  Kernels 0..3.
+void oracle_adjoint(void* h, int ktype, double l, double sigma2, const double* x,
+                    const double* y, int R, double* values, double* dX, int nthreads) {
+  OPlan* P = static_cast<OPlan*>(h);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  const int n = (int)P->rt.root.size, dim = (int)P->dim, q = P->ip.q();
+  std::vector<Scalar> z((size_t)n * R);
+  std::vector<Mat> Ux, Uy;
+  action_impl(P, ktype, l, 1., 1., x, R, z.data(), 1, nullptr, &Ux);
+  Scalar f1 = 0;
+  for (size_t e = 0; e < z.size(); ++e) f1 += y[e] * z[e];
+  action_impl(P, ktype + 10, l, 1., 1., x, R, z.data(), 1, nullptr, nullptr);
+  Scalar fl = 0;
+  for (size_t e = 0; e < z.size(); ++e) fl += y[e] * z[e];
+  values[0] = sigma2 * f1;
+  values[1] = sigma2 * fl;
+  values[2] = f1;
+  action_impl(P, ktype, l, 1., 1., y, R, z.data(), 1, nullptr, &Uy);
+  std::vector<Scalar> G((size_t)n * dim, 0.);
+  const Scalar* X = P->Pr.data();
+  const std::vector<Index>& idx = P->rt.indices;
+  // near field: both sides of every dense pair
+  for (const Block& b : P->blocks) {
+    if (b.low_rank) continue;
+    for (Index i = 0; i < b.row->size; ++i)
+      for (Index j = 0; j < b.col->size; ++j) {
+        const Index pi = idx[b.row->begin + i], pj = P->ct.indices[b.col->begin + j];
+        Scalar cij = 0;
+        for (int r = 0; r < R; ++r) cij += y[(size_t)r * n + pi] * x[(size_t)r * n + pj];
+        const Scalar g = kernel_grad_over_r(ktype, l, dist(X + (size_t)pi * dim,
+                                                              X + (size_t)pj * dim, dim));
+        for (int d = 0; d < dim; ++d) {
+          const Scalar diff = X[(size_t)pi * dim + d] - X[(size_t)pj * dim + d];
+          G[(size_t)pi * dim + d] += cij * g * diff;
+          G[(size_t)pj * dim + d] -= cij * g * diff;
+        }
+      }
+  }
+  // far field: gradients of the leaf bases against the leaf expansions
+  std::vector<Scalar> f((size_t)dim * (P->ip.deg + 1)), df(f.size());
+  const int p1 = (int)P->ip.deg + 1;
+  for (Node* nd : P->rt.by_id) {
+    if (nd->sons.size()) continue;
+    const Mat& ux = Ux[nd->block_id];
+    const Mat& uy = Uy[nd->block_id];
+    for (Index i = 0; i < nd->size; ++i) {
+      const Index pi = idx[nd->begin + i];
+      for (int d = 0; d < dim; ++d)
+        lagrange_product(P->ip.xi, (X[(size_t)pi * dim + d] - nd->bmin[d]) / nd->bext[d],
+                         &f[(size_t)d * p1], &df[(size_t)d * p1]);
+      for (int k = 0; k < q; ++k) {
+        Scalar hx = 0, hy = 0;
+        for (int r = 0; r < R; ++r) {
+          hx += ux(k, r) * y[(size_t)r * n + pi];
+          hy += uy(k, r) * x[(size_t)r * n + pi];
+        }
+        for (int d = 0; d < dim; ++d) {
+          Scalar gv = df[(size_t)d * p1 + P->ip.idcs[k][d]] / nd->bext[d];
+          for (int e = 0; e < dim; ++e)
+            if (e != d) gv *= f[(size_t)e * p1 + P->ip.idcs[k][e]];
+          G[(size_t)pi * dim + d] += (hx + hy) * gv;
+        }
+      }
+    }
+  }
+  for (size_t e = 0; e < G.size(); ++e) dX[e] = sigma2 * G[e];
+}
+
+// moves the points of a one-cloud plan (dim x n, natural order) keeping the
+// tree, boxes, transfer matrices and blocks; the leaf bases are recomputed
+void oracle_update_points(void* h, const double* Pnew) {
+  OPlan* P = static_cast<OPlan*>(h);
+  std::copy(Pnew, Pnew + P->Pr.size(), P->Pr.begin());
+  std::copy(Pnew, Pnew + P->Pc.size(), P->Pc.begin());
+  for (Tree* t : {&P->rt, &P->ct})
+    for (Node* nd : t->by_id)
+      if (!nd->sons.size()) nd->V = t->moments(*nd, P->ip);
 }
 
 // y = sigma2 * K(Pr, Pc) x  (dense FP64, CovarianceKernel::eval times x)

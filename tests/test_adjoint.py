@@ -1,0 +1,194 @@
+"""Adjoint of the H2 product: gradients of f = sum_r y_r^T K x_r with respect
+to the length scale, the variance and the point coordinates (tree, boxes and
+interpolation nodes fixed).
+
+CPU: the oracle's adjoint against central finite differences of the
+oracle's own FP64 product with the points moved inside the frozen structure
+(1e-6), against finite differences in l, and against dense FP64 torch
+autograd up to the compression error.
+GPU: the CUDA adjoint against the oracle (FP64: 1e-10), against central
+finite differences (h = 1e-4) of the GPU FP64 product with frozen structure
+(1e-6), and in FP32 / mixed precision against the FP64 oracle (1e-5 for the
+values, 1e-4 for the point gradient)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err, sphere_cloud, uniform_cloud
+
+KNAMES = ["EXPONENTIAL", "MATERN32", "MATERN52", "GAUSSIAN"]
+
+
+def _problem(n=1500, R=3, seed=0, sphere=False):
+    P = sphere_cloud(n, seed) if sphere else uniform_cloud(n, 3, seed)
+    rng = np.random.default_rng(seed + 100)
+    return P, rng.standard_normal((n, R)), rng.standard_normal((n, R))
+
+
+@pytest.mark.parametrize("kt", range(4))
+def test_oracle_adjoint_against_dense_autograd(kt):
+    # dense FP64 torch autograd of y^T K(l, sigma2, X) x; the H2 gradient
+    # differs by the compression error (p = 3, with far blocks present)
+    torch = pytest.importorskip("torch")
+    from fmca_gb300.autograd import dense_reference
+    P, x, y = _problem(3000, 2, seed=kt)
+    l, s2 = 0.4, 1.3
+    O = oracle.OraclePlan(P, None, 3, 0.8, 16)
+    assert O.n_far > 0
+    vals, dX = oracle.adjoint(O, kt, l, x, y, sigma2=s2)
+    Xt = torch.tensor(P, requires_grad=True)
+    lt = torch.tensor(l, requires_grad=True, dtype=torch.float64)
+    st = torch.tensor(s2, requires_grad=True, dtype=torch.float64)
+    f = (torch.tensor(y) * dense_reference(KNAMES[kt], lt, st, Xt, torch.tensor(x))).sum()
+    f.backward()
+    assert abs(vals[0] - f.item()) / abs(f.item()) < 1e-3
+    assert abs(vals[1] - lt.grad.item()) / abs(lt.grad.item()) < 2e-3
+    assert abs(vals[2] - st.grad.item()) / abs(st.grad.item()) < 1e-3
+    assert rel_err(dX, Xt.grad.numpy().T) < 5e-3
+
+
+@pytest.mark.parametrize("kt", range(4))
+def test_oracle_adjoint_against_finite_differences(kt):
+    # central differences of the oracle's own H2 product with the points
+    # moved inside the frozen structure (about 4000 far blocks)
+    P, x, y = _problem(6000, 2, seed=kt + 20)
+    O = oracle.OraclePlan(P, None, 2, 0.8, 0)
+    assert O.n_far > 1000
+    vals, dX = oracle.adjoint(O, kt, 0.3, x, y, sigma2=1.2)
+    rng = np.random.default_rng(kt)
+    h = 1e-5
+    for _ in range(4):
+        i, d = int(rng.integers(0, 6000)), int(rng.integers(0, 3))
+        Pp, Pm = P.copy(), P.copy()
+        Pp[d, i] += h
+        Pm[d, i] -= h
+        O.update_points(Pp)
+        fp = np.sum(y * O.action(kt, 0.3, x, sigma2=1.2)[0])
+        O.update_points(Pm)
+        fm = np.sum(y * O.action(kt, 0.3, x, sigma2=1.2)[0])
+        O.update_points(P)
+        fd = (fp - fm) / (2 * h)
+        assert abs(dX[i, d] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, d)
+
+
+def test_oracle_dl_against_finite_differences():
+    P, x, y = _problem(1500, 2, seed=7)
+    O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+    vals, _ = oracle.adjoint(O, 1, 0.3, x, y, sigma2=1.0)
+    h = 1e-4 * 0.3
+    fp, _ = O.action(1, 0.3 + h, x)
+    fm, _ = O.action(1, 0.3 - h, x)
+    fd = (np.sum(y * fp) - np.sum(y * fm)) / (2 * h)
+    assert abs(vals[1] - fd) / abs(fd) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kname", KNAMES)
+def test_gpu_adjoint_against_oracle(cuda_device, kname):
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    kt = KNAMES.index(kname)
+    P, x, y = _problem(6000, 4, seed=kt + 3)
+    l, s2 = 0.35, 0.8
+    O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+    assert O.n_far > 1000
+    vals_ref, dX_ref = oracle.adjoint(O, kt, l, x, y, sigma2=s2)
+    H = H2Matrix(CovarianceKernel(kname, l, sigma2=s2), P, P, 3, 0.8)
+    xt = torch.tensor(x, device=cuda_device)
+    yt = torch.tensor(y, device=cuda_device)
+    out = H.adjoint(xt, yt, precision="fp64", want_Kx=True, want_Ky=True)
+    vals = out["values"].cpu().numpy()
+    assert np.allclose(vals, vals_ref, rtol=1e-10, atol=0)
+    assert rel_err(out["dX"].cpu().numpy(), dX_ref) < 1e-10
+    Kx_ref, _ = O.action(kt, l, x, sigma2=s2)
+    Ky_ref, _ = O.action(kt, l, y, sigma2=s2)
+    assert rel_err(out["Kx"].cpu().numpy(), Kx_ref) < 1e-12
+    assert rel_err(out["Ky"].cpu().numpy(), Ky_ref) < 1e-12
+    # the lower precisions against the FP64 adjoint
+    for prec in ("fp32", "mixed"):
+        o = H.adjoint(xt, yt, precision=prec)
+        v = o["values"].cpu().numpy()
+        assert np.allclose(v, vals_ref, rtol=1e-5, atol=0), prec
+        assert rel_err(o["dX"].cpu().numpy(), dX_ref) < 1e-4, prec
+    H.check_device_error()
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_mixed_tensor_core_path(cuda_device):
+    # 24 right-hand sides: the mixed products run on the tensor cores
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    P, x, y = _problem(8000, 24, seed=11, sphere=True)
+    O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+    assert O.n_far > 1000
+    vals_ref, dX_ref = oracle.adjoint(O, 2, 0.3, x, y, sigma2=1.0)
+    H = H2Matrix(CovarianceKernel("MATERN52", 0.3), P, P, 3, 0.8)
+    out = H.adjoint(torch.tensor(x, device=cuda_device), torch.tensor(y, device=cuda_device),
+                    precision="mixed")
+    assert np.allclose(out["values"].cpu().numpy(), vals_ref, rtol=1e-5, atol=0)
+    assert rel_err(out["dX"].cpu().numpy(), dX_ref) < 1e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kname", ["MATERN32", "MATERN52", "GAUSSIAN"])
+def test_gpu_adjoint_against_finite_differences(cuda_device, kname):
+    # central differences (h = 1e-4) of the GPU FP64 product with the tree,
+    # boxes and nodes frozen
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    P, x, y = _problem(6000, 2, seed=5)
+    l = 0.3
+    H = H2Matrix(CovarianceKernel(kname, l), P, P, 2, 0.8, precision="fp64")
+    assert H.info["far_blocks"] > 1000
+    xt = torch.tensor(x, device=cuda_device)
+    yt = torch.tensor(y, device=cuda_device)
+    out = H.adjoint(xt, yt)
+    vals = out["values"].cpu().numpy()
+    dX = out["dX"].cpu().numpy()
+
+    def f(cov_l=l, P_=None):
+        if P_ is not None:
+            H.update_points(P_)
+        H.cov.l = cov_l
+        v = float((yt * H.matvec(xt)).sum())
+        H.cov.l = l
+        return v
+
+    h = 1e-4
+    fd_l = (f(l * (1 + h)) - f(l * (1 - h))) / (2 * l * h)
+    assert abs(vals[1] - fd_l) / abs(fd_l) < 1e-6
+    rng = np.random.default_rng(1)
+    for _ in range(4):
+        i, d = int(rng.integers(0, 6000)), int(rng.integers(0, 3))
+        Pp, Pm = P.copy(), P.copy()
+        Pp[d, i] += h
+        Pm[d, i] -= h
+        fd = (f(P_=Pp) - f(P_=Pm)) / (2 * h)
+        H.update_points(P)
+        assert abs(dX[i, d] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, d, dX[i, d], fd)
+
+
+@pytest.mark.gpu
+def test_autograd_function(cuda_device):
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    from fmca_gb300.autograd import h2_matvec
+    P, x, y = _problem(5000, 3, seed=9)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.4), P, P, 3, 0.8, precision="fp64")
+    xt = torch.tensor(x, device=cuda_device, requires_grad=True)
+    lt = torch.tensor(0.4, dtype=torch.float64, requires_grad=True)
+    st = torch.tensor(1.5, dtype=torch.float64, requires_grad=True)
+    Xt = torch.tensor(P, requires_grad=True)
+    yt = torch.tensor(y, device=cuda_device)
+    f = (yt * h2_matvec(H, xt, lt, st, Xt)).sum()
+    f.backward()
+    O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+    vals_ref, dX_ref = oracle.adjoint(O, 1, 0.4, x, y, sigma2=1.5)
+    assert abs(f.item() - vals_ref[0]) / abs(vals_ref[0]) < 1e-12
+    assert abs(lt.grad.item() - vals_ref[1]) / abs(vals_ref[1]) < 1e-10
+    assert abs(st.grad.item() - vals_ref[2]) / abs(vals_ref[2]) < 1e-10
+    assert rel_err(Xt.grad.numpy(), dX_ref.T) < 1e-10
+    Ky_ref, _ = O.action(1, 0.4, y, sigma2=1.5)
+    assert rel_err(xt.grad.cpu().numpy(), Ky_ref) < 1e-12

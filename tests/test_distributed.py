@@ -44,6 +44,9 @@ def _worker(rank, world, port, q):
 
 def test_replicas_max_over_ranks_gloo():
     import torch.multiprocessing as mp
+
+    from oracle import build as oracle_build
+    oracle_build.build()  # once, before the workers load it
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
