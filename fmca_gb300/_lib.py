@@ -47,6 +47,8 @@ EXPORTED = [
     "fmca_matvec_host", "fmca_plan_check_device_error", "fmca_kernel_eval",
     "fmca_plan_set_profiling", "fmca_plan_profile", "fmca_matvec_static_scratch",
     "fmca_matvec_adjoint_workspace_size", "fmca_matvec_adjoint", "fmca_plan_update_points",
+    "fmca_plan_create_batched", "fmca_matvec_graph_create", "fmca_graph_launch",
+    "fmca_graph_destroy",
 ]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
@@ -103,6 +105,13 @@ def load() -> C.CDLL:
                                         vp, i64, i64, vp, vp, i64, i64, vp, vp, vp, C.c_size_t,
                                         vp]
     lib.fmca_plan_update_points.argtypes = [vp, dp, dp]
+    lib.fmca_plan_create_batched.argtypes = [C.POINTER(dp), C.POINTER(C.c_int64), i32, i32,
+                                             i32, C.c_double, i64, C.POINTER(vp)]
+    lib.fmca_matvec_graph_create.argtypes = [vp, C.POINTER(KernelDesc), i32, i32, i32, i32,
+                                             vp, i64, i64, vp, i64, i64, vp, C.c_size_t,
+                                             C.POINTER(vp)]
+    lib.fmca_graph_launch.argtypes = [vp, vp]
+    lib.fmca_graph_destroy.argtypes = [vp]
     lib.fmca_plan_set_profiling.argtypes = [vp, i32]
     lib.fmca_plan_profile.argtypes = [vp, dp, C.POINTER(C.c_int64)]
     for name in EXPORTED:

@@ -1,11 +1,15 @@
 // extern "C" boundary of fmca_gb300 (declared in include/fmca_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "../../include/fmca_gb300.h"
 #include "c_api_internal.h"
@@ -133,6 +137,54 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
     p->min_leaf = min_leaf;
     p->plan.build(P_rows, (uint32_t)n_rows, same ? P_rows : P_cols,
                   (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same);
+    *out = p;
+  } catch (const std::bad_alloc&) {
+    return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
+  } catch (const std::exception& e) {
+    return fail(FMCA_ERR_INTERNAL, e.what());
+  }
+  return ok();
+}
+
+fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_points,
+                                     int count, int dim, int degree, double eta,
+                                     int64_t min_leaf, fmca_plan** out) {
+  if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!P || !n_points || count < 1)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "need at least one point cloud");
+  if (dim < 1 || degree < 0 || degree > 16 || !(eta >= 0) || !std::isfinite(eta) ||
+      min_leaf < 0 || min_leaf > (int64_t)0x7FFFFFFF)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "bad dim, degree, eta or min_leaf");
+  int64_t total = 0;
+  for (int i = 0; i < count; ++i) {
+    if (!P[i] || n_points[i] < 1)
+      return fail(FMCA_ERR_INVALID_ARGUMENT, "empty point cloud " + std::to_string(i));
+    total += n_points[i];
+    for (int64_t e = 0; e < (int64_t)dim * n_points[i]; ++e)
+      if (!std::isfinite(P[i][e]))
+        return fail(FMCA_ERR_INVALID_ARGUMENT,
+                    "point cloud " + std::to_string(i) + " holds a non-finite value");
+  }
+  if (total > (int64_t)0xFFFFFFFEll)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "too many points in total");
+  try {
+    std::vector<fmca::Plan> parts(count);
+    std::atomic<int> next(0);
+    const int nth = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nth; ++t)
+      pool.emplace_back([&]() {
+        for (int i = next++; i < count; i = next++)
+          parts[i].build(P[i], (uint32_t)n_points[i], P[i], (uint32_t)n_points[i], dim,
+                         degree, eta, (uint32_t)min_leaf, true);
+      });
+    for (auto& th : pool) th.join();
+    std::vector<const fmca::Plan*> ptrs;
+    for (auto& p : parts) ptrs.push_back(&p);
+    fmca_plan* p = new fmca_plan();
+    p->min_leaf = min_leaf;
+    p->plan.merge(ptrs);
     *out = p;
   } catch (const std::bad_alloc&) {
     return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
@@ -354,6 +406,88 @@ fmca_status fmca_plan_update_points(fmca_plan* p, const double* P_rows, const do
   std::string err;
   int st = fmca::gpu::update_points(P, p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+}  // extern "C"
+
+struct fmca_graph {
+  cudaGraphExec_t exec = nullptr;
+  void* own_ws = nullptr;
+  int device = -1;
+};
+
+extern "C" {
+
+fmca_status fmca_matvec_graph_create(fmca_plan* p, const fmca_kernel_desc* kernel,
+                                     int precision, int dtype, int order, int nrhs,
+                                     const void* x, int64_t x_stride_i, int64_t x_stride_r,
+                                     void* y, int64_t y_stride_i, int64_t y_stride_r,
+                                     void* workspace, size_t workspace_bytes,
+                                     fmca_graph** out) {
+  if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  fmca_status s =
+      fmca::capi::check_matvec_args(p, kernel, precision, dtype, order, nrhs, x, y);
+  if (s != FMCA_OK) return s;
+  fmca_graph* g = new fmca_graph();
+  cudaGetDevice(&g->device);
+  cudaStream_t st = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e;
+  auto cleanup = [&](fmca_status code, const std::string& msg) {
+    if (graph) cudaGraphDestroy(graph);
+    if (st) cudaStreamDestroy(st);
+    if (g->own_ws) cudaFree(g->own_ws);
+    delete g;
+    return fail(code, msg);
+  };
+  if (!workspace) {
+    workspace_bytes = fmca::gpu::workspace_bytes(p->plan, precision, nrhs);
+    if ((e = cudaMalloc(&g->own_ws, workspace_bytes)) != cudaSuccess)
+      return cleanup(FMCA_ERR_OUT_OF_MEMORY, cudaGetErrorString(e));
+    workspace = g->own_ws;
+  }
+  if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess)
+    return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  // one ordinary run first: uploads the plan and sets kernel attributes
+  s = fmca_matvec(p, kernel, precision, dtype, order, nrhs, x, x_stride_i, x_stride_r, y,
+                  y_stride_i, y_stride_r, workspace, workspace_bytes, st);
+  if (s != FMCA_OK) return cleanup(s, fmca_last_error());
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  const bool prof = p->profile;
+  p->profile = false;
+  if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+    p->profile = prof;
+    return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  }
+  s = fmca_matvec(p, kernel, precision, dtype, order, nrhs, x, x_stride_i, x_stride_r, y,
+                  y_stride_i, y_stride_r, workspace, workspace_bytes, st);
+  e = cudaStreamEndCapture(st, &graph);
+  p->profile = prof;
+  if (s != FMCA_OK) return cleanup(s, fmca_last_error());
+  if (e != cudaSuccess) return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = cudaGraphInstantiate(&g->exec, graph, 0)) != cudaSuccess)
+    return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  cudaGraphDestroy(graph);
+  cudaStreamDestroy(st);
+  *out = g;
+  return ok();
+}
+
+fmca_status fmca_graph_launch(fmca_graph* g, void* stream) {
+  if (!g || !g->exec) return fail(FMCA_ERR_INVALID_ARGUMENT, "graph is NULL");
+  cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(FMCA_ERR_CUDA, cudaGetErrorString(e));
+  return ok();
+}
+
+fmca_status fmca_graph_destroy(fmca_graph* g) {
+  if (!g) return ok();
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->own_ws) cudaFree(g->own_ws);
+  delete g;
   return ok();
 }
 

@@ -2,7 +2,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/fmca_gb300.h"
@@ -260,27 +262,29 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
   FMCA_TRY(to_device(dp, plan.col_leaves.data(), plan.col_leaves.size(), &dp->leaves_c, err));
   dp->nleaves_r = (int)plan.row_leaves.size();
   dp->nleaves_c = (int)plan.col_leaves.size();
-  // transfer level lists
-  {
-    const Tree& t = plan.cols;
-    std::vector<int32_t> lst;
-    dp->m2m_ptr.assign(t.nlevels() + 1, 0);
-    for (int l = 0; l < t.nlevels(); ++l) {
-      for (int c = t.level_ptr[l]; c < t.level_ptr[l + 1]; ++c)
-        if (t.nsons[c]) lst.push_back(c);
-      dp->m2m_ptr[l + 1] = (int)lst.size();
+  // transfer level lists, bucketed by level (a batched plan holds a forest
+  // whose clusters of one level are not contiguous)
+  auto by_level = [](const Tree& t, bool up, std::vector<int32_t>* lst, std::vector<int>* ptr) {
+    const int L = t.nlevels();
+    std::vector<std::vector<int32_t>> b(L);
+    for (int c = 0; c < t.nclusters(); ++c) {
+      if (up ? t.nsons[c] > 0 : t.level[c] >= 1) b[t.level[c]].push_back(c);
     }
+    ptr->assign(L + 1, 0);
+    lst->clear();
+    for (int l = 0; l < L; ++l) {
+      lst->insert(lst->end(), b[l].begin(), b[l].end());
+      (*ptr)[l + 1] = (int)lst->size();
+    }
+  };
+  {
+    std::vector<int32_t> lst;
+    by_level(plan.cols, true, &lst, &dp->m2m_ptr);
     FMCA_TRY(to_device(dp, lst.data(), lst.size(), &dp->m2m_list, err));
   }
   {
-    const Tree& t = plan.rows;
     std::vector<int32_t> lst;
-    dp->l2l_ptr.assign(t.nlevels() + 1, 0);
-    for (int l = 0; l < t.nlevels(); ++l) {
-      if (l >= 1)
-        for (int c = t.level_ptr[l]; c < t.level_ptr[l + 1]; ++c) lst.push_back(c);
-      dp->l2l_ptr[l + 1] = (int)lst.size();
-    }
+    by_level(plan.rows, false, &lst, &dp->l2l_ptr);
     FMCA_TRY(to_device(dp, lst.data(), lst.size(), &dp->l2l_list, err));
   }
   // far groups: targets = nodes of every row cluster, sources = node ranges
@@ -423,11 +427,21 @@ double output_scale(const KernelDesc& k) {
   return k.type >= K_DL_EXPONENTIAL ? k.sigma2 / k.l : k.sigma2;
 }
 
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device):
+// later calls (for instance inside a stream capture) make no runtime call.
 template <typename K>
 void ensure_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)bytes);
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[{reinterpret_cast<const void*>(kern), dev}];
+  if (cur >= bytes) return;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+      cudaSuccess)
+    cur = bytes;
 }
 
 template <typename T, int KT, int TPT, int RB>

@@ -507,6 +507,79 @@ void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
   }
 }
 
+namespace {
+// appends tree b to a with cluster ids offset by a's cluster count and point
+// indices by a's point count
+void append_tree(Tree* a, const Tree& b) {
+  const int32_t co = a->nclusters();
+  const uint32_t po = a->n;
+  a->dim = b.dim;
+  for (uint32_t v : b.perm) a->perm.push_back(v + po);
+  for (int c = 0; c < b.nclusters(); ++c) {
+    a->begin.push_back(b.begin[c] + po);
+    a->size.push_back(b.size[c]);
+    a->level.push_back(b.level[c]);
+    a->parent.push_back(b.parent[c] >= 0 ? b.parent[c] + co : -1);
+    a->son0.push_back(b.son0[c] >= 0 ? b.son0[c] + co : -1);
+    a->nsons.push_back(b.nsons[c]);
+  }
+  a->bbmin.insert(a->bbmin.end(), b.bbmin.begin(), b.bbmin.end());
+  a->bbmax.insert(a->bbmax.end(), b.bbmax.begin(), b.bbmax.end());
+  a->bbext.insert(a->bbext.end(), b.bbext.begin(), b.bbext.end());
+  const size_t L = std::max(a->level_ptr.size(), b.level_ptr.size());
+  a->level_ptr.assign(L, 0);  // only the number of levels is meaningful
+  a->n += b.n;
+}
+}  // namespace
+
+void Plan::merge(const std::vector<const Plan*>& parts) {
+  *this = Plan();
+  if (parts.empty()) return;
+  interp = parts[0]->interp;
+  eta = parts[0]->eta;
+  same_tree = true;
+  cloud_offsets.assign(1, 0);
+  const int dim = interp.dim;
+  const int q = interp.q;
+  pat.far_ptr.assign(1, 0);
+  pat.near_ptr.assign(1, 0);
+  for (const Plan* p : parts) {
+    same_tree = same_tree && p->same_tree;
+    const int32_t rco = rows.nclusters(), cco = cols.nclusters();
+    const uint32_t rpo = rows.n, cpo = cols.n;
+    // block lists
+    for (size_t b = 0; b < p->pat.far_row.size(); ++b) {
+      pat.far_row.push_back(p->pat.far_row[b] + rco);
+      pat.far_col.push_back(p->pat.far_col[b] + cco);
+    }
+    for (size_t b = 0; b < p->pat.near_row.size(); ++b) {
+      pat.near_row.push_back(p->pat.near_row[b] + rco);
+      pat.near_col.push_back(p->pat.near_col[b] + cco);
+    }
+    const int32_t fo = (int32_t)pat.far_idx.size();
+    for (int c = 0; c < p->rows.nclusters(); ++c) pat.far_ptr.push_back(p->pat.far_ptr[c + 1] + fo);
+    for (int32_t v : p->pat.far_idx) pat.far_idx.push_back(v + cco);
+    const int32_t io = (int32_t)(pat.near_ivl.size() / 2);
+    for (size_t l = 0; l + 1 < p->pat.near_ptr.size(); ++l)
+      pat.near_ptr.push_back(p->pat.near_ptr[l + 1] + io);
+    for (uint32_t v : p->pat.near_ivl) pat.near_ivl.push_back(v + cpo);
+    pat.near_pairs += p->pat.near_pairs;
+    for (int32_t c : p->row_leaves) row_leaves.push_back(c + rco);
+    for (int32_t c : p->col_leaves) col_leaves.push_back(c + cco);
+    row_E.insert(row_E.end(), p->row_E.begin(), p->row_E.end());
+    col_E.insert(col_E.end(), p->col_E.begin(), p->col_E.end());
+    row_nodes.insert(row_nodes.end(), p->row_nodes.begin(), p->row_nodes.end());
+    col_nodes.insert(col_nodes.end(), p->col_nodes.begin(), p->col_nodes.end());
+    points_r.insert(points_r.end(), p->points_r.begin(), p->points_r.end());
+    points_c.insert(points_c.end(), p->points_c.begin(), p->points_c.end());
+    append_tree(&rows, p->rows);
+    append_tree(&cols, p->cols);
+    cloud_offsets.push_back(rows.n);
+  }
+  (void)dim;
+  (void)q;
+}
+
 void Plan::statistics(double out[6]) const {
   size_t mem = 0;
   const uint32_t qq = (uint32_t)interp.q * (uint32_t)interp.q;

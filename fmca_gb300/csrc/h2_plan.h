@@ -125,6 +125,13 @@ struct Plan {
 
   void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
              int dim, int deg, double eta, uint32_t min_leaf, bool same);
+  // Block-diagonal plan of independent point clouds: trees, bases and block
+  // lists of the parts concatenated (cluster ids, point indices and node
+  // indices offset), so one launch per stage covers every cloud.  The parts
+  // must share dim and degree.  cloud_offsets receives the first point of
+  // every part (count + 1 entries).
+  void merge(const std::vector<const Plan*>& parts);
+  std::vector<int64_t> cloud_offsets;
   // (m, n, #low-rank blocks, #dense blocks, nz per row, GB)
   // exactly like H2MatrixBase::statistics (H2MatrixBase.h:70-105)
   void statistics(double out[6]) const;

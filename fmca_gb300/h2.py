@@ -105,6 +105,40 @@ class H2Matrix:
         self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
         self._ws = {}
 
+    @classmethod
+    def batched(cls, cov: CovarianceKernel, clouds, p: int = 3, eta: float = 0.8,
+                min_leaf: int = 0, precision: str = "mixed") -> "H2Matrix":
+        """Block-diagonal H2 matrix of independent point clouds (each dim x n_i).
+
+        Right-hand sides are the clouds' vectors stacked in cloud order;
+        ``offsets[i]`` is the first row of cloud i.  Every stage of a matvec
+        covers all clouds with one kernel launch."""
+        lib = _lib.load()
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
+        arrs = [np.asfortranarray(P, dtype=np.float64) for P in clouds]
+        if not arrs or any(a.ndim != 2 or a.shape[0] != arrs[0].shape[0] for a in arrs):
+            raise ValueError("clouds must be dim x n arrays of one dim")
+        self = cls.__new__(cls)
+        self.cov, self.p, self.eta, self.precision = cov, int(p), float(eta), precision
+        self.dim = arrs[0].shape[0]
+        ptrs = (C.POINTER(C.c_double) * len(arrs))(*[_dptr(a) for a in arrs])
+        ns = (C.c_int64 * len(arrs))(*[a.shape[1] for a in arrs])
+        handle = C.c_void_p()
+        check(lib.fmca_plan_create_batched(ptrs, ns, len(arrs), self.dim, self.p, self.eta,
+                                           int(min_leaf), C.byref(handle)))
+        self._h = handle
+        info = (C.c_int64 * _lib.INFO_COUNT)()
+        check(lib.fmca_plan_info(self._h, info))
+        self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
+        self._ws = {}
+        self.offsets = np.concatenate([[0], np.cumsum([a.shape[1] for a in arrs])])
+        return self
+
+    def graph(self, x, y, precision: Optional[str] = None) -> "MatvecGraph":
+        """Records y = K x for these CUDA tensors into a CUDA graph."""
+        return MatvecGraph(self, x, y, precision or self.precision)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -329,3 +363,42 @@ class H2Matrix:
 
     def check_device_error(self) -> None:
         check(_lib.load().fmca_plan_check_device_error(self._h))
+
+
+class MatvecGraph:
+    """A matvec recorded into a CUDA graph (fmca_matvec_graph_create); each
+    ``launch`` replays the whole product with a single graph launch."""
+
+    def __init__(self, H: H2Matrix, x, y, precision: str):
+        import torch
+        if not (x.is_cuda and y.is_cuda) or x.dtype != y.dtype:
+            raise ValueError("x and y must be CUDA tensors of one dtype")
+        self.H, self.x, self.y = H, x, y  # keep the bound buffers alive
+        dt = _lib.DTYPE_F64 if x.dtype == torch.float64 else _lib.DTYPE_F32
+        self.ws = torch.empty(H.workspace_bytes(x.shape[1], precision), dtype=torch.uint8,
+                              device=x.device)
+        g = C.c_void_p()
+        d = H.cov.desc()
+        with torch.cuda.device(x.device):
+            check(_lib.load().fmca_matvec_graph_create(
+                H.handle, C.byref(d), _PREC[precision], dt, _lib.ORDER_NATURAL, x.shape[1],
+                C.c_void_p(x.data_ptr()), x.stride(0), x.stride(1),
+                C.c_void_p(y.data_ptr()), y.stride(0), y.stride(1),
+                C.c_void_p(self.ws.data_ptr()), self.ws.numel(), C.byref(g)))
+        self._g = g
+
+    def launch(self, stream=None):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(self.x.device)
+        check(_lib.load().fmca_graph_launch(self._g, C.c_void_p(stream.cuda_stream)))
+        return self.y
+
+    def __del__(self):
+        g = getattr(self, "_g", None)
+        if g:
+            try:
+                _lib.load().fmca_graph_destroy(g)
+            except Exception:
+                pass
+            self._g = None

@@ -146,6 +146,30 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
                              const double* P_cols, int64_t n_cols, int degree,
                              double eta, int64_t min_leaf, fmca_plan** out);
 fmca_status fmca_plan_destroy(fmca_plan* plan);
+
+/* One plan for many independent point clouds (batching): cloud i has
+   n_points[i] points P[i] (dim x n_i, column-major FP64); every cloud gets
+   its own tree and block lists exactly as fmca_plan_create would build them
+   (for P_cols = NULL), and the plan is their block-diagonal union.  A matvec
+   on it takes the clouds' right-hand sides concatenated in cloud order
+   (sum n_i rows) and runs every stage for all clouds in one launch.  No
+   counterpart in the reference (one H2Matrix per cloud there). */
+fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_points,
+                                     int count, int dim, int degree, double eta,
+                                     int64_t min_leaf, fmca_plan** out);
+
+/* A matvec recorded once into a CUDA graph and replayed with one launch.
+   The graph binds the given x, y and workspace pointers (workspace NULL: the
+   graph allocates its own).  The plan must outlive the graph. */
+typedef struct fmca_graph fmca_graph;
+fmca_status fmca_matvec_graph_create(fmca_plan* plan, const fmca_kernel_desc* kernel,
+                                     int precision, int dtype, int order, int nrhs,
+                                     const void* x, int64_t x_stride_i,
+                                     int64_t x_stride_r, void* y, int64_t y_stride_i,
+                                     int64_t y_stride_r, void* workspace,
+                                     size_t workspace_bytes, fmca_graph** out);
+fmca_status fmca_graph_launch(fmca_graph* graph, void* stream);
+fmca_status fmca_graph_destroy(fmca_graph* graph);
 fmca_status fmca_plan_info(const fmca_plan* plan, int64_t out[FMCA_INFO_COUNT]);
 /* (rows, cols, #low-rank blocks, #dense blocks, nz per row, storage GB) */
 fmca_status fmca_plan_statistics(const fmca_plan* plan, double out[6]);
