@@ -170,6 +170,190 @@ def run_reference(args):
     return 0
 
 
+def _events_ms(torch, fn, steps, flush=None):
+    """Mean device time of fn() over steps, CUDA events on the current stream."""
+    times = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return sum(times) / len(times)
+
+
+def run_c3(args, torch, dev):
+    """Batching: 64 clouds, n log-uniform in [2e3, 2e5], 3-D Gaussian mixture
+    (8 components, sigma 0.05, centres U[0,1]^3 per cloud), GAUSSIAN l = 0.2,
+    p = 3, eta = 0.8, 8 right-hand sides each, float32.  One CUDA-graph
+    launch of the batched plan against per-instance launches."""
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    rng = np.random.default_rng(0)
+    clouds = []
+    for _ in range(64):
+        n = int(np.exp(rng.uniform(np.log(2e3), np.log(2e5))))
+        centres = rng.random((8, 3))
+        comp = rng.integers(0, 8, n)
+        clouds.append((centres[comp] + 0.05 * rng.standard_normal((n, 3))).T.copy())
+    cov = CovarianceKernel("GAUSSIAN", 0.2)
+    t0 = time.perf_counter()
+    B = H2Matrix.batched(cov, clouds, 3, 0.8, precision="mixed")
+    t_plan = time.perf_counter() - t0
+    N, R = B.rows(), 8
+    X = torch.tensor(rng.standard_normal((N, R)), dtype=torch.float32, device=dev)
+    Y = torch.empty_like(X)
+    g = B.graph(X, Y)
+    for _ in range(args.warmup):
+        g.launch()
+    ms_graph = _events_ms(torch, g.launch, args.steps)
+    singles = [H2Matrix(cov, P, P, 3, 0.8, precision="mixed") for P in clouds]
+    xs = [X[B.offsets[i]:B.offsets[i + 1]] for i in range(64)]
+    ys = [torch.empty_like(x) for x in xs]
+
+    def each():
+        for S, x, y in zip(singles, xs, ys):
+            S.matvec(x, y)
+    for _ in range(args.warmup):
+        each()
+    ms_each = _events_ms(torch, each, args.steps)
+    err = max(float((torch.linalg.norm(Y[B.offsets[i]:B.offsets[i + 1]] - ys[i]) /
+                     torch.linalg.norm(ys[i])).item()) for i in range(64))
+    return {
+        "metric": "batched H2 matvecs/sec (n·RHS/s), 64 clouds, one CUDA-graph launch",
+        "value": N * R / (ms_graph * 1e-3), "unit": UNIT, "ms_per_step": ms_graph,
+        "per_instance": {"value": N * R / (ms_each * 1e-3), "ms_per_step": ms_each,
+                         "launch": "64 plans, one matvec each, back to back"},
+        "speedup_graph_vs_per_instance": ms_each / ms_graph,
+        "max_rel_diff_batched_vs_single": err, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C3: 64 clouds, n log-uniform [2e3, 2e5], Gaussian mixture, "
+                               "GAUSSIAN l=0.2, p=3, eta=0.8, R=8, float32",
+                   "total_points": int(N), "far_blocks": B.info["far_blocks"],
+                   "near_pairs": B.info["near_pairs"], "plan_build_s": t_plan},
+    }
+
+
+def run_c4(args, torch, dev):
+    """Differentiation: n = 2e5 on S^2, MATERN52 l = 0.3, sigma2 = 1, p = 4,
+    eta = 0.8, leaf 96 (125 in effect); gradient of y^T K x w.r.t. l, sigma2
+    and X, x and y ~ N(0,1) float32; FP64 adjoint, central differences
+    (h = 1e-4) and the mixed-precision adjoint."""
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    rng = np.random.default_rng(0)
+    n = 200000
+    P = rng.standard_normal((3, n))
+    P /= np.linalg.norm(P, axis=0)
+    x = rng.standard_normal((n, 1))
+    y = rng.standard_normal((n, 1))
+    H = H2Matrix(CovarianceKernel("MATERN52", 0.3, sigma2=1.0), P, P, 4, 0.8, min_leaf=96)
+    x64, y64 = torch.tensor(x, device=dev), torch.tensor(y, device=dev)
+    x32, y32 = x64.float(), y64.float()
+    ref = H.adjoint(x64, y64, precision="fp64")
+    for _ in range(args.warmup):
+        H.adjoint(x32, y32, precision="mixed")
+    ms_mixed = _events_ms(torch, lambda: H.adjoint(x32, y32, precision="mixed"), args.steps)
+    ms_fp64 = _events_ms(torch, lambda: H.adjoint(x64, y64, precision="fp64"), 2)
+    out = H.adjoint(x32, y32, precision="mixed")
+    v64 = ref["values"].cpu().numpy()
+    v32 = out["values"].cpu().numpy()
+    d64 = ref["dX"].cpu().numpy()
+    d32 = out["dX"].double().cpu().numpy()
+
+    def f(l=0.3, Pn=None):
+        if Pn is not None:
+            H.update_points(Pn)
+        H.cov.l = l
+        v = float((y64 * H.matvec(x64, precision="fp64")).sum())
+        H.cov.l = 0.3
+        return v
+    h = 1e-4
+    fd_l = (f(0.3 * (1 + h)) - f(0.3 * (1 - h))) / (2 * 0.3 * h)
+    fd_err = [abs(v64[1] - fd_l) / abs(fd_l)]
+    for _ in range(3):
+        i, d = int(rng.integers(0, n)), int(rng.integers(0, 3))
+        Pp, Pm = P.copy(), P.copy()
+        Pp[d, i] += h
+        Pm[d, i] -= h
+        fd = (f(Pn=Pp) - f(Pn=Pm)) / (2 * h)
+        H.update_points(P)
+        fd_err.append(abs(d64[i, d] - fd) / max(1.0, abs(fd)))
+    return {
+        "metric": "H2 adjoint (f, df/dl, df/dsigma2, df/dX) evaluations/sec (n·RHS/s)",
+        "value": n / (ms_mixed * 1e-3), "unit": UNIT, "ms_per_step": ms_mixed,
+        "fp64": {"ms_per_step": ms_fp64, "value": n / (ms_fp64 * 1e-3)},
+        "mixed_rel_err_vs_fp64": {"f": abs(v32[0] - v64[0]) / abs(v64[0]),
+                                  "df_dl": abs(v32[1] - v64[1]) / abs(v64[1]),
+                                  "df_dsigma2": abs(v32[2] - v64[2]) / abs(v64[2]),
+                                  "df_dX": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))},
+        "fp64_vs_central_differences_h1e-4": {"max_rel_err": max(fd_err), "checks": fd_err},
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C4: n=2e5 on S^2, MATERN52 l=0.3 sigma2=1, p=4, eta=0.8, "
+                               "leaf 96 (125 effective), x,y ~ N(0,1) float32",
+                   "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"]},
+    }
+
+
+def run_c5(args, torch, dev):
+    """Combined GP hyperparameter step: n = 2e6 in [0,1]^2 with the first
+    coordinate scaled by 4, EXPONENTIAL l = 0.1, p = 5 (36 nodes), eta = 0.6,
+    leaf 128, 64 Rademacher probes z: K z and z^T (dK/dl) z in one adjoint
+    call, mixed precision against FP64."""
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    rng = np.random.default_rng(0)
+    n = 2000000
+    P = rng.random((2, n))
+    P[0] *= 4
+    z = rng.choice([-1.0, 1.0], size=(n, 64))
+    t0 = time.perf_counter()
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 0.1), P, P, 5, 0.6, min_leaf=128)
+    t_plan = time.perf_counter() - t0
+    z32 = torch.tensor(z, dtype=torch.float32, device=dev)
+    z64 = z32.double()
+
+    def step(zz, prec):
+        return H.adjoint(zz, zz, precision=prec, want_dX=False, want_Kx=True)
+    for _ in range(args.warmup):
+        step(z32, "mixed")
+    ms_mixed = _events_ms(torch, lambda: step(z32, "mixed"), args.steps)
+    ms_fp64 = _events_ms(torch, lambda: step(z64, "fp64"), 1)
+    a = step(z32, "mixed")
+    b = step(z64, "fp64")
+    va, vb = a["values"].cpu().numpy(), b["values"].cpu().numpy()
+    kz_err = float((torch.linalg.norm(a["Kx"].double() - b["Kx"]) /
+                    torch.linalg.norm(b["Kx"])).item())
+    return {
+        "metric": "GP hyperparameter step (K z and z^T dK/dl z, 64 probes) n·RHS/s",
+        "value": n * 64 / (ms_mixed * 1e-3), "unit": UNIT, "ms_per_step": ms_mixed,
+        "fp64": {"ms_per_step": ms_fp64, "value": n * 64 / (ms_fp64 * 1e-3),
+                 "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed},
+        "mixed_rel_err_vs_fp64": {"Kz": kz_err,
+                                  "zKz": abs(va[0] - vb[0]) / abs(vb[0]),
+                                  "z_dKdl_z": abs(va[1] - vb[1]) / abs(vb[1])},
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C5: n=2e6 in [0,4]x[0,1], EXPONENTIAL l=0.1, p=5 (q=36), "
+                               "eta=0.6, leaf 128, 64 Rademacher probes",
+                   "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"],
+                   "plan_build_s": t_plan},
+    }
+
+
+def run_other_config(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    fn = {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config]
+    sampler = ClockSampler(gpu_smi_id(torch, dev))
+    sampler.start()
+    line = fn(args, torch, dev)
+    line["clocks"] = sampler.stop()
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None})
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,11 +366,16 @@ def main():
     ap.add_argument("--ref-stride", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
+                    help="c2 (default): the headline workload; c3 batching, c4 gradients, "
+                         "c5 GP step (one JSON line each, not the headline)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.config != "c2":
+        return run_other_config(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

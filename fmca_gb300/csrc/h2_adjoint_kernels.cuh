@@ -68,7 +68,8 @@ __device__ __forceinline__ float kgrad<float>(int type, float r2, const KParams<
   return kgrad_fast(type, r2, kp);
 }
 
-// Near-field gradient: G[t] += scale * sum_s c_ts g(|p_t - q_s|) (p_t - q_s),
+// Near-field gradient: G[t] += scale * sum_s c_ts g(|p_t - q_s|) (p_t - q_s)
+// (accumulated pair by pair from the differences),
 // c_ts = sum_r tval[t][r] * colscale[r] * sval[s][r] over the RHS chunk.
 // One thread per target; sources stream through shared memory like ksum.
 template <typename T, int RB, int TS, int STAGES>
@@ -99,7 +100,7 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
     for (int r = 0; r < RB; ++r)
       if (r < rcount) yv[r] = (T)((double)tv[r] * colscale[r]);
   }
-  T as = T(0), ax = T(0), ay = T(0), az = T(0);
+  T ax = T(0), ay = T(0), az = T(0);
 
   int ntiles = 0;
   for (int i = g.ivl_begin; i < g.ivl_end; ++i)
@@ -147,10 +148,10 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
         for (int r = 0; r < RB; ++r) c += yv[r] * v[r];
         const T dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
         const T w = c * kgrad<T>(kp.type, dx * dx + dy * dy + dz * dz, kp);
-        as += w;
-        ax += w * s.x;
-        ay += w * s.y;
-        az += w * s.z;
+        // accumulate w (p - q) directly: p sum(w) - sum(w q) cancels badly
+        ax += w * dx;
+        ay += w * dy;
+        az += w * dz;
       }
     }
     if (__syncthreads_or(ok ? 0 : 1)) {
@@ -169,32 +170,35 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
   }
   if (active) {
     double* o = G + (size_t)(g.tbegin + tid) * 4;
-    o[0] += scale * ((double)p.x * (double)as - (double)ax);
-    o[1] += scale * ((double)p.y * (double)as - (double)ay);
-    o[2] += scale * ((double)p.z * (double)as - (double)az);
+    o[0] += scale * (double)ax;
+    o[1] += scale * (double)ay;
+    o[2] += scale * (double)az;
   }
 }
 
 // 1-D barycentric Lagrange factors and their derivatives
-// l_a'(x) = l_a(x) (W2(x) / W(x) - 1 / (x - xi_a)), W = sum w_b / (x - xi_b),
-// W2 = sum w_b / (x - xi_b)^2; at a node xi_m the differentiation-matrix
-// values l_a'(xi_m) = (w_a / w_m) / (xi_m - xi_a), l_m'(xi_m) = -sum of those
+// l_a'(x) = l_a(x) sum_{b != a} 1 / (x - xi_b)  (the logarithmic derivative
+// of prod_{b != a} (x - xi_b); summed without the a term, so nothing cancels
+// when x is close to xi_a); at a node xi_m the differentiation-matrix values
+// l_a'(xi_m) = (w_a / w_m) / (xi_m - xi_a), l_m'(xi_m) = -sum of those
 template <typename T>
 __device__ __forceinline__ void lagrange1d_deriv(const InterpDev<T>& ip, T x, T* f, T* df) {
   int m = -1;
   for (int a = 0; a < ip.p1; ++a)
     if (fabs(x - ip.xi[a]) <= T(kDblEps)) m = a;
   if (m < 0) {
-    T W = T(0), W2 = T(0);
+    T W = T(0);
+    T inv[8];
     for (int b = 0; b < ip.p1; ++b) {
-      const T q = ip.w[b] / (x - ip.xi[b]);
-      W += q;
-      W2 += q / (x - ip.xi[b]);
+      inv[b] = T(1) / (x - ip.xi[b]);
+      W += ip.w[b] * inv[b];
     }
     for (int a = 0; a < ip.p1; ++a) {
-      const T dxa = x - ip.xi[a];
-      f[a] = ip.w[a] / dxa / W;
-      df[a] = f[a] * (W2 / W - T(1) / dxa);
+      T s = T(0);
+      for (int b = 0; b < ip.p1; ++b)
+        if (b != a) s += inv[b];
+      f[a] = ip.w[a] * inv[a] / W;
+      df[a] = f[a] * s;
     }
   } else {
     T s = T(0);

@@ -108,6 +108,10 @@ struct DevPlan {
     event_stage[nevents] = stage;
     ++nevents;
   }
+  void reset_marks() {
+    nevents = 0;
+    launches = 0;
+  }
 };
 
 namespace {
@@ -576,9 +580,17 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     dp->launches += dp->nleaves_r ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFGATHER, st);
   }
-  // near field
-  e = launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, rofs, rcount,
-                     kp, 0, dp->err_flag, st);
+  return cudaGetLastError();
+}
+
+// near field of one right-hand-side chunk (the last stage of the chunk; it
+// fills the GPU on its own, so running it concurrently with the far-field
+// chain on a second stream gained nothing at n = 1e6)
+template <typename T, int RB>
+cudaError_t run_near(DevPlan* dp, DevSet<T>& S, Workspace<T>& w, int ld, int rcount,
+                     const KParams<T>& kp, cudaStream_t st) {
+  cudaError_t e = launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, 0,
+                                 rcount, kp, 0, dp->err_flag, st);
   dp->launches += dp->near.ngroups ? 1 : 0;
   dp->mark(FMCA_STAGE_NEAR, st);
   return e;
@@ -637,8 +649,7 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     state->nch = nchunks_for(nrhs);
     state->fp64 = sizeof(T) == 8;
   }
-  dp->nevents = 0;
-  dp->launches = 0;
+  dp->reset_marks();
   dp->mark(-1, st);
   const KParams<T> kp = make_kparams<T>(k);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
@@ -672,12 +683,15 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     switch (rb) {
       case 1:
         e = run_tree_stages<T, 1>(plan, dp, S, wc, ld, 0, rcount, kp, st);
+        if (e == cudaSuccess) e = run_near<T, 1>(dp, S, wc, ld, rcount, kp, st);
         break;
       case 8:
         e = run_tree_stages<T, 8>(plan, dp, S, wc, ld, 0, rcount, kp, st);
+        if (e == cudaSuccess) e = run_near<T, 8>(dp, S, wc, ld, rcount, kp, st);
         break;
       default:
         e = run_tree_stages<T, 32>(plan, dp, S, wc, ld, 0, rcount, kp, st);
+        if (e == cudaSuccess) e = run_near<T, 32>(dp, S, wc, ld, rcount, kp, st);
         break;
     }
     FMCA_CK(e);
@@ -797,8 +811,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     state->nch = (nrhs + RB - 1) / RB;
     state->fp64 = false;
   }
-  dp->nevents = 0;
-  dp->launches = 0;
+  dp->reset_marks();
   dp->mark(-1, st);
   const KParams<float> kp = make_kparams<float>(k);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
@@ -838,11 +851,8 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   for (int ch = 0; ch < nch; ++ch) {
     const int rcount = std::min(RB, nrhs - ch * RB);
     float* xc = w.xc + (size_t)ch * nc * ld;
-    const __half* xh = w.xh + (size_t)ch * nc * ld;
-    const __half* xl = w.xl + (size_t)ch * nc * ld;
     float* t = w.t + (size_t)ch * Cc * q * ld;
     float* s = w.s + (size_t)ch * Cr * q * ld;
-    float* ynear = w.ynear + (size_t)ch * nr * ld;
     float* yfar = w.yfar + (size_t)ch * nr * ld;
     {
       auto kern = leafmom_kernel<float, RB>;
@@ -903,7 +913,8 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_LEAFGATHER, st);
     }
-    FMCA_CK(launch_tc(dp->near_tc, S.pts_r, S.pts_c, xh, xl, ynear, rcount, kp,
+    FMCA_CK(launch_tc(dp->near_tc, S.pts_r, S.pts_c, w.xh + (size_t)ch * nc * ld,
+                      w.xl + (size_t)ch * nc * ld, w.ynear + (size_t)ch * nr * ld, rcount, kp,
                       dp->err_flag, st));
     dp->launches += dp->near_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);
