@@ -422,6 +422,25 @@ KParams<T> make_kparams(const KernelDesc& k) {
   kp.a = (T)a;
   kp.e2 = (T)e2;
   kp.il = (T)(1. / l);
+  // tensor-core path: coordinates multiplied by g turn the kernel argument
+  // into r' = g r with k = 2^-r' (EXPONENTIAL), (1 + r') e^-r' (MATERN32),
+  // (1 + r' + r'^2/3) e^-r' (MATERN52) or 2^-r'^2 (GAUSSIAN)
+  double g = 1;
+  switch (k.type) {
+    case FMCA_KERNEL_EXPONENTIAL:
+      g = log2e / l;
+      break;
+    case FMCA_KERNEL_MATERN32:
+    case FMCA_KERNEL_MATERN52:
+      g = a;
+      break;
+    case FMCA_KERNEL_GAUSSIAN:
+      g = std::sqrt(0.5 * log2e) / l;
+      break;
+    default:
+      break;
+  }
+  kp.g = (T)g;
   return kp;
 }
 
@@ -754,41 +773,44 @@ bool tc_supported(int type, int nrhs) {
   return bounded && nrhs > 16;
 }
 
-template <int KT, int MT>
+template <int KT, int MT, bool REL>
 cudaError_t launch_tc_t(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
                         const __half* vh, const __half* vl, float* out, int rcount,
-                        const KParams<float>& kp, int* errf, cudaStream_t st) {
-  auto kern = ksum_tc_kernel<KT, MT>;
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+  auto kern = ksum_tc_kernel<KT, MT, REL>;
   const size_t smem = 128 + (size_t)kTcStages * kTcTile * (16 + 4 * kTcRhs);
   ensure_smem(kern, smem);
   kern<<<gl.ngroups, 128, smem, st>>>(gl.groups, gl.ivl, tgt, src, vh, vl, out, kTcRhs,
-                                       rcount, kp, errf);
+                                       rcount, kp, q, errf);
   return cudaGetLastError();
 }
 
-// groups hold at most kTcGroupCap = 4 warps x 2 m-tiles x 16 targets
+// groups hold at most kTcGroupCap = 4 warps x 2 m-tiles x 16 targets.
+// q > 0: the sources are interpolation nodes (q per cluster) weighted by
+// their cluster's moment exponent; q = 0: points of weight 1.
 template <int KT>
 cudaError_t launch_tc_mt(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
                          const __half* vh, const __half* vl, float* out, int rcount,
-                         const KParams<float>& kp, int* errf, cudaStream_t st) {
-  return launch_tc_t<KT, 2>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+  if (q > 0) return launch_tc_t<KT, 2, true>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
+  return launch_tc_t<KT, 2, false>(gl, tgt, src, vh, vl, out, rcount, kp, 0, errf, st);
 }
 
 cudaError_t launch_tc(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
                       const __half* vh, const __half* vl, float* out, int rcount,
-                      const KParams<float>& kp, int* errf, cudaStream_t st) {
+                      const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
   if (gl.ngroups == 0) return cudaSuccess;
   switch (kp.type) {
     case 0:
-      return launch_tc_mt<0>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+      return launch_tc_mt<0>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
     case 1:
-      return launch_tc_mt<1>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+      return launch_tc_mt<1>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
     case 2:
-      return launch_tc_mt<2>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+      return launch_tc_mt<2>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
     case 3:
-      return launch_tc_mt<3>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+      return launch_tc_mt<3>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
     default:
-      return launch_tc_mt<-1>(gl, tgt, src, vh, vl, out, rcount, kp, errf, st);
+      return launch_tc_mt<-1>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
   }
 }
 
@@ -883,7 +905,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, w.th, w.tl,
                                        w.nodes_s);
     ++dp->launches;
-    FMCA_CK(launch_tc(dp->far_tc, S.nodes_r, w.nodes_s, w.th, w.tl, s, rcount, kp,
+    FMCA_CK(launch_tc(dp->far_tc, S.nodes_r, w.nodes_s, w.th, w.tl, s, rcount, kp, (int)q,
                       dp->err_flag, st));
     dp->launches += dp->far_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
@@ -915,7 +937,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     }
     FMCA_CK(launch_tc(dp->near_tc, S.pts_r, S.pts_c, w.xh + (size_t)ch * nc * ld,
                       w.xl + (size_t)ch * nc * ld, w.ynear + (size_t)ch * nr * ld, rcount, kp,
-                      dp->err_flag, st));
+                      0, dp->err_flag, st));
     dp->launches += dp->near_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);
   }

@@ -54,6 +54,7 @@ struct KParams {
   T a;   // sqrt(3)/l, sqrt(5)/l, ... (per type)
   T e2;  // scale of the exponent in base 2 (FP32 path)
   T il;  // 1 / l
+  T g;   // coordinate scale of the tensor-core path (1 for generic kernels)
 };
 
 template <typename T>

@@ -3,10 +3,11 @@
 // ksum_tc computes out[t][0..32) = sum_s a(t, s) * v[s][0..32) for one
 // group of targets per CTA, like ksum_kernel, with the contraction on the
 // tensor cores:
-//   * a(t, s) = k(|tgt_t - src_s|) * src_s.w is evaluated in FP32 by the
+//   * a(t, s) = k(|tgt_t - src_s|) * 2^(w_s - E) is evaluated in FP32 by the
 //     warp that owns the targets, directly in the register layout of the
 //     A operand of mma.m16n8k16 (no shared-memory round trip), and split
-//     into two FP16 halves a = a_hi + a_lo (22 significant bits);
+//     into two FP16 halves a = a_hi + a_lo (a_hi = a with its low 13
+//     mantissa bits cleared, a_lo = the exact rest rounded to FP16);
 //   * the source values arrive pre-split (v = v_hi + v_lo, FP16) in shared
 //     memory through cp.async.bulk copies completed on mbarriers, and are
 //     read as B fragments with ldmatrix.trans;
@@ -18,11 +19,22 @@
 // Values are kept inside the FP16 range by exact power-of-two scalings:
 // every right-hand side is divided by 2^ceil(log2 max|x_r|) before the
 // product (and multiplied back at the end), and the interpolated moments of
-// each column cluster by 2^e_sigma, which is folded into a through src.w.
+// each column cluster by 2^e_sigma. The exponent e_sigma travels in the w
+// field of the cluster's interpolation nodes and enters the exponential of
+// the kernel, so the weight costs no multiplication; a group subtracts the
+// largest exponent E of its sources (a <= 1) and multiplies its sums by 2^E.
+//
+// Per-pair FP32 work is kept small by three layouts: coordinates are
+// multiplied by a kernel-specific g so the kernel argument needs no further
+// scaling; each source tile is rewritten in shared memory as records of two
+// sources (x0 x1 y0 y1 | z0 z1 w0 w1, coordinates negated) so that packed
+// FP32x2 operands load directly; and rows past the end of a tile get w = -inf
+// (a = 0) once per tile instead of a select per pair.
 #pragma once
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+#include <math_constants.h>
 #include <stdint.h>
 
 #include "h2_gpu_kernels.cuh"
@@ -51,56 +63,67 @@ __device__ __forceinline__ uint32_t h2_bits(__half2 h) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// (a, b) -> hi = fp16(a, b), lo = fp16(a - hi, b - hi)
-__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
-  const __half2 h = __floats2half2_rn(a, b);
-  const float2 hf = __half22float2(h);
-  hi = h2_bits(h);
-  lo = h2_bits(__floats2half2_rn(a - hf.x, b - hf.y));
-}
-
 constexpr int kTcTile = 128;  // sources per pipeline stage
 constexpr int kTcStages = 3;
 constexpr int kTcRhs = 32;    // right-hand sides per product (4 n-tiles of 8)
+constexpr float kLog2e = 1.44269504088896341f;
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-// Radial kernel of two squared distances with packed FP32x2 arithmetic;
-// the approximate square root and exponential run per element on the SFU.
+// 2^e for an integral e; 0 below the normal range (e = -inf included)
+__device__ __forceinline__ float pow2i(float e) {
+  const int i = __float2int_rz(fminf(fmaxf(e, -127.f), 127.f));
+  return i <= -127 ? 0.f : __int_as_float((i + 127) << 23);
+}
+
+// a = k * 2^w of two squared distances in the coordinates scaled by g;
+// FP32x2 arithmetic, the square root and exponential per element on the SFU
 template <int KT>
-__device__ __forceinline__ float2 keval2(float2 r2, const KParams<float>& kp) {
-  if constexpr (KT == 3) {  // GAUSSIAN: exp(-r^2 / (2 l^2))
-    const float2 u = __fmul2_rn(r2, f2(kp.e2, kp.e2));
+__device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<float>& kp) {
+  if constexpr (KT == 3) {  // GAUSSIAN: 2^(w - r'^2)
+    const float2 u = __ffma2_rn(r2, f2(-1.f, -1.f), w);
     return f2(ex2_approx(u.x), ex2_approx(u.y));
   } else if constexpr (KT == 0 || KT == 1 || KT == 2) {
     const float2 r = f2(sqrt_approx(r2.x), sqrt_approx(r2.y));
-    const float2 u = __fmul2_rn(r, f2(kp.e2, kp.e2));
-    const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
-    if constexpr (KT == 0) return e;  // EXPONENTIAL
-    const float2 t = __fmul2_rn(r, f2(kp.a, kp.a));
-    if constexpr (KT == 1) return __ffma2_rn(t, e, e);  // MATERN32: (1 + t) e
-    // MATERN52: (1 + t + t^2 / 3) e
-    const float2 p = __ffma2_rn(__ffma2_rn(t, f2(0.333333343f, 0.333333343f), f2(1.f, 1.f)),
-                                t, f2(1.f, 1.f));
-    return __fmul2_rn(p, e);
+    if constexpr (KT == 0) {  // EXPONENTIAL: 2^(w - r')
+      const float2 u = __ffma2_rn(r, f2(-1.f, -1.f), w);
+      return f2(ex2_approx(u.x), ex2_approx(u.y));
+    } else {
+      const float2 u = __ffma2_rn(r, f2(-kLog2e, -kLog2e), w);
+      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+      if constexpr (KT == 1) return __ffma2_rn(r, e, e);  // MATERN32: (1 + r') e
+      // MATERN52: (1 + r' + r'^2 / 3) e
+      const float2 p = __ffma2_rn(__ffma2_rn(r, f2(0.333333343f, 0.333333343f), f2(1.f, 1.f)),
+                                  r, f2(1.f, 1.f));
+      return __fmul2_rn(p, e);
+    }
   } else {
-    return f2(keval_fast(kp.type, r2.x, kp), keval_fast(kp.type, r2.y, kp));
+    return f2(keval_fast(kp.type, r2.x, kp) * pow2i(w.x),
+              keval_fast(kp.type, r2.y, kp) * pow2i(w.y));
   }
 }
 
 // Shared memory: [bars | counts] (128 B) | STAGES x TS source points |
-// STAGES x TS x 32 FP16 v_hi | STAGES x TS x 32 FP16 v_lo
-template <int KT, int MT>
+// STAGES x TS x 32 FP16 v_hi | STAGES x TS x 32 FP16 v_lo.
+// Each point stage arrives as TS records (x, y, z, w) and is rewritten in
+// place, warp by warp (a warp's 32 points and their 16 pair records occupy
+// the same 512 bytes), as pair records (-g x0, -g x1, -g y0, -g y1, -g z0,
+// -g z1, w0 - E, w1 - E).
+// REL: the sources are interpolation nodes whose w holds their cluster's
+// moment exponent; clusters are q consecutive nodes. Otherwise w = 0.
+template <int KT, int MT, bool REL>
 __global__ void __launch_bounds__(128, 4)
     ksum_tc_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const Pt4<float>* __restrict__ src,
                    const __half* __restrict__ vhi, const __half* __restrict__ vlo,
-                   float* __restrict__ out, int ldo, int rcount, KParams<float> kp,
+                   float* __restrict__ out, int ldo, int rcount, KParams<float> kp, int q,
                    int* err) {
   constexpr int TS = kTcTile, STAGES = kTcStages;
+  static_assert(TS == 128, "the in-place pair layout assumes one point per thread");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
   int* scnt = reinterpret_cast<int*>(smem_raw + 8 * STAGES);
+  float* sred = reinterpret_cast<float*>(smem_raw + 64);
   Pt4<float>* spts = reinterpret_cast<Pt4<float>*>(smem_raw + 128);
   __half* shi = reinterpret_cast<__half*>(smem_raw + 128 + STAGES * TS * 16);
   __half* slo = shi + STAGES * TS * kTcRhs;
@@ -108,10 +131,11 @@ __global__ void __launch_bounds__(128, 4)
   const KGroup g = groups[blockIdx.x];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gid = lane >> 2, tig = lane & 3;
+  const float gs = kp.g;
 
   // zero the source buffers once, so rows past a partial tile always hold
-  // finite data (masked through a zero weight); the proxy fence orders these
-  // generic writes before the bulk copies
+  // finite data; the proxy fence orders these generic writes before the
+  // bulk copies
   {
     uint4* z = reinterpret_cast<uint4*>(spts);
     const int n16 = STAGES * TS * (16 + kTcRhs * 2 * 2) / 16;
@@ -120,7 +144,7 @@ __global__ void __launch_bounds__(128, 4)
   }
 
   // targets of this thread: rows gid and gid + 8 of each of the warp's
-  // m-tiles, duplicated into both halves of a packed pair
+  // m-tiles, scaled by g and duplicated into both halves of a packed pair
   float2 tx[MT][2], ty[MT][2], tz[MT][2];
 #pragma unroll
   for (int m = 0; m < MT; ++m)
@@ -130,9 +154,9 @@ __global__ void __launch_bounds__(128, 4)
       float px = 0.f, py = 0.f, pz = 0.f;
       if (i < g.tcount) {
         const Pt4<float> p = tgt[g.tbegin + i];
-        px = p.x;
-        py = p.y;
-        pz = p.z;
+        px = gs * p.x;
+        py = gs * p.y;
+        pz = gs * p.z;
       }
       tx[m][h] = f2(px, px);
       ty[m][h] = f2(py, py);
@@ -150,11 +174,26 @@ __global__ void __launch_bounds__(128, 4)
   for (int i = g.ivl_begin; i < g.ivl_end; ++i)
     ntiles += (int)((ivl[2 * i + 1] - ivl[2 * i] + TS - 1) / TS);
 
+  // largest moment exponent E of the group's source clusters
+  float E = 0.f;
+  if constexpr (REL) {
+    float m = -CUDART_INF_F;
+    for (int i = g.ivl_begin + tid; i < g.ivl_end; i += blockDim.x)
+      for (uint32_t s = ivl[2 * i], e = ivl[2 * i + 1]; s < e; s = (s / q + 1) * q)
+        m = fmaxf(m, src[s].w);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) sred[warp] = m;
+  }
+
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
     fence_mbar_init();
   }
   __syncthreads();
+  if constexpr (REL) {
+    E = fmaxf(fmaxf(sred[0], sred[1]), fmaxf(sred[2], sred[3]));
+    E = fmaxf(E, -1000.f);  // groups without sources
+  }
 
   int pi = g.ivl_begin;
   uint32_t poff = 0;
@@ -188,9 +227,29 @@ __global__ void __launch_bounds__(128, 4)
     const int stage = k % STAGES;
     const uint32_t parity = (uint32_t)((k / STAGES) & 1);
     const bool ok = mbar_wait_bounded(&bars[stage], parity, kWaitLimitNs);
+    const int cnt = scnt[stage];
     if (ok) {
-      const int cnt = scnt[stage];
-      const Pt4<float>* P = spts + stage * TS;
+      // rewrite this warp's 32 points as 16 pair records, in place
+      float4* P4 = reinterpret_cast<float4*>(spts + stage * TS);
+      const float4 p = P4[tid];
+      __syncwarp();
+      float* rec = reinterpret_cast<float*>(P4) + (tid >> 1) * 8 + (tid & 1);
+      // rows past the tile's end hold stale records: zero coordinates keep
+      // their (zero) kernel values finite
+      const bool valid = tid < cnt;
+      rec[0] = valid ? -gs * p.x : 0.f;
+      rec[2] = valid ? -gs * p.y : 0.f;
+      rec[4] = valid ? -gs * p.z : 0.f;
+      rec[6] = valid ? (REL ? p.w - E : 0.f) : -CUDART_INF_F;
+      // these generic writes precede the next bulk copy into the stage
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (__syncthreads_or(ok ? 0 : 1)) {
+      aborted = true;
+      break;
+    }
+    {
+      const float4* R4 = reinterpret_cast<const float4*>(spts + stage * TS);
       const __half* H = shi + (size_t)stage * TS * kTcRhs;
       const __half* L = slo + (size_t)stage * TS * kTcRhs;
       for (int ks = 0; ks < cnt; ks += 16) {
@@ -202,17 +261,17 @@ __global__ void __launch_bounds__(128, 4)
         ldsm_x4_trans(bh[2][0], bh[2][1], bh[3][0], bh[3][1], hrow + 16);
         ldsm_x4_trans(bl[0][0], bl[0][1], bl[1][0], bl[1][1], lrowp);
         ldsm_x4_trans(bl[2][0], bl[2][1], bl[3][0], bl[3][1], lrowp + 16);
-        // this thread's source columns, as two packed pairs:
+        // this thread's source columns as two pair records:
         // pair 0 = (2 tig, 2 tig + 1), pair 1 = (2 tig + 8, 2 tig + 9)
         float2 nsx[2], nsy[2], nsz[2], wv[2];
 #pragma unroll
         for (int pp = 0; pp < 2; ++pp) {
-          const int j = ks + 2 * tig + pp * 8;
-          const Pt4<float> a = P[j], b = P[j + 1];
-          nsx[pp] = f2(-a.x, -b.x);
-          nsy[pp] = f2(-a.y, -b.y);
-          nsz[pp] = f2(-a.z, -b.z);
-          wv[pp] = f2(j < cnt ? a.w : 0.f, j + 1 < cnt ? b.w : 0.f);
+          const int jp = (ks >> 1) + tig + 4 * pp;
+          const float4 a = R4[2 * jp], b = R4[2 * jp + 1];
+          nsx[pp] = f2(a.x, a.y);
+          nsy[pp] = f2(a.z, a.w);
+          nsz[pp] = f2(b.x, b.y);
+          wv[pp] = f2(b.z, b.w);
         }
 #pragma unroll
         for (int m = 0; m < MT; ++m) {
@@ -225,12 +284,14 @@ __global__ void __launch_bounds__(128, 4)
               const float2 dy = __fadd2_rn(ty[m][h], nsy[pp]);
               const float2 dz = __fadd2_rn(tz[m][h], nsz[pp]);
               const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-              const float2 av = __fmul2_rn(keval2<KT>(r2, kp), wv[pp]);
-              // register 2 pp + h of the A fragment: row gid + 8 h, pair pp
-              const __half2 hh = __floats2half2_rn(av.x, av.y);
-              const float2 hf = __half22float2(hh);
-              const float2 lo = __ffma2_rn(hf, f2(-1.f, -1.f), av);  // av - hf, exact
-              ahi[2 * pp + h] = h2_bits(hh);
+              const float2 av = kscaled2<KT>(r2, wv[pp], kp);
+              // register 2 pp + h of the A fragment: row gid + 8 h, pair pp;
+              // hi keeps the top 11 significant bits (exact in FP16 for
+              // |a| >= 2^-14), lo = a - hi exactly in FP32
+              const float2 hi = f2(__uint_as_float(__float_as_uint(av.x) & 0xffffe000u),
+                                   __uint_as_float(__float_as_uint(av.y) & 0xffffe000u));
+              const float2 lo = __ffma2_rn(hi, f2(-1.f, -1.f), av);
+              ahi[2 * pp + h] = h2_bits(__floats2half2_rn(hi.x, hi.y));
               alo[2 * pp + h] = h2_bits(__floats2half2_rn(lo.x, lo.y));
             }
 #pragma unroll
@@ -252,10 +313,7 @@ __global__ void __launch_bounds__(128, 4)
             acc[m][n][c] = 0.f;
           }
     }
-    if (__syncthreads_or(ok ? 0 : 1)) {
-      aborted = true;
-      break;
-    }
+    __syncthreads();
     if (tid == 0 && k + STAGES < ntiles) issue(stage);
   }
   if (aborted) {
@@ -266,6 +324,7 @@ __global__ void __launch_bounds__(128, 4)
     }
     return;
   }
+  const int eo = (int)E;
 #pragma unroll
   for (int m = 0; m < MT; ++m)
 #pragma unroll
@@ -276,8 +335,10 @@ __global__ void __launch_bounds__(128, 4)
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
         const int c = n * 8 + 2 * tig;
-        if (c < rcount) o[c] = tot[m][n][2 * h];
-        if (c + 1 < rcount) o[c + 1] = tot[m][n][2 * h + 1];
+        const float v0 = REL ? ldexpf(tot[m][n][2 * h], eo) : tot[m][n][2 * h];
+        const float v1 = REL ? ldexpf(tot[m][n][2 * h + 1], eo) : tot[m][n][2 * h + 1];
+        if (c < rcount) o[c] = v0;
+        if (c + 1 < rcount) o[c + 1] = v1;
       }
     }
 }
@@ -353,7 +414,8 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
 }
 
 // per column cluster: e = exponent of max |t|, t'' = t * 2^-e split into
-// FP16 hi / lo, and the cluster's node coordinates with w = 2^e
+// FP16 hi / lo, and the cluster's node coordinates with w = e (the moment
+// exponent; -1000 for a cluster without moments)
 __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict__ t,
                               const Pt4<float>* __restrict__ nodes,
                               __half* __restrict__ th, __half* __restrict__ tl,
@@ -376,7 +438,7 @@ __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict_
   __syncthreads();
   const float mx = red[0];
   const int ex = scale_exp(mx);
-  const float w = mx > 0.f ? ldexpf(1.f, ex) : 0.f;
+  const float w = mx > 0.f && isfinite(mx) ? (float)ex : -1000.f;
   for (int e = threadIdx.x; e < q * kTcRhs; e += blockDim.x) {
     const float v = (e % kTcRhs) < rcount ? ldexpf(t[base + e], -ex) : 0.f;
     const __half h = __float2half_rn(v);

@@ -196,6 +196,29 @@ def test_mixed_scaling_of_magnitudes(cuda_device, scale):
         assert rel_err(Y[:, r], Y_ref[:, r]) < 1e-5, r
 
 
+@pytest.mark.parametrize("kname", ["EXPONENTIAL", "MATERN32", "MATERN52", "GAUSSIAN",
+                                   "MATERN72"])
+def test_mixed_zero_and_positive_moment_regions(cuda_device, kname):
+    # x vanishes on half of the cube (clusters without moments) and is
+    # positive on the other half (large moments): each far group scales its
+    # sources by its own largest moment exponent
+    n = 20000
+    P = uniform_cloud(n, 3, seed=41)
+    rng = np.random.default_rng(41)
+    X = 1.0 + 0.1 * rng.standard_normal((n, 32))
+    X[P[0] < 0.5, :] = 0.0
+    X[:, 1] = np.where(P[0] < 0.5, 0.0, 1e-3)
+    X[:, 2] = np.where(P[1] < 0.25, 1e4, 1.0)
+    kt = KNAMES.index(kname)
+    O = oracle.OraclePlan(P, None, 4, 0.8, 0)
+    Y_ref, _ = O.action(kt, 0.2, X)
+    H = H2Matrix(CovarianceKernel(kname, 0.2), P, P, 4, 0.8, precision="mixed")
+    Y = H.action(X)
+    for r in range(32):
+        assert rel_err(Y[:, r], Y_ref[:, r]) < 1e-5, r
+    H.check_device_error()
+
+
 def test_mixed_uses_tensor_core_kernel_count(cuda_device):
     # the mixed path launches the split/scale kernels (two more launches per
     # chunk than the FP32 path)
