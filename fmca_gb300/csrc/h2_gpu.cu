@@ -12,6 +12,7 @@
 #include "h2_adjoint_kernels.cuh"
 #include "h2_gpu_kernels.cuh"
 #include "h2_tc_kernels.cuh"
+#include "h2_umma_kernels.cuh"
 
 namespace fmca {
 namespace gpu {
@@ -29,7 +30,8 @@ namespace {
   } while (0)
 
 constexpr int kGroupCap = 256;    // targets per ksum CTA (128 threads x 2)
-constexpr int kTcGroupCap = 128;  // targets per ksum_tc CTA (4 warps x 32)
+constexpr int kTcGroupCap = 128;  // targets per far-field tensor-core CTA
+constexpr int kUmSets = 4;        // sets of 4 evaluation warps per tensor-core CTA
 constexpr int kStages = 3;
 template <typename T>
 struct TileSize;
@@ -84,8 +86,8 @@ struct DevPlan {
   std::vector<int> m2m_ptr;
   int32_t* l2l_list = nullptr;  // row clusters of level >= 1, by level
   std::vector<int> l2l_ptr;
-  GroupList far, near;        // chunked to kGroupCap targets
-  GroupList far_tc, near_tc;  // chunked to kTcGroupCap targets
+  GroupList far, near;  // chunked to kGroupCap targets (near: also the tensor-core list)
+  GroupList far_tc;     // chunked to kTcGroupCap targets
   int* err_flag = nullptr;
   void* ws = nullptr;
   size_t ws_bytes = 0;
@@ -317,19 +319,19 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->far : &dp->far_tc, err));
   }
   // near groups: targets = points of every row leaf, sources = merged
-  // column point intervals
-  for (int pass = 0; pass < 2; ++pass) {
-    const uint32_t cap = pass == 0 ? kGroupCap : kTcGroupCap;
+  // column point intervals; kGroupCap = 256 targets suits both the CUDA-core
+  // kernel sum and the tensor-core one (two halves of 128)
+  {
     HostGroups hg;
     const Pattern& P = plan.pat;
     hg.ivl = P.near_ivl;
     for (size_t l = 0; l < plan.row_leaves.size(); ++l) {
       const int c = plan.row_leaves[l];
       add_target_range(&hg, plan.rows.begin[c], plan.rows.size[c], P.near_ptr[l],
-                       P.near_ptr[l + 1], cap);
+                       P.near_ptr[l + 1], kGroupCap);
     }
     sort_groups(&hg);
-    FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->near : &dp->near_tc, err));
+    FMCA_TRY(upload_groups(dp, hg, &dp->near, err));
   }
   {
     void* p = nullptr;
@@ -734,8 +736,9 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
 // mixed precision with tensor-core kernel sums
 struct TcWorkspace {
   float *xc, *t, *s, *ynear, *yfar;
-  __half *xh, *xl, *th, *tl;
-  Pt4<float>* nodes_s;
+  __half *xh, *xl, *th, *tl;  // tensor-core values layout
+  float4* pairs_c;            // column points as pair records
+  float4* pairs_n;            // column interpolation nodes as pair records
   unsigned int* cmax;
 };
 
@@ -750,13 +753,15 @@ size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
     return p;
   };
   TcWorkspace t;
+  const size_t npc = um_padded(plan.cols.n), npn = um_padded(Cc * q);
   t.xc = (float*)take(plan.cols.n * ld * nch * 4);
-  t.xh = (__half*)take(plan.cols.n * ld * nch * 2);
-  t.xl = (__half*)take(plan.cols.n * ld * nch * 2);
+  t.xh = (__half*)take(npc * ld * nch * 2);
+  t.xl = (__half*)take(npc * ld * nch * 2);
   t.t = (float*)take(Cc * q * ld * nch * 4);
-  t.th = (__half*)take(Cc * q * ld * 2);
-  t.tl = (__half*)take(Cc * q * ld * 2);
-  t.nodes_s = (Pt4<float>*)take(Cc * q * sizeof(Pt4<float>));
+  t.th = (__half*)take(npn * ld * 2);
+  t.tl = (__half*)take(npn * ld * 2);
+  t.pairs_c = (float4*)take(npc * 16);
+  t.pairs_n = (float4*)take(npn * 16);
   t.s = (float*)take(Cr * q * ld * nch * 4);
   t.ynear = (float*)take(plan.rows.n * ld * nch * 4);
   t.yfar = (float*)take(plan.rows.n * ld * nch * 4);
@@ -773,45 +778,53 @@ bool tc_supported(int type, int nrhs) {
   return bounded && nrhs > 16;
 }
 
-template <int KT, int MT, bool REL>
-cudaError_t launch_tc_t(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
+// Tensor-core kernel sum over a group list: H target halves of 128 per
+// CTA (groups of up to 128 H targets), NSETS sets of 4 evaluation warps.
+// q > 0: the sources are interpolation nodes (q per cluster) weighted by
+// their cluster's moment exponent; q = 0: points of weight 1.
+template <int KT, int H, int NSETS>
+cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vh, const __half* vl, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
-  auto kern = ksum_tc_kernel<KT, MT, REL>;
-  const size_t smem = 128 + (size_t)kTcStages * kTcTile * (16 + 4 * kTcRhs);
-  ensure_smem(kern, smem);
-  kern<<<gl.ngroups, 128, smem, st>>>(gl.groups, gl.ivl, tgt, src, vh, vl, out, kTcRhs,
-                                       rcount, kp, q, errf);
+  const int threads = 32 * (2 + 4 * NSETS);
+  if (q > 0) {
+    auto kern = ksum_um_kernel<KT, H, NSETS, true>;
+    ensure_smem(kern, kUmSmemBytes);
+    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vh, vl, out,
+                                                     kTcRhs, rcount, kp, q, errf);
+  } else {
+    auto kern = ksum_um_kernel<KT, H, NSETS, false>;
+    ensure_smem(kern, kUmSmemBytes);
+    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vh, vl, out,
+                                                     kTcRhs, rcount, kp, 0, errf);
+  }
   return cudaGetLastError();
 }
 
-// groups hold at most kTcGroupCap = 4 warps x 2 m-tiles x 16 targets.
-// q > 0: the sources are interpolation nodes (q per cluster) weighted by
-// their cluster's moment exponent; q = 0: points of weight 1.
-template <int KT>
-cudaError_t launch_tc_mt(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
-                         const __half* vh, const __half* vl, float* out, int rcount,
-                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
-  if (q > 0) return launch_tc_t<KT, 2, true>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-  return launch_tc_t<KT, 2, false>(gl, tgt, src, vh, vl, out, rcount, kp, 0, errf, st);
+template <int H, int NS>
+cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
+                        const __half* vh, const __half* vl, float* out, int rcount,
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+  switch (kp.type) {
+    case 0:
+      return launch_um_t<0, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+    case 1:
+      return launch_um_t<1, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+    case 2:
+      return launch_um_t<2, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+    case 3:
+      return launch_um_t<3, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+    default:
+      return launch_um_t<-1, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+  }
 }
 
-cudaError_t launch_tc(const GroupList& gl, const Pt4<float>* tgt, const Pt4<float>* src,
+template <int H>
+cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                       const __half* vh, const __half* vl, float* out, int rcount,
                       const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
   if (gl.ngroups == 0) return cudaSuccess;
-  switch (kp.type) {
-    case 0:
-      return launch_tc_mt<0>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-    case 1:
-      return launch_tc_mt<1>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-    case 2:
-      return launch_tc_mt<2>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-    case 3:
-      return launch_tc_mt<3>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-    default:
-      return launch_tc_mt<-1>(gl, tgt, src, vh, vl, out, rcount, kp, q, errf, st);
-  }
+  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
 }
 
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
@@ -858,14 +871,16 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
           nc, c0, ncol, static_cast<const float*>(x), sxi, sxr, w.cmax);
     ++dp->launches;
   }
+  const int64_t npc = (int64_t)um_padded(nc);
   if (dtype == FMCA_DTYPE_F64)
-    gather_split_kernel<double><<<blocks(nc * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<double><<<blocks(npc * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
   else
-    gather_split_kernel<float><<<blocks(nc * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<float><<<blocks(npc * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
+  point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
   FMCA_CK(cudaGetLastError());
-  dp->launches += 1;
+  dp->launches += 2;
   dp->mark(FMCA_STAGE_GATHER, st);
   const size_t q = plan.interp.q;
   const size_t midx_bytes = q * 3 * sizeof(int);
@@ -902,11 +917,11 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_M2M, st);
     }
-    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, w.th, w.tl,
-                                       w.nodes_s);
+    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.th, w.tl,
+                                       reinterpret_cast<float*>(w.pairs_n));
     ++dp->launches;
-    FMCA_CK(launch_tc(dp->far_tc, S.nodes_r, w.nodes_s, w.th, w.tl, s, rcount, kp, (int)q,
-                      dp->err_flag, st));
+    FMCA_CK(launch_um<1>(dp->far_tc, S.nodes_r, w.pairs_n, w.th, w.tl, s, rcount, kp, (int)q,
+                         dp->err_flag, st));
     dp->launches += dp->far_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
     {
@@ -935,10 +950,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_LEAFGATHER, st);
     }
-    FMCA_CK(launch_tc(dp->near_tc, S.pts_r, S.pts_c, w.xh + (size_t)ch * nc * ld,
-                      w.xl + (size_t)ch * nc * ld, w.ynear + (size_t)ch * nr * ld, rcount, kp,
-                      0, dp->err_flag, st));
-    dp->launches += dp->near_tc.ngroups ? 1 : 0;
+    FMCA_CK(launch_um<2>(dp->near, S.pts_r, w.pairs_c, w.xh + (size_t)ch * npc * ld,
+                         w.xl + (size_t)ch * npc * ld, w.ynear + (size_t)ch * nr * ld, rcount,
+                         kp, 0, dp->err_flag, st));
+    dp->launches += dp->near.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);
   }
   if (dtype == FMCA_DTYPE_F64)

@@ -1,0 +1,491 @@
+// Kernel sums of the mixed-precision matvec on the fifth-generation tensor
+// cores (tcgen05, sm_103a).
+//
+// ksum_um computes out[t][0..32) = sum_s a(t, s) v[s][0..32) for one group
+// of up to 128 H targets per CTA (one CTA per SM), with
+//   a(t, s) = k(|t - s|) 2^(w_s - E)
+// (w_s: the source's moment exponent, 0 for points; E: the largest w_s of
+// the group; the scaling of h2_tc_kernels.cuh),
+// split into FP16 halves a = a_hi + a_lo and contracted as
+//   a_hi v_hi + a_hi v_lo + a_lo v_hi
+// by tcgen05.mma (M = 128 targets, N = 32 right-hand sides, K = 16 sources)
+// with A in tensor memory, B in shared memory and FP32 accumulators in
+// tensor memory. Warp roles:
+//   warp 0       producer: packs the group's source intervals into tiles of
+//                128 sources (pieces aligned to 8 sources, rows outside the
+//                intervals masked) and loads them with cp.async.bulk;
+//   warp 1       one thread issues the tensor-core products;
+//   warps 2..    NSETS sets of 4 evaluation warps. Warp w owns tensor-memory
+//                lanes 32 (w % 4) .. + 31, i.e. targets h * 128 + lane for
+//                each half h < H. Set s evaluates the 16-source chunks
+//                kk = s, s + NSETS, ... of every tile into a ring of A
+//                slots in tensor memory, and after every NSETS-th tile adds
+//                that tile's accumulator into its own running total (the
+//                tensor cores round accumulations toward zero, so totals are
+//                kept with round-to-nearest FP32 adds per tile of 128
+//                sources).
+// Every wait is bounded (2 s); on a timeout the CTA raises the error flag,
+// drains its copies and products, frees tensor memory and returns, and
+// CTAs that start after the flag was raised return at once.
+//
+// Sources arrive as pair records and FP16 values in the layouts described
+// in h2_tc_kernels.cuh (pieces of whole 8-source blocks).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "h2_gpu_kernels.cuh"
+#include "h2_tc_kernels.cuh"
+#include "umma.cuh"
+
+namespace fmca {
+namespace gpu {
+
+constexpr int kUmTile = 128;  // sources per stage: 8 chunks of 16
+constexpr int kUmStages = 6;
+constexpr int kUmPtsBytes = kUmTile * 16;
+constexpr int kUmValBytes = kUmTile * kTcRhs * 2;
+constexpr int kUmStageBytes = kUmPtsBytes + 2 * kUmValBytes;
+constexpr int kUmHeader = 1024;
+// slack after the last stage, and enough shared memory that no second CTA
+// fits on the SM (each CTA allocates all 512 tensor-memory columns)
+constexpr int kUmPad = 6144;
+constexpr size_t kUmSmemBytes = kUmHeader + (size_t)kUmStages * kUmStageBytes + kUmPad;
+constexpr uint32_t kUmCols = 512;
+
+__device__ __forceinline__ void mbar_expect_tx_only(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(
+                   umma_smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive1(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma_smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// bounded wait that also gives up when another role of the CTA aborted
+__device__ __forceinline__ bool um_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (global_timer_ns() - t0 > kWaitLimitNs) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+// kernel values of one 16-source chunk (8 pair records) for the H targets
+// of this thread, split into FP16 hi / lo registers (two sources each)
+template <int KT, int H, bool MASKED, bool REL>
+__device__ __forceinline__ void um_eval_chunk(const float4* __restrict__ rec, uint32_t m16,
+                                              const float2 (&tx)[H], const float2 (&ty)[H],
+                                              const float2 (&tz)[H], float E,
+                                              const KParams<float>& kp, uint32_t (&hi)[H][8],
+                                              uint32_t (&lo)[H][8]) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 a = rec[2 * j], b = rec[2 * j + 1];
+    const float2 sx = f2(a.x, a.y), sy = f2(a.z, a.w), sz = f2(b.x, b.y);
+    float2 sw = REL ? __fadd2_rn(f2(b.z, b.w), f2(-E, -E)) : f2(b.z, b.w);
+    if constexpr (MASKED) {
+      if (!((m16 >> (2 * j)) & 1u)) sw.x = -CUDART_INF_F;
+      if (!((m16 >> (2 * j + 1)) & 1u)) sw.y = -CUDART_INF_F;
+    }
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const float2 dx = __fadd2_rn(tx[h], sx);
+      const float2 dy = __fadd2_rn(ty[h], sy);
+      const float2 dz = __fadd2_rn(tz[h], sz);
+      const float2 r2 =
+          __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __ffma2_rn(dx, dx, f2(1e-30f, 1e-30f))));
+      const float2 av = kscaled2<KT>(r2, sw, kp);
+      const float2 hv = f2(__uint_as_float(__float_as_uint(av.x) & 0xffffe000u),
+                           __uint_as_float(__float_as_uint(av.y) & 0xffffe000u));
+      const float2 lv = __ffma2_rn(hv, f2(-1.f, -1.f), av);
+      hi[h][j] = h2_bits(__floats2half2_rn(hv.x, hv.y));
+      lo[h][j] = h2_bits(__floats2half2_rn(lv.x, lv.y));
+    }
+  }
+}
+
+// bits of rows [vb, ve) inside the 32-row word starting at row w0
+__device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t w0) {
+  const uint32_t lo = max(vb, w0), hi = min(ve, w0 + 32u);
+  if (lo >= hi) return 0u;
+  const uint32_t n = hi - lo;
+  return (n == 32u ? 0xffffffffu : ((1u << n) - 1u)) << (lo - w0);
+}
+
+// H: target halves of 128 (groups of up to 128 H targets); NSETS: sets of
+// 4 evaluation warps; REL: sources are interpolation nodes (q per cluster)
+// weighted by their cluster's moment exponent, else points of weight 1.
+template <int KT, int H, int NSETS, bool REL>
+__global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
+    ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
+                   const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
+                   const __half* __restrict__ vhi, const __half* __restrict__ vlo,
+                   float* __restrict__ out, int ldo, int rcount, KParams<float> kp, int q,
+                   int* err) {
+  constexpr int NST = kUmStages;
+  constexpr int NEVAL = 4 * NSETS;  // evaluation warps
+  constexpr int ACC0 = 0;                       // [buffer][half] x 32 columns
+  constexpr int TOT0 = 2 * H * 32;              // [set][half] x 32 columns
+  constexpr int A0 = TOT0 + NSETS * H * 32;     // [slot][half] x (8 hi + 8 lo)
+  // A slots: at most one tile (8 chunks). Parity waits are exact only while
+  // a waiter is at most one phase ahead of its barrier; a longer ring would
+  // let a set finish the chunks of tile k + 1 before the products of tile
+  // k - 2 complete, and its accumulator wait for tile k could then pass on
+  // the parity of tile k - 4.
+  constexpr int NSLOT_FIT = ((int)kUmCols - A0) / (H * 16);
+  constexpr int NSLOT = NSLOT_FIT >= 8 ? 8 : 4;
+  static_assert(NSLOT_FIT >= 4, "tensor-memory budget");
+  constexpr uint32_t IDESC = umma_idesc_f16(128, 32);
+
+  if (*reinterpret_cast<volatile int*>(err)) return;
+
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);          // [NST]
+  uint64_t* empty = full + NST;                                      // [NST]
+  uint64_t* afull = empty + NST;                                     // [16]
+  uint64_t* aempty = afull + 16;                                     // [16]
+  uint64_t* accf = aempty + 16;                                      // [2]
+  uint64_t* acce = accf + 2;                                         // [2]
+  uint64_t* done = acce + 2;                                         // [1]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 400);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 404);
+  uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 416);   // [NST][4]
+  float* ered = reinterpret_cast<float*>(smem_raw + 640);           // [NEVAL]
+  unsigned char* stages = smem_raw + kUmHeader;
+
+  const KGroup g = groups[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // tiles of the group: its intervals widened to multiples of 8 sources
+  int ntiles;
+  {
+    uint32_t rows = 0;
+    for (int i = g.ivl_begin + lane; i < g.ivl_end; i += 32)
+      rows += ((ivl[2 * i + 1] + 7u) & ~7u) - (ivl[2 * i] & ~7u);
+    for (int o = 16; o > 0; o >>= 1) rows += __shfl_xor_sync(0xffffffffu, rows, o);
+    ntiles = (int)((rows + kUmTile - 1) / kUmTile);
+  }
+
+  // zero the stages once (rows past the last piece of a tile hold finite
+  // data); the proxy fence orders these writes before the bulk copies
+  {
+    uint4* z = reinterpret_cast<uint4*>(stages);
+    const int n16 = (NST * kUmStageBytes + kUmPad) / 16;
+    for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NEVAL + 1);
+    }
+    for (int s = 0; s < 16; ++s) {
+      mbar_init(&afull[s], 4);
+      mbar_init(&aempty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tslot, kUmCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (warp == 0) {
+    // ---------------- producer
+    if (lane == 0) {
+      int pi = g.ivl_begin;
+      uint32_t pos = 0xffffffffu;  // aligned start inside interval pi (none yet)
+      int issued = 0;
+      bool ok = true;
+      for (int k = 0; k < ntiles; ++k) {
+        const int stage = k % NST;
+        if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag)) {
+          ok = false;
+          break;
+        }
+        // pieces: the group's intervals widened to multiples of 8 sources,
+        // packed into the tile's 128 rows; every piece posts its bytes on
+        // the stage barrier before its copies, and the final arrival (after
+        // the row mask is written) lets the phase complete
+        uint32_t row = 0, m0 = 0u, m1 = 0u, m2 = 0u, m3 = 0u;
+        unsigned char* sp = stages + (size_t)stage * kUmStageBytes;
+        while (row < (uint32_t)kUmTile && pi < g.ivl_end) {
+          const uint32_t b = ivl[2 * pi], e = ivl[2 * pi + 1];
+          const uint32_t a0 = pos != 0xffffffffu ? pos : (b & ~7u);
+          const uint32_t ae = (e + 7u) & ~7u;
+          const uint32_t take = min(ae - a0, (uint32_t)kUmTile - row);
+          if (take > 0) {
+            mbar_expect_tx_only(&full[stage], take * (16u + 2u * kTcRhs * 2u));
+            bulk_g2s(sp + row * 16, pairs + a0, take * 16, &full[stage]);
+            bulk_g2s(sp + kUmPtsBytes + row * 64, vhi + (size_t)a0 * kTcRhs, take * 64,
+                     &full[stage]);
+            bulk_g2s(sp + kUmPtsBytes + kUmValBytes + row * 64, vlo + (size_t)a0 * kTcRhs,
+                     take * 64, &full[stage]);
+            // rows [vb, ve) hold sources of the interval
+            const uint32_t vb = max(b, a0) - a0 + row;
+            const uint32_t ve = e > a0 ? min(e, a0 + take) - a0 + row : vb;
+            m0 |= row_bits(vb, ve, 0);
+            m1 |= row_bits(vb, ve, 32);
+            m2 |= row_bits(vb, ve, 64);
+            m3 |= row_bits(vb, ve, 96);
+          }
+          row += take;
+          if (a0 + take >= ae) {
+            ++pi;
+            pos = 0xffffffffu;
+          } else {
+            pos = a0 + take;
+          }
+        }
+        masks[stage * 4 + 0] = m0;
+        masks[stage * 4 + 1] = m1;
+        masks[stage * 4 + 2] = m2;
+        masks[stage * 4 + 3] = m3;
+        mbar_arrive1(&full[stage]);
+        ++issued;
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // copies still in flight land before the CTA frees its memory
+        for (int k = issued > NST ? issued - NST : 0; k < issued; ++k)
+          mbar_wait_bounded(&full[k % NST], (uint32_t)((k / NST) & 1), kWaitLimitNs / 8);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- tensor-core products
+    if (lane == 0) {
+      bool ok = true;
+      for (int k = 0; k < ntiles && ok; ++k) {
+        const int stage = k % NST, b = k & 1;
+        if (!um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag) ||
+            (k >= 2 && !um_wait(&acce[b], (uint32_t)(((k >> 1) - 1) & 1), abort_flag))) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const unsigned char* vh = stages + (size_t)stage * kUmStageBytes + kUmPtsBytes;
+        const unsigned char* vl = vh + kUmValBytes;
+        for (int kk = 0; kk < 8; ++kk) {
+          const int c = k * 8 + kk, slot = c % NSLOT;
+          if (!um_wait(&afull[slot], (uint32_t)((c / NSLOT) & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t bh = umma_desc(vh + kk * 1024, 512, 128);
+          const uint64_t bl = umma_desc(vl + kk * 1024, 512, 128);
+#pragma unroll
+          for (int h = 0; h < H; ++h) {
+            const uint32_t d = tbase + ACC0 + (b * H + h) * 32;
+            const uint32_t a = tbase + A0 + (slot * H + h) * 16;
+            umma_f16_ts(d, a, bh, IDESC, kk > 0 ? 1u : 0u);
+            umma_f16_ts(d, a, bl, IDESC, 1u);
+            umma_f16_ts(d, a + 8, bh, IDESC, 1u);
+          }
+          umma_commit(&aempty[slot]);
+        }
+        if (!ok) break;
+        umma_commit(&empty[stage]);
+        umma_commit(&accf[b]);
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // products already issued complete before tensor memory is freed
+        umma_commit(done);
+        mbar_wait_bounded(done, 0, kWaitLimitNs / 8);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- evaluation warps
+    const int ew = warp - 2, set = ew >> 2;
+    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    const int row = (warp & 3) * 32 + lane;
+    const float gs = kp.g;
+    float2 tx[H], ty[H], tz[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const uint32_t i = (uint32_t)(h * 128 + row);
+      float px = 0.f, py = 0.f, pz = 0.f;
+      if (i < g.tcount) {
+        const Pt4<float> p = tgt[g.tbegin + i];
+        px = gs * p.x;
+        py = gs * p.y;
+        pz = gs * p.z;
+      }
+      tx[h] = f2(px, px);
+      ty[h] = f2(py, py);
+      tz[h] = f2(pz, pz);
+    }
+    // largest moment exponent E of the group's source clusters
+    float E = 0.f;
+    if constexpr (REL) {
+      float mx = -CUDART_INF_F;
+      for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32)
+        for (uint32_t s = ivl[2 * i], e = ivl[2 * i + 1]; s < e; s = (s / q + 1) * q) {
+          const float4 r = pairs[2 * (s >> 1) + 1];
+          mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
+        }
+      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0) ered[ew] = mx;
+      named_sync(1, NEVAL * 32);
+      float all = -CUDART_INF_F;
+      for (int w = 0; w < NEVAL; ++w) all = fmaxf(all, ered[w]);
+      E = fmaxf(all, -1000.f);  // groups without sources
+    }
+
+    bool ok = true;
+    auto flush = [&](int k) {
+      const int b = k & 1;
+      if (!__all_sync(0xffffffffu, um_wait(&accf[b], (uint32_t)((k >> 1) & 1), abort_flag))) {
+        ok = false;
+        return;
+      }
+      tc_fence_after();
+      const bool first = k < NSETS;
+#pragma unroll
+      for (int h = 0; h < H; ++h)
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 16) {
+          uint32_t v[16], t[16];
+          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 32 + c0, v);
+          if (!first) {
+            tmem_ld16(tbase + lanes + TOT0 + (set * H + h) * 32 + c0, t);
+            tmem_wait_ld16(t);
+          }
+          tmem_wait_ld16(v);
+          if (!first)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              v[j] = __float_as_uint(__uint_as_float(v[j]) + __uint_as_float(t[j]));
+          tmem_st8(tbase + lanes + TOT0 + (set * H + h) * 32 + c0, v);
+          tmem_st8(tbase + lanes + TOT0 + (set * H + h) * 32 + c0 + 8, v + 8);
+        }
+      tmem_wait_st();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive1(&acce[b]);
+    };
+
+    for (int k = 0; k < ntiles && ok; ++k) {
+      const int stage = k % NST;
+      if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag))) {
+        ok = false;
+        break;
+      }
+      const float4* R4 = reinterpret_cast<const float4*>(stages + (size_t)stage * kUmStageBytes);
+      for (int kk = set; kk < 8; kk += NSETS) {
+        const int c = k * 8 + kk, slot = c % NSLOT;
+        if (c >= NSLOT &&
+            !__all_sync(0xffffffffu,
+                        um_wait(&aempty[slot], (uint32_t)((c / NSLOT - 1) & 1), abort_flag))) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t m16 = (masks[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
+        uint32_t hi[H][8], lo[H][8];
+        if (m16 == 0xffffu) {
+          um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+        } else if (m16 == 0u) {
+#pragma unroll
+          for (int h = 0; h < H; ++h)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) hi[h][j] = lo[h][j] = 0u;
+        } else {
+          um_eval_chunk<KT, H, true, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+        }
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+          const uint32_t a = tbase + lanes + A0 + (slot * H + h) * 16;
+          tmem_st8(a, hi[h]);
+          tmem_st8(a + 8, lo[h]);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive1(&afull[slot]);
+      }
+      if (!ok) break;
+      __syncwarp();
+      if (lane == 0) mbar_arrive1(&empty[stage]);
+      if (k >= 1 && (k - 1) % NSETS == set) {
+        flush(k - 1);
+        if (!ok) break;
+      }
+    }
+    if (ok && ntiles >= 1 && (ntiles - 1) % NSETS == set) flush(ntiles - 1);
+    if (!ok) atomicExch(err, 1);
+
+    // every set's totals are complete: set 0 adds them and writes the rows
+    named_sync(1, NEVAL * 32);
+    if (set == 0 && !*abort_flag) {
+      tc_fence_after();
+      const int eo = (int)E;
+#pragma unroll 1
+      for (int h = 0; h < H; ++h) {
+        const uint32_t i = (uint32_t)(h * 128 + row);
+        float acc[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+        for (int s = 0; s < NSETS && s < ntiles; ++s)
+#pragma unroll
+          for (int c0 = 0; c0 < 32; c0 += 16) {
+            uint32_t t[16];
+            tmem_ld16(tbase + lanes + TOT0 + (s * H + h) * 32 + c0, t);
+            tmem_wait_ld16(t);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[c0 + j] += __uint_as_float(t[j]);
+          }
+        if (i < g.tcount) {
+          float* o = out + (size_t)(g.tbegin + i) * ldo;
+          if (REL)
+#pragma unroll
+            for (int j = 0; j < 32; ++j) acc[j] = ldexpf(acc[j], eo);
+          if (rcount == 32 && ldo == 32) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4*>(o + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (j < rcount) o[j] = acc[j];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tbase, kUmCols);
+  }
+}
+
+}  // namespace gpu
+}  // namespace fmca

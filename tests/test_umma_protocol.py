@@ -1,0 +1,142 @@
+"""The barrier protocol of the tensor-core kernel sum (ksum_um_kernel in
+fmca_gb300/csrc/h2_umma_kernels.cuh), modelled on the CPU.
+
+Roles and barriers follow the kernel: a producer fills stages (full /
+empty), one thread issues the products of each 16-source chunk (afull /
+aempty per A slot) and commits a tile's accumulator (accf), and NSETS sets
+of 4 evaluation warps write A slots, release stages and add finished
+accumulators into their totals (acce).  mbarrier waits are parity waits:
+they pass when the barrier's current phase has the other parity, which is
+the intended phase only while the waiter is at most one phase ahead.  Random
+schedules (with asynchronous product completions) must finish without a
+deadlock and without a wait that passes before its phase completed."""
+from __future__ import annotations
+
+import random
+
+import pytest
+
+
+class Bar:
+    def __init__(self, count):
+        self.count = count
+        self.pending = count
+        self.phase = 0          # index of the phase in progress
+
+    def arrive(self):
+        self.pending -= 1
+        if self.pending == 0:
+            self.phase += 1
+            self.pending = self.count
+
+    def parity_passes(self, parity):
+        return (self.phase & 1) != parity
+
+
+def nslot(H, NSETS, cols=512):
+    a0 = 2 * H * 32 + NSETS * H * 32
+    fit = (cols - a0) // (H * 16)
+    assert fit >= 4
+    return 8 if fit >= 8 else 4     # as in the kernel
+
+
+def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
+    """'ok', 'deadlock' or 'early' for one random schedule."""
+    rnd = random.Random(seed)
+    NSLOT = slots or nslot(H, NSETS)
+    NEVAL = 4 * NSETS
+    full = [Bar(1) for _ in range(NST)]
+    empty = [Bar(NEVAL + 1) for _ in range(NST)]
+    afull = [Bar(4) for _ in range(16)]
+    aempty = [Bar(1) for _ in range(16)]
+    accf = [Bar(1) for _ in range(2)]
+    acce = [Bar(4) for _ in range(2)]
+
+    def producer():
+        for k in range(ntiles):
+            st = k % NST
+            if k >= NST:
+                yield ("wait", empty[st], k // NST - 1)
+            yield ("arrive", full[st])
+
+    def products():
+        for k in range(ntiles):
+            st, b = k % NST, k & 1
+            yield ("wait", full[st], k // NST)
+            if k >= 2:
+                yield ("wait", acce[b], (k >> 1) - 1)
+            for kk in range(8):
+                c = k * 8 + kk
+                yield ("wait", afull[c % NSLOT], c // NSLOT)
+                yield ("commit", aempty[c % NSLOT])
+            yield ("commit", empty[st])
+            yield ("commit", accf[b])
+
+    def evaluation(s):
+        def flush(k):
+            yield ("wait", accf[k & 1], k >> 1)
+            yield ("arrive", acce[k & 1])
+        for k in range(ntiles):
+            st = k % NST
+            yield ("wait", full[st], k // NST)
+            for kk in range(s, 8, NSETS):
+                c = k * 8 + kk
+                if c >= NSLOT:
+                    yield ("wait", aempty[c % NSLOT], c // NSLOT - 1)
+                yield ("arrive", afull[c % NSLOT])
+            yield ("arrive", empty[st])
+            if k >= 1 and (k - 1) % NSETS == s:
+                yield from flush(k - 1)
+        if ntiles >= 1 and (ntiles - 1) % NSETS == s:
+            yield from flush(ntiles - 1)
+
+    roles = [producer(), products()] + [evaluation(s) for s in range(NSETS) for _ in range(4)]
+    cur = [None] * len(roles)
+    alive = [True] * len(roles)
+    inflight = []       # committed products complete later, in order
+    while True:
+        runnable = []
+        for i, r in enumerate(roles):
+            if not alive[i]:
+                continue
+            if cur[i] is None:
+                try:
+                    cur[i] = next(r)
+                except StopIteration:
+                    alive[i] = False
+                    continue
+            op = cur[i]
+            if op[0] == "wait" and not op[1].parity_passes(op[2] & 1):
+                continue
+            runnable.append(i)
+        if not any(alive) and not inflight:
+            return "ok"
+        choices = runnable + (["done"] if inflight else [])
+        if not choices:
+            return "deadlock"
+        ch = rnd.choice(choices)
+        if ch == "done":
+            inflight.pop(0).arrive()
+            continue
+        op = cur[ch]
+        cur[ch] = None
+        if op[0] == "wait":
+            if op[1].phase <= op[2]:
+                return "early"
+        elif op[0] == "arrive":
+            op[1].arrive()
+        else:
+            inflight.append(op[1])
+
+
+@pytest.mark.parametrize("NSETS,H", [(2, 2), (2, 1), (4, 2), (4, 1)])
+def test_protocol_has_no_deadlock_or_early_pass(NSETS, H):
+    for seed in range(60):
+        for ntiles in (1, 2, 3, 5, 9, 17):
+            assert simulate(ntiles, NSETS, H, seed) == "ok", (ntiles, seed)
+
+
+def test_model_detects_a_ring_longer_than_one_tile():
+    # 16 A slots with 4 sets of one half lets a set run two tiles ahead
+    bad = [simulate(n, 4, 1, s, slots=16) for s in range(40) for n in (9, 17)]
+    assert "early" in bad or "deadlock" in bad
