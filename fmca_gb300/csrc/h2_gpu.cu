@@ -736,7 +736,7 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
 // mixed precision with tensor-core kernel sums
 struct TcWorkspace {
   float *xc, *t, *s, *ynear, *yfar;
-  __half *xh, *xl, *th, *tl;  // tensor-core values layout
+  __half *xv, *tv;            // tensor-core values layout (hi and lo parts)
   float4* pairs_c;            // column points as pair records
   float4* pairs_n;            // column interpolation nodes as pair records
   unsigned int* cmax;
@@ -755,11 +755,9 @@ size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
   TcWorkspace t;
   const size_t npc = um_padded(plan.cols.n), npn = um_padded(Cc * q);
   t.xc = (float*)take(plan.cols.n * ld * nch * 4);
-  t.xh = (__half*)take(npc * ld * nch * 2);
-  t.xl = (__half*)take(npc * ld * nch * 2);
+  t.xv = (__half*)take(npc * ld * nch * 2 * 2);
   t.t = (float*)take(Cc * q * ld * nch * 4);
-  t.th = (__half*)take(npn * ld * 2);
-  t.tl = (__half*)take(npn * ld * 2);
+  t.tv = (__half*)take(npn * ld * 2 * 2);
   t.pairs_c = (float4*)take(npc * 16);
   t.pairs_n = (float4*)take(npn * 16);
   t.s = (float*)take(Cr * q * ld * nch * 4);
@@ -784,18 +782,18 @@ bool tc_supported(int type, int nrhs) {
 // their cluster's moment exponent; q = 0: points of weight 1.
 template <int KT, int H, int NSETS>
 cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
-                        const __half* vh, const __half* vl, float* out, int rcount,
+                        const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
   const int threads = 32 * (2 + 4 * NSETS);
   if (q > 0) {
     auto kern = ksum_um_kernel<KT, H, NSETS, true>;
     ensure_smem(kern, kUmSmemBytes);
-    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vh, vl, out,
+    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, q, errf);
   } else {
     auto kern = ksum_um_kernel<KT, H, NSETS, false>;
     ensure_smem(kern, kUmSmemBytes);
-    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vh, vl, out,
+    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, 0, errf);
   }
   return cudaGetLastError();
@@ -803,28 +801,28 @@ cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4
 
 template <int H, int NS>
 cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
-                        const __half* vh, const __half* vl, float* out, int rcount,
+                        const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
   switch (kp.type) {
     case 0:
-      return launch_um_t<0, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+      return launch_um_t<0, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
     case 1:
-      return launch_um_t<1, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+      return launch_um_t<1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
     case 2:
-      return launch_um_t<2, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+      return launch_um_t<2, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
     case 3:
-      return launch_um_t<3, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+      return launch_um_t<3, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
     default:
-      return launch_um_t<-1, H, NS>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+      return launch_um_t<-1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
   }
 }
 
 template <int H>
 cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
-                      const __half* vh, const __half* vl, float* out, int rcount,
+                      const __half* vals, float* out, int rcount,
                       const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
   if (gl.ngroups == 0) return cudaSuccess;
-  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vh, vl, out, rcount, kp, q, errf, st);
+  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
 }
 
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
@@ -874,10 +872,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   const int64_t npc = (int64_t)um_padded(nc);
   if (dtype == FMCA_DTYPE_F64)
     gather_split_kernel<double><<<blocks(npc * RB * nch), nthr, 0, st>>>(
-        pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
+        pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   else
     gather_split_kernel<float><<<blocks(npc * RB * nch), nthr, 0, st>>>(
-        pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xh, w.xl);
+        pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
   FMCA_CK(cudaGetLastError());
   dp->launches += 2;
@@ -917,10 +915,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_M2M, st);
     }
-    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.th, w.tl,
+    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.tv,
                                        reinterpret_cast<float*>(w.pairs_n));
     ++dp->launches;
-    FMCA_CK(launch_um<1>(dp->far_tc, S.nodes_r, w.pairs_n, w.th, w.tl, s, rcount, kp, (int)q,
+    FMCA_CK(launch_um<1>(dp->far_tc, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q,
                          dp->err_flag, st));
     dp->launches += dp->far_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
@@ -950,8 +948,8 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_LEAFGATHER, st);
     }
-    FMCA_CK(launch_um<2>(dp->near, S.pts_r, w.pairs_c, w.xh + (size_t)ch * npc * ld,
-                         w.xl + (size_t)ch * npc * ld, w.ynear + (size_t)ch * nr * ld, rcount,
+    FMCA_CK(launch_um<2>(dp->near, S.pts_r, w.pairs_c, w.xv + (size_t)ch * npc * ld * 2,
+                         w.ynear + (size_t)ch * nr * ld, rcount,
                          kp, 0, dp->err_flag, st));
     dp->launches += dp->near.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);

@@ -74,11 +74,13 @@ __device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<fl
 // after the last one):
 //   pairs   record p = sources 2p, 2p + 1 as two float4
 //           (-g x0, -g x1, -g y0, -g y1), (-g z0, -g z1, w0, w1);
-//   values  FP16, element (s, r) at half index um_val_index(s, r): 512 bytes
-//           per 8 sources, 8 x 8 blocks [r % 8][s % 8] ordered by r / 8 —
-//           the K-major core matrices of the B operand.
-__host__ __device__ __forceinline__ size_t um_val_index(size_t s, int r) {
-  return (s >> 3) * 256 + (size_t)(r >> 3) * 64 + (size_t)(r & 7) * 8 + (s & 7);
+//   values  FP16 hi and lo parts, element (s, r) of part p (0 hi, 1 lo) at
+//           half index um_val_index(s, r, p): 1 KB per 8 sources, 8 x 8
+//           blocks [r % 8][s % 8] ordered by p, r / 8 — the K-major core
+//           matrices of a B operand of 64 columns (32 hi | 32 lo).
+__host__ __device__ __forceinline__ size_t um_val_index(size_t s, int r, int p) {
+  return (s >> 3) * 512 + (size_t)p * 256 + (size_t)(r >> 3) * 64 + (size_t)(r & 7) * 8 +
+         (s & 7);
 }
 __host__ __device__ __forceinline__ size_t um_padded(size_t n) {
   return ((n + 7) & ~(size_t)7) + 8;
@@ -133,8 +135,7 @@ template <typename TI>
 __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,
                                     const TI* __restrict__ x, int64_t sxi, int64_t sxr,
                                     const unsigned int* __restrict__ cmax,
-                                    float* __restrict__ xc, __half* __restrict__ xh,
-                                    __half* __restrict__ xl) {
+                                    float* __restrict__ xc, __half* __restrict__ xv) {
   const int nchunks = (R + kTcRhs - 1) / kTcRhs;
   const int64_t np = (int64_t)um_padded(n);
   const int64_t per = np * kTcRhs;
@@ -153,9 +154,9 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
     }
     if (i < n) xc[(ch * n + i) * kTcRhs + rr] = v;
     const __half h = __float2half_rn(v);
-    const size_t o = (size_t)ch * per + um_val_index((size_t)i, rr);
-    xh[o] = h;
-    xl[o] = __float2half_rn(v - __half2float(h));
+    __half* o = xv + (size_t)ch * per * 2;
+    o[um_val_index((size_t)i, rr, 0)] = h;
+    o[um_val_index((size_t)i, rr, 1)] = __float2half_rn(v - __half2float(h));
   }
 }
 
@@ -182,8 +183,7 @@ __global__ void point_pairs_kernel(int64_t n, const Pt4<float>* __restrict__ pts
 // last block also zeroes the padding after node C q.
 __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict__ t,
                               const Pt4<float>* __restrict__ nodes, float g,
-                              __half* __restrict__ th, __half* __restrict__ tl,
-                              float* __restrict__ pairs) {
+                              __half* __restrict__ tv, float* __restrict__ pairs) {
   const int c = blockIdx.x;
   if (c >= C) return;
   __shared__ float red[32];
@@ -207,9 +207,9 @@ __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict_
     const int r = e % kTcRhs;
     const float v = r < rcount ? ldexpf(t[base + e], -ex) : 0.f;
     const __half h = __float2half_rn(v);
-    const size_t o = um_val_index((size_t)c * q + e / kTcRhs, r);
-    th[o] = h;
-    tl[o] = __float2half_rn(v - __half2float(h));
+    const size_t sidx = (size_t)c * q + e / kTcRhs;
+    tv[um_val_index(sidx, r, 0)] = h;
+    tv[um_val_index(sidx, r, 1)] = __float2half_rn(v - __half2float(h));
   }
   for (int k = threadIdx.x; k < q; k += blockDim.x) {
     const size_t s = (size_t)c * q + k;
@@ -226,8 +226,8 @@ __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict_
       float* rec = pairs + (s >> 1) * 8 + (s & 1);
       rec[0] = rec[2] = rec[4] = rec[6] = 0.f;
       for (int r = 0; r < kTcRhs; ++r) {
-        th[um_val_index(s, r)] = __float2half_rn(0.f);
-        tl[um_val_index(s, r)] = __float2half_rn(0.f);
+        tv[um_val_index(s, r, 0)] = __float2half_rn(0.f);
+        tv[um_val_index(s, r, 1)] = __float2half_rn(0.f);
       }
     }
   }

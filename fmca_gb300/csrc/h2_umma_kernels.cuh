@@ -8,9 +8,11 @@
 // the group; the scaling of h2_tc_kernels.cuh),
 // split into FP16 halves a = a_hi + a_lo and contracted as
 //   a_hi v_hi + a_hi v_lo + a_lo v_hi
-// by tcgen05.mma (M = 128 targets, N = 32 right-hand sides, K = 16 sources)
-// with A in tensor memory, B in shared memory and FP32 accumulators in
-// tensor memory. Warp roles:
+// by two tcgen05.mma per 16 sources and target half (M = 128 targets,
+// K = 16 sources): a_hi x [v_hi | v_lo] with N = 64 and a_lo x v_hi with
+// N = 32 (a product costs the same below N = 64, so merging the hi and lo
+// values saves a third of them), A in tensor memory, B in shared memory,
+// FP32 accumulators in tensor memory. Warp roles:
 //   warp 0       producer: packs the group's source intervals into tiles of
 //                128 sources (pieces aligned to 8 sources, rows outside the
 //                intervals masked) and loads them with cp.async.bulk;
@@ -19,11 +21,11 @@
 //                lanes 32 (w % 4) .. + 31, i.e. targets h * 128 + lane for
 //                each half h < H. Set s evaluates the 16-source chunks
 //                kk = s, s + NSETS, ... of every tile into a ring of A
-//                slots in tensor memory, and after every NSETS-th tile adds
-//                that tile's accumulator into its own running total (the
-//                tensor cores round accumulations toward zero, so totals are
-//                kept with round-to-nearest FP32 adds per tile of 128
-//                sources).
+//                slots in tensor memory, and the set of tile k adds that
+//                tile's accumulator into the running total once the total
+//                holds tile k - 1 (the tensor cores round accumulations
+//                toward zero, so totals are kept with round-to-nearest FP32
+//                adds per tile of 128 sources).
 // Every wait is bounded (2 s); on a timeout the CTA raises the error flag,
 // drains its copies and products, frees tensor memory and returns, and
 // CTAs that start after the flag was raised return at once.
@@ -47,8 +49,8 @@ namespace gpu {
 constexpr int kUmTile = 128;  // sources per stage: 8 chunks of 16
 constexpr int kUmStages = 6;
 constexpr int kUmPtsBytes = kUmTile * 16;
-constexpr int kUmValBytes = kUmTile * kTcRhs * 2;
-constexpr int kUmStageBytes = kUmPtsBytes + 2 * kUmValBytes;
+constexpr int kUmValBytes = kUmTile * kTcRhs * 2 * 2;  // hi and lo, interleaved
+constexpr int kUmStageBytes = kUmPtsBytes + kUmValBytes;
 constexpr int kUmHeader = 1024;
 // slack after the last stage, and enough shared memory that no second CTA
 // fits on the SM (each CTA allocates all 512 tensor-memory columns)
@@ -132,23 +134,26 @@ template <int KT, int H, int NSETS, bool REL>
 __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
-                   const __half* __restrict__ vhi, const __half* __restrict__ vlo,
-                   float* __restrict__ out, int ldo, int rcount, KParams<float> kp, int q,
-                   int* err) {
+                   const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
+                   KParams<float> kp, int q, int* err) {
   constexpr int NST = kUmStages;
   constexpr int NEVAL = 4 * NSETS;  // evaluation warps
-  constexpr int ACC0 = 0;                       // [buffer][half] x 32 columns
-  constexpr int TOT0 = 2 * H * 32;              // [set][half] x 32 columns
-  constexpr int A0 = TOT0 + NSETS * H * 32;     // [slot][half] x (8 hi + 8 lo)
+  // tensor-memory columns: accumulators [buffer][half] x 64 (0..31: the
+  // a_hi v_hi + a_lo v_hi products, 32..63: a_hi v_lo), the running total
+  // [half] x 32 shared by all sets, A slots [slot][half] x (8 hi + 8 lo)
+  constexpr int ACC0 = 0;
+  constexpr int TOT0 = 2 * H * 64;
+  constexpr int A0 = TOT0 + H * 32;
   // A slots: at most one tile (8 chunks). Parity waits are exact only while
   // a waiter is at most one phase ahead of its barrier; a longer ring would
   // let a set finish the chunks of tile k + 1 before the products of tile
   // k - 2 complete, and its accumulator wait for tile k could then pass on
   // the parity of tile k - 4.
   constexpr int NSLOT_FIT = ((int)kUmCols - A0) / (H * 16);
-  constexpr int NSLOT = NSLOT_FIT >= 8 ? 8 : 4;
+  constexpr int NSLOT = NSLOT_FIT >= 8 ? 8 : NSLOT_FIT;
   static_assert(NSLOT_FIT >= 4, "tensor-memory budget");
-  constexpr uint32_t IDESC = umma_idesc_f16(128, 32);
+  constexpr uint32_t IDESC64 = umma_idesc_f16(128, 64);
+  constexpr uint32_t IDESC32 = umma_idesc_f16(128, 32);
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -160,6 +165,7 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
   uint64_t* accf = aempty + 16;                                      // [2]
   uint64_t* acce = accf + 2;                                         // [2]
   uint64_t* done = acce + 2;                                         // [1]
+  uint64_t* tdone = done + 1;   // one phase per flush into the shared total
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 400);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 404);
   uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 416);   // [NST][4]
@@ -201,6 +207,7 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
       mbar_init(&acce[b], 4);
     }
     mbar_init(done, 1);
+    mbar_init(tdone, 4);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -240,10 +247,8 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
           if (take > 0) {
             mbar_expect_tx_only(&full[stage], take * (16u + 2u * kTcRhs * 2u));
             bulk_g2s(sp + row * 16, pairs + a0, take * 16, &full[stage]);
-            bulk_g2s(sp + kUmPtsBytes + row * 64, vhi + (size_t)a0 * kTcRhs, take * 64,
+            bulk_g2s(sp + kUmPtsBytes + row * 128, vals + (size_t)a0 * 2 * kTcRhs, take * 128,
                      &full[stage]);
-            bulk_g2s(sp + kUmPtsBytes + kUmValBytes + row * 64, vlo + (size_t)a0 * kTcRhs,
-                     take * 64, &full[stage]);
             // rows [vb, ve) hold sources of the interval
             const uint32_t vb = max(b, a0) - a0 + row;
             const uint32_t ve = e > a0 ? min(e, a0 + take) - a0 + row : vb;
@@ -287,8 +292,7 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
           break;
         }
         tc_fence_after();
-        const unsigned char* vh = stages + (size_t)stage * kUmStageBytes + kUmPtsBytes;
-        const unsigned char* vl = vh + kUmValBytes;
+        const unsigned char* vt = stages + (size_t)stage * kUmStageBytes + kUmPtsBytes;
         for (int kk = 0; kk < 8; ++kk) {
           const int c = k * 8 + kk, slot = c % NSLOT;
           if (!um_wait(&afull[slot], (uint32_t)((c / NSLOT) & 1), abort_flag)) {
@@ -296,15 +300,15 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
             break;
           }
           tc_fence_after();
-          const uint64_t bh = umma_desc(vh + kk * 1024, 512, 128);
-          const uint64_t bl = umma_desc(vl + kk * 1024, 512, 128);
+          // B: 16 sources x (32 hi | 32 lo) columns; the N = 32 product
+          // reads the hi half only
+          const uint64_t bd = umma_desc(vt + kk * 2048, 1024, 128);
 #pragma unroll
           for (int h = 0; h < H; ++h) {
-            const uint32_t d = tbase + ACC0 + (b * H + h) * 32;
+            const uint32_t d = tbase + ACC0 + (b * H + h) * 64;
             const uint32_t a = tbase + A0 + (slot * H + h) * 16;
-            umma_f16_ts(d, a, bh, IDESC, kk > 0 ? 1u : 0u);
-            umma_f16_ts(d, a, bl, IDESC, 1u);
-            umma_f16_ts(d, a + 8, bh, IDESC, 1u);
+            umma_f16_ts(d, a, bd, IDESC64, kk > 0 ? 1u : 0u);
+            umma_f16_ts(d, a + 8, bd, IDESC32, 1u);
           }
           umma_commit(&aempty[slot]);
         }
@@ -359,36 +363,46 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
     }
 
     bool ok = true;
+    // flushes run tile after tile (each waits for the previous one on
+    // tdone), so all sets share one running total
     auto flush = [&](int k) {
       const int b = k & 1;
-      if (!__all_sync(0xffffffffu, um_wait(&accf[b], (uint32_t)((k >> 1) & 1), abort_flag))) {
+      if (!__all_sync(0xffffffffu, um_wait(&accf[b], (uint32_t)((k >> 1) & 1), abort_flag)) ||
+          (k >= 1 &&
+           !__all_sync(0xffffffffu, um_wait(tdone, (uint32_t)((k - 1) & 1), abort_flag)))) {
         ok = false;
         return;
       }
       tc_fence_after();
-      const bool first = k < NSETS;
 #pragma unroll
       for (int h = 0; h < H; ++h)
 #pragma unroll
         for (int c0 = 0; c0 < 32; c0 += 16) {
-          uint32_t v[16], t[16];
-          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 32 + c0, v);
-          if (!first) {
-            tmem_ld16(tbase + lanes + TOT0 + (set * H + h) * 32 + c0, t);
+          uint32_t v[16], u[16], t[16];
+          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 64 + c0, v);
+          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 64 + 32 + c0, u);
+          if (k > 0) {
+            tmem_ld16(tbase + lanes + TOT0 + h * 32 + c0, t);
             tmem_wait_ld16(t);
           }
+          tmem_wait_ld16(u);
           tmem_wait_ld16(v);
-          if (!first)
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-              v[j] = __float_as_uint(__uint_as_float(v[j]) + __uint_as_float(t[j]));
-          tmem_st8(tbase + lanes + TOT0 + (set * H + h) * 32 + c0, v);
-          tmem_st8(tbase + lanes + TOT0 + (set * H + h) * 32 + c0 + 8, v + 8);
+          for (int j = 0; j < 16; ++j) {
+            float x = __uint_as_float(v[j]) + __uint_as_float(u[j]);
+            if (k > 0) x += __uint_as_float(t[j]);
+            v[j] = __float_as_uint(x);
+          }
+          tmem_st8(tbase + lanes + TOT0 + h * 32 + c0, v);
+          tmem_st8(tbase + lanes + TOT0 + h * 32 + c0 + 8, v + 8);
         }
       tmem_wait_st();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive1(&acce[b]);
+      if (lane == 0) {
+        mbar_arrive1(&acce[b]);
+        mbar_arrive1(tdone);
+      }
     };
 
     for (int k = 0; k < ntiles && ok; ++k) {
@@ -452,11 +466,11 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
         float acc[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) acc[j] = 0.f;
-        for (int s = 0; s < NSETS && s < ntiles; ++s)
+        if (ntiles > 0)
 #pragma unroll
           for (int c0 = 0; c0 < 32; c0 += 16) {
             uint32_t t[16];
-            tmem_ld16(tbase + lanes + TOT0 + (s * H + h) * 32 + c0, t);
+            tmem_ld16(tbase + lanes + TOT0 + h * 32 + c0, t);
             tmem_wait_ld16(t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) acc[c0 + j] += __uint_as_float(t[j]);

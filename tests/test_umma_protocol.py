@@ -5,7 +5,7 @@ Roles and barriers follow the kernel: a producer fills stages (full /
 empty), one thread issues the products of each 16-source chunk (afull /
 aempty per A slot) and commits a tile's accumulator (accf), and NSETS sets
 of 4 evaluation warps write A slots, release stages and add finished
-accumulators into their totals (acce).  mbarrier waits are parity waits:
+accumulators, tile after tile (tdone), into the shared total (acce).  mbarrier waits are parity waits:
 they pass when the barrier's current phase has the other parity, which is
 the intended phase only while the waiter is at most one phase ahead.  Random
 schedules (with asynchronous product completions) must finish without a
@@ -34,10 +34,12 @@ class Bar:
 
 
 def nslot(H, NSETS, cols=512):
-    a0 = 2 * H * 32 + NSETS * H * 32
+    # two accumulators of H x 64 columns, one total of H x 32, A slots of
+    # H x 16 columns, at most one tile (8 chunks) of them
+    a0 = 2 * H * 64 + H * 32
     fit = (cols - a0) // (H * 16)
     assert fit >= 4
-    return 8 if fit >= 8 else 4     # as in the kernel
+    return min(8, fit)              # as in the kernel
 
 
 def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
@@ -51,6 +53,7 @@ def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
     aempty = [Bar(1) for _ in range(16)]
     accf = [Bar(1) for _ in range(2)]
     acce = [Bar(4) for _ in range(2)]
+    tdone = Bar(4)      # one phase per finished flush (the shared total)
 
     def producer():
         for k in range(ntiles):
@@ -75,7 +78,10 @@ def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
     def evaluation(s):
         def flush(k):
             yield ("wait", accf[k & 1], k >> 1)
+            if k >= 1:
+                yield ("wait", tdone, k - 1)
             yield ("arrive", acce[k & 1])
+            yield ("arrive", tdone)
         for k in range(ntiles):
             st = k % NST
             yield ("wait", full[st], k // NST)
