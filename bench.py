@@ -4,8 +4,10 @@ Workload (the configuration the headline metric is quoted on): n = 1e6 points
 i.i.d. uniform in [0,1]^3 (numpy default_rng(0)), Matern-3/2 kernel l = 0.5,
 Chebyshev tensor-product interpolation p = 4 (q = 125 nodes), eta = 0.8,
 leaf size 128, R = 32 right-hand sides ~ N(0,1).  One step = one H2 matvec
-of all 32 right-hand sides in mixed precision (FP32 near field and coupling,
-FP64 final combination).  Metric: n * R / time ("n*RHS/s", higher is better).
+of all 32 right-hand sides in mixed precision (near field and coupling as
+tensor-core kernel sums on FP16 hi/lo splits with FP32 accumulation, tree
+passes in FP32, FP64 final combination).  Metric: n * R / time ("n*RHS/s",
+higher is better).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -34,7 +36,22 @@ if ROOT not in sys.path:
 METRIC = "H2 matvecs/sec (n·RHS/s) at n=1e6, mixed-precision batched vs FP64 GPU at 1e-5 rel err"
 UNIT = "n*RHS/s"
 SMS = 152
-FP32_LANES_PER_SM = 128
+SFU_PER_SM = 16      # special-function-unit results per clock per SM
+SFU_PER_PAIR = 2     # rsqrt and exp2 per point pair (MATERN32)
+# DRAM bytes (read + write) of one near-field kernel-sum launch of the default
+# workload, from one ncu capture (profiles/ksum_um_c2_full.md)
+NEAR_DRAM_BYTES_PER_LAUNCH = 2.607057e9 + 0.118970e9
+
+
+def _measured_bf16_tflops():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0  # fallback figure of an earlier GB300 measurement
+
+
+BF16_TFLOPS = _measured_bf16_tflops()
 
 
 def workload_config(args):
@@ -469,20 +486,32 @@ def main():
         fp64 = {"ms_per_step": ms64, "value": args.n * args.rhs / (ms64 * 1e-3),
                 "mixed_rel_err_vs_fp64": err, "speedup_mixed_vs_fp64": ms64 / ms}
 
-    # roofline of the dominant kernel (near-field ksum): FP32 FMA work 2 R N_nf
-    near_flops = 2.0 * args.rhs * info["near_pairs"]
+    # roofline of the dominant kernel, the near-field kernel sum (ksum_um_kernel):
+    # every point pair costs one reciprocal square root and one exponential on
+    # the special-function unit (16 results per clock per SM), the binding
+    # unit; the tensor cores run 2 products per 16 sources (N = 64 and N = 32
+    # columns, 192 flops per pair at R = 32)
+    pairs = float(info["near_pairs"])
     t_near = stage_ms["near"] * 1e-3
-    achieved = near_flops / t_near / 1e12
     sm_mhz = clocks.get("sm_mhz") or 2070.0
-    peak = SMS * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    sfu_peak = SMS * SFU_PER_SM * sm_mhz * 1e6 / 1e9
+    sfu_achieved = SFU_PER_PAIR * pairs / t_near / 1e9
+    tensor_flops = 2.0 * (2 * args.rhs + args.rhs) * pairs
     roofline = {
-        "bound": "fp32", "kernel": "ksum near field (FP32 CUDA cores)",
-        "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-        "traffic": None,
-        "work": f"2*R*N_nf = {near_flops:.4g} FP32 flops per launch (N_nf = {info['near_pairs']} pairs)",
-        "peak_source": ("FP32 FMA issue peak 152 SMs x 128 lanes x 2 flops at the median SM "
-                        "clock sampled during the timed region (MEASURED_PEAKS.json has no "
-                        "FP32 CUDA-core figure)"),
+        "bound": "sfu", "kernel": "ksum_um_kernel, near field (tcgen05 products, SFU kernel values)",
+        "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gop/s", "frac": sfu_achieved / sfu_peak,
+        "traffic": NEAR_DRAM_BYTES_PER_LAUNCH,
+        "work": (f"{SFU_PER_PAIR} SFU operations per point pair x N_nf = {info['near_pairs']} "
+                 "pairs per launch"),
+        "peak_source": (f"{SFU_PER_PAIR} x SFU throughput: {SFU_PER_SM} results/clock/SM x {SMS} "
+                        "SMs at the median SM clock sampled during the timed region (the SFU has "
+                        "no entry in MEASURED_PEAKS.json)"),
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one near-field launch "
+                          "(profiles/ksum_um_c2_full.md)",
+        "tensor": {"achieved": tensor_flops / t_near / 1e12, "peak": BF16_TFLOPS,
+                   "unit": "TFLOP/s", "frac": tensor_flops / t_near / 1e12 / BF16_TFLOPS,
+                   "work": "192 executed FP16 tensor flops per pair (3 products x 32 columns x 2)",
+                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst), of measured"},
         "stage_ms": stage_ms,
     }
 
