@@ -428,7 +428,7 @@ KParams<T> make_kparams(const KernelDesc& k) {
   // into r' = g r with k = 2^-r' (EXPONENTIAL), (1 + r') e^-r' (MATERN32),
   // (1 + r' + r'^2/3) e^-r' (MATERN52) or 2^-r'^2 (GAUSSIAN)
   double g = 1;
-  switch (k.type) {
+  switch (base) {  // l dk/dl kernels use the coordinates of their kernel
     case FMCA_KERNEL_EXPONENTIAL:
       g = log2e / l;
       break;
@@ -812,6 +812,18 @@ cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4
       return launch_um_t<2, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
     case 3:
       return launch_um_t<3, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+    case K_DL_EXPONENTIAL:
+      return launch_um_t<K_DL_EXPONENTIAL, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf,
+                                                  st);
+    case K_DL_EXPONENTIAL + 1:
+      return launch_um_t<K_DL_EXPONENTIAL + 1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
+                                                      errf, st);
+    case K_DL_EXPONENTIAL + 2:
+      return launch_um_t<K_DL_EXPONENTIAL + 2, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
+                                                      errf, st);
+    case K_DL_EXPONENTIAL + 3:
+      return launch_um_t<K_DL_EXPONENTIAL + 3, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
+                                                      errf, st);
     default:
       return launch_um_t<-1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
   }

@@ -32,6 +32,7 @@ __device__ __forceinline__ uint32_t h2_bits(__half2 h) {
 
 constexpr int kTcRhs = 32;  // right-hand sides per product
 constexpr float kLog2e = 1.44269504088896341f;
+constexpr float kLn2 = 0.693147180559945309f;
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
@@ -64,6 +65,27 @@ __device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<fl
                                   r, f2(1.f, 1.f));
       return __fmul2_rn(p, e);
     }
+  } else if constexpr (KT == 10 || KT == 11 || KT == 12) {
+    // l dk/dl of the kernels above, in the same scaled coordinates
+    const float2 r = __fmul2_rn(r2, f2(rsqrt_approx(r2.x), rsqrt_approx(r2.y)));
+    if constexpr (KT == 10) {  // EXPONENTIAL: (r / l) e^(-r / l) = ln2 r' 2^-r'
+      const float2 u = __ffma2_rn(r, f2(-1.f, -1.f), w);
+      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+      return __fmul2_rn(__fmul2_rn(r, f2(kLn2, kLn2)), e);
+    } else {
+      const float2 u = __ffma2_rn(r, f2(-kLog2e, -kLog2e), w);
+      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+      const float2 rr = __fmul2_rn(r, r);
+      if constexpr (KT == 11) return __fmul2_rn(rr, e);  // MATERN32: t^2 e^-t
+      // MATERN52: t^2 / 3 (1 + t) e^-t
+      const float2 p = __fmul2_rn(__fmul2_rn(rr, f2(0.333333343f, 0.333333343f)),
+                                  __fadd2_rn(r, f2(1.f, 1.f)));
+      return __fmul2_rn(p, e);
+    }
+  } else if constexpr (KT == 13) {  // GAUSSIAN: (r / l)^2 e^(-r^2 / 2 l^2) = 2 ln2 r'^2 2^-r'^2
+    const float2 u = __ffma2_rn(r2, f2(-1.f, -1.f), w);
+    const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+    return __fmul2_rn(__fmul2_rn(r2, f2(2.f * kLn2, 2.f * kLn2)), e);
   } else {
     return f2(keval_fast(kp.type, r2.x, kp) * pow2i(w.x),
               keval_fast(kp.type, r2.y, kp) * pow2i(w.y));
