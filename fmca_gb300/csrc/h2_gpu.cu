@@ -784,7 +784,7 @@ template <int KT, int H, int NSETS>
 cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
-  const int threads = 32 * (2 + 4 * NSETS);
+  const int threads = 32 * (3 + 4 * NSETS);
   if (q > 0) {
     auto kern = ksum_um_kernel<KT, H, NSETS, true>;
     ensure_smem(kern, kUmSmemBytes);

@@ -131,18 +131,22 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // 4 evaluation warps; REL: sources are interpolation nodes (q per cluster)
 // weighted by their cluster's moment exponent, else points of weight 1.
 template <int KT, int H, int NSETS, bool REL>
-__global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
+__global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
                    const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
                    KParams<float> kp, int q, int* err) {
   constexpr int NST = kUmStages;
   constexpr int NEVAL = 4 * NSETS;  // evaluation warps
-  // tensor-memory columns: accumulators [buffer][half] x 64 (0..31: the
+  // Two product threads (one tcgen05.mma takes ~70 cycles to issue from a
+  // thread, so one thread cannot keep the tensor cores busy): with two target
+  // halves thread j issues half j, with one half thread j issues the chunks
+  // kk = j mod 2 into its own accumulator.
+  // tensor-memory columns: accumulators [buffer][thread] x 64 (0..31: the
   // a_hi v_hi + a_lo v_hi products, 32..63: a_hi v_lo), the running total
   // [half] x 32 shared by all sets, A slots [slot][half] x (8 hi + 8 lo)
   constexpr int ACC0 = 0;
-  constexpr int TOT0 = 2 * H * 64;
+  constexpr int TOT0 = 2 * 2 * 64;
   constexpr int A0 = TOT0 + H * 32;
   // A slots: at most one tile (8 chunks). Parity waits are exact only while
   // a waiter is at most one phase ahead of its barrier; a longer ring would
@@ -162,13 +166,17 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
   uint64_t* empty = full + NST;                                      // [NST]
   uint64_t* afull = empty + NST;                                     // [16]
   uint64_t* aempty = afull + 16;                                     // [16]
-  uint64_t* accf = aempty + 16;                                      // [2]
-  uint64_t* acce = accf + 2;                                         // [2]
-  uint64_t* done = acce + 2;                                         // [1]
-  uint64_t* tdone = done + 1;   // one phase per flush into the shared total
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 400);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 404);
-  uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 416);   // [NST][4]
+  // tile accumulators complete on accf[k % 4] (two buffers, four barriers):
+  // with one product thread up to a tile behind the other, a flush of tile
+  // k may start before tile k - 2 completes, never before tile k - 4
+  uint64_t* accf = aempty + 16;                                      // [4]
+  uint64_t* acce = accf + 4;                                         // [2]
+  uint64_t* done = acce + 2;                                         // [2]
+  uint64_t* tdone = done + 2;   // one phase per flush into the shared total
+  static_assert(8 * (2 * NST + 16 + 16 + 4 + 2 + 2 + 1) <= 512, "barrier area");
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 512);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 516);
+  uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 528);   // [NST][4]
   float* ered = reinterpret_cast<float*>(smem_raw + 640);           // [NEVAL]
   unsigned char* stages = smem_raw + kUmHeader;
 
@@ -196,17 +204,16 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], NEVAL + 1);
+      mbar_init(&empty[s], NEVAL + 2);
     }
     for (int s = 0; s < 16; ++s) {
       mbar_init(&afull[s], 4);
-      mbar_init(&aempty[s], 1);
+      mbar_init(&aempty[s], H == 2 ? 2 : 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
-    }
-    mbar_init(done, 1);
+    for (int b = 0; b < 4; ++b) mbar_init(&accf[b], 2);
+    for (int b = 0; b < 2; ++b) mbar_init(&acce[b], 4);
+    mbar_init(&done[0], 1);
+    mbar_init(&done[1], 1);
     mbar_init(tdone, 4);
     *abort_flag = 0;
     fence_mbar_init();
@@ -280,8 +287,9 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
       }
     }
     __syncwarp();
-  } else if (warp == 1) {
-    // ---------------- tensor-core products
+  } else if (warp == 1 || warp == 2) {
+    // ---------------- tensor-core products (thread j of two)
+    const int j = warp - 1;
     if (lane == 0) {
       bool ok = true;
       for (int k = 0; k < ntiles && ok; ++k) {
@@ -293,7 +301,9 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
         }
         tc_fence_after();
         const unsigned char* vt = stages + (size_t)stage * kUmStageBytes + kUmPtsBytes;
-        for (int kk = 0; kk < 8; ++kk) {
+        const int h = H == 2 ? j : 0;
+        const uint32_t d = tbase + ACC0 + (b * 2 + j) * 64;
+        for (int kk = (H == 2 ? 0 : j); kk < 8; kk += (H == 2 ? 1 : 2)) {
           const int c = k * 8 + kk, slot = c % NSLOT;
           if (!um_wait(&afull[slot], (uint32_t)((c / NSLOT) & 1), abort_flag)) {
             ok = false;
@@ -303,30 +313,26 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
           // B: 16 sources x (32 hi | 32 lo) columns; the N = 32 product
           // reads the hi half only
           const uint64_t bd = umma_desc(vt + kk * 2048, 1024, 128);
-#pragma unroll
-          for (int h = 0; h < H; ++h) {
-            const uint32_t d = tbase + ACC0 + (b * H + h) * 64;
-            const uint32_t a = tbase + A0 + (slot * H + h) * 16;
-            umma_f16_ts(d, a, bd, IDESC64, kk > 0 ? 1u : 0u);
-            umma_f16_ts(d, a + 8, bd, IDESC32, 1u);
-          }
+          const uint32_t a = tbase + A0 + (slot * H + h) * 16;
+          umma_f16_ts(d, a, bd, IDESC64, kk > (H == 2 ? 0 : j) ? 1u : 0u);
+          umma_f16_ts(d, a + 8, bd, IDESC32, 1u);
           umma_commit(&aempty[slot]);
         }
         if (!ok) break;
         umma_commit(&empty[stage]);
-        umma_commit(&accf[b]);
+        umma_commit(&accf[k % 4]);
       }
       if (!ok) {
         atomicExch(err, 1);
         // products already issued complete before tensor memory is freed
-        umma_commit(done);
-        mbar_wait_bounded(done, 0, kWaitLimitNs / 8);
+        umma_commit(&done[j]);
+        mbar_wait_bounded(&done[j], 0, kWaitLimitNs / 8);
       }
     }
     __syncwarp();
   } else {
     // ---------------- evaluation warps
-    const int ew = warp - 2, set = ew >> 2;
+    const int ew = warp - 3, set = ew >> 2;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
     const int row = (warp & 3) * 32 + lane;
     const float gs = kp.g;
@@ -367,7 +373,7 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
     // tdone), so all sets share one running total
     auto flush = [&](int k) {
       const int b = k & 1;
-      if (!__all_sync(0xffffffffu, um_wait(&accf[b], (uint32_t)((k >> 1) & 1), abort_flag)) ||
+      if (!__all_sync(0xffffffffu, um_wait(&accf[k % 4], (uint32_t)((k / 4) & 1), abort_flag)) ||
           (k >= 1 &&
            !__all_sync(0xffffffffu, um_wait(tdone, (uint32_t)((k - 1) & 1), abort_flag)))) {
         ok = false;
@@ -378,20 +384,32 @@ __global__ void __launch_bounds__(32 * (2 + 4 * NSETS), 1)
       for (int h = 0; h < H; ++h)
 #pragma unroll
         for (int c0 = 0; c0 < 32; c0 += 16) {
+          // two target halves: accumulator of thread h; one half: the sum
+          // of both threads' accumulators
           uint32_t v[16], u[16], t[16];
-          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 64 + c0, v);
-          tmem_ld16(tbase + lanes + ACC0 + (b * H + h) * 64 + 32 + c0, u);
-          if (k > 0) {
-            tmem_ld16(tbase + lanes + TOT0 + h * 32 + c0, t);
-            tmem_wait_ld16(t);
-          }
+          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + c0, v);
+          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + 32 + c0, u);
           tmem_wait_ld16(u);
           tmem_wait_ld16(v);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float x = __uint_as_float(v[j]) + __uint_as_float(u[j]);
-            if (k > 0) x += __uint_as_float(t[j]);
-            v[j] = __float_as_uint(x);
+          for (int i = 0; i < 16; ++i)
+            v[i] = __float_as_uint(__uint_as_float(v[i]) + __uint_as_float(u[i]));
+          if (H == 1) {
+            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + c0, t);
+            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + 32 + c0, u);
+            tmem_wait_ld16(t);
+            tmem_wait_ld16(u);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              v[i] = __float_as_uint(__uint_as_float(v[i]) +
+                                     (__uint_as_float(t[i]) + __uint_as_float(u[i])));
+          }
+          if (k > 0) {
+            tmem_ld16(tbase + lanes + TOT0 + h * 32 + c0, t);
+            tmem_wait_ld16(t);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              v[i] = __float_as_uint(__uint_as_float(v[i]) + __uint_as_float(t[i]));
           }
           tmem_st8(tbase + lanes + TOT0 + h * 32 + c0, v);
           tmem_st8(tbase + lanes + TOT0 + h * 32 + c0 + 8, v + 8);

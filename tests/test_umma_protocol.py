@@ -2,8 +2,9 @@
 fmca_gb300/csrc/h2_umma_kernels.cuh), modelled on the CPU.
 
 Roles and barriers follow the kernel: a producer fills stages (full /
-empty), one thread issues the products of each 16-source chunk (afull /
-aempty per A slot) and commits a tile's accumulator (accf), and NSETS sets
+empty), two threads issue the products of each 16-source chunk (afull /
+aempty per A slot; one target half each, or alternate chunks with a single
+half) and commit a tile's accumulators (accf), and NSETS sets
 of 4 evaluation warps write A slots, release stages and add finished
 accumulators, tile after tile (tdone), into the shared total (acce).  mbarrier waits are parity waits:
 they pass when the barrier's current phase has the other parity, which is
@@ -34,24 +35,29 @@ class Bar:
 
 
 def nslot(H, NSETS, cols=512):
-    # two accumulators of H x 64 columns, one total of H x 32, A slots of
-    # H x 16 columns, at most one tile (8 chunks) of them
-    a0 = 2 * H * 64 + H * 32
+    # accumulators [buffer][product thread] x 64 columns, one total of
+    # H x 32, A slots of H x 16 columns, at most one tile (8 chunks) of them
+    a0 = 2 * 2 * 64 + H * 32
     fit = (cols - a0) // (H * 16)
     assert fit >= 4
     return min(8, fit)              # as in the kernel
 
 
-def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
+def simulate(ntiles, NSETS, H, seed, NST=6, slots=None, nbars=4):
     """'ok', 'deadlock' or 'early' for one random schedule."""
     rnd = random.Random(seed)
     NSLOT = slots or nslot(H, NSETS)
     NEVAL = 4 * NSETS
     full = [Bar(1) for _ in range(NST)]
-    empty = [Bar(NEVAL + 1) for _ in range(NST)]
+    empty = [Bar(NEVAL + 2) for _ in range(NST)]
     afull = [Bar(4) for _ in range(16)]
-    aempty = [Bar(1) for _ in range(16)]
-    accf = [Bar(1) for _ in range(2)]
+    # two product threads: with two target halves both read every A slot,
+    # with one half thread j takes the chunks kk = j mod 2
+    aempty = [Bar(2 if H == 2 else 1) for _ in range(16)]
+    # tile accumulators complete on accf[k % 4] (two buffers, four barriers):
+    # with one product thread up to a tile behind the other, a flush of tile
+    # k may start before tile k - 2 completes, but not before tile k - 4
+    accf = [Bar(2) for _ in range(nbars)]
     acce = [Bar(4) for _ in range(2)]
     tdone = Bar(4)      # one phase per finished flush (the shared total)
 
@@ -62,22 +68,24 @@ def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
                 yield ("wait", empty[st], k // NST - 1)
             yield ("arrive", full[st])
 
-    def products():
+    def products(j):
         for k in range(ntiles):
             st, b = k % NST, k & 1
             yield ("wait", full[st], k // NST)
             if k >= 2:
                 yield ("wait", acce[b], (k >> 1) - 1)
             for kk in range(8):
+                if H == 1 and kk % 2 != j:
+                    continue
                 c = k * 8 + kk
                 yield ("wait", afull[c % NSLOT], c // NSLOT)
                 yield ("commit", aempty[c % NSLOT])
             yield ("commit", empty[st])
-            yield ("commit", accf[b])
+            yield ("commit", accf[k % nbars])
 
     def evaluation(s):
         def flush(k):
-            yield ("wait", accf[k & 1], k >> 1)
+            yield ("wait", accf[k % nbars], k // nbars)
             if k >= 1:
                 yield ("wait", tdone, k - 1)
             yield ("arrive", acce[k & 1])
@@ -96,7 +104,8 @@ def simulate(ntiles, NSETS, H, seed, NST=6, slots=None):
         if ntiles >= 1 and (ntiles - 1) % NSETS == s:
             yield from flush(ntiles - 1)
 
-    roles = [producer(), products()] + [evaluation(s) for s in range(NSETS) for _ in range(4)]
+    roles = ([producer(), products(0), products(1)] +
+             [evaluation(s) for s in range(NSETS) for _ in range(4)])
     cur = [None] * len(roles)
     alive = [True] * len(roles)
     inflight = []       # committed products complete later, in order
@@ -142,7 +151,9 @@ def test_protocol_has_no_deadlock_or_early_pass(NSETS, H):
             assert simulate(ntiles, NSETS, H, seed) == "ok", (ntiles, seed)
 
 
-def test_model_detects_a_ring_longer_than_one_tile():
-    # 16 A slots with 4 sets of one half lets a set run two tiles ahead
-    bad = [simulate(n, 4, 1, s, slots=16) for s in range(40) for n in (9, 17)]
-    assert "early" in bad or "deadlock" in bad
+def test_model_detects_aliased_accumulator_waits():
+    # with one target half the two product threads drift up to a tile apart;
+    # two accumulator barriers (one per buffer) then let a flush pass the
+    # parity of tile k - 2 while waiting for tile k
+    bad = [simulate(n, 4, 1, s, nbars=2) for s in range(40) for n in (9, 17)]
+    assert "early" in bad
