@@ -753,7 +753,9 @@ size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
     return p;
   };
   TcWorkspace t;
-  const size_t npc = um_padded(plan.cols.n), npn = um_padded(Cc * q);
+  // far values: the tensor-grid layout (128 rows per cluster) or the general one
+  const size_t npc = um_padded(plan.cols.n);
+  const size_t npn = std::max(um_padded(Cc * q), Cc * (size_t)kGridRows);
   t.xc = (float*)take(plan.cols.n * ld * nch * 4);
   t.xv = (__half*)take(npc * ld * nch * 2 * 2);
   t.t = (float*)take(Cc * q * ld * nch * 4);
@@ -783,15 +785,25 @@ bool tc_supported(int type, int nrhs) {
 template <int KT, int H, int NSETS>
 cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
-                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st,
+                        bool grid = false) {
   const int threads = 32 * (3 + 4 * NSETS);
+  if constexpr (H == 1 && NSETS == 4) {
+    if (grid) {
+      auto kern = ksum_um_kernel<KT, H, NSETS, true, true>;
+      ensure_smem(kern, kUmSmemBytes);
+      kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
+                                                       kTcRhs, rcount, kp, q, errf);
+      return cudaGetLastError();
+    }
+  }
   if (q > 0) {
-    auto kern = ksum_um_kernel<KT, H, NSETS, true>;
+    auto kern = ksum_um_kernel<KT, H, NSETS, true, false>;
     ensure_smem(kern, kUmSmemBytes);
     kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, q, errf);
   } else {
-    auto kern = ksum_um_kernel<KT, H, NSETS, false>;
+    auto kern = ksum_um_kernel<KT, H, NSETS, false, false>;
     ensure_smem(kern, kUmSmemBytes);
     kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, 0, errf);
@@ -802,39 +814,46 @@ cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4
 template <int H, int NS>
 cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
-                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st,
+                        bool grid) {
+#define FMCA_UM(KT) \
+  launch_um_t<KT, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid)
   switch (kp.type) {
     case 0:
-      return launch_um_t<0, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return FMCA_UM(0);
     case 1:
-      return launch_um_t<1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return FMCA_UM(1);
     case 2:
-      return launch_um_t<2, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return FMCA_UM(2);
     case 3:
-      return launch_um_t<3, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return FMCA_UM(3);
     case K_DL_EXPONENTIAL:
-      return launch_um_t<K_DL_EXPONENTIAL, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf,
-                                                  st);
+      return FMCA_UM(K_DL_EXPONENTIAL);
     case K_DL_EXPONENTIAL + 1:
-      return launch_um_t<K_DL_EXPONENTIAL + 1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
-                                                      errf, st);
+      return FMCA_UM(K_DL_EXPONENTIAL + 1);
     case K_DL_EXPONENTIAL + 2:
-      return launch_um_t<K_DL_EXPONENTIAL + 2, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
-                                                      errf, st);
+      return FMCA_UM(K_DL_EXPONENTIAL + 2);
     case K_DL_EXPONENTIAL + 3:
-      return launch_um_t<K_DL_EXPONENTIAL + 3, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q,
-                                                      errf, st);
+      return FMCA_UM(K_DL_EXPONENTIAL + 3);
     default:
-      return launch_um_t<-1, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return FMCA_UM(-1);
   }
+#undef FMCA_UM
 }
 
+// grid: the far field of a 3-D plan of degree kGridP1 - 1 (sources in the
+// tscale_grid_kernel layout)
 template <int H>
 cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                       const __half* vals, float* out, int rcount,
-                      const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+                      const KParams<float>& kp, int q, int* errf, cudaStream_t st,
+                      bool grid = false) {
   if (gl.ngroups == 0) return cudaSuccess;
-  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid);
+}
+
+bool grid_far(const Plan& plan) {
+  return plan.interp.dim == 3 && plan.interp.deg + 1 == kGridP1;
 }
 
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
@@ -927,11 +946,16 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_M2M, st);
     }
-    tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.tv,
-                                       reinterpret_cast<float*>(w.pairs_n));
+    const bool grid = grid_far(plan);
+    if (grid)
+      tscale_grid_kernel<<<Cc, 128, 0, st>>>(Cc, rcount, t, S.nodes_c, dp->midx, kp.g, w.tv,
+                                              reinterpret_cast<float*>(w.pairs_n));
+    else
+      tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.tv,
+                                         reinterpret_cast<float*>(w.pairs_n));
     ++dp->launches;
     FMCA_CK(launch_um<1>(dp->far_tc, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q,
-                         dp->err_flag, st));
+                         dp->err_flag, st, grid));
     dp->launches += dp->far_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
     {

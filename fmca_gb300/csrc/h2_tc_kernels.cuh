@@ -255,6 +255,66 @@ __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict_
   }
 }
 
+// Far-field sources on tensor grids (dimension 3, kGridP1^3 nodes per
+// cluster): cluster c owns value rows [c * 128, c * 128 + 128) in grid order
+// (node with digits (a, b, c') at row (a P1 + b) P1 + c'), rows past P1^3
+// zero; and a 64-byte record rec[c] = (X[0][0..P1), X[1][0..P1),
+// X[2][0..P1), w): the coordinate -g x of each grid line and the moment
+// exponent w (-1000 for a cluster without moments).
+constexpr int kGridP1 = 5;
+constexpr int kGridRows = 128;
+
+// per column cluster c (one block each, q = kGridP1^3 nodes): moments t in
+// the plan's node order, midx = digits of each node (3 per node)
+__global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ t,
+                                   const Pt4<float>* __restrict__ nodes,
+                                   const int* __restrict__ midx, float g,
+                                   __half* __restrict__ tv, float* __restrict__ rec) {
+  constexpr int q = kGridP1 * kGridP1 * kGridP1;
+  const int c = blockIdx.x;
+  if (c >= C) return;
+  __shared__ float red[32];
+  const size_t base = (size_t)c * q * kTcRhs;
+  float m = 0.f;
+  for (int e = threadIdx.x; e < q * kTcRhs; e += blockDim.x)
+    if ((e % kTcRhs) < rcount) m = fmaxf(m, fabsf(t[base + e]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  const float mx = red[0];
+  const int ex = scale_exp(mx);
+  const size_t row0 = (size_t)c * kGridRows;
+  for (int e = threadIdx.x; e < kGridRows * kTcRhs; e += blockDim.x) {
+    const int k = e / kTcRhs, r = e % kTcRhs;
+    float v = 0.f;
+    int row = k;
+    if (k < q) {
+      row = (midx[3 * k] * kGridP1 + midx[3 * k + 1]) * kGridP1 + midx[3 * k + 2];
+      if (r < rcount) v = ldexpf(t[base + (size_t)k * kTcRhs + r], -ex);
+    }
+    const __half h = __float2half_rn(v);
+    tv[um_val_index(row0 + row, r, 0)] = h;
+    tv[um_val_index(row0 + row, r, 1)] = __float2half_rn(v - __half2float(h));
+  }
+  // grid lines: the nodes with digits (i, 0, 0), (0, i, 0), (0, 0, i) give
+  // X[d][i] (every node of a line shares that coordinate)
+  float* rc = rec + (size_t)c * 16;
+  for (int k = threadIdx.x; k < q; k += blockDim.x) {
+    const int a = midx[3 * k], b = midx[3 * k + 1], cc = midx[3 * k + 2];
+    const Pt4<float> p = nodes[(size_t)c * q + k];
+    if (b == 0 && cc == 0) rc[a] = -g * p.x;
+    if (a == 0 && cc == 0) rc[kGridP1 + b] = -g * p.y;
+    if (a == 0 && b == 0) rc[2 * kGridP1 + cc] = -g * p.z;
+  }
+  if (threadIdx.x == 0) rc[15] = mx > 0.f && isfinite(mx) ? (float)ex : -1000.f;
+}
+
 // y (natural order) = sigma2 * 2^e_r * (ynear + yfar), combined in FP64
 template <typename TO>
 __global__ void scatter_scaled_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,

@@ -119,6 +119,51 @@ __device__ __forceinline__ void um_eval_chunk(const float4* __restrict__ rec, ui
   }
 }
 
+// Tensor-grid sources (one column cluster per tile, nodes in grid order):
+// kernel values of the chunks 2 S and 2 S + 1 (grid rows 32 S .. 32 S + 31)
+// for target (tx, ty, tz) (scaled by g). With the grid lines X (scaled by
+// -g) the squared distance to node (a, b, c) is ux[a] + uy[b] + uz[c], so a
+// thread squares 3 x kGridP1 differences per tile instead of three per
+// pair, and the source positions are compile-time constants. wv = w - E of
+// the cluster; rows past kGridP1^3 give a = 0.
+template <int KT, int S>
+__device__ __forceinline__ void grid_eval_pair(float tx, float ty, float tz,
+                                               const float* __restrict__ X, float wv,
+                                               const KParams<float>& kp, uint32_t (&hi)[2][8],
+                                               uint32_t (&lo)[2][8]) {
+  constexpr int P = kGridP1, Q = P * P * P;
+  float ux[P], uy[P], uz[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const float dx = tx + X[i], dy = ty + X[P + i], dz = tz + X[2 * P + i];
+    ux[i] = dx * dx;
+    uy[i] = dy * dy;
+    uz[i] = fmaf(dz, dz, 1e-30f);
+  }
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int p0 = 32 * S + 16 * cc + 2 * j, p1 = p0 + 1;
+      if (p0 >= Q) {
+        hi[cc][j] = lo[cc][j] = 0u;
+        continue;
+      }
+      const float r0 = (ux[p0 / (P * P)] + uy[(p0 / P) % P]) + uz[p0 % P];
+      float r1 = 1.f, w1 = -CUDART_INF_F;
+      if (p1 < Q) {
+        r1 = (ux[p1 / (P * P)] + uy[(p1 / P) % P]) + uz[p1 % P];
+        w1 = wv;
+      }
+      const float2 av = kscaled2<KT>(f2(r0, r1), f2(wv, w1), kp);
+      const float2 hv = f2(__uint_as_float(__float_as_uint(av.x) & 0xffffe000u),
+                           __uint_as_float(__float_as_uint(av.y) & 0xffffe000u));
+      const float2 lv = __ffma2_rn(hv, f2(-1.f, -1.f), av);
+      hi[cc][j] = h2_bits(__floats2half2_rn(hv.x, hv.y));
+      lo[cc][j] = h2_bits(__floats2half2_rn(lv.x, lv.y));
+    }
+}
+
 // bits of rows [vb, ve) inside the 32-row word starting at row w0
 __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t w0) {
   const uint32_t lo = max(vb, w0), hi = min(ve, w0 + 32u);
@@ -130,7 +175,11 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // H: target halves of 128 (groups of up to 128 H targets); NSETS: sets of
 // 4 evaluation warps; REL: sources are interpolation nodes (q per cluster)
 // weighted by their cluster's moment exponent, else points of weight 1.
-template <int KT, int H, int NSETS, bool REL>
+// GRID (with REL, H = 1, NSETS = 4, q = kGridP1^3 in 3-D): every tile is one
+// source cluster on its tensor grid (tscale_grid_kernel layout; `pairs`
+// holds the clusters' 64-byte grid-line records) and set s evaluates the
+// chunks 2 s and 2 s + 1.
+template <int KT, int H, int NSETS, bool REL, bool GRID>
 __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
@@ -158,6 +207,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
   static_assert(NSLOT_FIT >= 4, "tensor-memory budget");
   constexpr uint32_t IDESC64 = umma_idesc_f16(128, 64);
   constexpr uint32_t IDESC32 = umma_idesc_f16(128, 32);
+  static_assert(!GRID || (REL && H == 1 && NSETS == 4), "grid tiles: one half, four sets");
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -184,13 +234,15 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // tiles of the group: its intervals widened to multiples of 8 sources
+  // (grid: one tile per source cluster)
   int ntiles;
   {
     uint32_t rows = 0;
     for (int i = g.ivl_begin + lane; i < g.ivl_end; i += 32)
-      rows += ((ivl[2 * i + 1] + 7u) & ~7u) - (ivl[2 * i] & ~7u);
+      rows += GRID ? (ivl[2 * i + 1] - ivl[2 * i]) / (uint32_t)q
+                   : ((ivl[2 * i + 1] + 7u) & ~7u) - (ivl[2 * i] & ~7u);
     for (int o = 16; o > 0; o >>= 1) rows += __shfl_xor_sync(0xffffffffu, rows, o);
-    ntiles = (int)((rows + kUmTile - 1) / kUmTile);
+    ntiles = GRID ? (int)rows : (int)((rows + kUmTile - 1) / kUmTile);
   }
 
   // zero the stages once (rows past the last piece of a tile hold finite
@@ -240,12 +292,26 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
           ok = false;
           break;
         }
+        unsigned char* sp = stages + (size_t)stage * kUmStageBytes;
+        if constexpr (GRID) {
+          // the next source cluster: its grid-line record and 128 value rows
+          while (pos == 0xffffffffu || pos >= ivl[2 * pi + 1] / (uint32_t)q) {
+            if (pos != 0xffffffffu) ++pi;
+            pos = ivl[2 * pi] / (uint32_t)q;
+          }
+          const uint32_t sigma = pos++;
+          mbar_expect_tx(&full[stage], 64u + (uint32_t)kUmValBytes);
+          bulk_g2s(sp, pairs + (size_t)sigma * 4, 64u, &full[stage]);
+          bulk_g2s(sp + kUmPtsBytes, vals + (size_t)sigma * kGridRows * 2 * kTcRhs,
+                   (uint32_t)kUmValBytes, &full[stage]);
+          ++issued;
+          continue;
+        }
         // pieces: the group's intervals widened to multiples of 8 sources,
         // packed into the tile's 128 rows; every piece posts its bytes on
         // the stage barrier before its copies, and the final arrival (after
         // the row mask is written) lets the phase complete
         uint32_t row = 0, m0 = 0u, m1 = 0u, m2 = 0u, m3 = 0u;
-        unsigned char* sp = stages + (size_t)stage * kUmStageBytes;
         while (row < (uint32_t)kUmTile && pi < g.ivl_end) {
           const uint32_t b = ivl[2 * pi], e = ivl[2 * pi + 1];
           const uint32_t a0 = pos != 0xffffffffu ? pos : (b & ~7u);
@@ -357,8 +423,12 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
       float mx = -CUDART_INF_F;
       for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32)
         for (uint32_t s = ivl[2 * i], e = ivl[2 * i + 1]; s < e; s = (s / q + 1) * q) {
-          const float4 r = pairs[2 * (s >> 1) + 1];
-          mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
+          if constexpr (GRID) {
+            mx = fmaxf(mx, pairs[(size_t)(s / q) * 4 + 3].w);
+          } else {
+            const float4 r = pairs[2 * (s >> 1) + 1];
+            mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
+          }
         }
       for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       if (lane == 0) ered[ew] = mx;
@@ -429,8 +499,46 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
         ok = false;
         break;
       }
+      if constexpr (GRID) {
+        // one source cluster: both chunks of this set from the grid lines
+        const float* X = reinterpret_cast<const float*>(stages + (size_t)stage * kUmStageBytes);
+        const float wv = X[15] - E;
+        uint32_t gh[2][8], gl[2][8];
+        switch (set) {
+          case 0:
+            grid_eval_pair<KT, 0>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
+            break;
+          case 1:
+            grid_eval_pair<KT, 1>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
+            break;
+          case 2:
+            grid_eval_pair<KT, 2>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
+            break;
+          default:
+            grid_eval_pair<KT, 3>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
+            break;
+        }
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+          const int c = k * 8 + 2 * set + cc, slot = c % NSLOT;
+          if (c >= NSLOT &&
+              !__all_sync(0xffffffffu,
+                          um_wait(&aempty[slot], (uint32_t)((c / NSLOT - 1) & 1), abort_flag))) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a = tbase + lanes + A0 + slot * 16;
+          tmem_st8(a, gh[cc]);
+          tmem_st8(a + 8, gl[cc]);
+          tmem_wait_st();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive1(&afull[slot]);
+        }
+      }
       const float4* R4 = reinterpret_cast<const float4*>(stages + (size_t)stage * kUmStageBytes);
-      for (int kk = set; kk < 8; kk += NSETS) {
+      for (int kk = set; kk < (GRID ? 0 : 8); kk += NSETS) {
         const int c = k * 8 + kk, slot = c % NSLOT;
         if (c >= NSLOT &&
             !__all_sync(0xffffffffu,

@@ -43,8 +43,10 @@ def nslot(H, NSETS, cols=512):
     return min(8, fit)              # as in the kernel
 
 
-def simulate(ntiles, NSETS, H, seed, NST=6, slots=None, nbars=4):
-    """'ok', 'deadlock' or 'early' for one random schedule."""
+def simulate(ntiles, NSETS, H, seed, NST=6, slots=None, nbars=4, pairs=False):
+    """'ok', 'deadlock' or 'early' for one random schedule.  pairs: set s
+    evaluates the consecutive chunks 2 s and 2 s + 1 (the tensor-grid far
+    field) instead of s, s + NSETS, ..."""
     rnd = random.Random(seed)
     NSLOT = slots or nslot(H, NSETS)
     NEVAL = 4 * NSETS
@@ -93,7 +95,7 @@ def simulate(ntiles, NSETS, H, seed, NST=6, slots=None, nbars=4):
         for k in range(ntiles):
             st = k % NST
             yield ("wait", full[st], k // NST)
-            for kk in range(s, 8, NSETS):
+            for kk in ([2 * s, 2 * s + 1] if pairs else range(s, 8, NSETS)):
                 c = k * 8 + kk
                 if c >= NSLOT:
                     yield ("wait", aempty[c % NSLOT], c // NSLOT - 1)
@@ -157,3 +159,9 @@ def test_model_detects_aliased_accumulator_waits():
     # parity of tile k - 2 while waiting for tile k
     bad = [simulate(n, 4, 1, s, nbars=2) for s in range(40) for n in (9, 17)]
     assert "early" in bad
+
+
+def test_protocol_with_chunk_pairs_per_set():
+    for seed in range(60):
+        for ntiles in (1, 2, 3, 5, 9, 17):
+            assert simulate(ntiles, 4, 1, seed, pairs=True) == "ok", (ntiles, seed)
