@@ -902,10 +902,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   }
   const int64_t npc = (int64_t)um_padded(nc);
   if (dtype == FMCA_DTYPE_F64)
-    gather_split_kernel<double><<<blocks(npc * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<double><<<blocks(npc / 8 * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   else
-    gather_split_kernel<float><<<blocks(npc * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<float><<<blocks(npc / 8 * RB * nch), nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
   FMCA_CK(cudaGetLastError());

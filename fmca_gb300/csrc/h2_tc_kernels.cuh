@@ -158,27 +158,42 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
                                     const TI* __restrict__ x, int64_t sxi, int64_t sxr,
                                     const unsigned int* __restrict__ cmax,
                                     float* __restrict__ xc, __half* __restrict__ xv) {
+  // one thread per 8 consecutive sources and right-hand side: the 8 FP16
+  // hi (lo) values of a core-matrix row are one 16-byte store
   const int nchunks = (R + kTcRhs - 1) / kTcRhs;
   const int64_t np = (int64_t)um_padded(n);
-  const int64_t per = np * kTcRhs;
-  const int64_t total = per * nchunks;
+  const int64_t nblk = np / 8;
+  const int64_t total = nblk * kTcRhs * nchunks;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ch = e / per, rem = e % per;
-    const int64_t i = rem / kTcRhs;
-    const int rr = (int)(rem % kTcRhs);
+    const int rr = (int)(e % kTcRhs);
+    const int64_t blk = (e / kTcRhs) % nblk, ch = e / (kTcRhs * nblk);
     const int r = (int)ch * kTcRhs + rr;
-    float v = 0.f;
-    if (r < R && i < n) {
-      const int64_t src = perm ? (int64_t)perm[i] : i;
-      const int ex = scale_exp(__uint_as_float(cmax[r]));
-      v = ldexpf((float)x[src * sxi + (int64_t)r * sxr], -ex);
+    const int ex = r < R ? scale_exp(__uint_as_float(cmax[r])) : 0;
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int jj = 0; jj < 8; jj += 2) {
+      float v[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int64_t i = blk * 8 + jj + t;
+        v[t] = 0.f;
+        if (r < R && i < n) {
+          const int64_t src = perm ? (int64_t)perm[i] : i;
+          v[t] = ldexpf((float)x[src * sxi + (int64_t)r * sxr], -ex);
+        }
+        if (i < n) xc[(ch * n + i) * kTcRhs + rr] = v[t];
+      }
+      const __half2 h = __floats2half2_rn(v[0], v[1]);
+      const float2 hf = __half22float2(h);
+      hw[jj / 2] = h2_bits(h);
+      lw[jj / 2] = h2_bits(__floats2half2_rn(v[0] - hf.x, v[1] - hf.y));
     }
-    if (i < n) xc[(ch * n + i) * kTcRhs + rr] = v;
-    const __half h = __float2half_rn(v);
-    __half* o = xv + (size_t)ch * per * 2;
-    o[um_val_index((size_t)i, rr, 0)] = h;
-    o[um_val_index((size_t)i, rr, 1)] = __float2half_rn(v - __half2float(h));
+    __half* o = xv + (size_t)ch * np * kTcRhs * 2;
+    *reinterpret_cast<uint4*>(o + um_val_index((size_t)blk * 8, rr, 0)) =
+        make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(o + um_val_index((size_t)blk * 8, rr, 1)) =
+        make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
 }
 
@@ -322,16 +337,28 @@ __global__ void scatter_scaled_kernel(const uint32_t* __restrict__ perm, int64_t
                                       const float* __restrict__ yfar,
                                       const unsigned int* __restrict__ cmax, double sigma2,
                                       TO* __restrict__ y, int64_t syi, int64_t syr) {
+  // FP64 arithmetic is scarce on this part: one add and one multiply per
+  // element, with the column's scale sigma2 * 2^e_r formed from its
+  // exponent bits (v * (sigma2 2^e) rounds once, like ldexp(sigma2 v, e))
   const int64_t total = n * (int64_t)R;
+  const bool small = total < (int64_t)1 << 31;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / R;
-    const int r = (int)(e % R);
+    int64_t i;
+    int r;
+    if (small) {
+      i = (uint32_t)e / (uint32_t)R;
+      r = (int)((uint32_t)e - (uint32_t)i * (uint32_t)R);
+    } else {
+      i = e / R;
+      r = (int)(e % R);
+    }
     const int64_t k = ((int64_t)(r / kTcRhs) * n + i) * kTcRhs + r % kTcRhs;
     const int64_t dst = perm ? (int64_t)perm[i] : i;
     const double v = (double)ynear[k] + (double)yfar[k];
     const int ex = scale_exp(__uint_as_float(cmax[r]));
-    y[dst * syi + (int64_t)r * syr] = (TO)(ldexp(sigma2 * v, ex));
+    const double sc = sigma2 * __longlong_as_double((long long)(ex + 1023) << 52);
+    y[dst * syi + (int64_t)r * syr] = (TO)(v * sc);
   }
 }
 
