@@ -533,17 +533,52 @@ cudaError_t launch_ksum(int rb, const GroupList& gl, const Pt4<T>* tgt,
   }
 }
 
+// one transfer level (M2M when UP, else L2L) over the nb clusters of list.
+// A level with fewer than two clusters per SM splits the right-hand sides
+// over blockIdx.y in slices of 8, so that it still spreads over the GPU.
+template <typename T, int RB, bool UP>
+void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
+                     const int32_t* nsons, const int32_t* parent, const T* E,
+                     const int* midx, const InterpDev<T>& ip, T* buf, int ld,
+                     int rofs, int rcount, cudaStream_t st) {
+  const size_t tail = (size_t)ip.q * sizeof(int);
+  if constexpr (RB > 8) {
+    if (nb < 2 * 152 && rcount > 8) {
+      constexpr int RS = 8;
+      auto kern = transfer_kernel<T, RS, UP>;
+      const size_t smem = (192 + kTransferChunk * RS) * sizeof(T) + tail;
+      ensure_smem(kern, smem);
+      kern<<<dim3(nb, (rcount + RS - 1) / RS), 128, smem, st>>>(
+          list, son0, nsons, parent, E, midx, ip, buf, ld, rofs, rcount);
+      return;
+    }
+  }
+  auto kern = transfer_kernel<T, RB, UP>;
+  const size_t smem = (192 + kTransferChunk * RB) * sizeof(T) + tail;
+  ensure_smem(kern, smem);
+  kern<<<nb, 128, smem, st>>>(list, son0, nsons, parent, E, midx, ip, buf, ld, rofs,
+                              rcount);
+}
+
+template <typename T, int RB>
+size_t leafmom_smem(int q) {
+  return (size_t)kLeafChunk * (24 + RB) * sizeof(T) + (size_t)q * sizeof(int);
+}
+template <typename T, int RB>
+size_t leafgather_smem(int q) {
+  return ((size_t)128 * 24 + (size_t)q * RB) * sizeof(T) + (size_t)q * sizeof(int);
+}
+
 template <typename T, int RB>
 cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
                             Workspace<T>& w, int ld, int rofs, int rcount,
                             const KParams<T>& kp, cudaStream_t st) {
   const int q = plan.interp.q;
-  const size_t midx_bytes = (size_t)q * 3 * sizeof(int);
   // upward pass: leaf moments
   {
     dp->launches += dp->nleaves_c ? 1 : 0;
     auto kern = leafmom_kernel<T, RB>;
-    const size_t smem = (64 * 24 + 64 * RB) * sizeof(T) + midx_bytes;
+    const size_t smem = leafmom_smem<T, RB>(q);
     ensure_smem(kern, smem);
     if (dp->nleaves_c)
       kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
@@ -552,21 +587,16 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     dp->mark(FMCA_STAGE_LEAFMOM, st);
   }
   // M2M, bottom-up
-  {
-    auto kern = transfer_kernel<T, RB, true>;
-    const size_t smem = (192 + 64 * RB) * sizeof(T) + midx_bytes;
-    ensure_smem(kern, smem);
-    for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
-      const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
-      if (nb) {
-        kern<<<nb, 128, smem, st>>>(dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
-                                    dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip,
-                                    w.t, ld, rofs, rcount);
-        ++dp->launches;
-      }
+  for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
+    const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
+    if (nb) {
+      launch_transfer<T, RB, true>(nb, dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
+                                   dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip, w.t, ld,
+                                   rofs, rcount, st);
+      ++dp->launches;
     }
-    dp->mark(FMCA_STAGE_M2M, st);
   }
+  dp->mark(FMCA_STAGE_M2M, st);
   // far-field coupling
   cudaError_t e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s,
                                  rofs, rcount, kp, 0, dp->err_flag, st);
@@ -574,25 +604,20 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
   dp->launches += dp->far.ngroups ? 1 : 0;
   dp->mark(FMCA_STAGE_FAR, st);
   // L2L, top-down
-  {
-    auto kern = transfer_kernel<T, RB, false>;
-    const size_t smem = (192 + 64 * RB) * sizeof(T) + midx_bytes;
-    ensure_smem(kern, smem);
-    for (int l = 1; l < plan.rows.nlevels(); ++l) {
-      const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
-      if (nb) {
-        kern<<<nb, 128, smem, st>>>(dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
-                                    dp->parent_r, S.E_r, dp->midx, S.ip, w.s, ld,
-                                    rofs, rcount);
-        ++dp->launches;
-      }
+  for (int l = 1; l < plan.rows.nlevels(); ++l) {
+    const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
+    if (nb) {
+      launch_transfer<T, RB, false>(nb, dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
+                                    dp->parent_r, S.E_r, dp->midx, S.ip, w.s, ld, rofs,
+                                    rcount, st);
+      ++dp->launches;
     }
-    dp->mark(FMCA_STAGE_L2L, st);
   }
+  dp->mark(FMCA_STAGE_L2L, st);
   // leaf gather
   {
     auto kern = leafgather_kernel<T, RB>;
-    const size_t smem = (128 * 24 + 64 * RB) * sizeof(T) + midx_bytes;
+    const size_t smem = leafgather_smem<T, RB>(q);
     ensure_smem(kern, smem);
     if (dp->nleaves_r)
       kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
@@ -912,7 +937,6 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   dp->launches += 2;
   dp->mark(FMCA_STAGE_GATHER, st);
   const size_t q = plan.interp.q;
-  const size_t midx_bytes = q * 3 * sizeof(int);
   const int Cc = plan.cols.nclusters(), Cr = plan.rows.nclusters();
   for (int ch = 0; ch < nch; ++ch) {
     const int rcount = std::min(RB, nrhs - ch * RB);
@@ -922,7 +946,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     float* yfar = w.yfar + (size_t)ch * nr * ld;
     {
       auto kern = leafmom_kernel<float, RB>;
-      const size_t smem = (64 * 24 + 64 * RB) * sizeof(float) + midx_bytes;
+      const size_t smem = leafmom_smem<float, RB>((int)q);
       ensure_smem(kern, smem);
       if (dp->nleaves_c) {
         kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
@@ -932,20 +956,16 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       }
       dp->mark(FMCA_STAGE_LEAFMOM, st);
     }
-    {
-      auto kern = transfer_kernel<float, RB, true>;
-      const size_t smem = (192 + 64 * RB) * sizeof(float) + midx_bytes;
-      ensure_smem(kern, smem);
-      for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
-        const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
-        if (nb) {
-          kern<<<nb, 128, smem, st>>>(dp->m2m_list + dp->m2m_ptr[l], dp->son0_c, dp->nsons_c,
-                                      nullptr, S.E_c, dp->midx, S.ip, t, ld, 0, rcount);
-          ++dp->launches;
-        }
+    for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
+      const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
+      if (nb) {
+        launch_transfer<float, RB, true>(nb, dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
+                                         dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip, t, ld,
+                                         0, rcount, st);
+        ++dp->launches;
       }
-      dp->mark(FMCA_STAGE_M2M, st);
     }
+    dp->mark(FMCA_STAGE_M2M, st);
     const bool grid = grid_far(plan);
     if (grid)
       tscale_grid_kernel<<<Cc, 128, 0, st>>>(Cc, rcount, t, S.nodes_c, dp->midx, kp.g, w.tv,
@@ -958,23 +978,19 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
                          dp->err_flag, st, grid));
     dp->launches += dp->far_tc.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
-    {
-      auto kern = transfer_kernel<float, RB, false>;
-      const size_t smem = (192 + 64 * RB) * sizeof(float) + midx_bytes;
-      ensure_smem(kern, smem);
-      for (int l = 1; l < plan.rows.nlevels(); ++l) {
-        const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
-        if (nb) {
-          kern<<<nb, 128, smem, st>>>(dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
-                                      dp->parent_r, S.E_r, dp->midx, S.ip, s, ld, 0, rcount);
-          ++dp->launches;
-        }
+    for (int l = 1; l < plan.rows.nlevels(); ++l) {
+      const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
+      if (nb) {
+        launch_transfer<float, RB, false>(nb, dp->l2l_list + dp->l2l_ptr[l], nullptr,
+                                          nullptr, dp->parent_r, S.E_r, dp->midx, S.ip, s,
+                                          ld, 0, rcount, st);
+        ++dp->launches;
       }
-      dp->mark(FMCA_STAGE_L2L, st);
     }
+    dp->mark(FMCA_STAGE_L2L, st);
     {
       auto kern = leafgather_kernel<float, RB>;
-      const size_t smem = (128 * 24 + 64 * RB) * sizeof(float) + midx_bytes;
+      const size_t smem = leafgather_smem<float, RB>((int)q);
       ensure_smem(kern, smem);
       if (dp->nleaves_r) {
         kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,

@@ -34,6 +34,8 @@ namespace fmca {
 namespace gpu {
 
 constexpr double kDblEps = 2.220446049250313080847263336181640625e-16;
+constexpr int kLeafChunk = 128;      // points per shared-memory chunk of leafmom_kernel
+constexpr int kTransferChunk = 128;  // source coefficients per chunk of transfer_kernel
 
 template <typename T>
 struct alignas(4 * sizeof(T)) Pt4 {
@@ -480,19 +482,107 @@ __global__ void ksum_kernel(const KGroup* __restrict__ groups,
 
 // ---------------------------------------------------------------------------
 // 1-D barycentric Lagrange factors, same guard and operation order as the
-// host (TensorProductInterpolator.h:65-81)
+// host (TensorProductInterpolator.h:65-81); factor a is stored at f[a * stride]
 template <typename T>
-__device__ __forceinline__ void lagrange1d(const InterpDev<T>& ip, T x, T* f) {
+__device__ __forceinline__ void lagrange1d(const InterpDev<T>& ip, T x, T* f,
+                                           int stride = 1) {
   T weight = T(0);
   for (int k = 0; k < ip.p1; ++k) weight += ip.w[k] / (x - ip.xi[k]);
   for (int a = 0; a < ip.p1; ++a) {
     const T dxa = x - ip.xi[a];
-    f[a] = (fabs(dxa) > T(kDblEps)) ? ip.w[a] / dxa / weight : T(1);
+    f[a * stride] = (fabs(dxa) > T(kDblEps)) ? ip.w[a] / dxa / weight : T(1);
   }
 }
 
+// multi-index k -> (k0, k1, k2) packed as k0 | k1 << 8 | k2 << 16 (digits < 8)
+__device__ __forceinline__ void pack_digits(const int* __restrict__ midx_g, int q,
+                                            int* __restrict__ pk) {
+  for (int i = threadIdx.x; i < q; i += blockDim.x)
+    pk[i] = midx_g[i * 3] | (midx_g[i * 3 + 1] << 8) | (midx_g[i * 3 + 2] << 16);
+}
+
+// Copies rows [0, cnt) of a block with leading dimension ldv, columns
+// rofs .. rofs + rcount - 1, into a dense cnt x RB tile in shared memory and
+// zero-fills columns rcount .. RB - 1.  Each thread issues U loads before it
+// stores any of them, so that their latencies overlap; full rows at 16-byte
+// aligned addresses move as 16-byte vectors.
+template <typename T, int RB>
+__device__ __forceinline__ void stage_rows(T* __restrict__ dst, const T* src, int cnt,
+                                           int ldv, int rofs, int rcount) {
+  constexpr int U = 8;
+  constexpr int VW = 16 / (int)sizeof(T);
+  const int nthr = blockDim.x, tid = threadIdx.x;
+  if constexpr (RB % VW == 0) {
+    if (rcount == RB && (ldv % VW) == 0 && (rofs % VW) == 0 &&
+        (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      constexpr int VPR = RB / VW;
+      const int total = cnt * VPR, ld4 = ldv / VW;
+      const uint4* s4 = reinterpret_cast<const uint4*>(src + rofs);
+      uint4* d4 = reinterpret_cast<uint4*>(dst);
+      for (int i0 = tid; i0 < total; i0 += U * nthr) {
+        uint4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * nthr;
+          v[u] = i < total ? s4[(size_t)(i / VPR) * ld4 + i % VPR] : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (i0 + u * nthr < total) d4[i0 + u * nthr] = v[u];
+      }
+      return;
+    }
+  }
+  const int total = cnt * RB;
+  for (int i0 = tid; i0 < total; i0 += U * nthr) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nthr, r = i % RB;
+      v[u] = (i < total && r < rcount) ? src[(size_t)(i / RB) * ldv + rofs + r] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i0 + u * nthr < total) dst[i0 + u * nthr] = v[u];
+  }
+}
+
+// o[r] = acc[r] (ADD: o[r] += acc[r]) for r < rc, as 16-byte vectors when the
+// row is full and aligned
+template <typename T, int RB, bool ADD>
+__device__ __forceinline__ void store_row(T* o, const T (&acc)[RB], int rc) {
+  if (rc == RB && (reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+    if constexpr (sizeof(T) == 4 && RB % 4 == 0) {
+#pragma unroll
+      for (int r = 0; r < RB; r += 4) {
+        float4 v = make_float4(acc[r], acc[r + 1], acc[r + 2], acc[r + 3]);
+        if (ADD) {
+          const float4 u = *reinterpret_cast<const float4*>(o + r);
+          v = make_float4(u.x + v.x, u.y + v.y, u.z + v.z, u.w + v.w);
+        }
+        *reinterpret_cast<float4*>(o + r) = v;
+      }
+      return;
+    } else if constexpr (sizeof(T) == 8 && RB % 2 == 0) {
+#pragma unroll
+      for (int r = 0; r < RB; r += 2) {
+        double2 v = make_double2(acc[r], acc[r + 1]);
+        if (ADD) {
+          const double2 u = *reinterpret_cast<const double2*>(o + r);
+          v = make_double2(u.x + v.x, u.y + v.y);
+        }
+        *reinterpret_cast<double2*>(o + r) = v;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RB; ++r)
+    if (r < rc) o[r] = ADD ? o[r] + acc[r] : acc[r];
+}
+
 // leaf moments: t[c][k][r] = sum_i V_c[k][i] x[i][r]
-// blockDim 128; shared: midx q*3 ints, F[64][3][8], X[64][RB]
+// blockDim 128; shared: F[CH][3][8], X[CH][RB], packed digits q ints
 template <typename T, int RB>
 __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
                                const uint32_t* __restrict__ cbegin,
@@ -503,62 +593,56 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
                                const T* __restrict__ xc, int ldv, int rofs,
                                int rcount, const int* __restrict__ midx_g,
                                InterpDev<T> ip, T* __restrict__ tout) {
-  constexpr int CH = 64;
+  constexpr int CH = kLeafChunk;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* F = reinterpret_cast<T*>(smem_raw);  // CH x 3 x 8
   T* X = F + CH * 24;                     // CH x RB
-  int* midx = reinterpret_cast<int*>(X + CH * RB);
+  int* pk = reinterpret_cast<int*>(X + CH * RB);
   const int c = leaves[blockIdx.x];
   const uint32_t b = cbegin[c], n = csize[c];
-  const int q = ip.q, tid = threadIdx.x;
-  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  const int q = ip.q, tid = threadIdx.x, nthr = blockDim.x;
+  pack_digits(midx_g, q, pk);
   T lo[3], ex[3];
   for (int d = 0; d < 3; ++d) {
     lo[d] = d < ip.dim ? bbmin[c * 3 + d] : T(0);
     ex[d] = d < ip.dim ? bbext[c * 3 + d] : T(1);
   }
-  __syncthreads();
-  for (int kc = 0; kc < q; kc += blockDim.x) {
+  for (int kc = 0; kc < q; kc += nthr) {
     const int k = kc + tid;
     const bool valid = k < q;
-    const int m0 = valid ? midx[k * 3 + 0] : 0;
-    const int m1 = valid ? midx[k * 3 + 1] : 0;
-    const int m2 = valid ? midx[k * 3 + 2] : 0;
+    __syncthreads();
+    const int kd = valid ? pk[k] : 0;
+    const int m0 = kd & 255, m1 = 8 + ((kd >> 8) & 255), m2 = kd >> 16;
     T acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = T(0);
     for (uint32_t i0 = 0; i0 < n; i0 += CH) {
       const int cnt = (int)((n - i0) < (uint32_t)CH ? (n - i0) : CH);
-      if (tid < cnt) {
-        const Pt4<T> p = pts[b + i0 + tid];
-        const T pc[3] = {p.x, p.y, p.z};
-        for (int d = 0; d < 3; ++d) {
-          T* f = F + (tid * 3 + d) * 8;
-          if (d < ip.dim)
-            lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f);
-          else
-            f[0] = T(1);
+      for (int t = tid; t < cnt * 3; t += nthr) {
+        const int i = t / 3, d = t - 3 * i;
+        T* f = F + t * 8;
+        if (d < ip.dim) {
+          const T x = reinterpret_cast<const T*>(pts + b + i0 + i)[d];
+          const T lod = d == 0 ? lo[0] : (d == 1 ? lo[1] : lo[2]);
+          const T exd = d == 0 ? ex[0] : (d == 1 ? ex[1] : ex[2]);
+          lagrange1d(ip, (x - lod) / exd, f);
+        } else {
+          f[0] = T(1);
         }
       }
-      for (int e = tid; e < cnt * RB; e += blockDim.x) {
-        const int i = e / RB, r = e % RB;
-        X[e] = (r < rcount) ? xc[(size_t)(b + i0 + i) * ldv + rofs + r] : T(0);
-      }
+      stage_rows<T, RB>(X, xc + (size_t)(b + i0) * ldv, cnt, ldv, rofs, rcount);
       __syncthreads();
       if (valid) {
         for (int i = 0; i < cnt; ++i) {
-          const T v = F[(i * 3 + 0) * 8 + m0] * F[(i * 3 + 1) * 8 + m1] *
-                      F[(i * 3 + 2) * 8 + m2];
+          const T* f = F + i * 24;
+          const T v = f[m0] * f[m1] * f[16 + m2];
 #pragma unroll
           for (int r = 0; r < RB; ++r) acc[r] += v * X[i * RB + r];
         }
       }
       __syncthreads();
     }
-    if (valid) {
-      T* o = tout + ((size_t)c * q + k) * ldv + rofs;
-      for (int r = 0; r < rcount; ++r) o[r] = acc[r];
-    }
+    if (valid) store_row<T, RB, false>(tout + ((size_t)c * q + k) * ldv + rofs, acc, rcount);
   }
 }
 
@@ -567,7 +651,9 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
 // up == false (L2L): for each cluster c in list (level >= 1),
 //   s[c][j] += sum_k E_c[k][j] s[parent][k]
 // E_c[k][j] = e_c[0][k0][j0] * e_c[1][k1][j1] * e_c[2][k2][j2]
-// shared: midx q*3, e[3][8][8], S[64][RB]
+// blockIdx.y selects right-hand sides rofs + RB * blockIdx.y onwards, so that
+// a level with few clusters still spreads over many SMs.
+// shared: e[3][8][8], S[JC][RB], packed digits q ints
 template <typename T, int RB, bool UP>
 __global__ void transfer_kernel(const int32_t* __restrict__ clist,
                                 const int32_t* __restrict__ son0,
@@ -575,68 +661,64 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
                                 const int32_t* __restrict__ parent,
                                 const T* __restrict__ E,
                                 const int* __restrict__ midx_g, InterpDev<T> ip,
-                                T* __restrict__ buf, int ldv, int rofs,
-                                int rcount) {
-  constexpr int JC = 64;
+                                T* buf, int ldv, int rofs, int rcount) {
+  constexpr int JC = kTransferChunk;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* e = reinterpret_cast<T*>(smem_raw);  // 3 x 8 x 8
   T* S = e + 192;                         // JC x RB
-  int* midx = reinterpret_cast<int*>(S + JC * RB);
+  int* pk = reinterpret_cast<int*>(S + JC * RB);
   const int c = clist[blockIdx.x];
-  const int q = ip.q, p1 = ip.p1, tid = threadIdx.x;
-  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  const int q = ip.q, p1 = ip.p1, tid = threadIdx.x, nthr = blockDim.x;
+  const int rofs_b = rofs + (int)blockIdx.y * RB;
+  const int rc = min(RB, rcount - (int)blockIdx.y * RB);
+  pack_digits(midx_g, q, pk);
   const int nsrc = UP ? nsons[c] : 1;
-  for (int kc = 0; kc < q; kc += blockDim.x) {
+  for (int kc = 0; kc < q; kc += nthr) {
     const int k = kc + tid;  // output index
     const bool valid = k < q;
+    __syncthreads();
+    const int kd = valid ? pk[k] : 0;
+    // UP: E_son[k][jj] = e[d][k_d][j_d]; DOWN: E_c[jj][k] = e[d][j_d][k_d]
+    const int b0 = UP ? (kd & 255) * 8 : (kd & 255);
+    const int b1 = 64 + (UP ? ((kd >> 8) & 255) * 8 : ((kd >> 8) & 255));
+    const int b2 = 128 + (UP ? (kd >> 16) * 8 : (kd >> 16));
+    const int sh = UP ? 0 : 3;
     T acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = T(0);
     for (int si = 0; si < nsrc; ++si) {
-      const int ec = UP ? son0[c] + si : c;       // cluster whose E is used
+      const int ec = UP ? son0[c] + si : c;          // cluster whose E is used
       const int sc = UP ? son0[c] + si : parent[c];  // source moments
-      __syncthreads();
-      for (int i = tid; i < 192; i += blockDim.x) {
-        const int d = i / 64, a = (i / 8) % 8, bb = i % 8;
-        e[i] = (d < ip.dim && a < p1 && bb < p1)
-                   ? E[(((size_t)ec * ip.dim + d) * p1 + a) * p1 + bb]
-                   : ((a == 0 && bb == 0) ? T(1) : T(0));
-      }
       for (int j0 = 0; j0 < q; j0 += JC) {
         const int cnt = (q - j0) < JC ? (q - j0) : JC;
         __syncthreads();
-        for (int i = tid; i < cnt * RB; i += blockDim.x) {
-          const int j = i / RB, r = i % RB;
-          S[i] = (r < rcount) ? buf[((size_t)sc * q + j0 + j) * ldv + rofs + r]
-                              : T(0);
+        if (j0 == 0) {
+          for (int i = tid; i < 192; i += nthr) {
+            const int d = i / 64, a = (i / 8) % 8, bb = i % 8;
+            e[i] = (d < ip.dim && a < p1 && bb < p1)
+                       ? E[(((size_t)ec * ip.dim + d) * p1 + a) * p1 + bb]
+                       : ((a == 0 && bb == 0) ? T(1) : T(0));
+          }
         }
+        stage_rows<T, RB>(S, buf + ((size_t)sc * q + j0) * ldv, cnt, ldv, rofs_b, rc);
         __syncthreads();
         if (valid) {
-          const int k0 = midx[k * 3], k1 = midx[k * 3 + 1], k2 = midx[k * 3 + 2];
           for (int j = 0; j < cnt; ++j) {
-            const int jj = j0 + j;
-            const int j0_ = midx[jj * 3], j1_ = midx[jj * 3 + 1],
-                      j2_ = midx[jj * 3 + 2];
-            // UP: E_son[k][jj]; DOWN: E_c[jj][k] (transpose)
-            const T ev = UP ? e[0 * 64 + k0 * 8 + j0_] * e[1 * 64 + k1 * 8 + j1_] *
-                                  e[2 * 64 + k2 * 8 + j2_]
-                            : e[0 * 64 + j0_ * 8 + k0] * e[1 * 64 + j1_ * 8 + k1] *
-                                  e[2 * 64 + j2_ * 8 + k2];
+            const int jd = pk[j0 + j];
+            const T ev = e[b0 + ((jd & 255) << sh)] * e[b1 + (((jd >> 8) & 255) << sh)] *
+                         e[b2 + ((jd >> 16) << sh)];
 #pragma unroll
             for (int r = 0; r < RB; ++r) acc[r] += ev * S[j * RB + r];
           }
         }
       }
     }
-    if (valid) {
-      T* o = buf + ((size_t)c * q + k) * ldv + rofs;
-      for (int r = 0; r < rcount; ++r) o[r] = UP ? acc[r] : o[r] + acc[r];
-    }
+    if (valid) store_row<T, RB, !UP>(buf + ((size_t)c * q + k) * ldv + rofs_b, acc, rc);
   }
 }
 
 // leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves
-// shared: F[blockDim][3][8], S[64][RB], midx q*3
+// shared: F[24][blockDim] (one column per thread), S[q][RB], packed digits q ints
 template <typename T, int RB>
 __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
                                   const uint32_t* __restrict__ cbegin,
@@ -647,59 +729,43 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
                                   const T* __restrict__ s, int ldv, int rofs,
                                   int rcount, const int* __restrict__ midx_g,
                                   InterpDev<T> ip, T* __restrict__ yout) {
-  constexpr int KC = 64;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  T* F = reinterpret_cast<T*>(smem_raw);   // blockDim x 24
-  T* S = F + blockDim.x * 24;              // KC x RB
-  int* midx = reinterpret_cast<int*>(S + KC * RB);
+  const int q = ip.q, tid = threadIdx.x, nthr = blockDim.x;
+  T* F = reinterpret_cast<T*>(smem_raw);  // 24 x blockDim
+  T* S = F + nthr * 24;                   // q x RB
+  int* pk = reinterpret_cast<int*>(S + (size_t)q * RB);
   const int c = leaves[blockIdx.x];
   const uint32_t b = cbegin[c], n = csize[c];
-  const int q = ip.q, tid = threadIdx.x;
-  for (int i = tid; i < q * 3; i += blockDim.x) midx[i] = midx_g[i];
+  pack_digits(midx_g, q, pk);
   T lo[3], ex[3];
   for (int d = 0; d < 3; ++d) {
     lo[d] = d < ip.dim ? bbmin[c * 3 + d] : T(0);
     ex[d] = d < ip.dim ? bbext[c * 3 + d] : T(1);
   }
-  T* f = F + tid * 24;
-  for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
-    const bool valid = i0 + tid < n;
-    if (valid) {
-      const Pt4<T> p = pts[b + i0 + tid];
-      const T pc[3] = {p.x, p.y, p.z};
-      for (int d = 0; d < 3; ++d) {
-        if (d < ip.dim)
-          lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8);
-        else
-          f[d * 8] = T(1);
-      }
+  stage_rows<T, RB>(S, s + (size_t)c * q * ldv, q, ldv, rofs, rcount);
+  __syncthreads();
+  T* f = F + tid;
+  for (uint32_t i0 = 0; i0 < n; i0 += nthr) {
+    if (i0 + tid >= n) break;
+    const Pt4<T> p = pts[b + i0 + tid];
+    const T pc[3] = {p.x, p.y, p.z};
+    for (int d = 0; d < 3; ++d) {
+      if (d < ip.dim)
+        lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8 * nthr, nthr);
+      else
+        f[d * 8 * nthr] = T(1);
     }
     T acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = T(0);
-    for (int k0 = 0; k0 < q; k0 += KC) {
-      const int cnt = (q - k0) < KC ? (q - k0) : KC;
-      __syncthreads();
-      for (int i = tid; i < cnt * RB; i += blockDim.x) {
-        const int k = i / RB, r = i % RB;
-        S[i] = (r < rcount) ? s[((size_t)c * q + k0 + k) * ldv + rofs + r] : T(0);
-      }
-      __syncthreads();
-      if (valid) {
-        for (int k = 0; k < cnt; ++k) {
-          const int kk = k0 + k;
-          const T v = f[midx[kk * 3]] * f[8 + midx[kk * 3 + 1]] *
-                      f[16 + midx[kk * 3 + 2]];
+    for (int k = 0; k < q; ++k) {
+      const int kd = pk[k];
+      const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
+                  f[(16 + (kd >> 16)) * nthr];
 #pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
-        }
-      }
+      for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
     }
-    if (valid) {
-      T* o = yout + (size_t)(b + i0 + tid) * ldv + rofs;
-      for (int r = 0; r < rcount; ++r) o[r] = acc[r];
-    }
-    __syncthreads();
+    store_row<T, RB, false>(yout + (size_t)(b + i0 + tid) * ldv + rofs, acc, rcount);
   }
 }
 
