@@ -813,22 +813,22 @@ cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                         bool grid = false) {
   const int threads = 32 * (3 + 4 * NSETS);
-  if constexpr (H == 1 && NSETS == 4) {
+  if constexpr (H == 1) {
     if (grid) {
-      auto kern = ksum_um_kernel<KT, H, NSETS, true, true>;
-      ensure_smem(kern, kUmSmemBytes);
-      kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
-                                                       kTcRhs, rcount, kp, q, errf);
+      auto kern = ksum_grid_kernel<KT>;
+      ensure_smem(kern, kGridSmemBytes);
+      kern<<<gl.ngroups, 32 * (3 + 4 * kGridSets), kGridSmemBytes, st>>>(
+          gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, errf);
       return cudaGetLastError();
     }
   }
   if (q > 0) {
-    auto kern = ksum_um_kernel<KT, H, NSETS, true, false>;
+    auto kern = ksum_um_kernel<KT, H, NSETS, true>;
     ensure_smem(kern, kUmSmemBytes);
     kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, q, errf);
   } else {
-    auto kern = ksum_um_kernel<KT, H, NSETS, false, false>;
+    auto kern = ksum_um_kernel<KT, H, NSETS, false>;
     ensure_smem(kern, kUmSmemBytes);
     kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
                                                      kTcRhs, rcount, kp, 0, errf);

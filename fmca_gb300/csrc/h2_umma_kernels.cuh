@@ -175,11 +175,7 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // H: target halves of 128 (groups of up to 128 H targets); NSETS: sets of
 // 4 evaluation warps; REL: sources are interpolation nodes (q per cluster)
 // weighted by their cluster's moment exponent, else points of weight 1.
-// GRID (with REL, H = 1, NSETS = 4, q = kGridP1^3 in 3-D): every tile is one
-// source cluster on its tensor grid (tscale_grid_kernel layout; `pairs`
-// holds the clusters' 64-byte grid-line records) and set s evaluates the
-// chunks 2 s and 2 s + 1.
-template <int KT, int H, int NSETS, bool REL, bool GRID>
+template <int KT, int H, int NSETS, bool REL>
 __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
@@ -207,7 +203,6 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
   static_assert(NSLOT_FIT >= 4, "tensor-memory budget");
   constexpr uint32_t IDESC64 = umma_idesc_f16(128, 64);
   constexpr uint32_t IDESC32 = umma_idesc_f16(128, 32);
-  static_assert(!GRID || (REL && H == 1 && NSETS == 4), "grid tiles: one half, four sets");
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -234,15 +229,13 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // tiles of the group: its intervals widened to multiples of 8 sources
-  // (grid: one tile per source cluster)
   int ntiles;
   {
     uint32_t rows = 0;
     for (int i = g.ivl_begin + lane; i < g.ivl_end; i += 32)
-      rows += GRID ? (ivl[2 * i + 1] - ivl[2 * i]) / (uint32_t)q
-                   : ((ivl[2 * i + 1] + 7u) & ~7u) - (ivl[2 * i] & ~7u);
+      rows += ((ivl[2 * i + 1] + 7u) & ~7u) - (ivl[2 * i] & ~7u);
     for (int o = 16; o > 0; o >>= 1) rows += __shfl_xor_sync(0xffffffffu, rows, o);
-    ntiles = GRID ? (int)rows : (int)((rows + kUmTile - 1) / kUmTile);
+    ntiles = (int)((rows + kUmTile - 1) / kUmTile);
   }
 
   // zero the stages once (rows past the last piece of a tile hold finite
@@ -293,20 +286,6 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
           break;
         }
         unsigned char* sp = stages + (size_t)stage * kUmStageBytes;
-        if constexpr (GRID) {
-          // the next source cluster: its grid-line record and 128 value rows
-          while (pos == 0xffffffffu || pos >= ivl[2 * pi + 1] / (uint32_t)q) {
-            if (pos != 0xffffffffu) ++pi;
-            pos = ivl[2 * pi] / (uint32_t)q;
-          }
-          const uint32_t sigma = pos++;
-          mbar_expect_tx(&full[stage], 64u + (uint32_t)kUmValBytes);
-          bulk_g2s(sp, pairs + (size_t)sigma * 4, 64u, &full[stage]);
-          bulk_g2s(sp + kUmPtsBytes, vals + (size_t)sigma * kGridRows * 2 * kTcRhs,
-                   (uint32_t)kUmValBytes, &full[stage]);
-          ++issued;
-          continue;
-        }
         // pieces: the group's intervals widened to multiples of 8 sources,
         // packed into the tile's 128 rows; every piece posts its bytes on
         // the stage barrier before its copies, and the final arrival (after
@@ -423,12 +402,8 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
       float mx = -CUDART_INF_F;
       for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32)
         for (uint32_t s = ivl[2 * i], e = ivl[2 * i + 1]; s < e; s = (s / q + 1) * q) {
-          if constexpr (GRID) {
-            mx = fmaxf(mx, pairs[(size_t)(s / q) * 4 + 3].w);
-          } else {
-            const float4 r = pairs[2 * (s >> 1) + 1];
-            mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
-          }
+          const float4 r = pairs[2 * (s >> 1) + 1];
+          mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
         }
       for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       if (lane == 0) ered[ew] = mx;
@@ -499,46 +474,8 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
         ok = false;
         break;
       }
-      if constexpr (GRID) {
-        // one source cluster: both chunks of this set from the grid lines
-        const float* X = reinterpret_cast<const float*>(stages + (size_t)stage * kUmStageBytes);
-        const float wv = X[15] - E;
-        uint32_t gh[2][8], gl[2][8];
-        switch (set) {
-          case 0:
-            grid_eval_pair<KT, 0>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          case 1:
-            grid_eval_pair<KT, 1>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          case 2:
-            grid_eval_pair<KT, 2>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          default:
-            grid_eval_pair<KT, 3>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-        }
-#pragma unroll
-        for (int cc = 0; cc < 2; ++cc) {
-          const int c = k * 8 + 2 * set + cc, slot = c % NSLOT;
-          if (c >= NSLOT &&
-              !__all_sync(0xffffffffu,
-                          um_wait(&aempty[slot], (uint32_t)((c / NSLOT - 1) & 1), abort_flag))) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t a = tbase + lanes + A0 + slot * 16;
-          tmem_st8(a, gh[cc]);
-          tmem_st8(a + 8, gl[cc]);
-          tmem_wait_st();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive1(&afull[slot]);
-        }
-      }
       const float4* R4 = reinterpret_cast<const float4*>(stages + (size_t)stage * kUmStageBytes);
-      for (int kk = set; kk < (GRID ? 0 : 8); kk += NSETS) {
+      for (int kk = set; kk < 8; kk += NSETS) {
         const int c = k * 8 + kk, slot = c % NSLOT;
         if (c >= NSLOT &&
             !__all_sync(0xffffffffu,
@@ -616,6 +553,325 @@ __global__ void __launch_bounds__(32 * (3 + 4 * NSETS), 1)
               if (j < rcount) o[j] = acc[j];
           }
         }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tbase, kUmCols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Far field on tensor grids (dimension 3, kGridP1^3 nodes per cluster): one
+// CTA per row cluster (its nodes are the up to 128 targets, one target
+// half) and one tile per admissible source cluster, in the
+// tscale_grid_kernel layout (a 64-byte grid-line record and 128 value rows
+// in grid order). Roles as in ksum_um_kernel (warp 0 producer, warps 1-2 the
+// product threads, warps 3-18 four sets of evaluation warps), with a
+// protocol that keeps the evaluation sets off the products' critical path:
+//   set s evaluates the chunks 2 s and 2 s + 1 of every tile (grid rows
+//     32 s .. 32 s + 31) into the A pair slot (4 k + s) mod 8, so the ring
+//     holds two tiles;
+//   product thread j issues the pairs of sets j and j + 2 of every tile into
+//     its own accumulator of buffer k & 1, commits each pair (aempty) and
+//     the tile (accf[k % 4]);
+//   set k mod 4 adds both accumulators of tile k into its own running total
+//     in shared memory (round-to-nearest FP32 adds per 128 sources, as the
+//     tensor cores truncate their accumulations) after it has written its
+//     A pair of tile k + 1, and then frees the accumulator buffer (acce) and
+//     the stage (empty): the products of tile k completing implies that
+//     every set has read the tile's grid lines. (Flushing before that A
+//     pair instead delays the products of tile k + 1, measured slower.)
+// The four totals are added at the end. Every wait is bounded as in
+// ksum_um_kernel.
+constexpr int kGridSets = 4;
+constexpr size_t kGridTotBytes = (size_t)kGridSets * kTcRhs * 128 * sizeof(float);
+constexpr size_t kGridSmemBytes = kUmHeader + (size_t)kUmStages * kUmStageBytes + kGridTotBytes;
+
+template <int KT>
+__global__ void __launch_bounds__(32 * (3 + 4 * kGridSets), 1)
+    ksum_grid_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
+                     const Pt4<float>* __restrict__ tgt, const float4* __restrict__ rec,
+                     const __half* __restrict__ vals, float* __restrict__ out, int ldo,
+                     int rcount, KParams<float> kp, int* err) {
+  constexpr int NST = kUmStages;
+  constexpr int NSETS = kGridSets, NEVAL = 4 * NSETS;
+  constexpr uint32_t q = kGridP1 * kGridP1 * kGridP1;
+  // tensor-memory columns: accumulators [buffer][thread] x 64 (0..31: the
+  // a_hi v_hi + a_lo v_hi products, 32..63: a_hi v_lo), then NPS pair slots
+  // of 32 (chunk 2 s: hi, lo; chunk 2 s + 1: hi, lo; 8 columns each)
+  constexpr int ACC0 = 0, A0 = 256, NPS = 8;
+  static_assert(A0 + NPS * 32 <= (int)kUmCols, "tensor-memory budget");
+  constexpr uint32_t IDESC64 = umma_idesc_f16(128, 64);
+  constexpr uint32_t IDESC32 = umma_idesc_f16(128, 32);
+
+  if (*reinterpret_cast<volatile int*>(err)) return;
+
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [NST]
+  uint64_t* empty = full + NST;                              // [NST]
+  uint64_t* afull = empty + NST;                             // [NPS]
+  uint64_t* aempty = afull + NPS;                            // [NPS]
+  uint64_t* accf = aempty + NPS;                             // [4]
+  uint64_t* acce = accf + 4;                                 // [2]
+  uint64_t* done = acce + 2;                                 // [2]
+  static_assert(8 * (2 * NST + 2 * NPS + 4 + 2 + 2) <= 512, "barrier area");
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 512);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 516);
+  float* ered = reinterpret_cast<float*>(smem_raw + 640);  // [NEVAL]
+  unsigned char* stages = smem_raw + kUmHeader;
+  // running totals [set][column][target]
+  float* tot = reinterpret_cast<float*>(stages + (size_t)NST * kUmStageBytes);
+
+  const KGroup g = groups[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  int ntiles;  // source clusters of the group
+  {
+    uint32_t n = 0;
+    for (int i = g.ivl_begin + lane; i < g.ivl_end; i += 32)
+      n += (ivl[2 * i + 1] - ivl[2 * i]) / q;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    ntiles = (int)n;
+  }
+  {
+    float4* z = reinterpret_cast<float4*>(tot);
+    for (int i = tid; i < (int)(kGridTotBytes / 16); i += blockDim.x)
+      z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int s = 0; s < NPS; ++s) {
+      mbar_init(&afull[s], 4);
+      mbar_init(&aempty[s], 1);
+    }
+    for (int b = 0; b < 4; ++b) mbar_init(&accf[b], 2);
+    for (int b = 0; b < 2; ++b) mbar_init(&acce[b], 4);
+    mbar_init(&done[0], 1);
+    mbar_init(&done[1], 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tslot, kUmCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (warp == 0) {
+    // ---------------- producer: one source cluster per stage
+    if (lane == 0) {
+      int pi = g.ivl_begin;
+      uint32_t pos = 0xffffffffu;  // next cluster inside interval pi (none yet)
+      int issued = 0;
+      bool ok = true;
+      for (int k = 0; k < ntiles; ++k) {
+        const int stage = k % NST;
+        if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag)) {
+          ok = false;
+          break;
+        }
+        while (pos == 0xffffffffu || pos >= ivl[2 * pi + 1] / q) {
+          if (pos != 0xffffffffu) ++pi;
+          pos = ivl[2 * pi] / q;
+        }
+        const uint32_t sigma = pos++;
+        unsigned char* sp = stages + (size_t)stage * kUmStageBytes;
+        mbar_expect_tx(&full[stage], 64u + (uint32_t)kUmValBytes);
+        bulk_g2s(sp, rec + (size_t)sigma * 4, 64u, &full[stage]);
+        bulk_g2s(sp + kUmPtsBytes, vals + (size_t)sigma * kGridRows * 2 * kTcRhs,
+                 (uint32_t)kUmValBytes, &full[stage]);
+        ++issued;
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // copies still in flight land before the CTA frees its memory
+        for (int k = issued > NST ? issued - NST : 0; k < issued; ++k)
+          mbar_wait_bounded(&full[k % NST], (uint32_t)((k / NST) & 1), kWaitLimitNs / 8);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1 || warp == 2) {
+    // ---------------- tensor-core products (thread j of two)
+    const int j = warp - 1;
+    if (lane == 0) {
+      bool ok = true;
+      for (int k = 0; k < ntiles && ok; ++k) {
+        const int stage = k % NST, b = k & 1;
+        if (!um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag) ||
+            (k >= 2 && !um_wait(&acce[b], (uint32_t)(((k >> 1) - 1) & 1), abort_flag))) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const unsigned char* vt = stages + (size_t)stage * kUmStageBytes + kUmPtsBytes;
+        const uint32_t d = tbase + ACC0 + (b * 2 + j) * 64;
+        for (int s = j; s < NSETS; s += 2) {
+          const int p = 4 * k + s, slot = p % NPS;
+          if (!um_wait(&afull[slot], (uint32_t)((p / NPS) & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+#pragma unroll
+          for (int cc = 0; cc < 2; ++cc) {
+            // B: 16 sources x (32 hi | 32 lo) columns; the N = 32 product
+            // reads the hi half only
+            const uint64_t bd = umma_desc(vt + (2 * s + cc) * 2048, 1024, 128);
+            const uint32_t a = tbase + A0 + slot * 32 + cc * 16;
+            umma_f16_ts(d, a, bd, IDESC64, (s == j && cc == 0) ? 0u : 1u);
+            umma_f16_ts(d, a + 8, bd, IDESC32, 1u);
+          }
+          umma_commit(&aempty[slot]);
+        }
+        if (!ok) break;
+        umma_commit(&accf[k % 4]);
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // products already issued complete before tensor memory is freed
+        umma_commit(&done[j]);
+        mbar_wait_bounded(&done[j], 0, kWaitLimitNs / 8);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- evaluation warps
+    const int ew = warp - 3, set = ew >> 2;
+    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    const int row = (warp & 3) * 32 + lane;
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+    if ((uint32_t)row < g.tcount) {
+      const Pt4<float> pt = tgt[g.tbegin + row];
+      tx = kp.g * pt.x;
+      ty = kp.g * pt.y;
+      tz = kp.g * pt.z;
+    }
+    // largest moment exponent E of the group's source clusters
+    float E;
+    {
+      float mx = -CUDART_INF_F;
+      for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32)
+        for (uint32_t c = ivl[2 * i] / q, ce = ivl[2 * i + 1] / q; c < ce; ++c)
+          mx = fmaxf(mx, rec[(size_t)c * 4 + 3].w);
+      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0) ered[ew] = mx;
+      named_sync(1, NEVAL * 32);
+      float all = -CUDART_INF_F;
+      for (int w = 0; w < NEVAL; ++w) all = fmaxf(all, ered[w]);
+      E = fmaxf(all, -1000.f);  // groups without sources
+    }
+    float* mytot = tot + (size_t)set * kTcRhs * 128 + row;
+
+    bool ok = true;
+    auto flush = [&](int k) {
+      const int b = k & 1;
+      if (!__all_sync(0xffffffffu, um_wait(&accf[k % 4], (uint32_t)((k / 4) & 1), abort_flag))) {
+        ok = false;
+        return;
+      }
+      tc_fence_after();
+#pragma unroll
+      for (int c0 = 0; c0 < 32; c0 += 16) {
+        uint32_t v[16], u[16], t[16], w[16];
+        tmem_ld16(tbase + lanes + ACC0 + b * 128 + c0, v);
+        tmem_ld16(tbase + lanes + ACC0 + b * 128 + 32 + c0, u);
+        tmem_ld16(tbase + lanes + ACC0 + b * 128 + 64 + c0, t);
+        tmem_ld16(tbase + lanes + ACC0 + b * 128 + 96 + c0, w);
+        tmem_wait_ld16(v);
+        tmem_wait_ld16(u);
+        tmem_wait_ld16(t);
+        tmem_wait_ld16(w);
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          mytot[(c0 + i) * 128] += (__uint_as_float(v[i]) + __uint_as_float(u[i])) +
+                                   (__uint_as_float(t[i]) + __uint_as_float(w[i]));
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive1(&acce[b]);
+        if ((warp & 3) == 0) mbar_arrive1(&empty[k % NST]);
+      }
+    };
+
+    for (int k = 0; k < ntiles && ok; ++k) {
+      const int stage = k % NST;
+      if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag))) {
+        ok = false;
+        break;
+      }
+      const float* X = reinterpret_cast<const float*>(stages + (size_t)stage * kUmStageBytes);
+      const float wv = X[15] - E;
+      uint32_t gh[2][8], gl[2][8];
+      switch (set) {
+        case 0:
+          grid_eval_pair<KT, 0>(tx, ty, tz, X, wv, kp, gh, gl);
+          break;
+        case 1:
+          grid_eval_pair<KT, 1>(tx, ty, tz, X, wv, kp, gh, gl);
+          break;
+        case 2:
+          grid_eval_pair<KT, 2>(tx, ty, tz, X, wv, kp, gh, gl);
+          break;
+        default:
+          grid_eval_pair<KT, 3>(tx, ty, tz, X, wv, kp, gh, gl);
+          break;
+      }
+      const int p = 4 * k + set, slot = p % NPS;
+      if (p >= NPS &&
+          !__all_sync(0xffffffffu,
+                      um_wait(&aempty[slot], (uint32_t)((p / NPS - 1) & 1), abort_flag))) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a = tbase + lanes + A0 + slot * 32;
+      tmem_st8(a, gh[0]);
+      tmem_st8(a + 8, gl[0]);
+      tmem_st8(a + 16, gh[1]);
+      tmem_st8(a + 24, gl[1]);
+      tmem_wait_st();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive1(&afull[slot]);
+      if (k >= 1 && (k - 1) % NSETS == set) {
+        flush(k - 1);
+        if (!ok) break;
+      }
+    }
+    if (ok && ntiles >= 1 && (ntiles - 1) % NSETS == set) flush(ntiles - 1);
+    if (!ok) atomicExch(err, 1);
+
+    // all totals are complete: set s adds the four totals of columns
+    // 8 s .. 8 s + 7 and writes them
+    named_sync(1, NEVAL * 32);
+    if (!*abort_flag && (uint32_t)row < g.tcount) {
+      const int eo = (int)E;
+      float acc[8];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const float* t = tot + (size_t)(8 * set + jj) * 128 + row;
+        acc[jj] = ldexpf(((t[0] + t[kTcRhs * 128]) + t[2 * kTcRhs * 128]) + t[3 * kTcRhs * 128],
+                         eo);
+      }
+      float* o = out + (size_t)(g.tbegin + row) * ldo + 8 * set;
+      if (rcount == 32 && ldo == 32) {
+        *reinterpret_cast<float4*>(o) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        *reinterpret_cast<float4*>(o + 4) = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj)
+          if (8 * set + jj < rcount) o[jj] = acc[jj];
       }
     }
   }
