@@ -31,7 +31,6 @@ namespace {
 
 constexpr int kGroupCap = 256;    // targets per ksum CTA (128 threads x 2)
 constexpr int kTcGroupCap = 128;  // targets per far-field tensor-core CTA
-constexpr int kUmSets = 4;        // sets of 4 evaluation warps per tensor-core CTA
 constexpr int kStages = 3;
 template <typename T>
 struct TileSize;
@@ -804,45 +803,42 @@ bool tc_supported(int type, int nrhs) {
 }
 
 // Tensor-core kernel sum over a group list: H target halves of 128 per
-// CTA (groups of up to 128 H targets), NSETS sets of 4 evaluation warps.
-// q > 0: the sources are interpolation nodes (q per cluster) weighted by
-// their cluster's moment exponent; q = 0: points of weight 1.
-template <int KT, int H, int NSETS>
-cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
+// CTA (groups of up to 128 H targets). q > 0: the sources are
+// interpolation nodes (q per cluster) weighted by their cluster's moment
+// exponent; q = 0: points of weight 1. grid: nodes on tensor grids
+// (tscale_grid_kernel layout).
+template <int KT, int H, bool REL, bool GRID>
+cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
-                        const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        bool grid = false) {
-  const int threads = 32 * (3 + 4 * NSETS);
-  if constexpr (H == 1) {
-    if (grid) {
-      auto kern = ksum_grid_kernel<KT>;
-      ensure_smem(kern, kGridSmemBytes);
-      kern<<<gl.ngroups, 32 * (3 + 4 * kGridSets), kGridSmemBytes, st>>>(
-          gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, errf);
-      return cudaGetLastError();
-    }
-  }
-  if (q > 0) {
-    auto kern = ksum_um_kernel<KT, H, NSETS, true>;
-    ensure_smem(kern, kUmSmemBytes);
-    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
-                                                     kTcRhs, rcount, kp, q, errf);
-  } else {
-    auto kern = ksum_um_kernel<KT, H, NSETS, false>;
-    ensure_smem(kern, kUmSmemBytes);
-    kern<<<gl.ngroups, threads, kUmSmemBytes, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out,
-                                                     kTcRhs, rcount, kp, 0, errf);
-  }
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+  auto kern = ksum_um_kernel<KT, H, REL, GRID>;
+  const size_t smem = um_smem_bytes(H);
+  ensure_smem(kern, smem);
+  kern<<<gl.ngroups, 32 * (3 + 4 * kUmSets), smem, st>>>(gl.groups, gl.ivl, tgt, pairs, vals,
+                                                         out, kTcRhs, rcount, kp, q, errf);
   return cudaGetLastError();
 }
 
-template <int H, int NS>
+template <int KT, int H>
+cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
+                        const __half* vals, float* out, int rcount,
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st,
+                        bool grid) {
+  if constexpr (H == 1) {
+    if (grid)
+      return launch_um_v<KT, 1, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+  }
+  if (q > 0)
+    return launch_um_v<KT, H, true, false>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+  return launch_um_v<KT, H, false, false>(gl, tgt, pairs, vals, out, rcount, kp, 0, errf, st);
+}
+
+template <int H>
 cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                         bool grid) {
-#define FMCA_UM(KT) \
-  launch_um_t<KT, H, NS>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid)
+#define FMCA_UM(KT) launch_um_t<KT, H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid)
   switch (kp.type) {
     case 0:
       return FMCA_UM(0);
@@ -874,7 +870,7 @@ cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* 
                       const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                       bool grid = false) {
   if (gl.ngroups == 0) return cudaSuccess;
-  return launch_um_k<H, kUmSets>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid);
+  return launch_um_k<H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid);
 }
 
 bool grid_far(const Plan& plan) {
