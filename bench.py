@@ -36,11 +36,14 @@ if ROOT not in sys.path:
 METRIC = "H2 matvecs/sec (n·RHS/s) at n=1e6, mixed-precision batched vs FP64 GPU at 1e-5 rel err"
 UNIT = "n*RHS/s"
 SMS = 152
-SFU_PER_SM = 16      # special-function-unit results per clock per SM
-SFU_PER_PAIR = 2     # rsqrt and exp2 per point pair (MATERN32)
+# point pairs per clock per SM on the special-function unit: every pair costs
+# one rsqrt.approx (16 results per clock per SM) and one ex2.approx (32 per
+# clock on GB300) on one pipe, 32 / 3 pairs per clock (tests/test_sfu_rates.py;
+# profiles/sfu_rates.md)
+SFU_PAIRS_PER_CLK = 32.0 / 3.0
 # DRAM bytes (read + write) of one near-field kernel-sum launch of the default
 # workload, from one ncu capture (profiles/ksum_um_c2_full.md)
-NEAR_DRAM_BYTES_PER_LAUNCH = 2.607057e9 + 0.118970e9
+NEAR_DRAM_BYTES_PER_LAUNCH = 2.606130e9 + 0.118500e9
 
 
 def _measured_bf16_tflops():
@@ -488,24 +491,25 @@ def main():
 
     # roofline of the dominant kernel, the near-field kernel sum (ksum_um_kernel):
     # every point pair costs one reciprocal square root and one exponential on
-    # the special-function unit (16 results per clock per SM), the binding
-    # unit; the tensor cores run 2 products per 16 sources (N = 64 and N = 32
-    # columns, 192 flops per pair at R = 32)
+    # the special-function unit, the busiest unit of the kernel; the tensor
+    # cores run 2 products per 16 sources (N = 64 and N = 32 columns, 192
+    # flops per pair at R = 32)
     pairs = float(info["near_pairs"])
     t_near = stage_ms["near"] * 1e-3
     sm_mhz = clocks.get("sm_mhz") or 2070.0
-    sfu_peak = SMS * SFU_PER_SM * sm_mhz * 1e6 / 1e9
-    sfu_achieved = SFU_PER_PAIR * pairs / t_near / 1e9
+    sfu_peak = SMS * SFU_PAIRS_PER_CLK * sm_mhz * 1e6 / 1e9
+    sfu_achieved = pairs / t_near / 1e9
     tensor_flops = 2.0 * (2 * args.rhs + args.rhs) * pairs
     roofline = {
         "bound": "sfu", "kernel": "ksum_um_kernel, near field (tcgen05 products, SFU kernel values)",
-        "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gop/s", "frac": sfu_achieved / sfu_peak,
+        "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gpair/s", "frac": sfu_achieved / sfu_peak,
         "traffic": NEAR_DRAM_BYTES_PER_LAUNCH,
-        "work": (f"{SFU_PER_PAIR} SFU operations per point pair x N_nf = {info['near_pairs']} "
-                 "pairs per launch"),
-        "peak_source": (f"{SFU_PER_PAIR} x SFU throughput: {SFU_PER_SM} results/clock/SM x {SMS} "
-                        "SMs at the median SM clock sampled during the timed region (the SFU has "
-                        "no entry in MEASURED_PEAKS.json)"),
+        "work": (f"N_nf = {info['near_pairs']} point pairs per launch, one rsqrt and one "
+                 "exp2 each"),
+        "peak_source": (f"special-function unit: {SFU_PAIRS_PER_CLK:.2f} pairs/clock/SM (rsqrt "
+                        "16 and ex2 32 results/clock/SM on one pipe, measured by "
+                        f"tests/test_sfu_rates.py) x {SMS} SMs at the median SM clock sampled "
+                        "during the timed region (the SFU has no entry in MEASURED_PEAKS.json)"),
         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one near-field launch "
                           "(profiles/ksum_um_c2_full.md)",
         "tensor": {"achieved": tensor_flops / t_near / 1e12, "peak": BF16_TFLOPS,
