@@ -423,9 +423,10 @@ KParams<T> make_kparams(const KernelDesc& k) {
   kp.a = (T)a;
   kp.e2 = (T)e2;
   kp.il = (T)(1. / l);
-  // tensor-core path: coordinates multiplied by g turn the kernel argument
-  // into r' = g r with k = 2^-r' (EXPONENTIAL), (1 + r') e^-r' (MATERN32),
-  // (1 + r' + r'^2/3) e^-r' (MATERN52) or 2^-r'^2 (GAUSSIAN)
+  // tensor-core path: coordinates multiplied by g turn the distance into
+  // r' = g r, the kernel argument t times log2(e): k = 2^-r' (EXPONENTIAL),
+  // (1 + t) 2^-r' (MATERN32), (1 + t + t^2/3) 2^-r' (MATERN52) with
+  // t = ln(2) r', or 2^-r'^2 (GAUSSIAN)
   double g = 1;
   switch (base) {  // l dk/dl kernels use the coordinates of their kernel
     case FMCA_KERNEL_EXPONENTIAL:
@@ -433,7 +434,7 @@ KParams<T> make_kparams(const KernelDesc& k) {
       break;
     case FMCA_KERNEL_MATERN32:
     case FMCA_KERNEL_MATERN52:
-      g = a;
+      g = log2e * a;
       break;
     case FMCA_KERNEL_GAUSSIAN:
       g = std::sqrt(0.5 * log2e) / l;

@@ -42,50 +42,45 @@ __device__ __forceinline__ float pow2i(float e) {
   return i <= -127 ? 0.f : __int_as_float((i + 127) << 23);
 }
 
-// a = k * 2^w of two squared distances in the coordinates scaled by g;
-// FP32x2 arithmetic, the square root and exponential per element on the SFU
-template <int KT>
+// a = k * 2^w of two squared distances in the coordinates scaled by g
+// (make_kparams: g = log2(e) / l for EXPONENTIAL, log2(e) sqrt(3) / l and
+// log2(e) sqrt(5) / l for MATERN32 / 52, so that r' = sqrt(r2) is the
+// kernel argument times log2(e) and e^-argument = 2^-r'). FP32x2
+// arithmetic, the square root and exponential per element on the SFU;
+// sqrt(0) = 0, so coincident points need no guard. ZEROW: w = 0 (point
+// sources), the exponent is -r' itself.
+template <int KT, bool ZEROW = false>
 __device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<float>& kp) {
+  constexpr float c1 = kLn2;                         // argument per unit of r'
+  constexpr float c2 = kLn2 * kLn2;
   if constexpr (KT == 3) {  // GAUSSIAN: 2^(w - r'^2)
-    const float2 u = __ffma2_rn(r2, f2(-1.f, -1.f), w);
+    const float2 u = ZEROW ? f2(-r2.x, -r2.y) : __ffma2_rn(r2, f2(-1.f, -1.f), w);
     return f2(ex2_approx(u.x), ex2_approx(u.y));
-  } else if constexpr (KT == 0 || KT == 1 || KT == 2) {
-    // r = r2 rsqrt(r2); callers keep r2 >= 1e-30 so that coincident points
-    // give r ~ 1e-15 instead of 0 * inf
-    const float2 r = __fmul2_rn(r2, f2(rsqrt_approx(r2.x), rsqrt_approx(r2.y)));
-    if constexpr (KT == 0) {  // EXPONENTIAL: 2^(w - r')
-      const float2 u = __ffma2_rn(r, f2(-1.f, -1.f), w);
-      return f2(ex2_approx(u.x), ex2_approx(u.y));
-    } else {
-      const float2 u = __ffma2_rn(r, f2(-kLog2e, -kLog2e), w);
-      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
-      if constexpr (KT == 1) return __ffma2_rn(r, e, e);  // MATERN32: (1 + r') e
-      // MATERN52: (1 + r' + r'^2 / 3) e
-      const float2 p = __ffma2_rn(__ffma2_rn(r, f2(0.333333343f, 0.333333343f), f2(1.f, 1.f)),
-                                  r, f2(1.f, 1.f));
-      return __fmul2_rn(p, e);
-    }
-  } else if constexpr (KT == 10 || KT == 11 || KT == 12) {
-    // l dk/dl of the kernels above, in the same scaled coordinates
-    const float2 r = __fmul2_rn(r2, f2(rsqrt_approx(r2.x), rsqrt_approx(r2.y)));
-    if constexpr (KT == 10) {  // EXPONENTIAL: (r / l) e^(-r / l) = ln2 r' 2^-r'
-      const float2 u = __ffma2_rn(r, f2(-1.f, -1.f), w);
-      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
-      return __fmul2_rn(__fmul2_rn(r, f2(kLn2, kLn2)), e);
-    } else {
-      const float2 u = __ffma2_rn(r, f2(-kLog2e, -kLog2e), w);
-      const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
-      const float2 rr = __fmul2_rn(r, r);
-      if constexpr (KT == 11) return __fmul2_rn(rr, e);  // MATERN32: t^2 e^-t
-      // MATERN52: t^2 / 3 (1 + t) e^-t
-      const float2 p = __fmul2_rn(__fmul2_rn(rr, f2(0.333333343f, 0.333333343f)),
-                                  __fadd2_rn(r, f2(1.f, 1.f)));
-      return __fmul2_rn(p, e);
-    }
-  } else if constexpr (KT == 13) {  // GAUSSIAN: (r / l)^2 e^(-r^2 / 2 l^2) = 2 ln2 r'^2 2^-r'^2
-    const float2 u = __ffma2_rn(r2, f2(-1.f, -1.f), w);
+  } else if constexpr (KT == 13) {  // l dk/dl of GAUSSIAN: 2 ln2 r'^2 2^-r'^2
+    const float2 u = ZEROW ? f2(-r2.x, -r2.y) : __ffma2_rn(r2, f2(-1.f, -1.f), w);
     const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
     return __fmul2_rn(__fmul2_rn(r2, f2(2.f * kLn2, 2.f * kLn2)), e);
+  } else if constexpr (KT == 0 || KT == 1 || KT == 2 || KT == 10 || KT == 11 || KT == 12) {
+    const float2 r = f2(sqrt_approx(r2.x), sqrt_approx(r2.y));
+    const float2 u = ZEROW ? f2(-r.x, -r.y) : __ffma2_rn(r, f2(-1.f, -1.f), w);
+    const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
+    if constexpr (KT == 0) {  // EXPONENTIAL: 2^(w - r')
+      return e;
+    } else if constexpr (KT == 1) {  // MATERN32: (1 + t) e^-t, t = ln2 r'
+      return __fmul2_rn(__ffma2_rn(r, f2(c1, c1), f2(1.f, 1.f)), e);
+    } else if constexpr (KT == 2) {  // MATERN52: (1 + t + t^2 / 3) e^-t
+      const float2 p = __ffma2_rn(__ffma2_rn(r, f2(c2 / 3.f, c2 / 3.f), f2(c1, c1)), r,
+                                  f2(1.f, 1.f));
+      return __fmul2_rn(p, e);
+    } else if constexpr (KT == 10) {  // l dk/dl of EXPONENTIAL: t e^-t
+      return __fmul2_rn(__fmul2_rn(r, f2(c1, c1)), e);
+    } else if constexpr (KT == 11) {  // l dk/dl of MATERN32: t^2 e^-t
+      return __fmul2_rn(__fmul2_rn(r2, f2(c2, c2)), e);
+    } else {  // l dk/dl of MATERN52: t^2 / 3 (1 + t) e^-t
+      const float2 p = __fmul2_rn(__fmul2_rn(r2, f2(c2 / 3.f, c2 / 3.f)),
+                                  __ffma2_rn(r, f2(c1, c1), f2(1.f, 1.f)));
+      return __fmul2_rn(p, e);
+    }
   } else {
     return f2(keval_fast(kp.type, r2.x, kp) * pow2i(w.x),
               keval_fast(kp.type, r2.y, kp) * pow2i(w.y));

@@ -121,9 +121,8 @@ __device__ __forceinline__ void um_eval_chunk(const float4* __restrict__ rec, ui
       const float2 dx = __fadd2_rn(tx[h], sx);
       const float2 dy = __fadd2_rn(ty[h], sy);
       const float2 dz = __fadd2_rn(tz[h], sz);
-      const float2 r2 =
-          __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __ffma2_rn(dx, dx, f2(1e-30f, 1e-30f))));
-      const float2 av = kscaled2<KT>(r2, sw, kp);
+      const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+      const float2 av = kscaled2<KT, !REL && !MASKED>(r2, sw, kp);
       const float2 hv = f2(__uint_as_float(__float_as_uint(av.x) & 0xffffe000u),
                            __uint_as_float(__float_as_uint(av.y) & 0xffffe000u));
       const float2 lv = __ffma2_rn(hv, f2(-1.f, -1.f), av);
@@ -152,7 +151,7 @@ __device__ __forceinline__ void grid_eval_pair(float tx, float ty, float tz,
     const float dx = tx + X[i], dy = ty + X[P + i], dz = tz + X[2 * P + i];
     ux[i] = dx * dx;
     uy[i] = dy * dy;
-    uz[i] = fmaf(dz, dz, 1e-30f);
+    uz[i] = dz * dz;
   }
 #pragma unroll
   for (int cc = 0; cc < 2; ++cc)
