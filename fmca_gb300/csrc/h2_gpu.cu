@@ -923,11 +923,12 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     ++dp->launches;
   }
   const int64_t npc = (int64_t)um_padded(nc);
+  const dim3 ggrid(blocks(npc / 8 * RB), nch);
   if (dtype == FMCA_DTYPE_F64)
-    gather_split_kernel<double><<<blocks(npc / 8 * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<double><<<ggrid, nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const double*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   else
-    gather_split_kernel<float><<<blocks(npc / 8 * RB * nch), nthr, 0, st>>>(
+    gather_split_kernel<float><<<ggrid, nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
   point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
   FMCA_CK(cudaGetLastError());

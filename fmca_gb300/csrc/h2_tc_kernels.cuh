@@ -16,6 +16,8 @@
 // argument needs no further scaling.
 #pragma once
 
+#include <type_traits>
+
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -103,33 +105,40 @@ __host__ __device__ __forceinline__ size_t um_padded(size_t n) {
   return ((n + 7) & ~(size_t)7) + 8;
 }
 
-// per-column max |x| as float bits (positive floats order like integers).
-// Columns [c0, c0 + nc) of this launch; a block reduces into shared memory
-// first (per-thread running maxima when the grid stride is a multiple of
-// nc, so every thread stays on one column) and flushes once per column.
+// per-column max |x| as FP32 bits (positive floats order like integers) for
+// columns [c0, c0 + nc); a block reduces into shared memory first and
+// flushes once per column
 template <typename TI>
 __global__ void colmax_kernel(int64_t n, int c0, int nc, const TI* __restrict__ x,
                               int64_t sxi, int64_t sxr, unsigned int* __restrict__ cmax) {
+  // lane = column of a group of 32, warps stride over the rows; the maximum
+  // is taken over the bit patterns of |x| (non-negative floating-point
+  // numbers order like their bits) and converted to FP32 once: conversion
+  // is monotone, so that equals the maximum of the converted elements
   extern __shared__ unsigned int smax[];
   for (int r = threadIdx.x; r < nc; r += blockDim.x) smax[r] = 0u;
   __syncthreads();
-  const int64_t total = n * (int64_t)nc;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t first = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (stride % nc == 0) {
-    unsigned int m = 0u;
-    const int r = (int)(first % nc);
-    for (int64_t e = first; e < total; e += stride) {
-      const int64_t i = e / nc;
-      m = max(m, __float_as_uint(fabsf((float)x[i * sxi + (int64_t)(c0 + r) * sxr])));
+  using U = typename std::conditional<sizeof(TI) == 8, unsigned long long, unsigned int>::type;
+  constexpr U kAbs = sizeof(TI) == 8 ? (U)0x7FFFFFFFFFFFFFFFull : (U)0x7FFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int cg = 0; cg < nc; cg += 32) {
+    const int r = cg + lane;
+    if (r >= nc) continue;
+    const U* p = reinterpret_cast<const U*>(x) + (int64_t)(c0 + r) * sxr + warp * sxi;
+    const int64_t step = nwarps * sxi;
+    U m = 0;
+    for (int64_t i = warp; i < n; i += nwarps, p += step) {
+      const U b = *p & kAbs;
+      m = b > m ? b : m;
     }
-    if (first < total) atomicMax(&smax[r], m);
-  } else {
-    for (int64_t e = first; e < total; e += stride) {
-      const int64_t i = e / nc;
-      const int r = (int)(e % nc);
-      atomicMax(&smax[r], __float_as_uint(fabsf((float)x[i * sxi + (int64_t)(c0 + r) * sxr])));
-    }
+    float mf;
+    if constexpr (sizeof(TI) == 8)
+      mf = (float)__longlong_as_double((long long)m);
+    else
+      mf = __uint_as_float(m);
+    atomicMax(&smax[r], __float_as_uint(mf));
   }
   __syncthreads();
   for (int r = threadIdx.x; r < nc; r += blockDim.x)
@@ -148,23 +157,33 @@ __device__ __forceinline__ int scale_exp(float m) {
 // (chunk-major [chunk][n][32], for the CUDA-core tree passes) and as FP16
 // hi / lo parts in the values layout ([chunk][um_padded(n) sources],
 // padding zero)
+// v * 2^-e, rounded once as ldexpf does: a multiply by an exact power of
+// two while 2^-e is a normal FP32 number
+__device__ __forceinline__ float scale_pow2(float v, int e) {
+  return (e >= -127 && e <= 126) ? v * __int_as_float((127 - e) << 23) : ldexpf(v, -e);
+}
+
 template <typename TI>
 __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,
                                     const TI* __restrict__ x, int64_t sxi, int64_t sxr,
                                     const unsigned int* __restrict__ cmax,
                                     float* __restrict__ xc, __half* __restrict__ xv) {
-  // one thread per 8 consecutive sources and right-hand side: the 8 FP16
-  // hi (lo) values of a core-matrix row are one 16-byte store
-  const int nchunks = (R + kTcRhs - 1) / kTcRhs;
+  // chunk blockIdx.y; one thread per 8 consecutive sources and right-hand
+  // side of the chunk (the thread count of the grid is a multiple of 32, so
+  // a thread keeps its right-hand side): the 8 FP16 hi (lo) values of a
+  // core-matrix row are one 16-byte store
+  const int64_t ch = blockIdx.y;
   const int64_t np = (int64_t)um_padded(n);
-  const int64_t nblk = np / 8;
-  const int64_t total = nblk * kTcRhs * nchunks;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int rr = (int)(e % kTcRhs);
-    const int64_t blk = (e / kTcRhs) % nblk, ch = e / (kTcRhs * nblk);
-    const int r = (int)ch * kTcRhs + rr;
-    const int ex = r < R ? scale_exp(__uint_as_float(cmax[r])) : 0;
+  const int64_t total = (np / 8) * kTcRhs;
+  const int64_t first = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int rr = (int)(first & (kTcRhs - 1));
+  const int r = (int)ch * kTcRhs + rr;
+  const int ex = r < R ? scale_exp(__uint_as_float(cmax[r])) : 0;
+  const TI* xr = x + (int64_t)r * sxr;
+  float* xo = xc + ch * n * kTcRhs + rr;
+  __half* o = xv + (size_t)ch * np * kTcRhs * 2;
+  for (int64_t e = first; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t blk = e >> 5;
     uint32_t hw[4], lw[4];
 #pragma unroll
     for (int jj = 0; jj < 8; jj += 2) {
@@ -175,16 +194,15 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
         v[t] = 0.f;
         if (r < R && i < n) {
           const int64_t src = perm ? (int64_t)perm[i] : i;
-          v[t] = ldexpf((float)x[src * sxi + (int64_t)r * sxr], -ex);
+          v[t] = scale_pow2((float)xr[src * sxi], ex);
         }
-        if (i < n) xc[(ch * n + i) * kTcRhs + rr] = v[t];
+        if (i < n) xo[i * kTcRhs] = v[t];
       }
       const __half2 h = __floats2half2_rn(v[0], v[1]);
       const float2 hf = __half22float2(h);
       hw[jj / 2] = h2_bits(h);
       lw[jj / 2] = h2_bits(__floats2half2_rn(v[0] - hf.x, v[1] - hf.y));
     }
-    __half* o = xv + (size_t)ch * np * kTcRhs * 2;
     *reinterpret_cast<uint4*>(o + um_val_index((size_t)blk * 8, rr, 0)) =
         make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *reinterpret_cast<uint4*>(o + um_val_index((size_t)blk * 8, rr, 1)) =
@@ -284,10 +302,22 @@ __global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ 
   const int c = blockIdx.x;
   if (c >= C) return;
   __shared__ float red[32];
+  __shared__ int node_of_row[kGridRows];  // node index of each grid row, -1 past q
   const size_t base = (size_t)c * q * kTcRhs;
+  for (int k = threadIdx.x; k < kGridRows; k += blockDim.x) node_of_row[k] = -1;
+  __syncthreads();
+  for (int k = threadIdx.x; k < q; k += blockDim.x)
+    node_of_row[(midx[3 * k] * kGridP1 + midx[3 * k + 1]) * kGridP1 + midx[3 * k + 2]] = k;
   float m = 0.f;
-  for (int e = threadIdx.x; e < q * kTcRhs; e += blockDim.x)
-    if ((e % kTcRhs) < rcount) m = fmaxf(m, fabsf(t[base + e]));
+  const float4* t4 = reinterpret_cast<const float4*>(t + base);
+  for (int e = threadIdx.x; e < q * kTcRhs / 4; e += blockDim.x) {
+    const float4 v = t4[e];
+    const int r0 = (4 * e) % kTcRhs;
+    if (r0 + 0 < rcount) m = fmaxf(m, fabsf(v.x));
+    if (r0 + 1 < rcount) m = fmaxf(m, fabsf(v.y));
+    if (r0 + 2 < rcount) m = fmaxf(m, fabsf(v.z));
+    if (r0 + 3 < rcount) m = fmaxf(m, fabsf(v.w));
+  }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
@@ -299,18 +329,29 @@ __global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ 
   __syncthreads();
   const float mx = red[0];
   const int ex = scale_exp(mx);
+  // one thread per 8 grid rows and right-hand side: the 8 FP16 hi (lo)
+  // values of a core-matrix row are one 16-byte store
   const size_t row0 = (size_t)c * kGridRows;
-  for (int e = threadIdx.x; e < kGridRows * kTcRhs; e += blockDim.x) {
-    const int k = e / kTcRhs, r = e % kTcRhs;
-    float v = 0.f;
-    int row = k;
-    if (k < q) {
-      row = (midx[3 * k] * kGridP1 + midx[3 * k + 1]) * kGridP1 + midx[3 * k + 2];
-      if (r < rcount) v = ldexpf(t[base + (size_t)k * kTcRhs + r], -ex);
+  for (int task = threadIdx.x; task < (kGridRows / 8) * kTcRhs; task += blockDim.x) {
+    const int rb = task / kTcRhs, r = task % kTcRhs;
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int jj = 0; jj < 8; jj += 2) {
+      float v[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = node_of_row[rb * 8 + jj + u];
+        v[u] = (k >= 0 && r < rcount) ? scale_pow2(t[base + (size_t)k * kTcRhs + r], ex) : 0.f;
+      }
+      const __half2 h = __floats2half2_rn(v[0], v[1]);
+      const float2 hf = __half22float2(h);
+      hw[jj / 2] = h2_bits(h);
+      lw[jj / 2] = h2_bits(__floats2half2_rn(v[0] - hf.x, v[1] - hf.y));
     }
-    const __half h = __float2half_rn(v);
-    tv[um_val_index(row0 + row, r, 0)] = h;
-    tv[um_val_index(row0 + row, r, 1)] = __float2half_rn(v - __half2float(h));
+    *reinterpret_cast<uint4*>(tv + um_val_index(row0 + rb * 8, r, 0)) =
+        make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(tv + um_val_index(row0 + rb * 8, r, 1)) =
+        make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
   // grid lines: the nodes with digits (i, 0, 0), (0, i, 0), (0, 0, i) give
   // X[d][i] (every node of a line shares that coordinate)
@@ -325,35 +366,36 @@ __global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ 
   if (threadIdx.x == 0) rc[15] = mx > 0.f && isfinite(mx) ? (float)ex : -1000.f;
 }
 
-// y (natural order) = sigma2 * 2^e_r * (ynear + yfar), combined in FP64
+// y (natural order) = sigma2 * 2^e_r * (ynear + yfar): the two FP32 parts
+// added in FP32 (one rounding, 6e-8 relative), the scaling in FP64. FP64
+// arithmetic is scarce on this part (two operations per clock and SM), so
+// an element costs one conversion and one multiply; the column's scale
+// sigma2 * 2^e_r is formed from its exponent bits once per thread (v *
+// (sigma2 2^e) rounds once, like ldexp(sigma2 v, e)). Lane = column of a
+// group of 32, warps stride over the rows.
 template <typename TO>
 __global__ void scatter_scaled_kernel(const uint32_t* __restrict__ perm, int64_t n, int R,
                                       const float* __restrict__ ynear,
                                       const float* __restrict__ yfar,
                                       const unsigned int* __restrict__ cmax, double sigma2,
                                       TO* __restrict__ y, int64_t syi, int64_t syr) {
-  // FP64 arithmetic is scarce on this part: one add and one multiply per
-  // element, with the column's scale sigma2 * 2^e_r formed from its
-  // exponent bits (v * (sigma2 2^e) rounds once, like ldexp(sigma2 v, e))
-  const int64_t total = n * (int64_t)R;
-  const bool small = total < (int64_t)1 << 31;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t i;
-    int r;
-    if (small) {
-      i = (uint32_t)e / (uint32_t)R;
-      r = (int)((uint32_t)e - (uint32_t)i * (uint32_t)R);
-    } else {
-      i = e / R;
-      r = (int)(e % R);
-    }
-    const int64_t k = ((int64_t)(r / kTcRhs) * n + i) * kTcRhs + r % kTcRhs;
-    const int64_t dst = perm ? (int64_t)perm[i] : i;
-    const double v = (double)ynear[k] + (double)yfar[k];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int cg = 0; cg < R; cg += kTcRhs) {
+    const int r = cg + lane;
+    if (r >= R) continue;
     const int ex = scale_exp(__uint_as_float(cmax[r]));
     const double sc = sigma2 * __longlong_as_double((long long)(ex + 1023) << 52);
-    y[dst * syi + (int64_t)r * syr] = (TO)(v * sc);
+    const int64_t off = (int64_t)(r / kTcRhs) * n * kTcRhs + r % kTcRhs;
+    const float* yn = ynear + off;
+    const float* yf = yfar + off;
+    TO* yr = y + (int64_t)r * syr;
+    for (int64_t i = warp; i < n; i += nwarps) {
+      const float v = yn[i * kTcRhs] + yf[i * kTcRhs];
+      const int64_t dst = perm ? (int64_t)perm[i] : i;
+      yr[dst * syi] = (TO)((double)v * sc);
+    }
   }
 }
 
