@@ -536,11 +536,57 @@ cudaError_t launch_ksum(int rb, const GroupList& gl, const Pt4<T>* tgt,
 // one transfer level (M2M when UP, else L2L) over the nb clusters of list.
 // A level with fewer than two clusters per SM splits the right-hand sides
 // over blockIdx.y in slices of 8, so that it still spreads over the GPU.
+template <int DIM, int P, bool UP>
+void launch_transfer_sf(int nb, const int32_t* list, const int32_t* son0,
+                        const int32_t* nsons, const int32_t* parent, const float* E,
+                        const int* midx, float* buf, int ld, int rofs, int rcount,
+                        cudaStream_t st) {
+  constexpr int Q = DIM == 2 ? P * P : P * P * P;
+  auto kern = transfer_sf_kernel<DIM, P, UP>;
+  const size_t smem = (size_t)(3 * Q * 32 + Q + DIM * P * P) * sizeof(float);
+  ensure_smem(kern, smem);
+  kern<<<nb, 128, smem, st>>>(list, son0, nsons, parent, E, midx, buf, ld, rofs, rcount);
+}
+
+// the sum-factorised transfer for the tensor grids it is instantiated for
+// (2-D with 4..8 nodes per dimension, 3-D with 4..6; FP32, up to 32
+// right-hand sides); false: use transfer_kernel
+template <bool UP>
+bool launch_transfer_sf_any(int nb, const int32_t* list, const int32_t* son0,
+                            const int32_t* nsons, const int32_t* parent, const float* E,
+                            const int* midx, const InterpDev<float>& ip, float* buf, int ld,
+                            int rofs, int rcount, cudaStream_t st) {
+  if (rcount > 32) return false;
+#define FMCA_SF(D, P)                                                                    \
+  case D * 16 + P:                                                                       \
+    launch_transfer_sf<D, P, UP>(nb, list, son0, nsons, parent, E, midx, buf, ld, rofs, \
+                                 rcount, st);                                            \
+    return true;
+  switch (ip.dim * 16 + ip.p1) {
+    FMCA_SF(2, 4)
+    FMCA_SF(2, 5)
+    FMCA_SF(2, 6)
+    FMCA_SF(2, 7)
+    FMCA_SF(2, 8)
+    FMCA_SF(3, 4)
+    FMCA_SF(3, 5)
+    FMCA_SF(3, 6)
+    default:
+      return false;
+  }
+#undef FMCA_SF
+}
+
 template <typename T, int RB, bool UP>
 void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
                      const int32_t* nsons, const int32_t* parent, const T* E,
                      const int* midx, const InterpDev<T>& ip, T* buf, int ld,
                      int rofs, int rcount, cudaStream_t st) {
+  if constexpr (std::is_same<T, float>::value && RB == 32) {
+    if (launch_transfer_sf_any<UP>(nb, list, son0, nsons, parent, E, midx, ip, buf, ld, rofs,
+                                   rcount, st))
+      return;
+  }
   const size_t tail = (size_t)ip.q * sizeof(int);
   if constexpr (RB > 8) {
     if (nb < 2 * 152 && rcount > 8) {

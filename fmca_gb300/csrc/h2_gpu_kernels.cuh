@@ -717,6 +717,120 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
   }
 }
 
+// One transfer level, sum-factorised (FP32, 32 right-hand sides):
+// E_c = e_c[0] (x) e_c[1] (x) ... applied as DIM contractions of P terms
+// each, on the coefficients held in tensor order (node with digits
+// (i_0, .., i_{DIM-1}) at position (i_0 P + i_1) P + ..). Block = one
+// cluster, 4 warps, lane = right-hand side rofs + lane; a contraction over
+// dimension d hands every warp whole columns (the P coefficients that
+// differ in digit d): P loads, P^2 FMAs and P stores per column.
+//   UP (M2M):   t[c] = sum_sons (e_son[0] (x) ..) t[son]   (e[k][j], k: c)
+//   DOWN (L2L): s[c] += (e_c[0] (x) ..)^T s[parent]        (e[k][j], j: c)
+// The same sums as transfer_kernel, in another order of the terms. Global
+// rows move in batches of 8 loads per lane, so that their latencies overlap.
+// shared: X, Y, Z [P^DIM][32] floats, sidx [P^DIM] ints, e [DIM][P][P]
+template <int DIM, int P, bool UP>
+__global__ void __launch_bounds__(128)
+    transfer_sf_kernel(const int32_t* __restrict__ clist, const int32_t* __restrict__ son0,
+                       const int32_t* __restrict__ nsons, const int32_t* __restrict__ parent,
+                       const float* __restrict__ E, const int* __restrict__ midx_g,
+                       float* buf, int ldv, int rofs, int rcount) {
+  constexpr int Q = DIM == 1 ? P : DIM == 2 ? P * P : P * P * P;
+  constexpr int NC = Q / P;  // columns of one contraction
+  extern __shared__ __align__(16) float smf[];
+  float* X = smf;
+  float* Y = X + Q * 32;
+  float* Z = Y + Q * 32;
+  int* sidx = reinterpret_cast<int*>(Z + Q * 32);  // tensor position -> storage index
+  float* ef = reinterpret_cast<float*>(sidx + Q);  // [DIM][P][P]
+  const int c = clist[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool live = lane < rcount;
+  const int r = rofs + lane;
+  for (int k = threadIdx.x; k < Q; k += blockDim.x) {
+    int pos = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) pos = pos * P + midx_g[k * 3 + d];
+    sidx[pos] = k;
+  }
+  for (int e = threadIdx.x; e < Q * 32; e += blockDim.x) Z[e] = 0.f;
+  constexpr int U = 8;
+  const int nsrc = UP ? nsons[c] : 1;
+  for (int si = 0; si < nsrc; ++si) {
+    const int ec = UP ? son0[c] + si : c;
+    const int sc = UP ? son0[c] + si : parent[c];
+    __syncthreads();  // previous source done with X, Y and ef; sidx ready
+    for (int e = threadIdx.x; e < DIM * P * P; e += blockDim.x) ef[e] = E[(size_t)ec * DIM * P * P + e];
+    for (int t0 = warp; t0 < Q; t0 += 4 * U) {
+      float v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = t0 + 4 * u;
+        v[u] = (t < Q && live) ? buf[((size_t)sc * Q + sidx[t]) * ldv + r] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (t0 + 4 * u < Q) X[(t0 + 4 * u) * 32 + lane] = v[u];
+    }
+    __syncthreads();
+    float* in = X;
+    float* out = Y;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      // stride of digit d and the factor, oriented output x input
+      const int stride = d == DIM - 1 ? 1 : (d == DIM - 2 ? P : P * P);
+      float f[P][P];
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b)
+          f[a][b] = UP ? ef[(d * P + a) * P + b] : ef[(d * P + b) * P + a];
+      const bool last = d == DIM - 1;
+      for (int col = warp; col < NC; col += 4) {
+        // base position of the column: digits other than d from col
+        const int hi = col / stride, lo = col % stride;
+        const int base = hi * stride * P + lo;
+        float v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) v[j] = in[(base + j * stride) * 32 + lane];
+#pragma unroll
+        for (int a = 0; a < P; ++a) {
+          float acc = 0.f;
+#pragma unroll
+          for (int j = 0; j < P; ++j) acc = fmaf(f[a][j], v[j], acc);
+          const int o = (base + a * stride) * 32 + lane;
+          if (!last)
+            out[o] = acc;
+          else
+            Z[o] += acc;
+        }
+      }
+      __syncthreads();
+      float* tmp = in;
+      in = out;
+      out = tmp;
+    }
+  }
+  // UP: t[c] = Z; DOWN: s[c] += Z
+  if (live)
+    for (int t0 = warp; t0 < Q; t0 += 4 * U) {
+      float v[U];
+      if (!UP) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int t = t0 + 4 * u;
+          v[u] = t < Q ? buf[((size_t)c * Q + sidx[t]) * ldv + r] : 0.f;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = t0 + 4 * u;
+        if (t < Q)
+          buf[((size_t)c * Q + sidx[t]) * ldv + r] = UP ? Z[t * 32 + lane] : v[u] + Z[t * 32 + lane];
+      }
+    }
+}
+
 // leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves
 // shared: F[24][blockDim] (one column per thread), S[q][RB], packed digits q ints
 template <typename T, int RB>
