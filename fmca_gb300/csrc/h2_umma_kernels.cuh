@@ -191,12 +191,11 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // kGridP1^3): every tile is one source cluster on its tensor grid
 // (tscale_grid_kernel layout; `pairs` holds the clusters' 64-byte grid-line
 // records). F: tiles per accumulation unit (the tensor cores accumulate F
-// tiles before a flush adds them into a running total): 2 on tensor grids,
-// whose tiles of one source cluster carry half the products of a point
-// tile; 256 sources per flush cost 5 % of the far field's time against a
-// 1.5x larger rounding error (5e-7 relative at n = 1e6, measured against
-// FP64).
-template <int KT, int H, bool REL, bool GRID, int F = (GRID ? 2 : 1)>
+// tiles before a flush adds them into a running total): 2 on tensor grids
+// and with two target halves. 256 sources per flush made the far field 5 %
+// and the near field 2 % faster, and the far field's rounding error 1.5x
+// larger (5e-7 relative at n = 1e6, measured against FP64).
+template <int KT, int H, bool REL, bool GRID, int F = ((GRID || H == 2) ? 2 : 1)>
 __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
