@@ -62,6 +62,7 @@ struct DevSet {
 struct GroupList {
   KGroup* groups = nullptr;
   uint32_t* ivl = nullptr;
+  uint32_t* imask = nullptr;  // per interval: target halves it serves (paired grid lists)
   int ngroups = 0;
   int maxcount = 0;
 };
@@ -87,6 +88,7 @@ struct DevPlan {
   std::vector<int> l2l_ptr;
   GroupList far, near;  // chunked to kGroupCap targets (near: also the tensor-core list)
   GroupList far_tc;     // chunked to kTcGroupCap targets
+  GroupList far_grid2;  // tensor grids: sibling row clusters paired as two target halves
   int* err_flag = nullptr;
   void* ws = nullptr;
   size_t ws_bytes = 0;
@@ -142,6 +144,7 @@ int to_device(DevPlan* dp, const V* host, size_t count, V** out,
 struct HostGroups {
   std::vector<KGroup> groups;
   std::vector<uint32_t> ivl;
+  std::vector<uint32_t> imask;  // optional, one per interval
   int maxcount = 0;
 };
 
@@ -179,6 +182,8 @@ int upload_groups(DevPlan* dp, const HostGroups& hg, GroupList* gl,
                   std::string* err) {
   FMCA_TRY(to_device(dp, hg.groups.data(), hg.groups.size(), &gl->groups, err));
   FMCA_TRY(to_device(dp, hg.ivl.data(), hg.ivl.size(), &gl->ivl, err));
+  if (!hg.imask.empty())
+    FMCA_TRY(to_device(dp, hg.imask.data(), hg.imask.size(), &gl->imask, err));
   gl->ngroups = (int)hg.groups.size();
   gl->maxcount = hg.maxcount;
   return FMCA_OK;
@@ -316,6 +321,56 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     }
     sort_groups(&hg);
     FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->far : &dp->far_tc, err));
+  }
+  // far groups on tensor grids, two sibling row clusters a, a + 1 per group
+  // (target halves of q nodes each): sources = the union of their
+  // admissible column clusters, consecutive clusters with the same halves
+  // merged into one interval, imask = the halves an interval serves
+  if (plan.interp.dim == 3 && plan.interp.deg + 1 == kGridP1) {
+    HostGroups hg;
+    const int q = ip.q;
+    const Pattern& P = plan.pat;
+    const Tree& T = plan.rows;
+    std::vector<std::pair<int, int>> pairs;  // (first cluster, clusters in the group)
+    for (int c = 0; c < T.nclusters(); ++c) {
+      if (T.parent[c] < 0) pairs.push_back({c, 1});
+      for (int i = 0; i < T.nsons[c]; i += 2)
+        pairs.push_back({T.son0[c] + i, std::min(2, T.nsons[c] - i)});
+    }
+    for (const auto& pr : pairs) {
+      const int a = pr.first, m = pr.second;
+      std::vector<std::pair<int, uint32_t>> u;  // (column cluster, halves)
+      for (int h = 0; h < m; ++h)
+        for (int k = P.far_ptr[a + h]; k < P.far_ptr[a + h + 1]; ++k)
+          u.push_back({P.far_idx[k], 1u << h});
+      // groups without sources stay: the kernel writes their zero locals
+      std::sort(u.begin(), u.end());
+      const int ib = (int)(hg.ivl.size() / 2);
+      for (size_t i = 0; i < u.size();) {
+        uint32_t mask = u[i].second;
+        size_t j = i + 1;
+        if (j < u.size() && u[j].first == u[i].first) mask |= u[j++].second;
+        const uint32_t b = (uint32_t)u[i].first * q, e = b + q;
+        if (hg.ivl.size() > (size_t)2 * ib && hg.ivl.back() == b && hg.imask.back() == mask) {
+          hg.ivl.back() = e;
+        } else {
+          hg.ivl.push_back(b);
+          hg.ivl.push_back(e);
+          hg.imask.push_back(mask);
+        }
+        i = j;
+      }
+      KGroup g;
+      g.tbegin = (uint32_t)a * q;
+      g.tcount = (uint32_t)(m * q);
+      g.ivl_begin = ib;
+      g.ivl_end = (int)(hg.ivl.size() / 2);
+      hg.groups.push_back(g);
+      hg.maxcount = std::max<int>(hg.maxcount, (int)g.tcount);
+    }
+    // most work first (the imask array stays aligned with the intervals)
+    sort_groups(&hg);
+    FMCA_TRY(upload_groups(dp, hg, &dp->far_grid2, err));
   }
   // near groups: targets = points of every row leaf, sources = merged
   // column point intervals; kGroupCap = 256 targets suits both the CUDA-core
@@ -862,7 +917,8 @@ cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4
   const size_t smem = um_smem_bytes(H);
   ensure_smem(kern, smem);
   kern<<<gl.ngroups, 32 * (3 + 4 * kUmSets), smem, st>>>(gl.groups, gl.ivl, tgt, pairs, vals,
-                                                         out, kTcRhs, rcount, kp, q, errf);
+                                                         out, kTcRhs, rcount, kp, q, errf,
+                                                         gl.imask);
   return cudaGetLastError();
 }
 
@@ -871,9 +927,9 @@ cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                         bool grid) {
-  if constexpr (H == 1) {
+  if constexpr (H == 2) {  // tensor grids: sibling row clusters as the two halves
     if (grid)
-      return launch_um_v<KT, 1, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return launch_um_v<KT, 2, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
   }
   if (q > 0)
     return launch_um_v<KT, H, true, false>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
@@ -1018,9 +1074,13 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
       tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.tv,
                                          reinterpret_cast<float*>(w.pairs_n));
     ++dp->launches;
-    FMCA_CK(launch_um<1>(dp->far_tc, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q,
-                         dp->err_flag, st, grid));
-    dp->launches += dp->far_tc.ngroups ? 1 : 0;
+    const GroupList& fl = grid ? dp->far_grid2 : dp->far_tc;
+    if (grid)
+      FMCA_CK(launch_um<2>(fl, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q, dp->err_flag, st,
+                           true));
+    else
+      FMCA_CK(launch_um<1>(fl, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q, dp->err_flag, st));
+    dp->launches += fl.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_FAR, st);
     for (int l = 1; l < plan.rows.nlevels(); ++l) {
       const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
                    const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
-                   KParams<float> kp, int q, int* err) {
+                   KParams<float> kp, int q, int* err, const uint32_t* __restrict__ imask) {
   constexpr int NST = um_stages(H);
   constexpr int NSETS = kUmSets, NEVAL = 4 * NSETS;
   constexpr int NT = 128 * H;  // targets of a group
@@ -213,7 +213,11 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
   static_assert(NPS % NSETS == 0, "pair slots: whole tiles (parity waits)");
   constexpr uint32_t IDESC64 = umma_idesc_f16(128, 64);
   constexpr uint32_t IDESC32 = umma_idesc_f16(128, 32);
-  static_assert(!GRID || (REL && H == 1), "grid tiles: node sources, one half");
+  static_assert(!GRID || REL, "grid tiles: node sources");
+  // targets of half h: g.tbegin + h HS + row for row < HS (on tensor grids
+  // every half is one row cluster of q nodes; imask[interval] holds the
+  // halves a source cluster serves)
+  const int HS = GRID ? q : 128;
   static_assert(F >= 1 && F <= NST, "accumulation unit: at most the stage ring");
 
   if (*reinterpret_cast<volatile int*>(err)) return;
@@ -234,7 +238,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 512);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 516);
   uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 528);  // [NST][4]
-  float* ered = reinterpret_cast<float*>(smem_raw + 640);          // [NEVAL]
+  float* ered = reinterpret_cast<float*>(smem_raw + 640);          // [NEVAL][H]
   unsigned char* stages = smem_raw + kUmHeader;
   float* tot = reinterpret_cast<float*>(stages + (size_t)NST * kUmStageBytes);
 
@@ -307,6 +311,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
             pos = ivl[2 * pi] / (uint32_t)q;
           }
           const uint32_t sigma = pos++;
+          masks[stage * 4] = imask ? imask[pi] : 1u;
           mbar_expect_tx(&full[stage], 64u + (uint32_t)kUmValBytes);
           bulk_g2s(sp, pairs + (size_t)sigma * 4, 64u, &full[stage]);
           bulk_g2s(sp + kUmPtsBytes, vals + (size_t)sigma * kGridRows * 2 * kTcRhs,
@@ -417,9 +422,9 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
     float2 tx[H], ty[H], tz[H];
 #pragma unroll
     for (int h = 0; h < H; ++h) {
-      const uint32_t i = (uint32_t)(h * 128 + row);
+      const uint32_t i = (uint32_t)(h * HS + row);
       float px = 0.f, py = 0.f, pz = 0.f;
-      if (i < g.tcount) {
+      if (row < HS && i < g.tcount) {
         const Pt4<float> pt = tgt[g.tbegin + i];
         px = gs * pt.x;
         py = gs * pt.y;
@@ -430,24 +435,45 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
       tz[h] = f2(pz, pz);
     }
     // largest moment exponent E of the group's source clusters
-    float E = 0.f;
+    // largest moment exponent E of the group's source clusters, per target
+    // half (Eh: over the intervals that serve the half) and overall (E)
+    float E = 0.f, Eh[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) Eh[h] = 0.f;
     if constexpr (REL) {
-      float mx = -CUDART_INF_F;
-      for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32)
+      float mx[H];
+#pragma unroll
+      for (int h = 0; h < H; ++h) mx[h] = -CUDART_INF_F;
+      for (int i = g.ivl_begin + ew * 32 + lane; i < g.ivl_end; i += NEVAL * 32) {
+        float mi = -CUDART_INF_F;
         for (uint32_t s = ivl[2 * i], e = ivl[2 * i + 1]; s < e; s = (s / q + 1) * q) {
           if constexpr (GRID) {
-            mx = fmaxf(mx, pairs[(size_t)(s / q) * 4 + 3].w);
+            mi = fmaxf(mi, pairs[(size_t)(s / q) * 4 + 3].w);
           } else {
             const float4 r = pairs[2 * (s >> 1) + 1];
-            mx = fmaxf(mx, (s & 1u) ? r.w : r.z);
+            mi = fmaxf(mi, (s & 1u) ? r.w : r.z);
           }
         }
-      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (lane == 0) ered[ew] = mx;
+        const uint32_t msk = imask ? imask[i] : (1u << H) - 1u;
+#pragma unroll
+        for (int h = 0; h < H; ++h)
+          if ((msk >> h) & 1u) mx[h] = fmaxf(mx[h], mi);
+      }
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        for (int o = 16; o > 0; o >>= 1)
+          mx[h] = fmaxf(mx[h], __shfl_xor_sync(0xffffffffu, mx[h], o));
+        if (lane == 0) ered[ew * H + h] = mx[h];
+      }
       named_sync(1, NEVAL * 32);
-      float all = -CUDART_INF_F;
-      for (int w = 0; w < NEVAL; ++w) all = fmaxf(all, ered[w]);
-      E = fmaxf(all, -1000.f);  // groups without sources
+      E = -1000.f;  // groups without sources
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        float all = -CUDART_INF_F;
+        for (int w = 0; w < NEVAL; ++w) all = fmaxf(all, ered[w * H + h]);
+        Eh[h] = fmaxf(all, -1000.f);
+        E = fmaxf(E, Eh[h]);
+      }
     }
     float* mytot = tot + (size_t)set * kTcRhs * NT + row;
 
@@ -510,33 +536,52 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
       };
       const uint32_t a = tbase + lanes + A0 + slot * (H * 32);
       if constexpr (GRID) {
-        // one source cluster: both chunks of this set from the grid lines
+        // one source cluster: both chunks of this set from the grid lines,
+        // half after half; a half the cluster does not serve gets zeros
         const float* X = reinterpret_cast<const float*>(sp);
-        const float wv = X[15] - E;
-        uint32_t gh[2][8], gl[2][8];
-        switch (set) {
-          case 0:
-            grid_eval_pair<KT, 0>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          case 1:
-            grid_eval_pair<KT, 1>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          case 2:
-            grid_eval_pair<KT, 2>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
-          default:
-            grid_eval_pair<KT, 3>(tx[0].x, ty[0].x, tz[0].x, X, wv, kp, gh, gl);
-            break;
+        const uint32_t hm = masks[stage * 4];
+        // one copy of each set's evaluation code: the half is a loop
+        // variable and its target is selected by value
+#pragma unroll 1
+        for (int h = 0; h < H; ++h) {
+          uint32_t gh[2][8], gl[2][8];
+          const float hx = h ? tx[H - 1].x : tx[0].x;
+          const float hy = h ? ty[H - 1].x : ty[0].x;
+          const float hz = h ? tz[H - 1].x : tz[0].x;
+          const float wv = X[15] - (h ? Eh[H - 1] : Eh[0]);
+          if ((hm >> h) & 1u) {
+            switch (set) {
+              case 0:
+                grid_eval_pair<KT, 0>(hx, hy, hz, X, wv, kp, gh, gl);
+                break;
+              case 1:
+                grid_eval_pair<KT, 1>(hx, hy, hz, X, wv, kp, gh, gl);
+                break;
+              case 2:
+                grid_eval_pair<KT, 2>(hx, hy, hz, X, wv, kp, gh, gl);
+                break;
+              default:
+                grid_eval_pair<KT, 3>(hx, hy, hz, X, wv, kp, gh, gl);
+                break;
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) gh[0][i] = gh[1][i] = gl[0][i] = gl[1][i] = 0u;
+          }
+          if (h == 0) {
+            if (!slot_free()) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+          }
+#pragma unroll
+          for (int cc = 0; cc < 2; ++cc) {
+            tmem_st8(a + (cc * H + h) * 16, gh[cc]);
+            tmem_st8(a + (cc * H + h) * 16 + 8, gl[cc]);
+          }
         }
-        if (!slot_free()) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        tmem_st8(a, gh[0]);
-        tmem_st8(a + 8, gl[0]);
-        tmem_st8(a + 16, gh[1]);
-        tmem_st8(a + 24, gl[1]);
+        if (!ok) break;
       } else {
         // chunk 2 s, then (once the slot is free) its A, chunk 2 s + 1 and
         // its A: one chunk of values in registers at a time
@@ -589,15 +634,15 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
     // 8 s .. 8 s + 7 and writes them
     named_sync(1, NEVAL * 32);
     if (!*abort_flag) {
-      const int eo = (int)E;
 #pragma unroll 1
       for (int h = 0; h < H; ++h) {
-        const uint32_t i = (uint32_t)(h * 128 + row);
-        if (i >= g.tcount) continue;
+        const int eo = (int)(h ? Eh[H - 1] : Eh[0]);
+        const uint32_t i = (uint32_t)(h * HS + row);  // target
+        if (row >= HS || i >= g.tcount) continue;
         float acc[8];
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
-          const float* t = tot + (size_t)(8 * set + jj) * NT + i;
+          const float* t = tot + (size_t)(8 * set + jj) * NT + h * 128 + row;
           acc[jj] = ((t[0] + t[kTcRhs * NT]) + t[2 * kTcRhs * NT]) + t[3 * kTcRhs * NT];
           if (REL) acc[jj] = ldexpf(acc[jj], eo);
         }
