@@ -37,13 +37,13 @@ METRIC = "H2 matvecs/sec (n·RHS/s) at n=1e6, mixed-precision batched vs FP64 GP
 UNIT = "n*RHS/s"
 SMS = 152
 # point pairs per clock per SM on the special-function unit: every pair costs
-# one rsqrt.approx (16 results per clock per SM) and one ex2.approx (32 per
+# one sqrt.approx (16 results per clock per SM) and one ex2.approx (32 per
 # clock on GB300) on one pipe, 32 / 3 pairs per clock (tests/test_sfu_rates.py;
 # profiles/sfu_rates.md)
 SFU_PAIRS_PER_CLK = 32.0 / 3.0
 # DRAM bytes (read + write) of one near-field kernel-sum launch of the default
 # workload, from one ncu capture (profiles/ksum_um_c2_full.md)
-NEAR_DRAM_BYTES_PER_LAUNCH = 2.606130e9 + 0.118500e9
+NEAR_DRAM_BYTES_PER_LAUNCH = 2.585309e9 + 0.118240e9
 
 
 def _measured_bf16_tflops():
@@ -490,7 +490,7 @@ def main():
                 "mixed_rel_err_vs_fp64": err, "speedup_mixed_vs_fp64": ms64 / ms}
 
     # roofline of the dominant kernel, the near-field kernel sum (ksum_um_kernel):
-    # every point pair costs one reciprocal square root and one exponential on
+    # every point pair costs one square root and one exponential on
     # the special-function unit, the busiest unit of the kernel; the tensor
     # cores run 2 products per 16 sources (N = 64 and N = 32 columns, 192
     # flops per pair at R = 32)
@@ -504,9 +504,9 @@ def main():
         "bound": "sfu", "kernel": "ksum_um_kernel, near field (tcgen05 products, SFU kernel values)",
         "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gpair/s", "frac": sfu_achieved / sfu_peak,
         "traffic": NEAR_DRAM_BYTES_PER_LAUNCH,
-        "work": (f"N_nf = {info['near_pairs']} point pairs per launch, one rsqrt and one "
+        "work": (f"N_nf = {info['near_pairs']} point pairs per launch, one sqrt and one "
                  "exp2 each"),
-        "peak_source": (f"special-function unit: {SFU_PAIRS_PER_CLK:.2f} pairs/clock/SM (rsqrt "
+        "peak_source": (f"special-function unit: {SFU_PAIRS_PER_CLK:.2f} pairs/clock/SM (sqrt "
                         "16 and ex2 32 results/clock/SM on one pipe, measured by "
                         f"tests/test_sfu_rates.py) x {SMS} SMs at the median SM clock sampled "
                         "during the timed region (the SFU has no entry in MEASURED_PEAKS.json)"),

@@ -1,8 +1,8 @@
 // Throughput of the special-function-unit operations that a kernel-sum pair
-// costs (rsqrt.approx and ex2.approx of FP32), alone and interleaved: every
+// costs (sqrt.approx and ex2.approx of FP32), alone and interleaved: every
 // thread keeps 8 independent chains, 4 blocks of 512 threads per SM.
 // sfu_probe(ms) fills ms[0..2] with the device time (ms) of 2^30 ex2, 2^30
-// rsqrt and 2^29 pairs (rsqrt then ex2 of its result) per launch.
+// sqrt and 2^29 pairs (sqrt then ex2 of its negated result) per launch.
 #include <cuda_runtime.h>
 
 namespace {
@@ -20,11 +20,11 @@ __global__ void sfu_loop(float* out, int iters) {
         asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v[i]));
         v[i] = y * -0.5f;
       } else if (OP == 1) {
-        asm volatile("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v[i]));
+        asm volatile("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(v[i]));
         v[i] = y + 0.5f;
       } else {
         float r;
-        asm volatile("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v[i]));
+        asm volatile("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v[i]));
         asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-r));
         v[i] = y * 0.5f + 0.75f;
       }

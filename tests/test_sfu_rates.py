@@ -1,6 +1,6 @@
 """Special-function-unit rates behind the roofline of the kernel sums
-(bench.py): ex2.approx runs at twice the rate of rsqrt.approx, and a pair
-(one rsqrt, one ex2) costs the time of both on one pipe, i.e. 32 / 3 pairs
+(bench.py): ex2.approx runs at twice the rate of sqrt.approx, and a pair
+(one sqrt, one ex2) costs the time of both on one pipe, i.e. 32 / 3 pairs
 per clock per SM when ex2 gives 32 results per clock. Built from
 tests/cuda/sfu_rate_probe.cu."""
 from __future__ import annotations
@@ -28,9 +28,9 @@ def test_sfu_rates_match_the_roofline_model(cuda_device, tmp_path):
     ms = (ctypes.c_float * 3)()
     sms = ctypes.c_int(0)
     assert lib.sfu_probe(ms, ctypes.byref(sms)) == 0
-    ex2, rsqrt, pair = (2 ** 30 / ms[0], 2 ** 30 / ms[1], 2 ** 29 / ms[2])  # per ms
-    per_sm_ns = [x / sms.value / 1e6 for x in (ex2, rsqrt, pair)]
-    print("sfu rates per SM per ns: ex2 %.2f, rsqrt %.2f, pairs %.2f" % tuple(per_sm_ns))
-    assert 1.7 < ex2 / rsqrt < 2.3, (ex2, rsqrt)
-    model = 1.0 / (1.0 / ex2 + 1.0 / rsqrt)
+    ex2, sqrt, pair = (2 ** 30 / ms[0], 2 ** 30 / ms[1], 2 ** 29 / ms[2])  # per ms
+    per_sm_ns = [x / sms.value / 1e6 for x in (ex2, sqrt, pair)]
+    print("sfu rates per SM per ns: ex2 %.2f, sqrt %.2f, pairs %.2f" % tuple(per_sm_ns))
+    assert 1.7 < ex2 / sqrt < 2.3, (ex2, sqrt)
+    model = 1.0 / (1.0 / ex2 + 1.0 / sqrt)
     assert 0.85 < pair / model < 1.1, (pair, model)
