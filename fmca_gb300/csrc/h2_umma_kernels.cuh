@@ -576,10 +576,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
             tc_fence_after();
           }
 #pragma unroll
-          for (int cc = 0; cc < 2; ++cc) {
-            tmem_st8(a + (cc * H + h) * 16, gh[cc]);
-            tmem_st8(a + (cc * H + h) * 16 + 8, gl[cc]);
-          }
+          for (int cc = 0; cc < 2; ++cc) tmem_st8x2(a + (cc * H + h) * 16, gh[cc], gl[cc]);
         }
         if (!ok) break;
       } else {
@@ -609,10 +606,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
             tc_fence_after();
           }
 #pragma unroll
-          for (int h = 0; h < H; ++h) {
-            tmem_st8(a + (cc * H + h) * 16, hi[h]);
-            tmem_st8(a + (cc * H + h) * 16 + 8, lo[h]);
-          }
+          for (int h = 0; h < H; ++h) tmem_st8x2(a + (cc * H + h) * 16, hi[h], lo[h]);
         }
         if (!ok) break;
       }
