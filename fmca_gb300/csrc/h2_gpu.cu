@@ -600,7 +600,9 @@ void launch_transfer_sf(int nb, const int32_t* list, const int32_t* son0,
   auto kern = transfer_sf_kernel<DIM, P, UP>;
   const size_t smem = (size_t)(3 * Q * 32 + Q + DIM * P * P) * sizeof(float);
   ensure_smem(kern, smem);
-  kern<<<nb, 128, smem, st>>>(list, son0, nsons, parent, E, midx, buf, ld, rofs, rcount);
+  // levels with few clusters: 8 warps per cluster shorten its latency chain
+  const int threads = nb < 4 * 152 ? 256 : 128;
+  kern<<<nb, threads, smem, st>>>(list, son0, nsons, parent, E, midx, buf, ld, rofs, rcount);
 }
 
 // the sum-factorised transfer for the tensor grids it is instantiated for

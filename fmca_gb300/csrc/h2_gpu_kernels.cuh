@@ -721,7 +721,7 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
 // E_c = e_c[0] (x) e_c[1] (x) ... applied as DIM contractions of P terms
 // each, on the coefficients held in tensor order (node with digits
 // (i_0, .., i_{DIM-1}) at position (i_0 P + i_1) P + ..). Block = one
-// cluster, 4 warps, lane = right-hand side rofs + lane; a contraction over
+// cluster, 4 or 8 warps, lane = right-hand side rofs + lane; a contraction over
 // dimension d hands every warp whole columns (the P coefficients that
 // differ in digit d): P loads, P^2 FMAs and P stores per column.
 //   UP (M2M):   t[c] = sum_sons (e_son[0] (x) ..) t[son]   (e[k][j], k: c)
@@ -730,7 +730,7 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
 // rows move in batches of 8 loads per lane, so that their latencies overlap.
 // shared: X, Y, Z [P^DIM][32] floats, sidx [P^DIM] ints, e [DIM][P][P]
 template <int DIM, int P, bool UP>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     transfer_sf_kernel(const int32_t* __restrict__ clist, const int32_t* __restrict__ son0,
                        const int32_t* __restrict__ nsons, const int32_t* __restrict__ parent,
                        const float* __restrict__ E, const int* __restrict__ midx_g,
@@ -744,7 +744,7 @@ __global__ void __launch_bounds__(128)
   int* sidx = reinterpret_cast<int*>(Z + Q * 32);  // tensor position -> storage index
   float* ef = reinterpret_cast<float*>(sidx + Q);  // [DIM][P][P]
   const int c = clist[blockIdx.x];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const bool live = lane < rcount;
   const int r = rofs + lane;
   for (int k = threadIdx.x; k < Q; k += blockDim.x) {
@@ -761,16 +761,16 @@ __global__ void __launch_bounds__(128)
     const int sc = UP ? son0[c] + si : parent[c];
     __syncthreads();  // previous source done with X, Y and ef; sidx ready
     for (int e = threadIdx.x; e < DIM * P * P; e += blockDim.x) ef[e] = E[(size_t)ec * DIM * P * P + e];
-    for (int t0 = warp; t0 < Q; t0 += 4 * U) {
+    for (int t0 = warp; t0 < Q; t0 += nw * U) {
       float v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int t = t0 + 4 * u;
+        const int t = t0 + nw * u;
         v[u] = (t < Q && live) ? buf[((size_t)sc * Q + sidx[t]) * ldv + r] : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < U; ++u)
-        if (t0 + 4 * u < Q) X[(t0 + 4 * u) * 32 + lane] = v[u];
+        if (t0 + nw * u < Q) X[(t0 + nw * u) * 32 + lane] = v[u];
     }
     __syncthreads();
     float* in = X;
@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(128)
         for (int b = 0; b < P; ++b)
           f[a][b] = UP ? ef[(d * P + a) * P + b] : ef[(d * P + b) * P + a];
       const bool last = d == DIM - 1;
-      for (int col = warp; col < NC; col += 4) {
+      for (int col = warp; col < NC; col += nw) {
         // base position of the column: digits other than d from col
         const int hi = col / stride, lo = col % stride;
         const int base = hi * stride * P + lo;
@@ -813,18 +813,18 @@ __global__ void __launch_bounds__(128)
   }
   // UP: t[c] = Z; DOWN: s[c] += Z
   if (live)
-    for (int t0 = warp; t0 < Q; t0 += 4 * U) {
+    for (int t0 = warp; t0 < Q; t0 += nw * U) {
       float v[U];
       if (!UP) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int t = t0 + 4 * u;
+          const int t = t0 + nw * u;
           v[u] = t < Q ? buf[((size_t)c * Q + sidx[t]) * ldv + r] : 0.f;
         }
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int t = t0 + 4 * u;
+        const int t = t0 + nw * u;
         if (t < Q)
           buf[((size_t)c * Q + sidx[t]) * ldv + r] = UP ? Z[t * 32 + lane] : v[u] + Z[t * 32 + lane];
       }
