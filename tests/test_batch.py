@@ -56,19 +56,21 @@ def test_batched_plan_is_union_of_single_plans():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "mixed"])
-def test_batched_matvec_against_oracle(cuda_device, prec):
+@pytest.mark.parametrize("prec,deg", [("fp64", 3), ("fp32", 3), ("mixed", 3), ("mixed", 4)])
+def test_batched_matvec_against_oracle(cuda_device, prec, deg):
+    # degree 4 in 3-D: the far field on tensor grids, sibling row clusters
+    # paired per CTA inside a forest of one tree per cloud
     import torch
     clouds = mixture_clouds(6, seed=2)
     R = 20
     cov = CovarianceKernel("GAUSSIAN", 0.2)
-    B = H2Matrix.batched(cov, clouds, 3, 0.8, precision=prec)
+    B = H2Matrix.batched(cov, clouds, deg, 0.8, precision=prec)
     rng = np.random.default_rng(3)
     X = rng.standard_normal((B.rows(), R))
     Y = B.matvec(torch.tensor(X, device=cuda_device)).cpu().numpy()
     for i, P in enumerate(clouds):
         o, e = B.offsets[i], B.offsets[i + 1]
-        O = oracle.OraclePlan(P, None, 3, 0.8, 0)
+        O = oracle.OraclePlan(P, None, deg, 0.8, 0)
         Yi, _ = O.action(3, 0.2, X[o:e])
         assert rel_err(Y[o:e], Yi) < TOL[prec], i
     B.check_device_error()

@@ -233,3 +233,18 @@ def test_mixed_uses_tensor_core_kernel_count(cuda_device):
     stages, nmx = H.profile()
     assert nmx == n32 + 3
     assert stages["near"] > 0 and stages["far"] > 0
+
+
+@pytest.mark.parametrize("dim,p", [(1, 4), (2, 3), (2, 4), (2, 6), (2, 7), (3, 3), (3, 5)])
+def test_mixed_interpolation_orders(cuda_device, dim, p):
+    # the sum-factorised transfers are compiled per (dimension, p + 1):
+    # 2-D with 4..8 and 3-D with 4..6 nodes per dimension; 1-D takes the
+    # dense transfer kernel
+    n = 4000
+    P = uniform_cloud(n, dim, seed=50 + 10 * dim + p)
+    X = np.random.default_rng(p).standard_normal((n, 32))
+    O = oracle.OraclePlan(P, None, p, 0.8, 0)
+    Y_ref, _ = O.action(1, 0.5, X)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, p, 0.8, precision="mixed")
+    assert rel_err(H.action(X), Y_ref) < 1e-5
+    H.check_device_error()
