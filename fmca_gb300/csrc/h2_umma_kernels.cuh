@@ -5,7 +5,7 @@
 // of up to 128 H targets per CTA (one CTA per SM), with
 //   a(t, s) = k(|t - s|) 2^(w_s - E)
 // (w_s: the source's moment exponent, 0 for points; E: the largest w_s of
-// the group; the scaling of h2_tc_kernels.cuh),
+// the sources that serve the target half; the scaling of h2_tc_kernels.cuh),
 // split into FP16 halves a = a_hi + a_lo and contracted as
 //   a_hi v_hi + a_hi v_lo + a_lo v_hi
 // by two tcgen05.mma per 16 sources and target half (M = 128 targets,
@@ -26,6 +26,11 @@
 //                lanes 32 (w % 4) .. + 31, i.e. targets h * 128 + lane for
 //                each half h < H. Set s evaluates the chunks 2 s and 2 s + 1
 //                of every tile into the A pair slot (4 k + s) mod NPS.
+// On tensor grids the two halves are two sibling row clusters (targets
+// g.tbegin + h q + lane, lane < q) over the union of their admissible column
+// clusters: every interval of the union carries the halves it serves
+// (imask), and a half that a source cluster does not serve gets zero A
+// values without an evaluation.
 // The products of F consecutive tiles (a unit) accumulate in one of two
 // accumulator buffers. The set of unit u (u mod 4) adds the unit's
 // accumulators into its own running total in shared memory
