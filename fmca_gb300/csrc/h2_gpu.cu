@@ -918,9 +918,8 @@ cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4
   auto kern = ksum_um_kernel<KT, H, REL, GRID>;
   const size_t smem = um_smem_bytes(H);
   ensure_smem(kern, smem);
-  kern<<<gl.ngroups, 32 * (3 + 4 * kUmSets), smem, st>>>(gl.groups, gl.ivl, tgt, pairs, vals,
-                                                         out, kTcRhs, rcount, kp, q, errf,
-                                                         gl.imask);
+  kern<<<gl.ngroups, kUmThreads, smem, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs,
+                                             rcount, kp, q, errf, gl.imask);
   return cudaGetLastError();
 }
 

@@ -25,20 +25,23 @@
 //   warps 3..18  four sets of 4 evaluation warps. Warp w owns tensor-memory
 //                lanes 32 (w % 4) .. + 31, i.e. targets h * 128 + lane for
 //                each half h < H. Set s evaluates the chunks 2 s and 2 s + 1
-//                of every tile into the A pair slot (4 k + s) mod NPS.
+//                of every tile into the A pair slot (4 k + s) mod NPS;
+//   warps 19..22 flush warps, one per tensor-memory lane quarter (below).
 // On tensor grids the two halves are two sibling row clusters (targets
 // g.tbegin + h q + lane, lane < q) over the union of their admissible column
 // clusters: every interval of the union carries the halves it serves
 // (imask), and a half that a source cluster does not serve gets zero A
 // values without an evaluation.
 // The products of F consecutive tiles (a unit) accumulate in one of two
-// accumulator buffers. The set of unit u (u mod 4) adds the unit's
-// accumulators into its own running total in shared memory
+// accumulator buffers. The flush warps take the units in order: they add a
+// unit's accumulators into the running total in shared memory
 // (round-to-nearest FP32 adds per unit, as the tensor cores truncate their
-// accumulations) after it has written its A pair of the next unit's first
-// tile; then it frees the accumulator buffer and the unit's stages: the
-// products of a unit completing implies that every set has read the
-// unit's source records. The four totals are added at the end.
+// accumulations), free the accumulator buffer and the unit's stages (the
+// products of a unit completing implies that every set has read the unit's
+// source records), and at the end scale and write the totals. Flushing in
+// separate warps keeps the evaluation sets, which run within a tile of
+// each other, from waiting on one set's flush (4-5 % faster than a flush by
+// the set of the unit).
 // Every wait is bounded (2 s); on a timeout the CTA raises the error flag,
 // drains its copies and products, frees tensor memory and returns, and
 // CTAs that start after the flag was raised return at once.
@@ -65,15 +68,19 @@ constexpr int kUmPtsBytes = kUmTile * 16;
 constexpr int kUmValBytes = kUmTile * kTcRhs * 2 * 2;  // hi and lo, interleaved
 constexpr int kUmStageBytes = kUmPtsBytes + kUmValBytes;
 constexpr int kUmHeader = 1024;
-constexpr int kUmSets = 4;  // sets of 4 evaluation warps
-// stages (the running totals of two target halves take 128 KB of shared
-// memory), and the shared memory of a CTA: header, stages, totals
-// [set][column][target]. Either size leaves no room for a second CTA on the
-// SM, which matters as each CTA allocates all 512 tensor-memory columns.
+constexpr int kUmSets = 4;        // sets of 4 evaluation warps
+constexpr int kUmFlushWarps = 4;  // one per tensor-memory lane quarter
+constexpr int kUmThreads = 32 * (3 + 4 * kUmSets + kUmFlushWarps);
+// floats per target row of the running total: 32 columns and a pad of 4,
+// so that a quarter warp's 16-byte accesses to 8 rows hit 32 banks
+constexpr int kUmTotStride = kTcRhs + 4;
+// stages, and the shared memory of a CTA: header, stages, running total
+// [target][column]. Either size leaves no room for a second CTA on the SM,
+// which matters as each CTA allocates all 512 tensor-memory columns.
 __host__ __device__ constexpr int um_stages(int H) { return H == 2 ? 5 : 6; }
 __host__ __device__ constexpr size_t um_smem_bytes(int H) {
   return kUmHeader + (size_t)um_stages(H) * kUmStageBytes +
-         (size_t)kUmSets * kTcRhs * 128 * H * sizeof(float);
+         (size_t)128 * H * kUmTotStride * sizeof(float);
 }
 constexpr uint32_t kUmCols = 512;
 
@@ -201,7 +208,7 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // and the near field 2 % faster, and the far field's rounding error 1.5x
 // larger (5e-7 relative at n = 1e6, measured against FP64).
 template <int KT, int H, bool REL, bool GRID, int F = ((GRID || H == 2) ? 2 : 1)>
-__global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
+__global__ void __launch_bounds__(kUmThreads, 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
                    const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
@@ -232,10 +239,9 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
   uint64_t* empty = full + NST;                              // [NST]
   uint64_t* afull = empty + NST;                             // [NPS]
   uint64_t* aempty = afull + NPS;                            // [NPS]
-  // tile accumulators complete on accf[k % 4] (two buffers, four barriers):
-  // with one half a product thread may run up to a tile ahead of the other,
-  // so a flush of tile k may start before tile k - 2 completes, never before
-  // tile k - 4
+  // unit accumulators complete on accf[u % 4] (two buffers; a product
+  // thread may run a tile ahead of the other, but starts unit u + 2 only
+  // after unit u was flushed, so two barriers would do)
   uint64_t* accf = aempty + NPS;                             // [4]
   uint64_t* acce = accf + 4;                                 // [2]
   uint64_t* done = acce + 2;                                 // [2]
@@ -418,7 +424,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
       }
     }
     __syncwarp();
-  } else {
+  } else if (warp < 3 + NEVAL) {
     // ---------------- evaluation warps
     const int ew = warp - 3, set = ew >> 2;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
@@ -470,7 +476,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
           mx[h] = fmaxf(mx[h], __shfl_xor_sync(0xffffffffu, mx[h], o));
         if (lane == 0) ered[ew * H + h] = mx[h];
       }
-      named_sync(1, NEVAL * 32);
+      named_sync(1, (NEVAL + kUmFlushWarps) * 32);
       E = -1000.f;  // groups without sources
 #pragma unroll
       for (int h = 0; h < H; ++h) {
@@ -480,52 +486,7 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
         E = fmaxf(E, Eh[h]);
       }
     }
-    float* mytot = tot + (size_t)set * kTcRhs * NT + row;
-
     bool ok = true;
-    // adds the accumulators of unit u (tiles u F .. u F + F - 1)
-    auto flush = [&](int u) {
-      const int b = u & 1;
-      if (!__all_sync(0xffffffffu, um_wait(&accf[u % 4], (uint32_t)((u / 4) & 1), abort_flag))) {
-        ok = false;
-        return;
-      }
-      tc_fence_after();
-#pragma unroll
-      for (int h = 0; h < H; ++h)
-#pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += 16) {
-          // two target halves: the accumulator of thread h; one half: the
-          // sum of both threads' accumulators
-          uint32_t v[16], u[16];
-          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + c0, v);
-          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + 32 + c0, u);
-          tmem_wait_ld16(v);
-          tmem_wait_ld16(u);
-          float x[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) x[i] = __uint_as_float(v[i]) + __uint_as_float(u[i]);
-          if (H == 1) {
-            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + c0, v);
-            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + 32 + c0, u);
-            tmem_wait_ld16(v);
-            tmem_wait_ld16(u);
-#pragma unroll
-            for (int i = 0; i < 16; ++i)
-              x[i] += __uint_as_float(v[i]) + __uint_as_float(u[i]);
-          }
-#pragma unroll
-          for (int i = 0; i < 16; ++i) mytot[(c0 + i) * NT + h * 128] += x[i];
-        }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        mbar_arrive1(&acce[b]);
-        if ((warp & 3) == 0)
-          for (int t = u * F; t < u * F + F && t < ntiles; ++t) mbar_arrive1(&empty[t % NST]);
-      }
-    };
-
     for (int k = 0; k < ntiles && ok; ++k) {
       const int stage = k % NST;
       if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag))) {
@@ -619,40 +580,106 @@ __global__ void __launch_bounds__(32 * (3 + 4 * kUmSets), 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive1(&afull[slot]);
-      const int u = k / F;
-      if (k % F == 0 && u >= 1 && (u - 1) % NSETS == set) {
-        flush(u - 1);
-        if (!ok) break;
+    }
+    if (!ok) atomicExch(err, 1);
+  } else {
+    // ---------------- flush warps: warp w owns tensor-memory lanes
+    // 32 (w % 4) .. + 31 and adds the accumulators of every unit, in order,
+    // into the running total of its targets
+    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    const int row = (warp & 3) * 32 + lane;
+    float Eh[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) Eh[h] = 0.f;
+    if constexpr (REL) {
+      // the evaluation warps' per-warp maxima of the moment exponents
+      named_sync(1, (NEVAL + kUmFlushWarps) * 32);
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        float all = -CUDART_INF_F;
+        for (int w = 0; w < NEVAL; ++w) all = fmaxf(all, ered[w * H + h]);
+        Eh[h] = fmaxf(all, -1000.f);
       }
     }
+    float* mytot = tot + (size_t)row * kUmTotStride;
+    bool ok = true;
     const int nunits = (ntiles + F - 1) / F;
-    if (ok && nunits >= 1 && (nunits - 1) % NSETS == set) flush(nunits - 1);
+    for (int u = 0; u < nunits; ++u) {
+      const int b = u & 1;
+      if (!__all_sync(0xffffffffu, um_wait(&accf[u % 4], (uint32_t)((u / 4) & 1), abort_flag))) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+#pragma unroll
+      for (int h = 0; h < H; ++h)
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 16) {
+          // two target halves: the accumulator of thread h; one half: the
+          // sum of both threads' accumulators
+          uint32_t v[16], w[16];
+          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + c0, v);
+          tmem_ld16(tbase + lanes + ACC0 + (b * 2 + h) * 64 + 32 + c0, w);
+          tmem_wait_ld16(v);
+          tmem_wait_ld16(w);
+          float x[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) x[i] = __uint_as_float(v[i]) + __uint_as_float(w[i]);
+          if (H == 1) {
+            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + c0, v);
+            tmem_ld16(tbase + lanes + ACC0 + (b * 2 + 1) * 64 + 32 + c0, w);
+            tmem_wait_ld16(v);
+            tmem_wait_ld16(w);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              x[i] += __uint_as_float(v[i]) + __uint_as_float(w[i]);
+          }
+          float4* t4 = reinterpret_cast<float4*>(mytot + (size_t)h * 128 * kUmTotStride + c0);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            float4 t = t4[i];
+            t.x += x[4 * i];
+            t.y += x[4 * i + 1];
+            t.z += x[4 * i + 2];
+            t.w += x[4 * i + 3];
+            t4[i] = t;
+          }
+        }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive1(&acce[b]);
+        if ((warp & 3) == 0)
+          for (int t = u * F; t < u * F + F && t < ntiles; ++t) mbar_arrive1(&empty[t % NST]);
+      }
+    }
     if (!ok) atomicExch(err, 1);
-
-    // all totals are complete: set s adds the four totals of columns
-    // 8 s .. 8 s + 7 and writes them
-    named_sync(1, NEVAL * 32);
-    if (!*abort_flag) {
+    if (ok && !*abort_flag) {
 #pragma unroll 1
       for (int h = 0; h < H; ++h) {
         const int eo = (int)(h ? Eh[H - 1] : Eh[0]);
         const uint32_t i = (uint32_t)(h * HS + row);  // target
         if (row >= HS || i >= g.tcount) continue;
-        float acc[8];
+        const float4* t4 = reinterpret_cast<const float4*>(mytot + (size_t)h * 128 * kUmTotStride);
+        float* o = out + (size_t)(g.tbegin + i) * ldo;
+        const bool whole = rcount == 32 && ldo == 32;
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const float* t = tot + (size_t)(8 * set + jj) * NT + h * 128 + row;
-          acc[jj] = ((t[0] + t[kTcRhs * NT]) + t[2 * kTcRhs * NT]) + t[3 * kTcRhs * NT];
-          if (REL) acc[jj] = ldexpf(acc[jj], eo);
-        }
-        float* o = out + (size_t)(g.tbegin + i) * ldo + 8 * set;
-        if (rcount == 32 && ldo == 32) {
-          *reinterpret_cast<float4*>(o) = make_float4(acc[0], acc[1], acc[2], acc[3]);
-          *reinterpret_cast<float4*>(o + 4) = make_float4(acc[4], acc[5], acc[6], acc[7]);
-        } else {
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj)
-            if (8 * set + jj < rcount) o[jj] = acc[jj];
+        for (int c = 0; c < 8; ++c) {
+          float4 t = t4[c];
+          if (REL) {
+            t.x = ldexpf(t.x, eo);
+            t.y = ldexpf(t.y, eo);
+            t.z = ldexpf(t.z, eo);
+            t.w = ldexpf(t.w, eo);
+          }
+          if (whole) {
+            reinterpret_cast<float4*>(o)[c] = t;
+          } else {
+            if (4 * c + 0 < rcount) o[4 * c + 0] = t.x;
+            if (4 * c + 1 < rcount) o[4 * c + 1] = t.y;
+            if (4 * c + 2 < rcount) o[4 * c + 2] = t.z;
+            if (4 * c + 3 < rcount) o[4 * c + 3] = t.w;
+          }
         }
       }
     }
