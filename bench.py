@@ -43,7 +43,7 @@ SMS = 152
 SFU_PAIRS_PER_CLK = 32.0 / 3.0
 # DRAM bytes (read + write) of one near-field kernel-sum launch of the default
 # workload, from one ncu capture (profiles/ksum_um_c2_full.md)
-NEAR_DRAM_BYTES_PER_LAUNCH = 2.585309e9 + 0.118240e9
+NEAR_DRAM_BYTES_PER_LAUNCH = 2.644428e9 + 0.149038e9
 
 
 def _measured_bf16_tflops():
