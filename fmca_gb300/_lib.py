@@ -34,8 +34,9 @@ ORDER_CLUSTER = 1
 INFO_KEYS = [
     "n_rows", "n_cols", "dim", "degree", "q", "row_clusters", "col_clusters",
     "far_blocks", "near_blocks", "near_pairs", "row_levels", "col_levels",
-    "row_leaves", "col_leaves", "min_leaf",
+    "row_leaves", "col_leaves", "min_leaf", "interpolator",
 ]
+INTERPOLATORS = {"tensor": 0, "total_degree": 1}
 INFO_COUNT = 16
 
 # every symbol the header declares; tests check the library exports them all
@@ -48,7 +49,7 @@ EXPORTED = [
     "fmca_plan_set_profiling", "fmca_plan_profile", "fmca_matvec_static_scratch",
     "fmca_matvec_adjoint_workspace_size", "fmca_matvec_adjoint", "fmca_plan_update_points",
     "fmca_plan_create_batched", "fmca_matvec_graph_create", "fmca_graph_launch",
-    "fmca_graph_destroy",
+    "fmca_graph_destroy", "fmca_plan_create_ex", "fmca_plan_interpolator",
 ]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
@@ -86,6 +87,9 @@ def load() -> C.CDLL:
     lib.fmca_kernel_type_from_name.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     lib.fmca_plan_create.argtypes = [dp, i32, i64, dp, i64, i32, C.c_double, i64,
                                      C.POINTER(vp)]
+    lib.fmca_plan_create_ex.argtypes = [dp, i32, i64, dp, i64, i32, i32, C.c_double, i64,
+                                        C.POINTER(vp)]
+    lib.fmca_plan_interpolator.argtypes = [vp, dp, dp]
     lib.fmca_plan_destroy.argtypes = [vp]
     lib.fmca_plan_info.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.fmca_plan_statistics.argtypes = [vp, dp]

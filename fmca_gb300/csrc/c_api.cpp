@@ -109,6 +109,13 @@ fmca_status fmca_kernel_type_from_name(const char* name, int* type) {
 fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
                              const double* P_cols, int64_t n_cols, int degree,
                              double eta, int64_t min_leaf, fmca_plan** out) {
+  return fmca_plan_create_ex(P_rows, dim, n_rows, P_cols, n_cols,
+                             FMCA_INTERP_TENSOR_PRODUCT, degree, eta, min_leaf, out);
+}
+
+fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
+                                const double* P_cols, int64_t n_cols, int interpolator,
+                                int degree, double eta, int64_t min_leaf, fmca_plan** out) {
   if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!P_rows) return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows is NULL");
@@ -121,6 +128,12 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
     return fail(FMCA_ERR_INVALID_ARGUMENT, "n_cols out of range");
   if (degree < 0 || degree > 16)
     return fail(FMCA_ERR_INVALID_ARGUMENT, "degree out of range");
+  if (interpolator != FMCA_INTERP_TENSOR_PRODUCT && interpolator != FMCA_INTERP_TOTAL_DEGREE)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown interpolator");
+  // the total-degree nodes come from Halton sequences in the first three
+  // prime bases, and the GPU passes take at most 8 polynomial factors
+  if (interpolator == FMCA_INTERP_TOTAL_DEGREE && (dim > 3 || degree > 7))
+    return fail(FMCA_ERR_UNSUPPORTED, "total-degree interpolation needs dim <= 3, degree <= 7");
   if (!(eta >= 0) || !std::isfinite(eta))
     return fail(FMCA_ERR_INVALID_ARGUMENT, "eta must be finite and >= 0");
   if (min_leaf < 0 || min_leaf > (int64_t)0x7FFFFFFF)
@@ -136,7 +149,9 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
     fmca_plan* p = new fmca_plan();
     p->min_leaf = min_leaf;
     p->plan.build(P_rows, (uint32_t)n_rows, same ? P_rows : P_cols,
-                  (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same);
+                  (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same,
+                  interpolator == FMCA_INTERP_TOTAL_DEGREE ? fmca::kInterpTotalDegree
+                                                           : fmca::kInterpTensor);
     *out = p;
   } catch (const std::bad_alloc&) {
     return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
@@ -203,6 +218,16 @@ fmca_status fmca_plan_destroy(fmca_plan* plan) {
   return ok();
 }
 
+fmca_status fmca_plan_interpolator(const fmca_plan* p, double* nodes, double* invV) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  const fmca::Interp& ip = p->plan.interp;
+  if (nodes) std::copy(ip.Xi.begin(), ip.Xi.end(), nodes);
+  if (invV && ip.kind == fmca::kInterpTotalDegree)
+    for (int i = 0; i < ip.q; ++i)
+      for (int j = 0; j < ip.q; ++j) invV[(size_t)j * ip.q + i] = ip.invV[(size_t)i * ip.q + j];
+  return ok();
+}
+
 fmca_status fmca_plan_info(const fmca_plan* p, int64_t out[FMCA_INFO_COUNT]) {
   if (!p || !out) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
   for (int i = 0; i < FMCA_INFO_COUNT; ++i) out[i] = 0;
@@ -212,6 +237,9 @@ fmca_status fmca_plan_info(const fmca_plan* p, int64_t out[FMCA_INFO_COUNT]) {
   out[FMCA_INFO_DIM] = P.interp.dim;
   out[FMCA_INFO_DEGREE] = P.interp.deg;
   out[FMCA_INFO_Q] = P.interp.q;
+  out[FMCA_INFO_INTERPOLATOR] = P.interp.kind == fmca::kInterpTotalDegree
+                                    ? FMCA_INTERP_TOTAL_DEGREE
+                                    : FMCA_INTERP_TENSOR_PRODUCT;
   out[FMCA_INFO_ROW_CLUSTERS] = P.rows.nclusters();
   out[FMCA_INFO_COL_CLUSTERS] = P.cols.nclusters();
   out[FMCA_INFO_FAR_BLOCKS] = (int64_t)P.pat.far_row.size();
@@ -372,6 +400,8 @@ fmca_status fmca_matvec_adjoint(fmca_plan* p, const fmca_kernel_desc* kernel, in
       fmca::capi::check_matvec_args(p, kernel, precision, dtype, FMCA_ORDER_NATURAL, nrhs,
                                     x, y);
   if (s != FMCA_OK) return s;
+  if (p->plan.interp.kind != fmca::kInterpTensor)
+    return fail(FMCA_ERR_UNSUPPORTED, "the adjoint needs a tensor-product plan");
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);

@@ -56,6 +56,8 @@ struct DevSet {
   T* bbext_c = nullptr;
   T* E_r = nullptr;
   T* E_c = nullptr;
+  T* to_nodal = nullptr;    // total degree: invV^T (row-major q x q)
+  T* from_nodal = nullptr;  // total degree: invV
   InterpDev<T> ip;
 };
 
@@ -242,6 +244,15 @@ int upload_set(const Plan& plan, DevPlan* dp, DevSet<T>* s, std::string* err) {
   FMCA_TRY(to_device(dp, hv.data(), hv.size(), &s->E_r, err));
   hv.assign(plan.col_E.begin(), plan.col_E.end());
   FMCA_TRY(to_device(dp, hv.data(), hv.size(), &s->E_c, err));
+  if (plan.interp.kind == kInterpTotalDegree) {
+    hv.assign((size_t)q * q, T(0));
+    for (int k = 0; k < q; ++k)
+      for (int j = 0; j < q; ++j) hv[(size_t)k * q + j] = (T)plan.interp.invV[(size_t)j * q + k];
+    FMCA_TRY(to_device(dp, hv.data(), hv.size(), &s->to_nodal, err));
+    hv.assign(plan.interp.invV.begin(), plan.interp.invV.end());
+    FMCA_TRY(to_device(dp, hv.data(), hv.size(), &s->from_nodal, err));
+  }
+  s->ip.kind = plan.interp.kind;
   s->ip.dim = dim;
   s->ip.p1 = plan.interp.deg + 1;
   s->ip.q = q;
@@ -326,7 +337,8 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
   // (target halves of q nodes each): sources = the union of their
   // admissible column clusters, consecutive clusters with the same halves
   // merged into one interval, imask = the halves an interval serves
-  if (plan.interp.dim == 3 && plan.interp.deg + 1 == kGridP1) {
+  if (plan.interp.kind == kInterpTensor && plan.interp.dim == 3 &&
+      plan.interp.deg + 1 == kGridP1) {
     HostGroups hg;
     const int q = ip.q;
     const Pattern& P = plan.pat;
@@ -639,6 +651,25 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
                      const int32_t* nsons, const int32_t* parent, const T* E,
                      const int* midx, const InterpDev<T>& ip, T* buf, int ld,
                      int rofs, int rcount, cudaStream_t st) {
+  if (ip.kind == kInterpTotalDegree) {
+    // dense E per cluster; levels with few clusters split the right-hand
+    // sides in slices of 8
+    const int q = ip.q;
+    if (nb < 2 * 152 && rcount > 8 && RB > 8) {
+      auto kern = transfer_dense_kernel<T, 8, UP>;
+      const size_t smem = (dense_pad(q) + (size_t)q * 8) * sizeof(T);
+      ensure_smem(kern, smem);
+      kern<<<dim3(nb, (rcount + 7) / 8), 128, smem, st>>>(list, son0, nsons, parent, E, q,
+                                                           buf, ld, rofs, rcount);
+    } else {
+      auto kern = transfer_dense_kernel<T, RB, UP>;
+      const size_t smem = (dense_pad(q) + (size_t)q * RB) * sizeof(T);
+      ensure_smem(kern, smem);
+      kern<<<dim3(nb, (rcount + RB - 1) / RB), 128, smem, st>>>(list, son0, nsons, parent, E,
+                                                                 q, buf, ld, rofs, rcount);
+    }
+    return;
+  }
   if constexpr (std::is_same<T, float>::value && RB == 32) {
     if (launch_transfer_sf_any<UP>(nb, list, son0, nsons, parent, E, midx, ip, buf, ld, rofs,
                                    rcount, st))
@@ -661,6 +692,21 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
   ensure_smem(kern, smem);
   kern<<<nb, 128, smem, st>>>(list, son0, nsons, parent, E, midx, ip, buf, ld, rofs,
                               rcount);
+}
+
+// total degree: coefficients of clusters 0 .. ncl - 1 to (M = invV^T) or
+// from (M = invV) the nodal basis of the far field; one launch (or none for
+// the tensor product, whose basis is nodal already)
+template <typename T, int RB>
+bool launch_basis_change(const InterpDev<T>& ip, int ncl, const T* M, T* buf, int ld, int rofs,
+                         int rcount, cudaStream_t st) {
+  if (ip.kind != kInterpTotalDegree || ncl == 0) return false;
+  auto kern = basis_change_kernel<T, RB>;
+  const size_t smem = (dense_pad(ip.q) + (size_t)ip.q * RB) * sizeof(T);
+  ensure_smem(kern, smem);
+  kern<<<dim3(ncl, (rcount + RB - 1) / RB), 128, smem, st>>>(ncl, M, ip.q, buf, ld, rofs,
+                                                              rcount);
+  return true;
 }
 
 template <typename T, int RB>
@@ -699,12 +745,16 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
       ++dp->launches;
     }
   }
+  dp->launches += launch_basis_change<T, RB>(S.ip, plan.cols.nclusters(), S.to_nodal, w.t, ld,
+                                             rofs, rcount, st);
   dp->mark(FMCA_STAGE_M2M, st);
   // far-field coupling
   cudaError_t e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s,
                                  rofs, rcount, kp, 0, dp->err_flag, st);
   if (e != cudaSuccess) return e;
   dp->launches += dp->far.ngroups ? 1 : 0;
+  dp->launches += launch_basis_change<T, RB>(S.ip, plan.rows.nclusters(), S.from_nodal, w.s,
+                                             ld, rofs, rcount, st);
   dp->mark(FMCA_STAGE_FAR, st);
   // L2L, top-down
   for (int l = 1; l < plan.rows.nlevels(); ++l) {
@@ -978,7 +1028,8 @@ cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* 
 }
 
 bool grid_far(const Plan& plan) {
-  return plan.interp.dim == 3 && plan.interp.deg + 1 == kGridP1;
+  return plan.interp.kind == kInterpTensor && plan.interp.dim == 3 &&
+         plan.interp.deg + 1 == kGridP1;
 }
 
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
@@ -1066,6 +1117,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
         ++dp->launches;
       }
     }
+    dp->launches += launch_basis_change<float, RB>(S.ip, Cc, S.to_nodal, t, ld, 0, rcount, st);
     dp->mark(FMCA_STAGE_M2M, st);
     const bool grid = grid_far(plan);
     if (grid)
@@ -1082,6 +1134,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     else
       FMCA_CK(launch_um<1>(fl, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q, dp->err_flag, st));
     dp->launches += fl.ngroups ? 1 : 0;
+    dp->launches += launch_basis_change<float, RB>(S.ip, Cr, S.from_nodal, s, ld, 0, rcount, st);
     dp->mark(FMCA_STAGE_FAR, st);
     for (int l = 1; l < plan.rows.nlevels(); ++l) {
       const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];

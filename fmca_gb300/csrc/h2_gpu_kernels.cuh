@@ -59,9 +59,11 @@ struct KParams {
   T g;   // coordinate scale of the tensor-core path (1 for generic kernels)
 };
 
+// kind 0: Chebyshev tensor product (Lagrange factors from xi, w); kind 1:
+// total degree (L2-normalised Legendre factors)
 template <typename T>
 struct InterpDev {
-  int dim, p1, q;
+  int kind, dim, p1, q;
   T xi[8], w[8];
 };
 
@@ -494,6 +496,26 @@ __device__ __forceinline__ void lagrange1d(const InterpDev<T>& ip, T x, T* f,
   }
 }
 
+// the p1 one-dimensional factors of the interpolator's basis at x in [0, 1]:
+// Lagrange factors, or Legendre polynomials scaled to unit L2 norm
+// (evalPolynomials.h:19-38: the three-term recurrence on the unscaled
+// polynomials, each scaled by sqrt(2 i + 1))
+template <typename T>
+__device__ __forceinline__ void basis1d(const InterpDev<T>& ip, T x, T* f, int stride = 1) {
+  if (ip.kind == 0) {
+    lagrange1d(ip, x, f, stride);
+    return;
+  }
+  T p0 = T(0), p1 = T(1);
+  f[0] = T(1);
+  for (int i = 1; i < ip.p1; ++i) {
+    const T v = T(2 * i - 1) / T(i) * (T(2) * x - T(1)) * p1 - T(i - 1) / T(i) * p0;
+    p0 = p1;
+    p1 = v;
+    f[i * stride] = v * sqrt(T(2 * i + 1));
+  }
+}
+
 // multi-index k -> (k0, k1, k2) packed as k0 | k1 << 8 | k2 << 16 (digits < 8)
 __device__ __forceinline__ void pack_digits(const int* __restrict__ midx_g, int q,
                                             int* __restrict__ pk) {
@@ -625,7 +647,7 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
           const T x = reinterpret_cast<const T*>(pts + b + i0 + i)[d];
           const T lod = d == 0 ? lo[0] : (d == 1 ? lo[1] : lo[2]);
           const T exd = d == 0 ? ex[0] : (d == 1 ? ex[1] : ex[2]);
-          lagrange1d(ip, (x - lod) / exd, f);
+          basis1d(ip, (x - lod) / exd, f);
         } else {
           f[0] = T(1);
         }
@@ -714,6 +736,89 @@ __global__ void transfer_kernel(const int32_t* __restrict__ clist,
       }
     }
     if (valid) store_row<T, RB, !UP>(buf + ((size_t)c * q + k) * ldv + rofs_b, acc, rc);
+  }
+}
+
+// elements of a q x q matrix in shared memory rounded up to a multiple of
+// 4, so that the rows staged after it start on a 16-byte boundary (the
+// 16-byte vector stores of stage_rows)
+__host__ __device__ constexpr size_t dense_pad(int q) { return ((size_t)q * q + 3) & ~(size_t)3; }
+
+// One transfer level with dense per-cluster matrices E_c (q x q, row-major;
+// total-degree interpolation):
+//   UP (M2M):   t[c][k] = sum_sons sum_j E_son[k][j] t[son][j]
+//   DOWN (L2L): s[c][j] += sum_k E_c[k][j] s[parent][k]
+// Block = one cluster and a slice of RB right-hand sides (blockIdx.y), one
+// thread per output coefficient (q <= blockDim); E and the source rows
+// staged in shared memory. shared: E [q][q] (padded), S [q][RB]
+template <typename T, int RB, bool UP>
+__global__ void transfer_dense_kernel(const int32_t* __restrict__ clist,
+                                      const int32_t* __restrict__ son0,
+                                      const int32_t* __restrict__ nsons,
+                                      const int32_t* __restrict__ parent,
+                                      const T* __restrict__ E, int q, T* buf, int ldv,
+                                      int rofs, int rcount) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* e = reinterpret_cast<T*>(smem_raw);  // q x q
+  T* S = e + dense_pad(q);                 // q x RB, 16-byte aligned
+  const int c = clist[blockIdx.x];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int rofs_b = rofs + (int)blockIdx.y * RB;
+  const int rc = min(RB, rcount - (int)blockIdx.y * RB);
+  const int nsrc = UP ? nsons[c] : 1;
+  const int k = tid;  // output coefficient (q <= blockDim)
+  T acc[RB];
+#pragma unroll
+  for (int r = 0; r < RB; ++r) acc[r] = T(0);
+  for (int si = 0; si < nsrc; ++si) {
+    const int ec = UP ? son0[c] + si : c;          // cluster whose E is used
+    const int sc = UP ? son0[c] + si : parent[c];  // source coefficients
+    __syncthreads();
+    for (int i = tid; i < q * q; i += nthr) e[i] = E[(size_t)ec * q * q + i];
+    stage_rows<T, RB>(S, buf + (size_t)sc * q * ldv, q, ldv, rofs_b, rc);
+    __syncthreads();
+    if (k < q) {
+      for (int j = 0; j < q; ++j) {
+        const T ev = UP ? e[k * q + j] : e[j * q + k];
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] += ev * S[j * RB + r];
+      }
+    }
+  }
+  if (k < q) store_row<T, RB, !UP>(buf + ((size_t)c * q + k) * ldv + rofs_b, acc, rc);
+}
+
+// Change of basis of every cluster's coefficients, in place:
+//   buf[c][k] = sum_j M[k][j] buf[c][j]   (M: q x q, row-major)
+// for clusters 0 .. ncl - 1. With total-degree interpolation the moments of
+// the upward pass are taken to the nodal basis by M = invV^T before the
+// far field, and the far-field expansions back by M = invV after it, so that
+// the coupling invV K invV^T (NystromEvaluator.h:40-56) becomes a kernel sum
+// over the interpolation nodes. shared: M [q][q] (padded), S [q][RB]
+template <typename T, int RB>
+__global__ void basis_change_kernel(int ncl, const T* __restrict__ M, int q, T* buf, int ldv,
+                                    int rofs, int rcount) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* m = reinterpret_cast<T*>(smem_raw);  // q x q
+  T* S = m + dense_pad(q);                 // q x RB, 16-byte aligned
+  const int c = blockIdx.x;
+  if (c >= ncl) return;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int rofs_b = rofs + (int)blockIdx.y * RB;
+  const int rc = min(RB, rcount - (int)blockIdx.y * RB);
+  for (int i = tid; i < q * q; i += nthr) m[i] = M[i];
+  stage_rows<T, RB>(S, buf + (size_t)c * q * ldv, q, ldv, rofs_b, rc);
+  __syncthreads();
+  for (int k = tid; k < q; k += nthr) {
+    T acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = T(0);
+    for (int j = 0; j < q; ++j) {
+      const T mv = m[k * q + j];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] += mv * S[j * RB + r];
+    }
+    store_row<T, RB, false>(buf + ((size_t)c * q + k) * ldv + rofs_b, acc, rc);
   }
 }
 
@@ -865,7 +970,7 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
     const T pc[3] = {p.x, p.y, p.z};
     for (int d = 0; d < 3; ++d) {
       if (d < ip.dim)
-        lagrange1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8 * nthr, nthr);
+        basis1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8 * nthr, nthr);
       else
         f[d * 8 * nthr] = T(1);
     }

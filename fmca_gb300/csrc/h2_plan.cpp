@@ -85,8 +85,135 @@ double kernel_eval_host(int type, double l, double c, double r) {
 }
 
 // ---------------------------------------------------------------------------
-// interpolation (TensorProductInterpolator.h:39-61, MultiIndexSet.h:87-100)
-void Interp::init(int dim_, int deg_) {
+// interpolation (TensorProductInterpolator.h:39-61, TotalDegreeInterpolator.h:
+// 26-47, MultiIndexSet.h:39-100)
+namespace {
+// the multi-indices of the tensor (max entry <= deg) or total-degree (sum
+// <= deg) set, ordered by 1-norm, then lexicographically (FMCA_Compare)
+std::vector<std::vector<int>> index_set(int dim, int deg, bool total) {
+  std::vector<std::vector<int>> set;
+  std::vector<int> cur(dim, 0);
+  int count = 1;
+  for (int i = 0; i < dim; ++i) count *= (deg + 1);
+  for (int k = 0; k < count; ++k) {
+    int r = k, sum = 0;
+    for (int i = dim - 1; i >= 0; --i) {
+      cur[i] = r % (deg + 1);
+      r /= (deg + 1);
+      sum += cur[i];
+    }
+    if (!total || sum <= deg) set.push_back(cur);
+  }
+  std::sort(set.begin(), set.end(), [](const std::vector<int>& a, const std::vector<int>& b) {
+    int na = 0, nb = 0;
+    for (int v : a) na += v;
+    for (int v : b) nb += v;
+    if (na != nb) return na < nb;
+    return std::lexicographical_compare(a.begin(), a.end(), b.begin(), b.end());
+  });
+  return set;
+}
+
+// radical inverse of m in base b: the digits of m mirrored at the radix
+// point, as one correctly rounded division of two exact integers (the
+// Halton sequence of HaltonSet.h:30-55)
+double radical_inverse(uint64_t m, uint64_t b) {
+  uint64_t num = 0, den = 1;
+  while (m) {
+    num = num * b + m % b;
+    den *= b;
+    m /= b;
+  }
+  return (double)num / (double)den;
+}
+
+// DeMarchi points (DeMarchiPoints.h:20-43): the Halton points 100 ..
+// 100 + 10 q - 1 (HaltonSet<100>: 100 points skipped) are candidates; the
+// nodes are the first q columns chosen by a column-pivoted QR
+// factorisation of the q x 10 q matrix of polynomial values, in the order
+// chosen. Householder reflections; the remaining column norms are
+// recomputed at every step instead of downdated.
+void demarchi_nodes(const Interp& ip, std::vector<double>* nodes) {
+  const int q = ip.q, dim = ip.dim, M = 10 * q;
+  static const uint64_t primes[3] = {2, 3, 5};
+  std::vector<double> cand((size_t)M * dim), A((size_t)q * M);
+  for (int m = 0; m < M; ++m) {
+    for (int d = 0; d < dim; ++d)
+      cand[(size_t)m * dim + d] = radical_inverse((uint64_t)(100 + m), primes[d]);
+    ip.poly(&cand[(size_t)m * dim], &A[(size_t)m * q]);
+  }
+  std::vector<int> col(M);
+  for (int m = 0; m < M; ++m) col[m] = m;
+  std::vector<double> v(q);
+  for (int s = 0; s < q; ++s) {
+    int best = s;
+    double bn = -1.;
+    for (int j = s; j < M; ++j) {
+      double n2 = 0;
+      for (int i = s; i < q; ++i) n2 += A[(size_t)j * q + i] * A[(size_t)j * q + i];
+      if (n2 > bn) {
+        bn = n2;
+        best = j;
+      }
+    }
+    if (best != s) {
+      std::swap(col[s], col[best]);
+      for (int i = 0; i < q; ++i) std::swap(A[(size_t)s * q + i], A[(size_t)best * q + i]);
+    }
+    // reflector H = I - 2 v v^T / (v^T v) mapping column s onto e_s
+    const double alpha = A[(size_t)s * q + s] >= 0 ? -std::sqrt(bn) : std::sqrt(bn);
+    double vv = 0;
+    for (int i = s; i < q; ++i) {
+      v[i] = A[(size_t)s * q + i] - (i == s ? alpha : 0.);
+      vv += v[i] * v[i];
+    }
+    if (vv == 0) continue;
+    for (int j = s; j < M; ++j) {
+      double dot = 0;
+      for (int i = s; i < q; ++i) dot += v[i] * A[(size_t)j * q + i];
+      const double f = 2. * dot / vv;
+      for (int i = s; i < q; ++i) A[(size_t)j * q + i] -= f * v[i];
+    }
+  }
+  nodes->assign((size_t)q * dim, 0.);
+  for (int k = 0; k < q; ++k)
+    for (int d = 0; d < dim; ++d) (*nodes)[(size_t)k * dim + d] = cand[(size_t)col[k] * dim + d];
+}
+
+// inverse of the n x n row-major matrix a (Gauss-Jordan, partial pivoting)
+std::vector<double> invert(std::vector<double> a, int n) {
+  std::vector<double> b((size_t)n * n, 0.);
+  for (int i = 0; i < n; ++i) b[(size_t)i * n + i] = 1.;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::abs(a[(size_t)r * n + c]) > std::abs(a[(size_t)piv * n + c])) piv = r;
+    if (piv != c)
+      for (int j = 0; j < n; ++j) {
+        std::swap(a[(size_t)c * n + j], a[(size_t)piv * n + j]);
+        std::swap(b[(size_t)c * n + j], b[(size_t)piv * n + j]);
+      }
+    const double d = a[(size_t)c * n + c];
+    for (int j = 0; j < n; ++j) {
+      a[(size_t)c * n + j] /= d;
+      b[(size_t)c * n + j] /= d;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[(size_t)r * n + c];
+      if (f == 0) continue;
+      for (int j = 0; j < n; ++j) {
+        a[(size_t)r * n + j] -= f * a[(size_t)c * n + j];
+        b[(size_t)r * n + j] -= f * b[(size_t)c * n + j];
+      }
+    }
+  }
+  return b;
+}
+}  // namespace
+
+void Interp::init(int dim_, int deg_, int kind_) {
+  kind = kind_;
   dim = dim_;
   deg = deg_;
   const double weight = 2. * M_PI / (2. * double(deg) + 2.);
@@ -98,33 +225,44 @@ void Interp::init(int dim_, int deg_) {
     w[k] = std::sin(weight * (double(k) + 0.5));
     if (k % 2 == 1) w[k] *= -1.;
   }
-  // all multi-indices with entries <= deg, ordered by 1-norm, then lex
-  q = 1;
-  for (int i = 0; i < dim; ++i) q *= (deg + 1);
-  std::vector<std::vector<int>> set(q, std::vector<int>(dim));
-  for (int k = 0; k < q; ++k) {
-    int r = k;
-    for (int i = dim - 1; i >= 0; --i) {
-      set[k][i] = r % (deg + 1);
-      r /= (deg + 1);
-    }
-  }
-  std::sort(set.begin(), set.end(),
-            [](const std::vector<int>& a, const std::vector<int>& b) {
-              int na = 0, nb = 0;
-              for (int v : a) na += v;
-              for (int v : b) nb += v;
-              if (na != nb) return na < nb;
-              return std::lexicographical_compare(a.begin(), a.end(), b.begin(),
-                                                  b.end());
-            });
+  const std::vector<std::vector<int>> set = index_set(dim, deg, kind == kInterpTotalDegree);
+  q = (int)set.size();
   midx.assign((size_t)q * dim, 0);
-  Xi.assign((size_t)q * dim, 0.);
   for (int k = 0; k < q; ++k)
-    for (int i = 0; i < dim; ++i) {
-      midx[(size_t)k * dim + i] = set[k][i];
-      Xi[(size_t)k * dim + i] = xi[set[k][i]];
-    }
+    for (int i = 0; i < dim; ++i) midx[(size_t)k * dim + i] = set[k][i];
+  Xi.assign((size_t)q * dim, 0.);
+  invV.clear();
+  if (kind == kInterpTotalDegree) {
+    demarchi_nodes(*this, &Xi);
+    std::vector<double> V((size_t)q * q);
+    for (int i = 0; i < q; ++i) poly(&Xi[(size_t)i * dim], &V[(size_t)i * q]);
+    invV = invert(V, q);
+  } else {
+    for (int k = 0; k < q; ++k)
+      for (int i = 0; i < dim; ++i) Xi[(size_t)k * dim + i] = xi[set[k][i]];
+  }
+}
+
+void Interp::legendre1d(double x, double* f) const {
+  double p0 = 0., p1 = 1.;
+  f[0] = 1.;
+  for (int i = 1; i <= deg; ++i) {
+    const double v = double(2 * i - 1) / double(i) * (2. * x - 1.) * p1 -
+                     double(i - 1) / double(i) * p0;
+    p0 = p1;
+    p1 = v;
+    f[i] = v * std::sqrt(double(2 * i + 1));
+  }
+}
+
+void Interp::poly(const double* u, double* out) const {
+  double f[3][32];
+  for (int d = 0; d < dim; ++d) legendre1d(u[d], f[d]);
+  for (int k = 0; k < q; ++k) {
+    double v = 1.;
+    for (int d = 0; d < dim; ++d) v *= f[d][midx[(size_t)k * dim + d]];
+    out[k] = v;
+  }
 }
 
 // Barycentric Lagrange basis in one variable (TensorProductInterpolator.h:65-81).
@@ -317,6 +455,33 @@ void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize) {
 void compute_transfer_factors(const Tree& t, const Interp& ip,
                               std::vector<double>* E) {
   const int C = t.nclusters(), dim = t.dim, p1 = ip.deg + 1;
+  if (ip.kind == kInterpTotalDegree) {
+    // E = P(son nodes in the father's cell) invV^T
+    // (compute_cluster_bases_impl.h:36-50), row-major q x q per son
+    const int q = ip.q;
+    E->assign((size_t)C * q * q, 0.);
+    std::vector<double> u(dim), P((size_t)q * q);
+    for (int c = 1; c < C; ++c) {
+      const int fa = t.parent[c];
+      if (fa < 0 || t.size[c] == 0) continue;  // E stays zero for empty sons
+      for (int j = 0; j < q; ++j) {
+        for (int d = 0; d < dim; ++d)
+          u[d] = ip.Xi[(size_t)j * dim + d] * t.bbext[(size_t)c * dim + d] /
+                     t.bbext[(size_t)fa * dim + d] +
+                 (t.bbmin[(size_t)c * dim + d] - t.bbmin[(size_t)fa * dim + d]) /
+                     t.bbext[(size_t)fa * dim + d];
+        ip.poly(u.data(), &P[(size_t)j * q]);  // P[j][k]: polynomial k at node j
+      }
+      double* e = E->data() + (size_t)c * q * q;
+      for (int k = 0; k < q; ++k)
+        for (int jj = 0; jj < q; ++jj) {
+          double acc = 0;
+          for (int j = 0; j < q; ++j) acc += P[(size_t)j * q + k] * ip.invV[(size_t)jj * q + j];
+          e[(size_t)k * q + jj] = acc;
+        }
+    }
+    return;
+  }
   const size_t per = (size_t)dim * p1 * p1;
   E->assign((size_t)C * per, 0.);
   std::vector<double> f(p1);
@@ -389,8 +554,9 @@ Adm compare(const Tree& r, int i, const Tree& c, int j, double eta) {
 }  // namespace
 
 void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
-                 int dim, int deg, double eta_, uint32_t min_leaf, bool same) {
-  interp.init(dim, deg);
+                 int dim, int deg, double eta_, uint32_t min_leaf, bool same,
+                 int interp_kind) {
+  interp.init(dim, deg, interp_kind);
   eta = eta_;
   points_r.assign(Pr, Pr + (size_t)dim * nr);
   if (same)

@@ -62,19 +62,31 @@ const char* kernel_type_name(int type);
 // expression order; used by the host (statistics, tests) only.
 double kernel_eval_host(int type, double l, double c, double r);
 
-// Chebyshev tensor-product interpolator on [0,1]^d.
+// Interpolator on [0,1]^d: the Chebyshev tensor-product interpolator
+// (kind 0, TensorProductInterpolator.h) or the total-degree interpolator
+// (kind 1, TotalDegreeInterpolator.h: DeMarchi nodes, L2-normalised Legendre
+// polynomials, dense inverse Vandermonde matrix).
+enum { kInterpTensor = 0, kInterpTotalDegree = 1 };
 struct Interp {
+  int kind = kInterpTensor;
   int dim = 0;
   int deg = 0;
-  int q = 0;                 // (deg+1)^dim
-  std::vector<double> xi;    // deg+1 univariate nodes
-  std::vector<double> w;     // deg+1 barycentric weights
+  int q = 0;                 // (deg+1)^dim, or binom(deg+dim, dim)
+  std::vector<double> xi;    // tensor: deg+1 univariate nodes
+  std::vector<double> w;     // tensor: deg+1 barycentric weights
   std::vector<int> midx;     // q x dim multi-indices, graded-lex order
   std::vector<double> Xi;    // dim x q node coordinates (column-major)
-  void init(int dim, int deg);
+  std::vector<double> invV;  // total degree: q x q inverse of V (row-major),
+                             // V(i, k) = polynomial k at node i
+  void init(int dim, int deg, int kind = kInterpTensor);
   // 1-D Lagrange factors f[a] = l_a(x), a = 0..deg, with the reference's
   // coincident-node guard (TensorProductInterpolator.h:70-79).
   void lagrange1d(double x, double* f) const;
+  // 1-D L2-normalised Legendre polynomials on [0,1], f[a], a = 0..deg
+  // (evalPolynomials.h:19-38)
+  void legendre1d(double x, double* f) const;
+  // total degree: the q polynomial values at u (evalPolynomials.h:50-63)
+  void poly(const double* u, double* out) const;
 };
 
 // Cluster tree in level order.  Cluster c owns cluster-ordered points
@@ -117,14 +129,16 @@ struct Plan {
   double eta = 0.8;
   Pattern pat;
   std::vector<int32_t> row_leaves, col_leaves;  // cluster ids of leaves
-  // per-cluster transfer factors e[c][dd][a][b] (dim x (p+1) x (p+1)):
-  // E_c (son c -> its father) = kron over dd of e[c][dd]
+  // tensor: per-cluster transfer factors e[c][dd][a][b] (dim x (p+1) x
+  // (p+1)): E_c (son c -> its father) = kron over dd of e[c][dd];
+  // total degree: dense E_c[k][j] (q x q per cluster, polynomial basis)
   std::vector<double> row_E, col_E;
   // interpolation node coordinates per cluster: C x q x dim
   std::vector<double> row_nodes, col_nodes;
 
   void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
-             int dim, int deg, double eta, uint32_t min_leaf, bool same);
+             int dim, int deg, double eta, uint32_t min_leaf, bool same,
+             int interp_kind = kInterpTensor);
   // Block-diagonal plan of independent point clouds: trees, bases and block
   // lists of the parts concatenated (cluster ids, point indices and node
   // indices offset), so one launch per stage covers every cloud.  The parts

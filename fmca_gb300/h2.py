@@ -8,9 +8,10 @@ defaults of the reference's pybind module (py/FMCA.cpp:209-250, 448-468):
     y = H.action(x)                      # x: n x R, natural order
     H.statistics()                       # (6, 1): m, n, #LR, #dense, nz/row, GB
 
-Differences, all additive: the interpolation is the Chebyshev tensor-product
-interpolator (the reference's pybind module instantiates the total-degree
-one); ``min_leaf`` and ``precision`` keyword arguments; ``CovarianceKernel``
+Differences, all additive: the interpolation defaults to the Chebyshev
+tensor-product interpolator; ``interpolator="total_degree"`` selects the
+total-degree one that the reference's pybind module instantiates
+(py/FMCA.cpp:37-40); ``min_leaf`` and ``precision`` keyword arguments; ``CovarianceKernel``
 accepts a variance ``sigma2``; ``action`` also takes torch tensors (CPU or
 CUDA) and returns the same kind of tensor.
 """
@@ -76,11 +77,15 @@ class H2Matrix:
     """
 
     def __init__(self, cov: CovarianceKernel, Pr, Pc=None, p: int = 3,
-                 eta: float = 0.8, min_leaf: int = 0, precision: str = "mixed"):
+                 eta: float = 0.8, min_leaf: int = 0, precision: str = "mixed",
+                 interpolator: str = "tensor"):
         lib = _lib.load()
         self.cov = cov
         self.p = int(p)
         self.eta = float(eta)
+        if interpolator not in _lib.INTERPOLATORS:
+            raise ValueError("interpolator must be 'tensor' or 'total_degree'")
+        self.interpolator = interpolator
         if precision not in _PREC:
             raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
         self.precision = precision
@@ -97,8 +102,9 @@ class H2Matrix:
         handle = C.c_void_p()
         Pcp = None if same else _dptr(Pc)
         nc = Pr.shape[1] if same else Pc.shape[1]
-        check(lib.fmca_plan_create(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc, self.p,
-                                   self.eta, int(min_leaf), C.byref(handle)))
+        check(lib.fmca_plan_create_ex(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
+                                      _lib.INTERPOLATORS[interpolator], self.p, self.eta,
+                                      int(min_leaf), C.byref(handle)))
         self._h = handle
         info = (C.c_int64 * _lib.INFO_COUNT)()
         check(lib.fmca_plan_info(self._h, info))
@@ -159,6 +165,16 @@ class H2Matrix:
         return self.info["n_cols"]
 
     # -- reference methods -------------------------------------------------
+    def interpolation_nodes(self):
+        """(nodes dim x q on [0, 1]^dim, invV q x q or None): the plan's
+        interpolation nodes and, for total degree, the inverse Vandermonde
+        matrix of its Legendre basis at those nodes."""
+        q = self.info["q"]
+        nodes = np.zeros((self.dim, q), order="F")
+        invV = np.zeros((q, q), order="F")
+        check(_lib.load().fmca_plan_interpolator(self._h, _dptr(nodes), _dptr(invV)))
+        return nodes, (invV if self.interpolator == "total_degree" else None)
+
     def statistics(self, verbose: bool = True) -> np.ndarray:
         out = np.zeros(6, dtype=np.float64)
         check(_lib.load().fmca_plan_statistics(self._h, _dptr(out)))

@@ -125,6 +125,7 @@ enum {
   FMCA_INFO_ROW_LEAVES = 12,
   FMCA_INFO_COL_LEAVES = 13,
   FMCA_INFO_MIN_LEAF = 14,
+  FMCA_INFO_INTERPOLATOR = 15, /* FMCA_INTERP_* */
   FMCA_INFO_COUNT = 16
 };
 
@@ -146,6 +147,23 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
                              const double* P_cols, int64_t n_cols, int degree,
                              double eta, int64_t min_leaf, fmca_plan** out);
 fmca_status fmca_plan_destroy(fmca_plan* plan);
+
+/* Interpolators of fmca_plan_create_ex. */
+enum { FMCA_INTERP_TENSOR_PRODUCT = 0, FMCA_INTERP_TOTAL_DEGREE = 1 };
+
+/* fmca_plan_create with a choice of interpolator.  Replaces the Interpolator
+   parameter of NystromMoments<Interpolator> (FMCA/src/Moments/
+   NystromMoments.h:15-31): FMCA_INTERP_TENSOR_PRODUCT is
+   TensorProductInterpolator (q = (p+1)^dim, what fmca_plan_create builds);
+   FMCA_INTERP_TOTAL_DEGREE is TotalDegreeInterpolator
+   (FMCA/src/Interpolator/TotalDegreeInterpolator.h:26-47: q = binom(p+dim,
+   dim) DeMarchi nodes, Legendre polynomials, coupling invV K invV^T), the
+   interpolator the reference's Python module instantiates
+   (py/FMCA.cpp:37-40).  Total degree: dim <= 3, degree <= 7; the adjoint
+   and batched plans are tensor-product only (FMCA_ERR_UNSUPPORTED). */
+fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
+                                const double* P_cols, int64_t n_cols, int interpolator,
+                                int degree, double eta, int64_t min_leaf, fmca_plan** out);
 
 /* One plan for many independent point clouds (batching): cloud i has
    n_points[i] points P[i] (dim x n_i, column-major FP64); every cloud gets
@@ -181,6 +199,12 @@ fmca_status fmca_plan_permutation(const fmca_plan* plan, int side,
    be NULL. */
 fmca_status fmca_plan_clusters(const fmca_plan* plan, int side, int32_t* meta,
                                double* bb);
+/* The interpolator of the plan: nodes (dim x q, column-major, on [0,1]^dim
+   in the plan's node order: TensorProductInterpolator::Xi or the DeMarchi
+   points of TotalDegreeInterpolator::Xi) and, for total degree, invV (q x q,
+   column-major; TotalDegreeInterpolator::invV).  Either pointer may be NULL;
+   invV is left untouched for a tensor-product plan. */
+fmca_status fmca_plan_interpolator(const fmca_plan* plan, double* nodes, double* invV);
 /* kind 0: low-rank (far) blocks, 1: dense (near) blocks; row/col cluster ids
    in the order the pattern recursion produced them. */
 fmca_status fmca_plan_blocks(const fmca_plan* plan, int kind, int32_t* rows,

@@ -23,6 +23,10 @@ def load() -> C.CDLL:
     dp, vp, i64, i32 = C.POINTER(C.c_double), C.c_void_p, C.c_int64, C.c_int
     lib.oracle_plan_create.restype = vp
     lib.oracle_plan_create.argtypes = [dp, i32, i64, dp, i64, i32, C.c_double, i64]
+    lib.oracle_plan_create_ex.restype = vp
+    lib.oracle_plan_create_ex.argtypes = [dp, i32, i64, dp, i64, i32, C.c_double, i64, i32]
+    lib.oracle_interp.restype = i32
+    lib.oracle_interp.argtypes = [vp, dp, dp]
     lib.oracle_plan_destroy.argtypes = [vp]
     lib.oracle_counts.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.oracle_perm.argtypes = [vp, i32, C.POINTER(C.c_uint32)]
@@ -50,19 +54,31 @@ def _d(a):
 class OraclePlan:
     """FP64 CPU H2 restatement over the same inputs as fmca_gb300.H2Matrix."""
 
-    def __init__(self, Pr, Pc=None, p=3, eta=0.8, min_leaf=0):
+    def __init__(self, Pr, Pc=None, p=3, eta=0.8, min_leaf=0, interpolator="tensor"):
         lib = load()
+        if interpolator not in ("tensor", "total_degree"):
+            raise ValueError("interpolator must be 'tensor' or 'total_degree'")
+        self.interpolator = interpolator
         self.Pr = np.asfortranarray(Pr, dtype=np.float64)
         self.same = Pc is None
         self.Pc = self.Pr if self.same else np.asfortranarray(Pc, dtype=np.float64)
         self.dim = self.Pr.shape[0]
-        self._h = lib.oracle_plan_create(_d(self.Pr), self.dim, self.Pr.shape[1],
-                                         None if self.same else _d(self.Pc), self.Pc.shape[1],
-                                         int(p), float(eta), int(min_leaf))
+        self._h = lib.oracle_plan_create_ex(_d(self.Pr), self.dim, self.Pr.shape[1],
+                                            None if self.same else _d(self.Pc),
+                                            self.Pc.shape[1], int(p), float(eta),
+                                            int(min_leaf), int(interpolator == "total_degree"))
         cnt = (C.c_int64 * 6)()
         lib.oracle_counts(self._h, cnt)
         (self.row_clusters, self.col_clusters, self.n_far, self.n_near, self.q,
          self.near_pairs) = list(cnt)
+
+    def interp(self):
+        """(nodes dim x q, invV q x q or None for the tensor product)"""
+        lib = load()
+        nodes = np.zeros((self.dim, self.q), order="F")
+        invV = np.zeros((self.q, self.q), order="F")
+        lib.oracle_interp(self._h, _d(nodes), _d(invV))
+        return nodes, (invV if self.interpolator == "total_degree" else None)
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -21,11 +21,14 @@
 //   tree       ClusterTreeInitializer_ClusterTree.h:24-132 (init, bounding
 //              box, refinement, shrinkToFit), ClusterTreeSplitter.h:198-219
 //              (CardinalityBisection), IDDFSForwardIterator.h:37-63 (ids)
-//   interp     TensorProductInterpolator.h:39-81, MultiIndexSet.h:87-187
+//   interp     TensorProductInterpolator.h:39-81, MultiIndexSet.h:87-187;
+//              TotalDegreeInterpolator.h:26-47, DeMarchiPoints.h:20-43,
+//              evalPolynomials.h:19-63, HaltonSet.h:30-55 (total degree)
 //   bases      NystromMoments.h:24-34, compute_cluster_bases_impl.h:28-57
 //   pattern    H2MatrixBase.h:160-191, Admissibility.h:19-29,95-115
 //   statistics H2MatrixBase.h:70-105
 //   action     H2MatrixBase.h:113-152, forward_transform_impl.h:21-43,
+//              NystromEvaluator.h:40-56 (S = invV K invV^T, total degree),
 //              backward_transform_impl.h:21-33, unsymmetricNystromEvaluator.h:
 //              42-73, pyH2Matrix::action py/FMCA.cpp:230-240
 //   kernel     CovarianceKernel.h:56-143
@@ -88,12 +91,15 @@ void gemmT_acc(const Mat& A, const Scalar* B, int ldb, int n, Scalar* C, int ldc
 // ---------------------------------------------------------------------------
 struct Interpolator {
   Index dim = 0, deg = 0;
+  bool td = false;  // TotalDegreeInterpolator instead of TensorProductInterpolator
   std::vector<Scalar> xi, w;
   std::vector<std::vector<Index>> idcs;  // multi-index set in set order
-  Mat TP_xi;                             // dim x q
-  void init(Index d, Index p) {
+  Mat TP_xi;                             // dim x q nodes
+  Mat invV;                              // total degree: inverse Vandermonde
+  void init(Index d, Index p, bool total_degree = false) {
     dim = d;
     deg = p;
+    td = total_degree;
     const Scalar weight = 2. * M_PI / (2. * Scalar(deg) + 2.);
     xi.resize(deg + 1);
     w.resize(deg + 1);
@@ -104,6 +110,8 @@ struct Interpolator {
     for (auto& v : xi) v = 0.5 * (v + 1);
     for (Index i = 1; i < w.size(); i += 2) w[i] *= -1.;
     // std::set with the graded lexicographic order; generated recursively
+    // (MultiIndexSet.h:147-187) under the set's criterion: max entry <= deg
+    // (tensor product) or entry sum <= deg (total degree)
     struct Cmp {
       bool operator()(const std::vector<Index>& a, const std::vector<Index>& b) const {
         Index na = 0, nb = 0;
@@ -118,9 +126,12 @@ struct Interpolator {
     std::function<void(Index)> add = [&](Index max_bit) {
       for (Index i = max_bit; i < dim; ++i) {
         index[i] += 1;
-        Index mx = 0;
-        for (auto v : index) mx = std::max(mx, v);
-        if (mx <= deg) {
+        Index mx = 0, sum = 0;
+        for (auto v : index) {
+          mx = std::max(mx, v);
+          sum += v;
+        }
+        if ((td ? sum : mx) <= deg) {
           s.insert(index);
           add(i);
         }
@@ -131,12 +142,138 @@ struct Interpolator {
     add(0);
     idcs.assign(s.begin(), s.end());
     TP_xi = Mat(dim, (int)idcs.size());
-    for (size_t k = 0; k < idcs.size(); ++k)
-      for (Index i = 0; i < dim; ++i) TP_xi(i, (int)k) = xi[idcs[k][i]];
+    if (td) {
+      demarchi();
+    } else {
+      for (size_t k = 0; k < idcs.size(); ++k)
+        for (Index i = 0; i < dim; ++i) TP_xi(i, (int)k) = xi[idcs[k][i]];
+    }
   }
   int q() const { return (int)idcs.size(); }
-  // full multivariate evaluation, like evalPolynomials
+
+  // L2-normalised Legendre polynomials on [0, 1] (evalPolynomials.h:19-38)
+  void legendre(Scalar x, Scalar* f) const {
+    Scalar p0 = 0, p1 = 1;
+    f[0] = 1;
+    for (Index i = 1; i <= deg; ++i) {
+      const Scalar v = Scalar(2 * i - 1) / Scalar(i) * (2 * x - 1) * p1 -
+                       Scalar(i - 1) / Scalar(i) * p0;
+      p0 = p1;
+      p1 = v;
+      f[i] = v * std::sqrt(Scalar(2 * i + 1));
+    }
+  }
+
+  // i-th point of the Halton sequence in base b, by Horner's scheme in long
+  // double on the b-adic digits (HaltonSet.h:30-55)
+  static Scalar halton(unsigned long i, unsigned long b) {
+    std::vector<unsigned long> dig;
+    while (i) {
+      dig.push_back(i % b);
+      i /= b;
+    }
+    if (dig.empty()) return 0;
+    const long double binv = (long double)1 / (long double)b;
+    long double r = dig.back();
+    for (int j = (int)dig.size() - 2; j >= 0; --j) r = binv * r + dig[j];
+    r *= binv;
+    return (Scalar)r;
+  }
+
+  // DeMarchi points (DeMarchiPoints.h:20-43): greedy selection among the
+  // Halton points 100 .. 100 + 10 q - 1 of the candidate whose polynomial
+  // vector has the largest component orthogonal to the ones chosen (the
+  // pivot order of a column-pivoted QR), here by modified Gram-Schmidt
+  // with a second orthogonalisation pass; then invV = V^{-1}, V(i, k) =
+  // polynomial k at node i, by LU with partial pivoting
+  // (TotalDegreeInterpolator.h:40-45)
+  void demarchi() {
+    const int n = q(), M = 10 * n;
+    static const unsigned long primes[3] = {2, 3, 5};
+    std::vector<std::vector<Scalar>> cand(M, std::vector<Scalar>(dim));
+    std::vector<std::vector<Scalar>> R(M, std::vector<Scalar>(n));
+    for (int m = 0; m < M; ++m) {
+      for (Index d = 0; d < dim; ++d) cand[m][d] = halton(100 + m, primes[d]);
+      eval(cand[m].data(), R[m].data());
+    }
+    std::vector<char> used(M, 0);
+    for (int s = 0; s < n; ++s) {
+      int best = -1;
+      Scalar bn = -1;
+      for (int m = 0; m < M; ++m) {
+        if (used[m]) continue;
+        Scalar n2 = 0;
+        for (int k = 0; k < n; ++k) n2 += R[m][k] * R[m][k];
+        if (n2 > bn) {
+          bn = n2;
+          best = m;
+        }
+      }
+      used[best] = 1;
+      for (Index d = 0; d < dim; ++d) TP_xi(d, s) = cand[best][d];
+      std::vector<Scalar> u = R[best];
+      const Scalar nu = std::sqrt(bn);
+      for (auto& v : u) v /= nu;
+      for (int m = 0; m < M; ++m) {
+        if (used[m]) continue;
+        for (int pass = 0; pass < 2; ++pass) {
+          Scalar dot = 0;
+          for (int k = 0; k < n; ++k) dot += u[k] * R[m][k];
+          for (int k = 0; k < n; ++k) R[m][k] -= dot * u[k];
+        }
+      }
+    }
+    Mat V(n, n);
+    std::vector<Scalar> row(n);
+    for (int i = 0; i < n; ++i) {
+      std::vector<Scalar> pt(dim);
+      for (Index d = 0; d < dim; ++d) pt[d] = TP_xi(d, i);
+      eval(pt.data(), row.data());
+      for (int k = 0; k < n; ++k) V(i, k) = row[k];
+    }
+    // LU with partial pivoting, then one solve per unit vector
+    std::vector<int> piv(n);
+    Mat LU = V;
+    for (int k = 0; k < n; ++k) piv[k] = k;
+    for (int k = 0; k < n; ++k) {
+      int pr = k;
+      for (int i = k + 1; i < n; ++i)
+        if (std::abs(LU(i, k)) > std::abs(LU(pr, k))) pr = i;
+      if (pr != k) {
+        for (int j = 0; j < n; ++j) std::swap(LU(k, j), LU(pr, j));
+        std::swap(piv[k], piv[pr]);
+      }
+      for (int i = k + 1; i < n; ++i) {
+        LU(i, k) /= LU(k, k);
+        for (int j = k + 1; j < n; ++j) LU(i, j) -= LU(i, k) * LU(k, j);
+      }
+    }
+    invV = Mat(n, n);
+    std::vector<Scalar> b(n);
+    for (int c = 0; c < n; ++c) {
+      for (int i = 0; i < n; ++i) b[i] = piv[i] == c ? 1. : 0.;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j) b[i] -= LU(i, j) * b[j];
+      for (int i = n - 1; i >= 0; --i) {
+        for (int j = i + 1; j < n; ++j) b[i] -= LU(i, j) * b[j];
+        b[i] /= LU(i, i);
+      }
+      for (int i = 0; i < n; ++i) invV(i, c) = b[i];
+    }
+  }
+
+  // full multivariate evaluation, like evalPolynomials / the Lagrange basis
   void eval(const Scalar* pt, Scalar* out) const {
+    if (td) {
+      std::vector<std::vector<Scalar>> f(dim, std::vector<Scalar>(deg + 1));
+      for (Index i = 0; i < dim; ++i) legendre(pt[i], f[i].data());
+      for (size_t k = 0; k < idcs.size(); ++k) {
+        Scalar v = 1;
+        for (Index i = 0; i < dim; ++i) v *= f[i][idcs[k][i]];
+        out[k] = v;
+      }
+      return;
+    }
     std::vector<Scalar> weight(dim);
     for (Index i = 0; i < dim; ++i) {
       Scalar s = 0;
@@ -317,6 +454,15 @@ struct Tree {
                       (s.bmin[d] - nd.bmin[d]) / nd.bext[d];
             ip.eval(pt.data(), &E.a[(size_t)j * q]);
           }
+        if (ip.td) {  // E = E invV^T (compute_cluster_bases_impl.h:50)
+          Mat F(q, q);
+          for (int jj = 0; jj < q; ++jj)
+            for (int j = 0; j < q; ++j) {
+              const Scalar v = ip.invV(jj, j);
+              for (int k = 0; k < q; ++k) F(k, jj) += E(k, j) * v;
+            }
+          E = std::move(F);
+        }
         nd.E.push_back(std::move(E));
       }
     } else {
@@ -493,12 +639,13 @@ Scalar check_transfer(Node& nd, const Tree& t, const Interpolator& ip, Mat* Vout
 
 extern "C" {
 
-void* oracle_plan_create(const double* Pr, int dim, int64_t nr, const double* Pc,
-                         int64_t nc, int deg, double eta, int64_t min_leaf) {
+void* oracle_plan_create_ex(const double* Pr, int dim, int64_t nr, const double* Pc,
+                            int64_t nc, int deg, double eta, int64_t min_leaf,
+                            int total_degree) {
   OPlan* P = new OPlan();
   P->dim = (Index)dim;
   P->eta = eta;
-  P->ip.init((Index)dim, (Index)deg);
+  P->ip.init((Index)dim, (Index)deg, total_degree != 0);
   const bool same = (Pc == nullptr || Pc == Pr);
   P->Pr.assign(Pr, Pr + (size_t)dim * nr);
   if (same) {
@@ -515,6 +662,21 @@ void* oracle_plan_create(const double* Pr, int dim, int64_t nr, const double* Pc
   P->ct.bases(P->ct.root, P->ip);
   pattern(P);
   return P;
+}
+
+void* oracle_plan_create(const double* Pr, int dim, int64_t nr, const double* Pc,
+                         int64_t nc, int deg, double eta, int64_t min_leaf) {
+  return oracle_plan_create_ex(Pr, dim, nr, Pc, nc, deg, eta, min_leaf, 0);
+}
+
+// total degree: the q nodes (dim x q, column-major) and invV (q x q,
+// column-major); returns q
+int oracle_interp(void* h, double* nodes, double* invV) {
+  const Interpolator& ip = static_cast<OPlan*>(h)->ip;
+  const int q = ip.q();
+  if (nodes) std::copy(ip.TP_xi.a.begin(), ip.TP_xi.a.end(), nodes);
+  if (invV && ip.td) std::copy(ip.invV.a.begin(), ip.invV.a.end(), invV);
+  return q;
 }
 
 void oracle_plan_destroy(void* h) { delete static_cast<OPlan*>(h); }
@@ -670,6 +832,20 @@ static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
         for (int j = 0; j < q; ++j)
           for (int i = 0; i < q; ++i)
             S(i, j) = kern(dist(&XiX.a[(size_t)i * dim], &XiY.a[(size_t)j * dim], dim));
+        if (P->ip.td) {  // S = invV S invV^T (NystromEvaluator.h:50-54)
+          Mat A(q, q), B(q, q);
+          for (int j = 0; j < q; ++j)
+            for (int m = 0; m < q; ++m) {
+              const Scalar v = S(m, j);
+              for (int i = 0; i < q; ++i) A(i, j) += P->ip.invV(i, m) * v;
+            }
+          for (int j = 0; j < q; ++j)
+            for (int m = 0; m < q; ++m) {
+              const Scalar v = P->ip.invV(j, m);
+              for (int i = 0; i < q; ++i) B(i, j) += A(i, m) * v;
+            }
+          S = std::move(B);
+        }
         const Mat& t = trhs[col.block_id];
         gemm_acc(S, t.a.data(), q, R, tlhs[row.block_id].a.data(), q);
         lr_pairs += (double)q * q;
