@@ -137,3 +137,24 @@ def test_gpu_adjoint_refuses_total_degree(cuda_device):
     with pytest.raises(_lib.FmcaError) as e:
         H.adjoint(x, x)
     assert e.value.status == ERR["FMCA_ERR_UNSUPPORTED"]
+
+
+def test_nodes_match_the_lapack_golden_fixture():
+    """DeMarchi nodes and invV against tests/golden/total_degree.json (scipy's
+    Halton points, LAPACK's column-pivoted QR; gen_total_degree.py): the same
+    pivots, coordinates within an ulp."""
+    import json
+    import os
+    G = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                    "total_degree.json")))
+    assert len(G) == 6
+    for g in G.values():
+        P = uniform_cloud(300, g["dim"], seed=1)
+        H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, g["degree"], 0.8,
+                     interpolator="total_degree")
+        assert H.info["q"] == g["q"]
+        nodes, invV = H.interpolation_nodes()
+        assert np.abs(nodes - np.array(g["nodes"]).T).max() <= 4.5e-16
+        if "invV" in g:
+            ref = np.array(g["invV"])
+            assert np.abs(invV - ref).max() <= 1e-13 * np.abs(ref).max()
