@@ -188,11 +188,15 @@ fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_po
     std::atomic<int> next(0);
     const int nth = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
     std::vector<std::thread> pool;
+    // the cores not taken by whole clouds go to each cloud's tree build
+    const int per = std::max(1, (int)std::thread::hardware_concurrency() / nth);
     for (int t = 0; t < nth; ++t)
       pool.emplace_back([&]() {
-        for (int i = next++; i < count; i = next++)
+        for (int i = next++; i < count; i = next++) {
+          parts[i].build_threads = per;
           parts[i].build(P[i], (uint32_t)n_points[i], P[i], (uint32_t)n_points[i], dim,
                          degree, eta, (uint32_t)min_leaf, true);
+        }
       });
     for (auto& th : pool) th.join();
     std::vector<const fmca::Plan*> ptrs;

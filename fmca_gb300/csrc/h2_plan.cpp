@@ -2,6 +2,8 @@
 #include "h2_plan.h"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cctype>
 #include <cmath>
 #include <cstring>
@@ -296,24 +298,35 @@ struct TreeBuilder {
   double coord(uint32_t i, int d) const { return P[(size_t)i * dim + d]; }
 
   // ClusterTreeInitializer<ClusterTree>::init_ClusterTree_impl + the
-  // CardinalityBisection splitter
-  void refine(int me) {
-    if (nodes[me].size <= split_threshold) return;
-    TmpNode s0 = nodes[me], s1 = nodes[me];
-    s0.level = s1.level = nodes[me].level + 1;
+  // CardinalityBisection splitter, for one node: sorts the node's index
+  // range along the longest edge of its (propagated) box and halves it.
+  // Reads nodes[me] and writes only its own index range and sons, so nodes
+  // of one level split concurrently. False: the node is a leaf.
+  bool split(int me, TmpNode* sons) const {
+    const TmpNode& f = nodes[me];
+    if (f.size <= split_threshold) return false;
+    TmpNode s0 = f, s1 = f;
+    s0.level = s1.level = f.level + 1;
     s0.nsons = s1.nsons = 0;
     // longest edge of the (propagated) father box, first maximum
     int longest = 0;
     for (int d = 1; d < dim; ++d)
       if (s0.bb[2 * dim + d] > s0.bb[2 * dim + longest]) longest = d;
+    // std::sort of the index range by the coordinate, done on (coordinate,
+    // index) records: the algorithm makes the same comparisons and moves
+    // whatever the element type, so the index order is that of sorting the
+    // indices with an indirect comparator, without a cache miss per
+    // comparison
     uint32_t* ids = idx->data();
-    const double* Pl = P;
-    const int D = dim;
-    const int L = longest;
-    std::sort(ids + s0.begin, ids + s0.begin + s0.size,
-              [Pl, D, L](uint32_t i, uint32_t j) {
-                return Pl[(size_t)i * D + L] < Pl[(size_t)j * D + L];
-              });
+    struct Rec {
+      double key;
+      uint32_t id;
+    };
+    std::vector<Rec> rec(s0.size);
+    for (uint32_t i = 0; i < s0.size; ++i)
+      rec[i] = Rec{coord(ids[s0.begin + i], longest), ids[s0.begin + i]};
+    std::sort(rec.begin(), rec.end(), [](const Rec& a, const Rec& b) { return a.key < b.key; });
+    for (uint32_t i = 0; i < s0.size; ++i) ids[s0.begin + i] = rec[i].id;
     s0.size /= 2;
     s1.size -= s0.size;
     s1.begin += s0.size;
@@ -321,14 +334,52 @@ struct TreeBuilder {
     s0.bb[2 * dim + longest] = s0.bb[dim + longest] - s0.bb[longest];
     s1.bb[longest] = coord(ids[s1.begin], longest);
     s1.bb[2 * dim + longest] = s1.bb[dim + longest] - s1.bb[longest];
-    const int i0 = (int)nodes.size();
-    nodes.push_back(std::move(s0));
-    nodes.push_back(std::move(s1));
-    nodes[me].sons[0] = i0;
-    nodes[me].sons[1] = i0 + 1;
-    nodes[me].nsons = 2;
-    refine(i0);
-    refine(i0 + 1);
+    sons[0] = std::move(s0);
+    sons[1] = std::move(s1);
+    return true;
+  }
+
+  // the whole refinement, level by level: the nodes of a level split in
+  // parallel (each std::sort on its own index range, the same calls on the
+  // same data as the reference's depth-first recursion, so the permutation
+  // is identical), then their sons are appended in order. Node storage order
+  // differs from the recursion's; the ids are assigned afterwards in level
+  // order, so they do not depend on it.
+  void refine_all(int nthreads) {
+    std::vector<int> cur{0};
+    while (!cur.empty()) {
+      const size_t m = cur.size();
+      std::vector<TmpNode> out(2 * m);
+      std::vector<char> did(m, 0);
+      uint64_t work = 0;
+      for (int c : cur) work += nodes[c].size;
+      const int nt = (work < (1u << 16)) ? 1 : (int)std::min<size_t>((size_t)nthreads, m);
+      if (nt <= 1) {
+        for (size_t i = 0; i < m; ++i) did[i] = split(cur[i], &out[2 * i]);
+      } else {
+        std::atomic<size_t> next(0);
+        auto body = [&]() {
+          for (size_t i; (i = next.fetch_add(1)) < m;) did[i] = split(cur[i], &out[2 * i]);
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(body);
+        body();
+        for (auto& th : pool) th.join();
+      }
+      std::vector<int> nxt;
+      for (size_t i = 0; i < m; ++i) {
+        if (!did[i]) continue;
+        const int i0 = (int)nodes.size();
+        nodes.push_back(std::move(out[2 * i]));
+        nodes.push_back(std::move(out[2 * i + 1]));
+        nodes[cur[i]].sons[0] = i0;
+        nodes[cur[i]].sons[1] = i0 + 1;
+        nodes[cur[i]].nsons = 2;
+        nxt.push_back(i0);
+        nxt.push_back(i0 + 1);
+      }
+      cur.swap(nxt);
+    }
   }
 
   // shrinkToFit_impl (ClusterTreeInitializer_ClusterTree.h:88-132)
@@ -374,7 +425,7 @@ struct TreeBuilder {
 };
 }  // namespace
 
-void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize) {
+void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize, int threads) {
   dim = dim_;
   n = n_;
   perm.resize(n);
@@ -405,7 +456,8 @@ void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize) {
   }
   tb.nodes.reserve(2 * (n / std::max<uint32_t>(1, min_csize)) + 8);
   tb.nodes.push_back(std::move(root));
-  tb.refine(0);
+  if (threads <= 0) threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  tb.refine_all(threads);
   tb.shrink(0);
   // level-order numbering (IDDFSForwardIterator): breadth first, sons in order
   const int C = (int)tb.nodes.size();
@@ -566,11 +618,11 @@ void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
   same_tree = same;
   const uint32_t mincsize =
       min_leaf > (uint32_t)interp.q ? min_leaf : (uint32_t)interp.q;
-  rows.build(Pr, dim, nr, mincsize);
+  rows.build(Pr, dim, nr, mincsize, build_threads);
   if (same)
     cols = rows;
   else
-    cols.build(Pc, dim, nc, mincsize);
+    cols.build(Pc, dim, nc, mincsize, build_threads);
   compute_transfer_factors(rows, interp, &row_E);
   compute_node_coords(rows, interp, &row_nodes);
   if (same) {

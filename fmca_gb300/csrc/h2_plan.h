@@ -103,8 +103,10 @@ struct Tree {
   int nclusters() const { return (int)begin.size(); }
   int nlevels() const { return (int)level_ptr.size() - 1; }
   // Builds the tree: min_csize is the effective minimum leaf size
-  // (H2ClusterTree.h:68-70 passes max(min_cluster_size, q)).
-  void build(const double* P, int dim, uint32_t n, uint32_t min_csize);
+  // (H2ClusterTree.h:68-70 passes max(min_cluster_size, q)). The clusters of
+  // one level split on up to `threads` host threads (0: one per core, at
+  // most 16); the result does not depend on the thread count.
+  void build(const double* P, int dim, uint32_t n, uint32_t min_csize, int threads = 0);
 };
 
 // Row-owned block lists.
@@ -139,6 +141,7 @@ struct Plan {
   void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
              int dim, int deg, double eta, uint32_t min_leaf, bool same,
              int interp_kind = kInterpTensor);
+  int build_threads = 0;  // host threads of the tree builds (0: one per core)
   // Block-diagonal plan of independent point clouds: trees, bases and block
   // lists of the parts concatenated (cluster ids, point indices and node
   // indices offset), so one launch per stage covers every cloud.  The parts

@@ -119,3 +119,22 @@ def test_single_point_and_tiny():
         H = H2Matrix(CovarianceKernel("EXPONENTIAL"), P, P, 2, 0.8)
         assert H.info["row_clusters"] == 1
         assert H.info["far_blocks"] == 0 and H.info["near_blocks"] == 1
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_parallel_tree_build_equals_oracle(dim):
+    # clouds large enough that the plan splits the clusters of a level on
+    # several host threads (from 65,536 points per level), with a third of
+    # the coordinates quantised so that the sorts meet ties; the oracle
+    # builds the same tree by the reference's serial depth-first recursion
+    rng = np.random.default_rng(40 + dim)
+    P = rng.random((dim, 150000))
+    P[:, ::3] = np.floor(P[:, ::3] * 32) / 32
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, 2, 0.8, min_leaf=32)
+    O = oracle.OraclePlan(P, None, 2, 0.8, 32)
+    assert np.array_equal(H.rindices(), O.perm(0))
+    mh, bh = H.clusters(0)
+    mo, bo = O.clusters(0)
+    assert np.array_equal(mh, mo) and np.array_equal(bh, bo)
+    for kind in (0, 1):
+        assert sorted(zip(*H.blocks(kind))) == sorted(zip(*O.blocks(kind)))
