@@ -190,15 +190,23 @@ fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_po
     std::vector<std::thread> pool;
     // the cores not taken by whole clouds go to each cloud's tree build
     const int per = std::max(1, (int)std::thread::hardware_concurrency() / nth);
+    std::vector<std::exception_ptr> errs(nth);
     for (int t = 0; t < nth; ++t)
-      pool.emplace_back([&]() {
-        for (int i = next++; i < count; i = next++) {
-          parts[i].build_threads = per;
-          parts[i].build(P[i], (uint32_t)n_points[i], P[i], (uint32_t)n_points[i], dim,
-                         degree, eta, (uint32_t)min_leaf, true);
+      pool.emplace_back([&, t]() {
+        try {
+          for (int i = next++; i < count; i = next++) {
+            parts[i].build_threads = per;
+            parts[i].build(P[i], (uint32_t)n_points[i], P[i], (uint32_t)n_points[i], dim,
+                           degree, eta, (uint32_t)min_leaf, true);
+          }
+        } catch (...) {
+          errs[t] = std::current_exception();
+          next = count;
         }
       });
     for (auto& th : pool) th.join();
+    for (auto& e : errs)
+      if (e) std::rethrow_exception(e);
     std::vector<const fmca::Plan*> ptrs;
     for (auto& p : parts) ptrs.push_back(&p);
     fmca_plan* p = new fmca_plan();

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <exception>
 #include <thread>
 #include <cctype>
 #include <cmath>
@@ -357,14 +358,23 @@ struct TreeBuilder {
       if (nt <= 1) {
         for (size_t i = 0; i < m; ++i) did[i] = split(cur[i], &out[2 * i]);
       } else {
+        // a failure (bad_alloc) in a worker is rethrown here, after the join
         std::atomic<size_t> next(0);
-        auto body = [&]() {
-          for (size_t i; (i = next.fetch_add(1)) < m;) did[i] = split(cur[i], &out[2 * i]);
+        std::vector<std::exception_ptr> errs(nt);
+        auto body = [&](int t) {
+          try {
+            for (size_t i; (i = next.fetch_add(1)) < m;) did[i] = split(cur[i], &out[2 * i]);
+          } catch (...) {
+            errs[t] = std::current_exception();
+            next.store(m);
+          }
         };
         std::vector<std::thread> pool;
-        for (int t = 1; t < nt; ++t) pool.emplace_back(body);
-        body();
+        for (int t = 1; t < nt; ++t) pool.emplace_back(body, t);
+        body(0);
         for (auto& th : pool) th.join();
+        for (auto& e : errs)
+          if (e) std::rethrow_exception(e);
       }
       std::vector<int> nxt;
       for (size_t i = 0; i < m; ++i) {
