@@ -30,6 +30,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "compensated_sum.h"
+
 namespace fmca {
 namespace gpu {
 
@@ -936,7 +938,8 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves
+// leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves; in
+// FP32 the sum over k is compensated (compensated_sum.h)
 // shared: F[24][blockDim] (one column per thread), S[q][RB], packed digits q ints
 template <typename T, int RB>
 __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
@@ -977,12 +980,35 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
     T acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = T(0);
-    for (int k = 0; k < q; ++k) {
-      const int kd = pk[k];
-      const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
-                  f[(16 + (kd >> 16)) * nthr];
+    if constexpr (sizeof(T) == 4) {
+      // compensated: plain partial sums of kGatherBlock terms, each added
+      // into the total with Kahan's compensation (compensated_sum.h)
+      T cmp[RB];
 #pragma unroll
-      for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
+      for (int r = 0; r < RB; ++r) cmp[r] = T(0);
+      for (int k0 = 0; k0 < q; k0 += kGatherBlock) {
+        const int k1 = min(q, k0 + kGatherBlock);
+        T part[RB];
+#pragma unroll
+        for (int r = 0; r < RB; ++r) part[r] = T(0);
+        for (int k = k0; k < k1; ++k) {
+          const int kd = pk[k];
+          const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
+                      f[(16 + (kd >> 16)) * nthr];
+#pragma unroll
+          for (int r = 0; r < RB; ++r) part[r] += v * S[k * RB + r];
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r) kahan_add(acc[r], cmp[r], part[r]);
+      }
+    } else {
+      for (int k = 0; k < q; ++k) {
+        const int kd = pk[k];
+        const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
+                    f[(16 + (kd >> 16)) * nthr];
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
+      }
     }
     store_row<T, RB, false>(yout + (size_t)(b + i0 + tid) * ldv + rofs, acc, rcount);
   }
