@@ -89,3 +89,61 @@ def test_workspace_size_grows_with_rhs():
     assert H.workspace_bytes(1, "fp32") < H.workspace_bytes(32, "fp32")
     assert H.workspace_bytes(32, "fp64") > H.workspace_bytes(32, "fp32")
     assert b >= H.workspace_bytes(32, "fp32")
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "fmca_gb300.h"
+
+int main(void) {
+  enum { N = 3000 };
+  double* P = (double*)malloc(sizeof(double) * 3 * N);
+  unsigned s = 1u;
+  for (int i = 0; i < 3 * N; ++i) {
+    s = s * 1664525u + 1013904223u;
+    P[i] = (s >> 8) / 16777216.0;
+  }
+  fmca_plan* tp = NULL;
+  fmca_plan* td = NULL;
+  if (fmca_plan_create(P, 3, N, NULL, N, 3, 0.8, 64, &tp) != FMCA_OK) return 1;
+  if (fmca_plan_create_ex(P, 3, N, NULL, N, FMCA_INTERP_TOTAL_DEGREE, 4, 0.8, 0, &td) != FMCA_OK)
+    return 2;
+  int64_t a[FMCA_INFO_COUNT], b[FMCA_INFO_COUNT];
+  double st[6], nodes[3 * 35];
+  if (fmca_plan_info(tp, a) != FMCA_OK || fmca_plan_info(td, b) != FMCA_OK) return 3;
+  if (fmca_plan_statistics(td, st) != FMCA_OK) return 4;
+  if (fmca_plan_interpolator(td, nodes, NULL) != FMCA_OK) return 5;
+  printf("%lld %lld %lld %lld %.17g %.17g\n", (long long)a[FMCA_INFO_Q],
+         (long long)b[FMCA_INFO_Q], (long long)a[FMCA_INFO_INTERPOLATOR],
+         (long long)b[FMCA_INFO_INTERPOLATOR], st[0], nodes[0]);
+  fmca_plan_destroy(tp);
+  fmca_plan_destroy(td);
+  free(P);
+  return 0;
+}
+"""
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """A plain C99 program against include/fmca_gb300.h and the library, as a
+    non-Python binding would use them (plan calls only, no GPU)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    _lib.load()
+    src = tmp_path / "prog.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "prog"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I",
+                    os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", libdir,
+                    "-lfmca_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out[:4] == ["64", "35", "0", "1"]
+    assert float(out[4]) == 3000.0
+    P = np.random.default_rng(0).random((3, 10))  # any plan: the nodes do not depend on points
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 4, 0.8, interpolator="total_degree")
+    assert float(out[5]) == H.interpolation_nodes()[0][0, 0]
