@@ -398,6 +398,8 @@ fmca_status fmca_matvec_adjoint_workspace_size(const fmca_plan* p, int precision
   fmca_status s = check_gpu_plan(p, precision);
   if (s != FMCA_OK) return s;
   if (!bytes || nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "bad nrhs or NULL bytes");
+  if (p->plan.interp.kind != fmca::kInterpTensor)
+    return fail(FMCA_ERR_UNSUPPORTED, "the adjoint needs a tensor-product plan");
   *bytes = fmca::gpu::adjoint_workspace_bytes(p->plan, precision, nrhs);
   return ok();
 }
