@@ -9,10 +9,12 @@
 //               (forward_transform_impl.h:24-30)
 //   ksum far    s_tau = sum_sigma K(xi_tau, xi_sigma) t_sigma over the
 //               admissible list of every row cluster (NystromEvaluator.h:
-//               40-56 + H2MatrixBase.h:140-142)
+//               40-56 + H2MatrixBase.h:140-142); with total-degree
+//               interpolation between two changes of basis (t to the nodal
+//               basis by invV^T, s back by invV)
 //   l2l         s_son += E_son^T s_dad, one launch per level, top-down
 //               (backward_transform_impl.h:21-28)
-//   leafgather  yfar_tau = V_tau^T s_tau for row leaves
+//   leafgather  yfar_tau = V_tau^T s_tau for row leaves, compensated in FP32
 //               (backward_transform_impl.h:29-31)
 //   ksum near   ynear_tau = sum K(X_tau, X_sigma) xc_sigma over the dense
 //               list of every row leaf (NystromEvaluator.h:61-71 +
