@@ -13,6 +13,7 @@
 
 #include "../../include/fmca_gb300.h"
 #include "c_api_internal.h"
+#include "plan_io.h"
 #include "h2_gpu.h"
 #include "h2_plan.h"
 
@@ -227,6 +228,37 @@ fmca_status fmca_plan_destroy(fmca_plan* plan) {
   if (plan->hx) cudaFree(plan->hx);
   if (plan->hy) cudaFree(plan->hy);
   delete plan;
+  return ok();
+}
+
+fmca_status fmca_plan_save(const fmca_plan* p, const char* path) {
+  if (!p || !path) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  try {
+    fmca::save_plan(p->plan, p->min_leaf, path);
+  } catch (const std::bad_alloc&) {
+    return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while saving the plan");
+  } catch (const std::exception& e) {
+    return fail(FMCA_ERR_INVALID_ARGUMENT, e.what());
+  }
+  return ok();
+}
+
+fmca_status fmca_plan_load(const char* path, fmca_plan** out) {
+  if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!path) return fail(FMCA_ERR_INVALID_ARGUMENT, "path is NULL");
+  fmca_plan* p = new (std::nothrow) fmca_plan();
+  if (!p) return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed");
+  try {
+    fmca::load_plan(path, &p->plan, &p->min_leaf);
+  } catch (const std::bad_alloc&) {
+    delete p;
+    return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while loading the plan");
+  } catch (const std::exception& e) {
+    delete p;
+    return fail(FMCA_ERR_INVALID_ARGUMENT, e.what());
+  }
+  *out = p;
   return ok();
 }
 

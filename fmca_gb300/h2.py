@@ -18,6 +18,7 @@ CUDA) and returns the same kind of tensor.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional
 
 import numpy as np
@@ -127,6 +128,7 @@ class H2Matrix:
             raise ValueError("clouds must be dim x n arrays of one dim")
         self = cls.__new__(cls)
         self.cov, self.p, self.eta, self.precision = cov, int(p), float(eta), precision
+        self.interpolator = "tensor"
         self.dim = arrs[0].shape[0]
         ptrs = (C.POINTER(C.c_double) * len(arrs))(*[_dptr(a) for a in arrs])
         ns = (C.c_int64 * len(arrs))(*[a.shape[1] for a in arrs])
@@ -139,6 +141,31 @@ class H2Matrix:
         self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
         self._ws = {}
         self.offsets = np.concatenate([[0], np.cumsum([a.shape[1] for a in arrs])])
+        return self
+
+    def save(self, path) -> None:
+        """Writes the plan to a file (fmca_plan_save): points, trees, block
+        lists and interpolation data, not the kernel or the precision."""
+        check(_lib.load().fmca_plan_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path, cov: CovarianceKernel, precision: str = "mixed") -> "H2Matrix":
+        """A plan written by ``save`` (fmca_plan_load), without rebuilding the
+        trees or the block pattern; kernel and precision are chosen anew."""
+        lib = _lib.load()
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
+        self = cls.__new__(cls)
+        handle = C.c_void_p()
+        check(lib.fmca_plan_load(os.fsencode(path), C.byref(handle)))
+        self._h = handle
+        info = (C.c_int64 * _lib.INFO_COUNT)()
+        check(lib.fmca_plan_info(self._h, info))
+        self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
+        self.cov, self.precision = cov, precision
+        self.p, self.dim, self.eta = self.info["degree"], self.info["dim"], None
+        self.interpolator = "total_degree" if self.info["interpolator"] == 1 else "tensor"
+        self._ws = {}
         return self
 
     def graph(self, x, y, precision: Optional[str] = None) -> "MatvecGraph":

@@ -205,6 +205,16 @@ fmca_status fmca_plan_clusters(const fmca_plan* plan, int side, int32_t* meta,
    column-major; TotalDegreeInterpolator::invV).  Either pointer may be NULL;
    invV is left untouched for a tensor-product plan. */
 fmca_status fmca_plan_interpolator(const fmca_plan* plan, double* nodes, double* invV);
+/* Plan files.  fmca_plan_save writes the host plan (points, both cluster
+   trees, block lists, transfer and node data) as a sequence of matrices in
+   the binary layout of FMCA's print2bin / bin2Mat (FMCA/src/util/IO.h:
+   532-626: element size, row-major flag, rows and cols as size_t, then the
+   column-major data); fmca_plan_load reads it back into a new plan that
+   behaves exactly like the saved one, without rebuilding the trees or the
+   block pattern.  Device data is not stored: it is uploaded on the first
+   matvec as for a new plan.  Malformed files give FMCA_ERR_INVALID_ARGUMENT. */
+fmca_status fmca_plan_save(const fmca_plan* plan, const char* path);
+fmca_status fmca_plan_load(const char* path, fmca_plan** out);
 /* kind 0: low-rank (far) blocks, 1: dense (near) blocks; row/col cluster ids
    in the order the pattern recursion produced them. */
 fmca_status fmca_plan_blocks(const fmca_plan* plan, int kind, int32_t* rows,

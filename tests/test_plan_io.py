@@ -1,0 +1,125 @@
+"""Plan files (fmca_plan_save / fmca_plan_load): a loaded plan equals the
+saved one (trees, permutations, block lists, statistics, interpolation
+nodes), the file is a sequence of matrices in the binary layout of FMCA's
+print2bin (FMCA/src/util/IO.h:532-580), and malformed files are refused."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err, sphere_cloud, uniform_cloud
+from fmca_gb300 import CovarianceKernel, FmcaError, H2Matrix, _lib
+
+ERR = {v: k for k, v in _lib.STATUS_NAMES.items()}
+
+
+def same_plan(A, B):
+    assert A.info == B.info
+    for side in (0, 1):
+        ma, ba = A.clusters(side)
+        mb, bb = B.clusters(side)
+        assert np.array_equal(ma, mb) and np.array_equal(ba, bb)
+    assert np.array_equal(A.rindices(), B.rindices())
+    assert np.array_equal(A.cindices(), B.cindices())
+    for kind in (0, 1):
+        ra, ca = A.blocks(kind)
+        rb, cb = B.blocks(kind)
+        assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+    assert np.array_equal(A.statistics(False), B.statistics(False))
+    na, ia = A.interpolation_nodes()
+    nb, ib = B.interpolation_nodes()
+    assert np.array_equal(na, nb)
+    assert (ia is None and ib is None) or np.array_equal(ia, ib)
+
+
+def read_print2bin(path):
+    """The file as a list of (element size, rows, cols, raw bytes) records,
+    read the way bin2Mat reads one matrix (IO.h:585-626)."""
+    raw = open(path, "rb").read()
+    out, pos = [], 0
+    while pos < len(raw):
+        size, rowmajor, rows, cols = np.frombuffer(raw, dtype=np.uint64, count=4, offset=pos)
+        pos += 32
+        assert rowmajor == 0
+        nbytes = int(size * rows * cols)
+        out.append((int(size), int(rows), int(cols), raw[pos:pos + nbytes]))
+        pos += nbytes
+    assert pos == len(raw)
+    return out
+
+
+CASES = {
+    "tensor": lambda: (uniform_cloud(6000, 3, seed=1), None, 3, "tensor"),
+    "total_degree": lambda: (uniform_cloud(6000, 3, seed=2), None, 4, "total_degree"),
+    "unsymmetric": lambda: (sphere_cloud(5000, seed=3), sphere_cloud(3000, seed=4), 3, "tensor"),
+    "two_dim": lambda: (uniform_cloud(4000, 2, seed=5), None, 5, "total_degree"),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_round_trip(tmp_path, case):
+    Pr, Pc, p, interp = CASES[case]()
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), Pr, Pr if Pc is None else Pc, p, 0.8,
+                 min_leaf=32, interpolator=interp)
+    f = tmp_path / "plan.bin"
+    H.save(f)
+    G = H2Matrix.load(f, CovarianceKernel("MATERN32", 0.5))
+    same_plan(H, G)
+    assert G.interpolator == interp and G.p == p
+    recs = read_print2bin(f)
+    head = np.frombuffer(recs[0][3], dtype=np.int64)
+    assert recs[0][:3] == (8, 16, 1) and head[0] == 0x464D4341 and head[2] == Pr.shape[0]
+    assert recs[1][:3] == (8, 1, 1) and np.frombuffer(recs[1][3])[0] == 0.8
+    pts = np.frombuffer(recs[2][3]).reshape(recs[2][2], recs[2][1]).T
+    assert recs[2][1] == Pr.shape[0] and np.array_equal(pts, Pr)
+
+
+def test_batched_round_trip(tmp_path):
+    rng = np.random.default_rng(6)
+    clouds = [rng.random((3, n)) for n in (700, 2500, 1300)]
+    H = H2Matrix.batched(CovarianceKernel("GAUSSIAN", 0.2), clouds, p=3, eta=0.8)
+    f = tmp_path / "batch.bin"
+    H.save(f)
+    G = H2Matrix.load(f, CovarianceKernel("GAUSSIAN", 0.2))
+    same_plan(H, G)
+
+
+def test_malformed_files_are_refused(tmp_path):
+    P = uniform_cloud(3000, 3, seed=7)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 3, 0.8)
+    f = tmp_path / "plan.bin"
+    H.save(f)
+    raw = bytearray(open(f, "rb").read())
+
+    def refused(data):
+        g = tmp_path / "bad.bin"
+        g.write_bytes(bytes(data))
+        with pytest.raises(FmcaError) as e:
+            H2Matrix.load(g, CovarianceKernel("MATERN32", 0.5))
+        assert e.value.status == ERR["FMCA_ERR_INVALID_ARGUMENT"]
+
+    refused(raw[:len(raw) // 2])                # truncated
+    bad = bytearray(raw)
+    bad[32] ^= 0xFF                              # magic of the header
+    refused(bad)
+    recs = read_print2bin(f)
+    # first entry of the row permutation: an index out of range
+    off = sum(32 + len(r[3]) for r in recs[:4]) + 32
+    bad = bytearray(raw)
+    bad[off:off + 4] = np.uint32(10**8).tobytes()
+    refused(bad)
+    with pytest.raises(FmcaError):
+        H2Matrix.load(tmp_path / "missing.bin", CovarianceKernel("MATERN32", 0.5))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("interp", ["tensor", "total_degree"])
+def test_loaded_plan_gives_the_same_product(cuda_device, tmp_path, interp):
+    P = uniform_cloud(20000, 3, seed=8)
+    x = np.random.default_rng(8).standard_normal((20000, 4))
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 4, 0.8, min_leaf=64,
+                 precision="fp64", interpolator=interp)
+    f = tmp_path / "plan.bin"
+    H.save(f)
+    G = H2Matrix.load(f, CovarianceKernel("MATERN32", 0.5), precision="fp64")
+    assert rel_err(G.action(x), H.action(x)) <= 1e-14
