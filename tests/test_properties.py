@@ -13,7 +13,8 @@ the reference's tests (EXPONENTIAL, MATERN32, MATERN52, GAUSSIAN):
   for both interpolators;
 - with eta = 0 no block is admissible and the H2 product is the dense
   product;
-- total degree: the plan's DeMarchi nodes equal the oracle's."""
+- total degree: the plan's DeMarchi nodes equal the oracle's;
+- a plan written to a file and read back is the same plan."""
 from __future__ import annotations
 
 import numpy as np
@@ -112,3 +113,24 @@ def test_total_degree_nodes_equal_oracle(dim, p, seed):
     n2, i2 = O.interp()
     assert np.array_equal(n1, n2)
     assert np.abs(i1 - i2).max() <= 1e-12 * np.abs(i2).max()
+
+
+@given(P=clouds(max_n=300), p=st.integers(1, 4), eta=st.floats(0.1, 1.0),
+       leaf=st.integers(1, 50), td=st.booleans())
+@settings(max_examples=60, deadline=None)
+def test_plan_file_round_trip(tmp_path_factory, P, p, eta, leaf, td):
+    if td and P.shape[0] > 3:
+        return
+    interp = "total_degree" if td else "tensor"
+    H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, p, eta, min_leaf=leaf,
+                 interpolator=interp)
+    f = tmp_path_factory.mktemp("plan") / "p.bin"
+    H.save(f)
+    G = H2Matrix.load(f, CovarianceKernel("EXPONENTIAL", 1.0))
+    assert G.info == H.info
+    assert np.array_equal(G.rindices(), H.rindices())
+    mh, bh = H.clusters(0)
+    mg, bg = G.clusters(0)
+    assert np.array_equal(mh, mg) and np.array_equal(bh, bg)
+    for kind in (0, 1):
+        assert sorted(zip(*G.blocks(kind))) == sorted(zip(*H.blocks(kind)))
