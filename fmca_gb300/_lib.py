@@ -50,7 +50,7 @@ EXPORTED = [
     "fmca_matvec_adjoint_workspace_size", "fmca_matvec_adjoint", "fmca_plan_update_points",
     "fmca_plan_create_batched", "fmca_matvec_graph_create", "fmca_graph_launch",
     "fmca_graph_destroy", "fmca_plan_create_ex", "fmca_plan_interpolator",
-    "fmca_plan_save", "fmca_plan_load",
+    "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets",
 ]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
@@ -93,6 +93,7 @@ def load() -> C.CDLL:
     lib.fmca_plan_interpolator.argtypes = [vp, dp, dp]
     lib.fmca_plan_save.argtypes = [vp, C.c_char_p]
     lib.fmca_plan_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+    lib.fmca_plan_cloud_offsets.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
     lib.fmca_plan_destroy.argtypes = [vp]
     lib.fmca_plan_info.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.fmca_plan_statistics.argtypes = [vp, dp]

@@ -231,6 +231,22 @@ fmca_status fmca_plan_destroy(fmca_plan* plan) {
   return ok();
 }
 
+fmca_status fmca_plan_cloud_offsets(const fmca_plan* p, int64_t* offsets, int* count) {
+  if (!p || !count) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  const std::vector<int64_t>& co = p->plan.cloud_offsets;
+  if (co.size() >= 2) {
+    *count = (int)co.size() - 1;
+    if (offsets) std::copy(co.begin(), co.end(), offsets);
+  } else {
+    *count = 1;
+    if (offsets) {
+      offsets[0] = 0;
+      offsets[1] = (int64_t)p->plan.rows.n;
+    }
+  }
+  return ok();
+}
+
 fmca_status fmca_plan_save(const fmca_plan* p, const char* path) {
   if (!p || !path) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
   try {

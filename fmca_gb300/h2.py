@@ -166,7 +166,19 @@ class H2Matrix:
         self.p, self.dim, self.eta = self.info["degree"], self.info["dim"], None
         self.interpolator = "total_degree" if self.info["interpolator"] == 1 else "tensor"
         self._ws = {}
+        self.offsets = self.cloud_offsets()
         return self
+
+    def cloud_offsets(self) -> np.ndarray:
+        """First row of every point cloud, then the row count
+        (fmca_plan_cloud_offsets); [0, n] for a plan of one cloud."""
+        lib = _lib.load()
+        cnt = C.c_int(0)
+        check(lib.fmca_plan_cloud_offsets(self._h, None, C.byref(cnt)))
+        out = np.zeros(cnt.value + 1, dtype=np.int64)
+        check(lib.fmca_plan_cloud_offsets(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          C.byref(cnt)))
+        return out
 
     def graph(self, x, y, precision: Optional[str] = None) -> "MatvecGraph":
         """Records y = K x for these CUDA tensors into a CUDA graph."""

@@ -205,6 +205,11 @@ fmca_status fmca_plan_clusters(const fmca_plan* plan, int side, int32_t* meta,
    column-major; TotalDegreeInterpolator::invV).  Either pointer may be NULL;
    invV is left untouched for a tensor-product plan. */
 fmca_status fmca_plan_interpolator(const fmca_plan* plan, double* nodes, double* invV);
+/* Clouds of a plan: *count receives their number (1 for a plan of one
+   point cloud) and, when offsets is not NULL, offsets[0 .. count] the first
+   row of every cloud followed by the total row count, in the order the
+   clouds were given to fmca_plan_create_batched. */
+fmca_status fmca_plan_cloud_offsets(const fmca_plan* plan, int64_t* offsets, int* count);
 /* Plan files.  fmca_plan_save writes the host plan (points, both cluster
    trees, block lists, transfer and node data) as a sequence of matrices in
    the binary layout of FMCA's print2bin / bin2Mat (FMCA/src/util/IO.h:

@@ -66,6 +66,7 @@ def test_round_trip(tmp_path, case):
     G = H2Matrix.load(f, CovarianceKernel("MATERN32", 0.5))
     same_plan(H, G)
     assert G.interpolator == interp and G.p == p
+    assert np.array_equal(G.offsets, [0, Pr.shape[1]])
     recs = read_print2bin(f)
     head = np.frombuffer(recs[0][3], dtype=np.int64)
     assert recs[0][:3] == (8, 16, 1) and head[0] == 0x464D4341 and head[2] == Pr.shape[0]
@@ -82,6 +83,8 @@ def test_batched_round_trip(tmp_path):
     H.save(f)
     G = H2Matrix.load(f, CovarianceKernel("GAUSSIAN", 0.2))
     same_plan(H, G)
+    assert np.array_equal(G.offsets, [0, 700, 3200, 4500])
+    assert np.array_equal(H.cloud_offsets(), H.offsets)
 
 
 def test_malformed_files_are_refused(tmp_path):
