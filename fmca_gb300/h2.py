@@ -75,6 +75,12 @@ class H2Matrix:
     """Matrix-free H2 approximation of K(Pr, Pc) with a GPU matvec.
 
     Mirrors pyH2Matrix(ker, Pr, Pc, p=3, eta=0.8) (py/FMCA.cpp:209-220).
+    Keywords: ``min_leaf`` (minimum cluster size; the effective value is
+    max(min_leaf, q) like H2ClusterTree::init), ``precision`` ("fp64",
+    "fp32" or "mixed"; the default of ``action``) and ``interpolator``
+    ("tensor": Chebyshev tensor product, q = (p+1)^dim; "total_degree":
+    TotalDegreeInterpolator, q = binom(p+dim, dim), as the reference module
+    builds it). ``fmca_gb300.FMCA`` gives the reference module's defaults.
     """
 
     def __init__(self, cov: CovarianceKernel, Pr, Pc=None, p: int = 3,
