@@ -15,7 +15,11 @@ Under torchrun (N > 1) every rank runs an independent replica of the
 workload on its own GPU (weak scaling, no data-path collective); the step
 time is the maximum over ranks.  ``--impl reference`` times the CPU FP64
 restatement of the reference's matvec (the oracle; the reference itself
-cannot be built here) on all host cores, rank 0 only.
+cannot be built here) on all host cores, rank 0 only: one full product,
+then one part of the product per step (a row subtree of the cluster tree
+with exactly the work the full product spends on it), so that no number is
+extrapolated.  The default run also computes the full FP64 oracle product
+once and reports the GPU results' error against it.
 """
 from __future__ import annotations
 
@@ -35,15 +39,18 @@ if ROOT not in sys.path:
 
 METRIC = "H2 matvecs/sec (n·RHS/s) at n=1e6, mixed-precision batched vs FP64 GPU at 1e-5 rel err"
 UNIT = "n*RHS/s"
-SMS = 152
 # point pairs per clock per SM on the special-function unit: every pair costs
 # one sqrt.approx (16 results per clock per SM) and one ex2.approx (32 per
-# clock on GB300) on one pipe, 32 / 3 pairs per clock (tests/test_sfu_rates.py;
-# profiles/sfu_rates.md)
+# clock on GB300) on one pipe, 32 / 3 pairs per clock (measured by
+# tests/test_sfu_rates.py)
 SFU_PAIRS_PER_CLK = 32.0 / 3.0
 # DRAM bytes (read + write) of one near-field kernel-sum launch of the default
-# workload, from one ncu capture (profiles/ksum_um_c2_full.md)
+# workload: a fixed figure from one ncu capture of the current kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum), not measured by this script
 NEAR_DRAM_BYTES_PER_LAUNCH = 2.644428e9 + 0.149038e9
+# parts of the CPU reference's product per timed step (a level of the
+# cluster tree with this many clusters)
+REF_PARTS = 16
 
 
 def _measured_bf16_tflops():
@@ -147,44 +154,57 @@ def replica_throughput(units_per_replica: float, ms: float, world: int) -> float
 
 
 def run_reference(args):
+    """The CPU FP64 restatement of the reference's matvec on all host cores:
+    one full product (warm-up, also timed and reported), then one part of the
+    product per step, rotating over the REF_PARTS row subtrees of one tree
+    level (oracle_action_part: exactly the work the full product spends on
+    those rows, plus the small shared work of the levels above).  value =
+    rows computed x R / time, summed over the timed steps: nothing is
+    extrapolated."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     P, X = make_problem(args)
     import oracle
+    t0 = time.perf_counter()
     O = oracle.OraclePlan(P, None, 4, 0.8, 128)
-    stride = args.ref_stride
-    t_tr = None
-    times = []
-    total = None
-    for step in range(args.warmup + args.steps):
-        if t_tr is None:
-            t0 = time.perf_counter()
-            O.action(1, 0.5, X, bucket_stride=1 << 30, nthreads=threads)
-            t_tr = time.perf_counter() - t0
+    t_build = time.perf_counter() - t0
+    O.set_keep(True)
+    t0 = time.perf_counter()
+    Y, _ = O.action(1, 0.5, X, nthreads=threads)
+    t_full = time.perf_counter() - t0
+    Yp = np.zeros_like(Y, order="F")
+    times, units = [], 0.0
+    for step in range(args.warmup - 1 + args.steps):
         t0 = time.perf_counter()
-        _, work = O.action(1, 0.5, X, bucket_stride=stride, nthreads=threads)
+        (b, cnt), _ = O.action_part(1, 0.5, X, Yp, step % REF_PARTS, REF_PARTS, nthreads=threads)
         dt = time.perf_counter() - t0
-        if total is None:
-            total = O.near_pairs + O.q ** 2 * O.n_far
-        frac = (work[0] + work[1]) / total
-        t_full = t_tr + max(dt - t_tr, 0.0) / frac
-        if step >= args.warmup:
-            times.append(t_full)
-    t_full = statistics.median(times)
-    value = args.n * args.rhs / t_full
+        if step >= args.warmup - 1:
+            times.append(dt)
+            units += cnt * args.rhs
+    rows = O.perm(0)
+    exact = bool(np.array_equal(Yp[rows[b:b + cnt]], Y[rows[b:b + cnt]]))
+    value = units / sum(times)
+    ms = 1e3 * sum(times) / len(times)
+    sample = (f"oracle FP64 CPU restatement of the reference matvec (the reference needs Eigen, "
+              f"absent here; OpenMP, {threads} threads). Warm-up: one full product, "
+              f"{t_full:.1f} s = {args.n * args.rhs / t_full:.4g} n*RHS/s. Each step: one of "
+              f"{REF_PARTS} parts (a row subtree with its column subtree's upward pass, every "
+              f"block of its rows and its downward pass; about {100 / REF_PARTS:.1f}% of the "
+              f"work; its blocks in one OpenMP loop over its row clusters, every row summed in "
+              f"the full product's column-bucket order), rows x R computed / time, no "
+              f"extrapolation; the last part's rows equal the full product's: {exact}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_full * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": (f"each step: oracle FP64 CPU restatement (the reference "
-                                    f"needs Eigen, absent here) on every {stride}th column "
-                                    f"bucket ({frac:.3%} of the pair work) + full upward/"
-                                    f"downward passes, extrapolated; median of {args.steps}")},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "full_product": {"seconds": t_full, "value": args.n * args.rhs / t_full,
+                         "plan_build_s": t_build},
     }
     print(json.dumps(line))
     return 0
@@ -382,8 +402,6 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--rhs", type=int, default=32)
-    ap.add_argument("--cpu-stride", type=int, default=8)
-    ap.add_argument("--ref-stride", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
@@ -497,7 +515,8 @@ def main():
     pairs = float(info["near_pairs"])
     t_near = stage_ms["near"] * 1e-3
     sm_mhz = clocks.get("sm_mhz") or 2070.0
-    sfu_peak = SMS * SFU_PAIRS_PER_CLK * sm_mhz * 1e6 / 1e9
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sfu_peak = sms * SFU_PAIRS_PER_CLK * sm_mhz * 1e6 / 1e9
     sfu_achieved = pairs / t_near / 1e9
     tensor_flops = 2.0 * (2 * args.rhs + args.rhs) * pairs
     roofline = {
@@ -508,10 +527,11 @@ def main():
                  "exp2 each"),
         "peak_source": (f"special-function unit: {SFU_PAIRS_PER_CLK:.2f} pairs/clock/SM (sqrt "
                         "16 and ex2 32 results/clock/SM on one pipe, measured by "
-                        f"tests/test_sfu_rates.py) x {SMS} SMs at the median SM clock sampled "
+                        f"tests/test_sfu_rates.py) x {sms} SMs at the median SM clock sampled "
                         "during the timed region (the SFU has no entry in MEASURED_PEAKS.json)"),
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one near-field launch "
-                          "(profiles/ksum_um_c2_full.md)",
+        "traffic_source": ("fixed figure, not measured by this run: ncu "
+                           "dram__bytes_read.sum + dram__bytes_write.sum of one near-field launch "
+                           "of this workload, captured once with the current kernel"),
         "tensor": {"achieved": tensor_flops / t_near / 1e12, "peak": BF16_TFLOPS,
                    "unit": "TFLOP/s", "frac": tensor_flops / t_near / 1e12 / BF16_TFLOPS,
                    "work": "192 executed FP16 tensor flops per pair (3 products x 32 columns x 2)",
@@ -519,31 +539,33 @@ def main():
         "stage_ms": stage_ms,
     }
 
-    cpu = None
+    # the full FP64 oracle product on the host cores: the CPU baseline
+    # (timed, not extrapolated) and the reference the GPU results are
+    # checked against at this size
+    cpu, vs_oracle = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        total = info["near_pairs"] + info["q"] ** 2 * info["far_blocks"]
         import oracle
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()
         O = oracle.OraclePlan(P, None, 4, 0.8, 128)
         t_build = time.perf_counter() - t0
         t0 = time.perf_counter()
-        O.action(1, 0.5, X, bucket_stride=1 << 30, nthreads=threads)
-        t_tr = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        _, work = O.action(1, 0.5, X, bucket_stride=args.cpu_stride, nthreads=threads)
-        t_s = time.perf_counter() - t0
-        frac = (work[0] + work[1]) / total
-        t_full = t_tr + max(t_s - t_tr, 0.0) / frac
+        Y_or, _ = O.action(1, 0.5, X, nthreads=threads)
+        t_full = time.perf_counter() - t0
         cpu = {"value": args.n * args.rhs / t_full, "unit": UNIT, "cores": threads,
                "kind": "port",
-               "sample": (f"oracle FP64 CPU restatement of the reference matvec (OpenMP, "
-                          f"{threads} threads): every {args.cpu_stride}th column bucket "
-                          f"({frac:.3%} of the pair work) + full upward/downward passes on "
-                          f"the full workload took {t_s:.1f} s; extrapolated full matvec "
-                          f"{t_full:.1f} s (passes alone {t_tr:.1f} s, plan build "
-                          f"{t_build:.1f} s untimed)")}
-        del O
+               "sample": (f"one full product of this workload by the oracle FP64 CPU "
+                          f"restatement of the reference matvec (OpenMP, {threads} threads): "
+                          f"{t_full:.1f} s (plan build {t_build:.1f} s, not timed)")}
+        yo = torch.tensor(Y_or, device=dev)
+        H.matvec(Xd, Y)
+        barrier()
+        vs_oracle = {"mixed_rel_err": float((torch.linalg.norm(Y - yo) /
+                                             torch.linalg.norm(yo)).item())}
+        if fp64 is not None:
+            vs_oracle["fp64_rel_err"] = float((torch.linalg.norm(Y64 - yo) /
+                                               torch.linalg.norm(yo)).item())
+        del O, yo
 
     if rank == 0:
         line = {
@@ -557,6 +579,7 @@ def main():
                     "ms_per_step": e2e_ms},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "fp64_gpu": fp64,
+            "vs_fp64_oracle": vs_oracle,
             "plan": {"build_s": t_plan, "far_blocks": info["far_blocks"],
                      "near_blocks": info["near_blocks"], "near_pairs": info["near_pairs"],
                      "clusters": info["row_clusters"]},

@@ -50,7 +50,8 @@ EXPORTED = [
     "fmca_matvec_adjoint_workspace_size", "fmca_matvec_adjoint", "fmca_plan_update_points",
     "fmca_plan_create_batched", "fmca_matvec_graph_create", "fmca_graph_launch",
     "fmca_graph_destroy", "fmca_plan_create_ex", "fmca_plan_interpolator",
-    "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets",
+    "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets", "fmca_plan_device_bytes",
+    "fmca_plan_set_wait_limit",
 ]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
@@ -122,6 +123,8 @@ def load() -> C.CDLL:
     lib.fmca_graph_destroy.argtypes = [vp]
     lib.fmca_plan_set_profiling.argtypes = [vp, i32]
     lib.fmca_plan_profile.argtypes = [vp, dp, C.POINTER(C.c_int64)]
+    lib.fmca_plan_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    lib.fmca_plan_set_wait_limit.argtypes = [vp, C.c_uint64]
     for name in EXPORTED:
         if name not in ("fmca_last_error", "fmca_version"):
             getattr(lib, name).restype = C.c_int

@@ -19,6 +19,11 @@ from .h2 import H2Matrix
 
 
 class _H2Matvec(torch.autograd.Function):
+    # Every forward records the state it ran with (point coordinates, l and
+    # sigma2), and its backward puts that state back on H before the adjoint:
+    # several forwards on one H may run before their backwards (for instance
+    # two losses at different X summed into one objective), and each backward
+    # must differentiate at its own forward's points.
     @staticmethod
     def forward(ctx, H: H2Matrix, precision, x, l, sigma2, X):
         if X is not None:
@@ -26,6 +31,7 @@ class _H2Matvec(torch.autograd.Function):
         ctx.H = H
         ctx.precision = precision
         ctx.l, ctx.sigma2 = float(l), float(sigma2)
+        ctx.points = H.current_points()
         ctx.X_meta = None if X is None else (X.dtype, X.device)
         H.cov.l, H.cov.sigma2 = ctx.l, ctx.sigma2
         ctx.save_for_backward(x)
@@ -36,6 +42,8 @@ class _H2Matvec(torch.autograd.Function):
         (x,) = ctx.saved_tensors
         H = ctx.H
         H.cov.l, H.cov.sigma2 = ctx.l, ctx.sigma2
+        if ctx.points is not None and H.current_points() is not ctx.points:
+            H.update_points(ctx.points)
         need_x = ctx.needs_input_grad[2]
         need_X = ctx.X_meta is not None and ctx.needs_input_grad[5]
         out = H.adjoint(x, gy.contiguous(), precision=ctx.precision, want_dX=need_X,

@@ -71,6 +71,12 @@ gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
   return d;
 }
 
+gpu::KernelDesc to_desc(const fmca_plan* p, const fmca_kernel_desc* k) {
+  gpu::KernelDesc d = to_desc(k);
+  d.wait_ns = p->wait_ns.load();
+  return d;
+}
+
 fmca_status check_matvec_args(const fmca_plan* p, const fmca_kernel_desc* kernel,
                               int precision, int dtype, int order, int nrhs,
                               const void* x, const void* y) {
@@ -389,10 +395,10 @@ fmca_status fmca_matvec(fmca_plan* p, const fmca_kernel_desc* kernel,
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
-  fmca::gpu::set_profiling(p->dev, p->profile);
-  st = fmca::gpu::matvec(p->plan, p->dev, to_desc(kernel), precision, dtype, order,
+  st = fmca::gpu::matvec(p->plan, p->dev, to_desc(p, kernel), precision, dtype, order,
                          nrhs, x, x_stride_i, x_stride_r, y, y_stride_i, y_stride_r,
-                         workspace, workspace_bytes, (cudaStream_t)stream, &err);
+                         workspace, workspace_bytes, (cudaStream_t)stream, &err,
+                         p->profile.load());
   if (st != FMCA_OK) return fail((fmca_status)st, err);
   return ok();
 }
@@ -467,11 +473,10 @@ fmca_status fmca_matvec_adjoint(fmca_plan* p, const fmca_kernel_desc* kernel, in
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
-  fmca::gpu::set_profiling(p->dev, p->profile);
-  st = fmca::gpu::adjoint(p->plan, p->dev, to_desc(kernel), precision, dtype, nrhs, x,
+  st = fmca::gpu::adjoint(p->plan, p->dev, to_desc(p, kernel), precision, dtype, nrhs, x,
                           x_stride_i, x_stride_r, y, y_stride_i, y_stride_r, values, dX,
                           dX_stride_i, dX_stride_d, Kx, Ky, workspace, workspace_bytes,
-                          (cudaStream_t)stream, &err);
+                          (cudaStream_t)stream, &err, p->profile.load());
   if (st != FMCA_OK) return fail((fmca_status)st, err);
   return ok();
 }
@@ -548,8 +553,7 @@ fmca_status fmca_matvec_graph_create(fmca_plan* p, const fmca_kernel_desc* kerne
   if (s != FMCA_OK) return cleanup(s, fmca_last_error());
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
     return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
-  const bool prof = p->profile;
-  p->profile = false;
+  const bool prof = p->profile.exchange(false);
   if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
     p->profile = prof;
     return cleanup(FMCA_ERR_CUDA, cudaGetErrorString(e));
@@ -586,7 +590,18 @@ fmca_status fmca_graph_destroy(fmca_graph* g) {
 fmca_status fmca_plan_set_profiling(fmca_plan* p, int enable) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   p->profile = enable != 0;
-  fmca::gpu::set_profiling(p->dev, p->profile);
+  return ok();
+}
+
+fmca_status fmca_plan_set_wait_limit(fmca_plan* p, uint64_t ns) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->wait_ns = ns;
+  return ok();
+}
+
+fmca_status fmca_plan_device_bytes(const fmca_plan* p, size_t* bytes) {
+  if (!p || !bytes) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  *bytes = fmca::gpu::device_bytes(p->dev) + p->hx_bytes + p->hy_bytes;
   return ok();
 }
 

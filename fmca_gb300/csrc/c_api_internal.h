@@ -2,6 +2,7 @@
 // translation units.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -18,7 +19,10 @@ struct fmca_plan {
   void* hy = nullptr;
   size_t hx_bytes = 0, hy_bytes = 0;
   int64_t min_leaf = 0;
-  bool profile = false;
+  // stage events on the following matvecs (fmca_plan_set_profiling)
+  std::atomic<bool> profile{false};
+  // limit of the kernel sums' bounded waits in ns (0: the default of 2 s)
+  std::atomic<uint64_t> wait_ns{0};
 };
 
 namespace fmca {
@@ -30,5 +34,7 @@ fmca_status check_matvec_args(const fmca_plan* p, const fmca_kernel_desc* kernel
                               int precision, int dtype, int order, int nrhs,
                               const void* x, const void* y);
 gpu::KernelDesc to_desc(const fmca_kernel_desc* k);
+// the same with the plan's settings (wait limit)
+gpu::KernelDesc to_desc(const fmca_plan* p, const fmca_kernel_desc* k);
 }  // namespace capi
 }  // namespace fmca

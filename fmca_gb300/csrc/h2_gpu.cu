@@ -74,6 +74,7 @@ struct GroupList {
 struct DevPlan {
   int device = -1;
   std::vector<void*> allocs;
+  size_t alloc_bytes = 0;  // sum of the sizes of allocs
   DevSet<double> d;
   DevSet<float> f;
   int* midx = nullptr;
@@ -129,6 +130,7 @@ int to_device(DevPlan* dp, const V* host, size_t count, V** out,
   void* p = nullptr;
   FMCA_CK(cudaMalloc(&p, count * sizeof(V)));
   dp->allocs.push_back(p);
+  dp->alloc_bytes += count * sizeof(V);
   FMCA_CK(cudaMemcpy(p, host, count * sizeof(V), cudaMemcpyHostToDevice));
   *out = static_cast<V*>(p);
   return FMCA_OK;
@@ -403,6 +405,7 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     void* p = nullptr;
     FMCA_CK(cudaMalloc(&p, sizeof(int)));
     dp->allocs.push_back(p);
+    dp->alloc_bytes += sizeof(int);
     FMCA_CK(cudaMemset(p, 0, sizeof(int)));
     dp->err_flag = static_cast<int*>(p);
   }
@@ -510,6 +513,7 @@ KParams<T> make_kparams(const KernelDesc& k) {
       break;
   }
   kp.g = (T)g;
+  kp.wait_ns = k.wait_ns ? k.wait_ns : kWaitLimitNs;
   return kp;
 }
 
@@ -1222,8 +1226,9 @@ size_t workspace_bytes(const Plan& plan, int precision, int nrhs) {
 int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
            int dtype, int order, int nrhs, const void* x, int64_t sxi,
            int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-           size_t ws_bytes, cudaStream_t st, std::string* err) {
+           size_t ws_bytes, cudaStream_t st, std::string* err, bool profile) {
   std::lock_guard<std::mutex> lock(dp->mu);
+  dp->profile = profile;
   if (precision == FMCA_PREC_FP64)
     return matvec_t<double>(plan, dp, dp->d, k, dtype, order, nrhs, x, sxi, sxr, y,
                             syi, syr, ws, ws_bytes, st, err);
@@ -1402,8 +1407,9 @@ size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs) {
 int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int dtype,
             int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
             int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx, void* Ky,
-            void* ws, size_t wsb, cudaStream_t st, std::string* err) {
+            void* ws, size_t wsb, cudaStream_t st, std::string* err, bool profile) {
   std::lock_guard<std::mutex> lock(dp->mu);
+  dp->profile = profile;
   const bool base_kernel = k.type >= FMCA_KERNEL_EXPONENTIAL && k.type <= FMCA_KERNEL_GAUSSIAN;
   if ((dX || Ky) && !plan.same_tree) {
     *err = "gradients w.r.t. the points and K^T y need one point cloud (Pr == Pc)";
@@ -1554,8 +1560,8 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
 
 int device_of(const DevPlan* dp) { return dp ? dp->device : -1; }
 
-void set_profiling(DevPlan* dp, bool on) {
-  if (dp) dp->profile = on;
+size_t device_bytes(const DevPlan* dp) {
+  return dp ? dp->alloc_bytes + dp->ws_bytes : 0;
 }
 
 bool resident(const DevPlan* dp, int precision) {

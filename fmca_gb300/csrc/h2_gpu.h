@@ -17,22 +17,25 @@ struct DevPlan;
 struct KernelDesc {
   int type;
   double l, c, nu, sigma2;
+  // limit of every bounded wait of the kernel sums in ns (0: the default)
+  uint64_t wait_ns = 0;
 };
 
-// status codes are the fmca_status values of include/fmca_gb300.h
+// status codes are the fmca_status values of include/fmca_gb300.h.
+// profile: record stage events for fmca_plan_profile during this call (set
+// on the device plan under its mutex, so concurrent calls do not race on it)
 int upload(const Plan& plan, int precision, DevPlan** dev, std::string* err);
 void destroy(DevPlan* dev);
 size_t workspace_bytes(const Plan& plan, int precision, int nrhs);
 int matvec(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision,
            int dtype, int order, int nrhs, const void* x, int64_t sxi,
            int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-           size_t ws_bytes, cudaStream_t stream, std::string* err);
+           size_t ws_bytes, cudaStream_t stream, std::string* err, bool profile);
 int check_device_error(DevPlan* dev, std::string* err);
 int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
                const double* PC, int64_t nc, double* out, std::string* err);
 // device the plan lives on (-1 if not uploaded)
 int device_of(const DevPlan* dev);
-void set_profiling(DevPlan* dev, bool on);
 size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs);
 // values (device, 3 doubles): f, df/dl, df/dsigma2; dX (device, natural
 // order); Kx (strides of y) = K x, Ky (strides of x) = K y.  Any output may
@@ -40,12 +43,15 @@ size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs);
 int adjoint(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision, int dtype,
             int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
             int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx,
-            void* Ky, void* ws, size_t ws_bytes, cudaStream_t stream, std::string* err);
+            void* Ky, void* ws, size_t ws_bytes, cudaStream_t stream, std::string* err,
+            bool profile);
 // re-uploads the point coordinates held by the plan (tree and boxes fixed)
 int update_points(const Plan& plan, DevPlan* dev, std::string* err);
 // true if the plan's device data for this precision lives on the current
 // device (so a matvec needs no further device allocation besides workspace)
 bool resident(const DevPlan* dev, int precision);
+// device bytes the plan holds: uploaded data plus the workspace it owns
+size_t device_bytes(const DevPlan* dev);
 int profile(DevPlan* dev, double* stage_ms, int64_t* launches, std::string* err);
 
 }  // namespace gpu

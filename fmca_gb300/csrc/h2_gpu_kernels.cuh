@@ -61,6 +61,7 @@ struct KParams {
   T e2;  // scale of the exponent in base 2 (FP32 path)
   T il;  // 1 / l
   T g;   // coordinate scale of the tensor-core path (1 for generic kernels)
+  unsigned long long wait_ns;  // limit of the kernel sums' bounded waits
 };
 
 // kind 0: Chebyshev tensor product (Lagrange factors from xi, w); kind 1:
@@ -410,7 +411,7 @@ __global__ void ksum_kernel(const KGroup* __restrict__ groups,
   for (int k = 0; k < ntiles; ++k) {
     const int stage = k % STAGES;
     const uint32_t parity = (uint32_t)((k / STAGES) & 1);
-    const bool ok = mbar_wait_bounded(&bars[stage], parity, kWaitLimitNs);
+    const bool ok = mbar_wait_bounded(&bars[stage], parity, kp.wait_ns);
     if (ok) {
       const int cnt = scnt[stage];
       const Pt4<T>* P = spts + stage * TS;

@@ -5,7 +5,7 @@
 //   * two cluster trees (rows, columns) built exactly like FMCA's
 //     ClusterTree with CardinalityBisection
 //     (FMCA/src/Clustering/ClusterTreeInitializer_ClusterTree.h:24-132,
-//      FMCA/src/Clustering/ClusterTreeSplitter.h:198-219),
+//      FMCA/src/Clustering/ClusterTreeSplitter.h:60-81),
 //     clusters numbered in level order like FMCA's IDDFS iterator
 //     (FMCA/src/util/IDDFSForwardIterator.h:37-63);
 //   * the Chebyshev tensor-product interpolation tables

@@ -90,14 +90,13 @@ extern "C" fmca_status fmca_matvec_static_scratch(
   void* scratch = nullptr;
   s = scratch_address(&scratch);
   if (s != FMCA_OK) return s;
-  // no stage events: they would be created (allocated) on first use
-  fmca::gpu::set_profiling(p->dev, false);
+  // no stage events (profile = false): they would be created, that is
+  // allocated, on first use
   std::string err;
-  const int st = fmca::gpu::matvec(p->plan, p->dev, fmca::capi::to_desc(kernel), precision,
+  const int st = fmca::gpu::matvec(p->plan, p->dev, fmca::capi::to_desc(p, kernel), precision,
                                    dtype, order, nrhs, x, x_stride_i, x_stride_r, y,
                                    y_stride_i, y_stride_r, scratch, kStaticScratchBytes,
-                                   (cudaStream_t)stream, &err);
-  fmca::gpu::set_profiling(p->dev, p->profile);
+                                   (cudaStream_t)stream, &err, false);
   if (st != FMCA_OK) return fmca::capi::fail((fmca_status)st, err);
   return FMCA_OK;
 }

@@ -97,14 +97,16 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// bounded wait that also gives up when another role of the CTA aborted
-__device__ __forceinline__ bool um_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+// bounded wait (limit_ns) that also gives up when another role of the CTA
+// aborted
+__device__ __forceinline__ bool um_wait(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                        uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_timer_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort) return false;
-    if (global_timer_ns() - t0 > kWaitLimitNs) {
+    if (global_timer_ns() - t0 > limit_ns) {
       *abort = 1;
       return false;
     }
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
 
   const KGroup g = groups[blockIdx.x];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t wlim = kp.wait_ns;  // limit of the waits below (not of the drains)
 
   // tiles of the group: its intervals widened to multiples of 8 sources
   // (grid: one tile per source cluster)
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       bool ok = true;
       for (int k = 0; k < ntiles; ++k) {
         const int stage = k % NST;
-        if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag)) {
+        if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag, wlim)) {
           ok = false;
           break;
         }
@@ -385,9 +388,9 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       for (int k = 0; k < ntiles && ok; ++k) {
         const int stage = k % NST, u = k / F, b = u & 1;
         const bool first = k % F == 0;
-        if (!um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag) ||
+        if (!um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag, wlim) ||
             (first && u >= 2 &&
-             !um_wait(&acce[b], (uint32_t)(((u >> 1) - 1) & 1), abort_flag))) {
+             !um_wait(&acce[b], (uint32_t)(((u >> 1) - 1) & 1), abort_flag, wlim))) {
           ok = false;
           break;
         }
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         const int s0 = H == 2 ? 0 : j;
         for (int s = s0; s < NSETS; s += H == 2 ? 1 : 2) {
           const int p = 4 * k + s, slot = p % NPS;
-          if (!um_wait(&afull[slot], (uint32_t)((p / NPS) & 1), abort_flag)) {
+          if (!um_wait(&afull[slot], (uint32_t)((p / NPS) & 1), abort_flag, wlim)) {
             ok = false;
             break;
           }
@@ -489,7 +492,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     bool ok = true;
     for (int k = 0; k < ntiles && ok; ++k) {
       const int stage = k % NST;
-      if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag))) {
+      if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag, wlim))) {
         ok = false;
         break;
       }
@@ -498,7 +501,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       auto slot_free = [&]() {
         return p < NPS ||
                __all_sync(0xffffffffu,
-                          um_wait(&aempty[slot], (uint32_t)((p / NPS - 1) & 1), abort_flag));
+                          um_wait(&aempty[slot], (uint32_t)((p / NPS - 1) & 1), abort_flag, wlim));
       };
       const uint32_t a = tbase + lanes + A0 + slot * (H * 32);
       if constexpr (GRID) {
@@ -606,7 +609,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int nunits = (ntiles + F - 1) / F;
     for (int u = 0; u < nunits; ++u) {
       const int b = u & 1;
-      if (!__all_sync(0xffffffffu, um_wait(&accf[u % 4], (uint32_t)((u / 4) & 1), abort_flag))) {
+      if (!__all_sync(0xffffffffu, um_wait(&accf[u % 4], (uint32_t)((u / 4) & 1), abort_flag, wlim))) {
         ok = false;
         break;
       }

@@ -82,11 +82,51 @@ void get_tree(std::ifstream& f, Tree* t, int dim, int64_t n, int64_t C) {
       t->nsons.size() != c || t->bbmin.size() != c * dim || t->bbmax.size() != c * dim ||
       t->bbext.size() != c * dim || t->level_ptr.empty())
     throw std::runtime_error("plan file: inconsistent cluster tree");
-  for (uint32_t p : t->perm)
+  std::vector<unsigned char> seen((size_t)n, 0);
+  for (uint32_t p : t->perm) {
     if (p >= (uint32_t)n) throw std::runtime_error("plan file: permutation out of range");
+    if (seen[p]++) throw std::runtime_error("plan file: permutation repeats an index");
+  }
   for (size_t i = 0; i < c; ++i)
     if ((uint64_t)t->begin[i] + t->size[i] > (uint64_t)n)
       throw std::runtime_error("plan file: cluster range out of range");
+  // level_ptr: nlevels + 1 non-decreasing offsets from 0 to C (a forest of
+  // several clouds keeps only the number of levels: every entry 0)
+  const int64_t L = (int64_t)t->level_ptr.size() - 1;
+  if (L < 1 || t->level_ptr[0] != 0)
+    throw std::runtime_error("plan file: bad level offsets");
+  bool all_zero = true;
+  for (int64_t l = 0; l < L; ++l) {
+    if (t->level_ptr[l + 1] < t->level_ptr[l])
+      throw std::runtime_error("plan file: level offsets not monotone");
+    all_zero = all_zero && t->level_ptr[l + 1] == 0;
+  }
+  if (!all_zero && t->level_ptr[L] != (int32_t)C)
+    throw std::runtime_error("plan file: level offsets do not end at the cluster count");
+  // tree links: levels in range, parents before their sons, every son's
+  // parent and level consistent with its father
+  for (size_t i = 0; i < c; ++i) {
+    const int32_t lv = t->level[i], pa = t->parent[i], s0 = t->son0[i], ns = t->nsons[i];
+    if (lv < 0 || lv >= L) throw std::runtime_error("plan file: cluster level out of range");
+    if (pa < -1 || pa >= (int64_t)C || pa == (int32_t)i)
+      throw std::runtime_error("plan file: parent out of range");
+    if (ns < 0) throw std::runtime_error("plan file: negative son count");
+    if (ns > 0) {
+      if (s0 <= (int32_t)i || (int64_t)s0 + ns > C)
+        throw std::runtime_error("plan file: sons out of range");
+      for (int32_t s = s0; s < s0 + ns; ++s)
+        if (t->parent[s] != (int32_t)i || t->level[s] != lv + 1)
+          throw std::runtime_error("plan file: inconsistent parent links");
+    }
+  }
+}
+
+// offsets of a CSR list: first 0, non-decreasing
+bool csr_ok(const std::vector<int32_t>& ptr) {
+  if (ptr.empty() || ptr[0] != 0) return false;
+  for (size_t i = 1; i < ptr.size(); ++i)
+    if (ptr[i] < ptr[i - 1]) return false;
+  return true;
 }
 
 }  // namespace
@@ -195,11 +235,31 @@ void load_plan(const std::string& path, Plan* P, int64_t* min_leaf) {
       P->row_nodes.size() != (size_t)Cr * P->interp.q * dim ||
       P->col_nodes.size() != (size_t)Cc * P->interp.q * dim)
     throw std::runtime_error("plan file: inconsistent block lists");
-  if (pt.far_ptr.back() != (int32_t)pt.far_idx.size() ||
+  if (!csr_ok(pt.far_ptr) || !csr_ok(pt.near_ptr) ||
+      pt.far_ptr.back() != (int32_t)pt.far_idx.size() ||
       (size_t)pt.near_ptr.back() * 2 != pt.near_ivl.size())
     throw std::runtime_error("plan file: inconsistent CSR lists");
-  for (uint32_t e : pt.near_ivl)
-    if (e > (uint32_t)h[8]) throw std::runtime_error("plan file: interval out of range");
+  for (size_t i = 0; i < pt.near_ivl.size(); i += 2)
+    if (pt.near_ivl[i] > pt.near_ivl[i + 1] || pt.near_ivl[i + 1] > (uint32_t)h[8])
+      throw std::runtime_error("plan file: interval out of range");
+  for (int32_t c : P->row_leaves)
+    if (P->rows.nsons[c] != 0) throw std::runtime_error("plan file: row leaf with sons");
+  for (int32_t c : P->col_leaves)
+    if (P->cols.nsons[c] != 0) throw std::runtime_error("plan file: column leaf with sons");
+  // transfer data: d Kronecker factors of (p + 1)^2 (tensor) or a dense
+  // q x q matrix (total degree) per cluster
+  const size_t p1 = (size_t)deg + 1, q = (size_t)P->interp.q;
+  const size_t per = kind == kInterpTensor ? (size_t)dim * p1 * p1 : q * q;
+  if (P->row_E.size() != (size_t)Cr * per || P->col_E.size() != (size_t)Cc * per)
+    throw std::runtime_error("plan file: inconsistent transfer data");
+  // cloud offsets: none (one cloud) or count + 1 non-decreasing row offsets
+  // from 0 to the row count
+  const std::vector<int64_t>& co = P->cloud_offsets;
+  if (!co.empty()) {
+    bool ok = co.size() >= 2 && co[0] == 0 && co.back() == h[7];
+    for (size_t i = 1; ok && i < co.size(); ++i) ok = co[i] >= co[i - 1];
+    if (!ok) throw std::runtime_error("plan file: inconsistent cloud offsets");
+  }
 }
 
 }  // namespace fmca

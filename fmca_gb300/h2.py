@@ -117,6 +117,9 @@ class H2Matrix:
         check(lib.fmca_plan_info(self._h, info))
         self.info = {k: int(info[i]) for i, k in enumerate(_lib.INFO_KEYS)}
         self._ws = {}
+        # the row points the plan holds (one point cloud), never modified in
+        # place: update_points replaces the array
+        self._points = np.array(Pr, order="F", copy=True) if same else None
 
     @classmethod
     def batched(cls, cov: CovarianceKernel, clouds, p: int = 3, eta: float = 0.8,
@@ -360,6 +363,14 @@ class H2Matrix:
                 raise ValueError("Pc must have the shape of the plan's column points")
             Pcp = _dptr(Pc)
         check(_lib.load().fmca_plan_update_points(self._h, _dptr(Pr), Pcp))
+        if Pc is None and getattr(self, "_points", None) is not None:
+            self._points = np.array(Pr, order="F", copy=True)
+
+    def current_points(self):
+        """The point coordinates (dim x n FP64) a plan of one point cloud
+        holds now, as last set by the constructor or update_points; None for
+        batched and loaded plans."""
+        return getattr(self, "_points", None)
 
     def adjoint(self, x, y, precision: Optional[str] = None, want_dX: bool = True,
                 want_Kx: bool = False, want_Ky: bool = False, stream=None):
@@ -421,6 +432,17 @@ class H2Matrix:
         n = C.c_int64(0)
         check(_lib.load().fmca_plan_profile(self._h, _dptr(ms), C.byref(n)))
         return dict(zip(_lib.STAGES, ms.tolist())), int(n.value)
+
+    def set_wait_limit(self, ns: int = 0) -> None:
+        """Limit in ns of the bounded waits inside the kernel sums of the
+        following matvecs (fmca_plan_set_wait_limit); 0: the default 2 s."""
+        check(_lib.load().fmca_plan_set_wait_limit(self._h, int(ns)))
+
+    def device_bytes(self) -> int:
+        """Device memory the plan holds now (fmca_plan_device_bytes)."""
+        n = C.c_size_t(0)
+        check(_lib.load().fmca_plan_device_bytes(self._h, C.byref(n)))
+        return int(n.value)
 
     def check_device_error(self) -> None:
         check(_lib.load().fmca_plan_check_device_error(self._h))

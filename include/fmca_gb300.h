@@ -225,6 +225,14 @@ fmca_status fmca_plan_load(const char* path, fmca_plan** out);
 fmca_status fmca_plan_blocks(const fmca_plan* plan, int kind, int32_t* rows,
                              int32_t* cols);
 
+/* Device memory the plan holds now, in bytes: its uploaded data (lists,
+   points, nodes, transfers), the workspace it owns (allocated or grown by
+   matvecs called without a workspace) and the staging buffers of
+   fmca_matvec_host.  0 before the first matvec.  No reference counterpart
+   (H2MatrixBase::statistics, H2MatrixBase.h:70-105, reports the storage of
+   an assembled matrix, not device memory). */
+fmca_status fmca_plan_device_bytes(const fmca_plan* plan, size_t* bytes);
+
 /* Bytes of device workspace fmca_matvec needs for nrhs right-hand sides. */
 fmca_status fmca_matvec_workspace_size(const fmca_plan* plan, int precision,
                                        int nrhs, size_t* bytes);
@@ -310,6 +318,16 @@ fmca_status fmca_plan_update_points(fmca_plan* plan, const double* P_rows,
 /* Returns FMCA_ERR_TIMEOUT if a kernel of this plan gave up a bounded wait
    since the last call, and clears the flag.  Synchronises the device. */
 fmca_status fmca_plan_check_device_error(fmca_plan* plan);
+
+/* Limit, in ns, of every bounded wait inside the kernel sums (near and far
+   field) of this plan's following matvecs and adjoints; 0 restores the
+   default of 2 s.  A kernel whose wait runs out raises the plan's device
+   error flag (FMCA_ERR_TIMEOUT from fmca_plan_check_device_error), drains
+   its own copies and tensor-core products under a fixed limit, frees its
+   tensor memory and returns; the results of that call are undefined and
+   the GPU context stays usable.  A short limit is how a test makes a wait
+   run out.  No counterpart in the reference (which has no GPU waits). */
+fmca_status fmca_plan_set_wait_limit(fmca_plan* plan, uint64_t ns);
 
 /* Stages of one matvec, indices of fmca_plan_profile's output. */
 enum {

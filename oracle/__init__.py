@@ -41,6 +41,9 @@ def load() -> C.CDLL:
                                         dp, i64, dp, i32, dp, i32]
     lib.oracle_adjoint.argtypes = [vp, i32, C.c_double, C.c_double, dp, dp, i32, dp, dp, i32]
     lib.oracle_update_points.argtypes = [vp, dp]
+    lib.oracle_set_keep.argtypes = [vp, i32]
+    lib.oracle_action_part.argtypes = [vp, i32, C.c_double, C.c_double, C.c_double, dp, i32,
+                                       dp, i32, i32, i32, dp, C.POINTER(C.c_int64)]
     lib.oracle_kernel.restype = C.c_double
     lib.oracle_kernel.argtypes = [i32, C.c_double, C.c_double, C.c_double]
     _lib = lib
@@ -120,6 +123,27 @@ class OraclePlan:
 
     def check_transfer(self):
         return load().oracle_check_transfer(self._h)
+
+    def set_keep(self, on=True):
+        """Keep x (cluster order) and the moments of the following ``action``
+        calls, for ``action_part``."""
+        load().oracle_set_keep(self._h, int(bool(on)))
+
+    def action_part(self, ktype, l, x, y, part, nparts, c=1.0, sigma2=1.0, nthreads=0):
+        """Rows of one part of the product (oracle_action_part): writes them
+        into y (n_r x R, natural order, F-order float64) and returns
+        ((first row, row count) in cluster order, (dense_pairs, lr_pairs))."""
+        x = np.asfortranarray(x, dtype=np.float64)
+        assert y.flags.f_contiguous and y.dtype == np.float64 and y.shape[1] == x.shape[1]
+        work = np.zeros(2)
+        rows = (C.c_int64 * 2)()
+        load().oracle_action_part(self._h, int(ktype), float(l), float(c), float(sigma2), _d(x),
+                                  x.shape[1], _d(y), int(part), int(nparts), int(nthreads),
+                                  _d(work), rows)
+        if rows[0] < 0:
+            raise ValueError("action_part: no kept state for this R, or no level with "
+                             f"{nparts} clusters")
+        return (int(rows[0]), int(rows[1])), tuple(work)
 
     def action(self, ktype, l, x, c=1.0, sigma2=1.0, bucket_stride=1, nthreads=0):
         """y = sigma2 * H2(x) in natural order; returns (y, (dense_pairs, lr_pairs))."""

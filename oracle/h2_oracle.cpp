@@ -11,7 +11,7 @@
 // no reference outputs to compare with.  Its tests ship no golden vectors for
 // this path.  This restatement is pinned to the reference's own known-answer
 // checks only: the transfer-matrix identity < 1e-13
-// (FMCA/src/H2Matrix/compute_cluster_bases_impl.h:150-171, run by
+// (FMCA/src/H2Matrix/compute_cluster_bases_impl.h:59-80, run by
 // tests/test_H2Matrix.cpp:46-49), permutation completeness
 // (tests/test_ClusterTree.cpp:50-57) and the H2-vs-dense compression error
 // measured the way tests/test_H2Matrix.cpp:59-74 does.  Value-level parity
@@ -19,7 +19,7 @@
 //
 // Followed, function by function:
 //   tree       ClusterTreeInitializer_ClusterTree.h:24-132 (init, bounding
-//              box, refinement, shrinkToFit), ClusterTreeSplitter.h:198-219
+//              box, refinement, shrinkToFit), ClusterTreeSplitter.h:60-81
 //              (CardinalityBisection), IDDFSForwardIterator.h:37-63 (ids)
 //   interp     TensorProductInterpolator.h:39-81, MultiIndexSet.h:87-187;
 //              TotalDegreeInterpolator.h:26-47, DeMarchiPoints.h:20-43,
@@ -538,6 +538,12 @@ struct OPlan {
   std::vector<Scalar> Pr, Pc;
   std::vector<Block> blocks;  // leaves of the block tree, in DFS pop order
   Scalar eta = 0.8;
+  // kept by oracle_action when asked (keep != 0), for oracle_action_part:
+  // x in cluster order and the column clusters' moments of that call
+  std::vector<Scalar> kept_srhs;
+  std::vector<Mat> kept_t;
+  int kept_R = 0;
+  bool keep = false;
 };
 
 enum { kRefine = 0, kLowRank = 1, kDense = 2 };
@@ -606,6 +612,21 @@ void backward(const Node& nd, Scalar* y, int ldy, int R, std::vector<Mat>& tv) {
   } else {
     const Mat& s = tv[nd.block_id];
     gemmT_acc(nd.V, s.a.data(), s.r, R, y + nd.begin, ldy);
+  }
+}
+
+// backward() for a subtree whose rows start at row0 of y
+void backward_part(const Node& nd, Index row0, Scalar* y, int ldy, int R, std::vector<Mat>& tv) {
+  if (nd.sons.size()) {
+    for (size_t i = 0; i < nd.sons.size(); ++i) {
+      const Mat& dad = tv[nd.block_id];
+      gemmT_acc(nd.E[i], dad.a.data(), dad.r, R, tv[nd.sons[i].block_id].a.data(),
+                tv[nd.sons[i].block_id].r);
+      backward_part(nd.sons[i], row0, y, ldy, R, tv);
+    }
+  } else {
+    const Mat& s = tv[nd.block_id];
+    gemmT_acc(nd.V, s.a.data(), s.r, R, y + (nd.begin - row0), ldy);
   }
 }
 
@@ -788,13 +809,68 @@ void oracle_action(void* h, int ktype, double l, double c, double sigma2,
 
 }  // extern "C"
 
+// One leaf of the block tree applied to the product (the body of the
+// column-bucket loop of H2MatrixBase::action, H2MatrixBase.h:127-148):
+// low-rank blocks add S t_sigma to the row cluster's expansion, dense blocks
+// S x_sigma to the rows of lhs (row i of the product at lhs[i - row0], column
+// stride ldl).
+static void apply_block(const OPlan* P, const KernelFn& kern, const Block& b,
+                        const Scalar* srhs, int nc, int R, const std::vector<Mat>& trhs,
+                        std::vector<Mat>* tlhs_p, Scalar* lhs, Index row0, int ldl,
+                        double* dense_pairs, double* lr_pairs) {
+  const Index dim = P->dim;
+  const int q = P->ip.q();
+  std::vector<Mat>& tlhs = *tlhs_p;
+  // node coordinates of a cluster (XiX in NystromEvaluator::interpolate_kernel)
+  auto nodes = [&](const Node& nd) {
+    Mat X(dim, q);
+    for (int k = 0; k < q; ++k)
+      for (Index d = 0; d < dim; ++d) X(d, k) = P->ip.TP_xi(d, k) * nd.bext[d] + nd.bmin[d];
+    return X;
+  };
+  const Node& row = *b.row;
+  const Node& col = *b.col;
+  if (b.low_rank) {
+    const Mat XiX = nodes(row), XiY = nodes(col);
+    Mat S(q, q);
+    for (int j = 0; j < q; ++j)
+      for (int i = 0; i < q; ++i)
+        S(i, j) = kern(dist(&XiX.a[(size_t)i * dim], &XiY.a[(size_t)j * dim], dim));
+    if (P->ip.td) {  // S = invV S invV^T (NystromEvaluator.h:50-54)
+      Mat A(q, q), B(q, q);
+      for (int j = 0; j < q; ++j)
+        for (int m = 0; m < q; ++m) {
+          const Scalar v = S(m, j);
+          for (int i = 0; i < q; ++i) A(i, j) += P->ip.invV(i, m) * v;
+        }
+      for (int j = 0; j < q; ++j)
+        for (int m = 0; m < q; ++m) {
+          const Scalar v = P->ip.invV(j, m);
+          for (int i = 0; i < q; ++i) B(i, j) += A(i, m) * v;
+        }
+      S = std::move(B);
+    }
+    const Mat& t = trhs[col.block_id];
+    gemm_acc(S, t.a.data(), q, R, tlhs[row.block_id].a.data(), q);
+    *lr_pairs += (double)q * q;
+  } else {
+    Mat S((int)row.size, (int)col.size);
+    for (Index j = 0; j < col.size; ++j)
+      for (Index i = 0; i < row.size; ++i)
+        S((int)i, (int)j) =
+            kern(dist(&P->Pr[(size_t)P->rt.indices[row.begin + i] * dim],
+                      &P->Pc[(size_t)P->ct.indices[col.begin + j] * dim], dim));
+    gemm_acc(S, srhs + col.begin, nc, R, lhs + (row.begin - row0), ldl);
+    *dense_pairs += (double)row.size * col.size;
+  }
+}
+
 // the action; optionally returns the row-cluster expansions after the
 // downward pass (at the leaves: what V^T multiplies)
 static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
                         const double* x, int R, double* y, int bucket_stride, double* work,
                         std::vector<Mat>* leaf_expansions) {
   const KernelFn kern = make_kernel(ktype, l, c);
-  const Index dim = P->dim;
   const int nr = (int)P->rt.root.size, nc = (int)P->ct.root.size;
   const int q = P->ip.q();
   // srhs = P^T rhs: cluster order
@@ -809,57 +885,15 @@ static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
   for (auto* nd : P->rt.by_id) tlhs[nd->block_id] = Mat(q, R);
   std::vector<std::vector<const Block*>> sched(P->ct.by_id.size());
   for (auto& b : P->blocks) sched[b.col->block_id].push_back(&b);
-  // node coordinates of a cluster (XiX in NystromEvaluator::interpolate_kernel)
-  auto nodes = [&](const Node& nd) {
-    Mat X(dim, q);
-    for (int k = 0; k < q; ++k)
-      for (Index d = 0; d < dim; ++d) X(d, k) = P->ip.TP_xi(d, k) * nd.bext[d] + nd.bmin[d];
-    return X;
-  };
   double dense_pairs = 0, lr_pairs = 0;
   const int stride = bucket_stride > 1 ? bucket_stride : 1;
   for (size_t bj = 0; bj < sched.size(); ++bj) {
     if ((int)(bj % stride) != 0) continue;
     const auto& bucket = sched[bj];
 #pragma omp parallel for schedule(dynamic) reduction(+ : dense_pairs, lr_pairs)
-    for (long k = 0; k < (long)bucket.size(); ++k) {
-      const Block& b = *bucket[k];
-      const Node& row = *b.row;
-      const Node& col = *b.col;
-      if (b.low_rank) {
-        const Mat XiX = nodes(row), XiY = nodes(col);
-        Mat S(q, q);
-        for (int j = 0; j < q; ++j)
-          for (int i = 0; i < q; ++i)
-            S(i, j) = kern(dist(&XiX.a[(size_t)i * dim], &XiY.a[(size_t)j * dim], dim));
-        if (P->ip.td) {  // S = invV S invV^T (NystromEvaluator.h:50-54)
-          Mat A(q, q), B(q, q);
-          for (int j = 0; j < q; ++j)
-            for (int m = 0; m < q; ++m) {
-              const Scalar v = S(m, j);
-              for (int i = 0; i < q; ++i) A(i, j) += P->ip.invV(i, m) * v;
-            }
-          for (int j = 0; j < q; ++j)
-            for (int m = 0; m < q; ++m) {
-              const Scalar v = P->ip.invV(j, m);
-              for (int i = 0; i < q; ++i) B(i, j) += A(i, m) * v;
-            }
-          S = std::move(B);
-        }
-        const Mat& t = trhs[col.block_id];
-        gemm_acc(S, t.a.data(), q, R, tlhs[row.block_id].a.data(), q);
-        lr_pairs += (double)q * q;
-      } else {
-        Mat S((int)row.size, (int)col.size);
-        for (Index j = 0; j < col.size; ++j)
-          for (Index i = 0; i < row.size; ++i)
-            S((int)i, (int)j) =
-                kern(dist(&P->Pr[(size_t)P->rt.indices[row.begin + i] * dim],
-                          &P->Pc[(size_t)P->ct.indices[col.begin + j] * dim], dim));
-        gemm_acc(S, srhs.data() + col.begin, nc, R, lhs.data() + row.begin, nr);
-        dense_pairs += (double)row.size * col.size;
-      }
-    }
+    for (long k = 0; k < (long)bucket.size(); ++k)
+      apply_block(P, kern, *bucket[k], srhs.data(), nc, R, trhs, &tlhs, lhs.data(), 0, nr,
+                  &dense_pairs, &lr_pairs);
   }
   backward(P->rt.root, lhs.data(), nr, R, tlhs);
   for (int r = 0; r < R; ++r)
@@ -870,7 +904,187 @@ static void action_impl(OPlan* P, int ktype, double l, double c, double sigma2,
     work[1] = lr_pairs;
   }
   if (leaf_expansions) *leaf_expansions = std::move(tlhs);
+  if (P->keep) {
+    P->kept_srhs = std::move(srhs);
+    P->kept_t = std::move(trhs);
+    P->kept_R = R;
+  }
 }
+
+// marks nd and every cluster below it
+static void mark_subtree(const Node& nd, std::vector<char>* mark) {
+  (*mark)[nd.block_id] = 1;
+  for (const Node& s : nd.sons) mark_subtree(s, mark);
+}
+
+extern "C" {
+
+// Keep (on != 0) x in cluster order and the moments of the following
+// oracle_action calls for oracle_action_part.
+void oracle_set_keep(void* h, int on) {
+  OPlan* P = static_cast<OPlan*>(h);
+  P->keep = on != 0;
+  if (!P->keep) {
+    P->kept_srhs = std::vector<Scalar>();
+    P->kept_t = std::vector<Mat>();
+    P->kept_R = 0;
+  }
+}
+
+// Part `part` of `nparts` of one product, for bounded timing samples of the
+// CPU baseline without extrapolation.  nparts must be the number of clusters
+// of one level L of both trees (a power of two for these binary trees); the
+// part is row cluster and column cluster number `part` of level L.  The part
+// does exactly the work the full product spends on them: x gathered to
+// cluster order for the column cluster's points, the upward pass inside the
+// column subtree, every block whose row cluster lies in the row subtree
+// (column buckets in the order of the full product), the downward pass
+// inside the row subtree.  The work of the levels above L is shared by all
+// parts and is done by each of them (moments of the column ancestors, blocks
+// of the row ancestors, the downward pass along the path to the part).
+// The other column clusters' moments and x values come from the last
+// oracle_action with oracle_set_keep on, which must have had the same x: the
+// rows of the row subtree then equal that product's rows bit for bit.
+// Writes y (n_r x R, natural order) on those rows only and returns their
+// first cluster-order row and count in rows[0..1] (-1, -1 if the plan kept
+// nothing for this R or nparts is not a level's cluster count).
+void oracle_action_part(void* h, int ktype, double l, double c, double sigma2,
+                        const double* x, int R, double* y, int part, int nparts,
+                        int nthreads, double* work, int64_t* rows) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  OPlan* P = static_cast<OPlan*>(h);
+  rows[0] = rows[1] = -1;
+  if (P->kept_R != R || P->kept_t.size() != P->ct.by_id.size() || part < 0 || part >= nparts)
+    return;
+  // the clusters of the first level with nparts clusters (level order)
+  auto level_nodes = [nparts](const Tree& t) {
+    std::vector<Node*> out;
+    for (Node* nd : t.by_id) {
+      if (!out.empty() && nd->level != out.back()->level) {
+        if ((int)out.size() == nparts) break;
+        out.clear();
+      }
+      out.push_back(nd);
+    }
+    if ((int)out.size() != nparts) out.clear();
+    return out;
+  };
+  const std::vector<Node*> rl = level_nodes(P->rt), cl = level_nodes(P->ct);
+  if ((int)rl.size() != nparts || (int)cl.size() != nparts) return;
+  const Node& rs = *rl[part];
+  const Node& cs = *cl[part];
+  const KernelFn kern = make_kernel(ktype, l, c);
+  const int nr = (int)P->rt.root.size, nc = (int)P->ct.root.size;
+  const int q = P->ip.q();
+  std::vector<Scalar>& srhs = P->kept_srhs;
+  std::vector<Mat>& trhs = P->kept_t;
+  // x of the column subtree in cluster order; its moments, then those of
+  // its ancestors
+  for (int r = 0; r < R; ++r)
+    for (Index i = cs.begin; i < cs.begin + cs.size; ++i)
+      srhs[(size_t)r * nc + i] = x[(size_t)r * nc + P->ct.indices[i]];
+  forward(cs, P->ct, srhs.data(), nc, R, &trhs);
+  for (const Node* a = cs.dad; a; a = a->dad) {
+    Mat& out = trhs[a->block_id];
+    out = Mat(q, R);
+    for (size_t i = 0; i < a->sons.size(); ++i)
+      gemm_acc(a->E[i], trhs[a->sons[i].block_id].a.data(), q, R, out.a.data(), q);
+  }
+  // blocks whose row cluster is in the row subtree or one of its ancestors
+  std::vector<char> mine(P->rt.by_id.size(), 0);
+  mark_subtree(rs, &mine);
+  for (const Node* a = rs.dad; a; a = a->dad) mine[a->block_id] = 1;
+  std::vector<Mat> tlhs(P->rt.by_id.size());
+  for (const Node* nd : P->rt.by_id)
+    if (mine[nd->block_id]) tlhs[nd->block_id] = Mat(q, R);
+  // the part's blocks grouped by row cluster, each group in column-bucket
+  // order: every row then accumulates its blocks in the order of the full
+  // product.  The groups run in parallel (one OpenMP loop over the part's
+  // row clusters: its column buckets are too small to keep the threads
+  // busy one bucket at a time), which is exact as long as no two row
+  // clusters with dense blocks share points; otherwise the full product's
+  // bucket-by-bucket loop is used.
+  std::vector<std::vector<const Block*>> byrow(P->rt.by_id.size());
+  // rows [row0, row1) of lhs: the subtree's, and those of dense blocks of
+  // ancestors (which also cover rows outside the part; they are dropped)
+  Index row0 = rs.begin, row1 = rs.begin + rs.size;
+  for (auto& b : P->blocks)
+    if (mine[b.row->block_id]) {
+      byrow[b.row->block_id].push_back(&b);
+      if (!b.low_rank) {
+        row0 = std::min(row0, b.row->begin);
+        row1 = std::max(row1, b.row->begin + b.row->size);
+      }
+    }
+  std::vector<const Node*> groups;
+  std::vector<std::pair<Index, Index>> dense_rows;  // (begin, end) of rows with dense blocks
+  for (const Node* nd : P->rt.by_id) {
+    auto& g = byrow[nd->block_id];
+    if (g.empty()) continue;
+    std::sort(g.begin(), g.end(), [](const Block* a, const Block* b) {
+      return a->col->block_id < b->col->block_id;
+    });
+    groups.push_back(nd);
+    for (const Block* b : g)
+      if (!b->low_rank && nd->size) {
+        dense_rows.emplace_back(nd->begin, nd->begin + nd->size);
+        break;
+      }
+  }
+  std::sort(dense_rows.begin(), dense_rows.end());
+  bool disjoint = true;
+  for (size_t i = 1; i < dense_rows.size(); ++i)
+    disjoint = disjoint && dense_rows[i].first >= dense_rows[i - 1].second;
+  const int ldl = (int)(row1 - row0);
+  std::vector<Scalar> lhs((size_t)ldl * R, 0.);
+  double dense_pairs = 0, lr_pairs = 0;
+  if (disjoint) {
+#pragma omp parallel for schedule(dynamic) reduction(+ : dense_pairs, lr_pairs)
+    for (long gi = 0; gi < (long)groups.size(); ++gi)
+      for (const Block* b : byrow[groups[gi]->block_id])
+        apply_block(P, kern, *b, srhs.data(), nc, R, trhs, &tlhs, lhs.data(), row0, ldl,
+                    &dense_pairs, &lr_pairs);
+  } else {
+    std::vector<std::vector<const Block*>> sched(P->ct.by_id.size());
+    for (const Node* nd : groups)
+      for (const Block* b : byrow[nd->block_id]) sched[b->col->block_id].push_back(b);
+    for (size_t bj = 0; bj < sched.size(); ++bj) {
+      const auto& bucket = sched[bj];
+      if (bucket.empty()) continue;
+#pragma omp parallel for schedule(dynamic) reduction(+ : dense_pairs, lr_pairs)
+      for (long k = 0; k < (long)bucket.size(); ++k)
+        apply_block(P, kern, *bucket[k], srhs.data(), nc, R, trhs, &tlhs, lhs.data(), row0, ldl,
+                    &dense_pairs, &lr_pairs);
+    }
+  }
+  // downward pass: along the path from the root to the row subtree (dense
+  // blocks of ancestors write rows of the subtree only through lhs), then
+  // inside it
+  std::vector<const Node*> path;
+  for (const Node* a = &rs; a; a = a->dad) path.push_back(a);
+  for (size_t k = path.size() - 1; k >= 1; --k) {
+    const Node& dad = *path[k];
+    const Node& son = *path[k - 1];
+    const size_t i = (size_t)(&son - dad.sons.data());
+    gemmT_acc(dad.E[i], tlhs[dad.block_id].a.data(), q, R, tlhs[son.block_id].a.data(), q);
+  }
+  backward_part(rs, row0, lhs.data(), ldl, R, tlhs);
+  for (int r = 0; r < R; ++r)
+    for (Index i = rs.begin; i < rs.begin + rs.size; ++i)
+      y[(size_t)r * nr + P->rt.indices[i]] = sigma2 * lhs[(size_t)r * ldl + (i - row0)];
+  if (work) {
+    work[0] = dense_pairs;
+    work[1] = lr_pairs;
+  }
+  rows[0] = rs.begin;
+  rows[1] = rs.size;
+}
+
+}  // extern "C"
 
 namespace {
 // Lagrange basis of the nodes xi in product form and its derivative:

@@ -5,7 +5,7 @@ fingerprints from a pure numpy/Python restatement of FMCA's ClusterTree
 This restatement is independent of both the C++ plan builder and the C++
 oracle; the fixture pins their tree, permutation and block lists.  Followed:
 FMCA/src/Clustering/ClusterTreeInitializer_ClusterTree.h:24-132,
-FMCA/src/Clustering/ClusterTreeSplitter.h:198-219,
+FMCA/src/Clustering/ClusterTreeSplitter.h:60-81,
 FMCA/src/Clustering/Admissibility.h:19-29,95-115,
 FMCA/src/H2Matrix/H2MatrixBase.h:160-191.
 

@@ -192,3 +192,46 @@ def test_autograd_function(cuda_device):
     assert rel_err(Xt.grad.numpy(), dX_ref.T) < 1e-10
     Ky_ref, _ = O.action(1, 0.4, y, sigma2=1.5)
     assert rel_err(xt.grad.cpu().numpy(), Ky_ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_autograd_two_forwards_before_their_backwards(cuda_device):
+    # two forwards on one H at different points and length scales, then both
+    # backwards: each backward must differentiate at its own forward's state
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    from fmca_gb300.autograd import dense_reference, h2_matvec
+    P, x, y = _problem(4000, 2, seed=11)
+    P2 = P + 1e-3 * np.random.default_rng(12).standard_normal(P.shape)
+    H = H2Matrix(CovarianceKernel("MATERN52", 0.4), P, P, 4, 0.8, precision="fp64")
+
+    def leaf(v, dev=None):
+        return torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=True)
+
+    def grads(X, l, s2):
+        xt, lt, st, Xt = leaf(x, cuda_device), leaf(l), leaf(s2), leaf(X)
+        f = (torch.tensor(y, device=cuda_device) * h2_matvec(H, xt, lt, st, Xt)).sum()
+        return f, (xt, lt, st, Xt)
+
+    # one at a time
+    ref = []
+    for X, l, s2 in ((P, 0.4, 1.5), (P2, 0.3, 0.7)):
+        f, leaves = grads(X, l, s2)
+        f.backward()
+        ref.append((f.item(), [t.grad.cpu().numpy().copy() for t in leaves]))
+    # both forwards first, then the backwards in reverse order
+    f1, a = grads(P, 0.4, 1.5)
+    f2, b = grads(P2, 0.3, 0.7)
+    f2.backward()
+    f1.backward()
+    for (fr, gr), f, leaves in zip(ref, (f1, f2), (a, b)):
+        assert abs(f.item() - fr) <= 1e-13 * abs(fr)
+        for t, g in zip(leaves, gr):
+            assert rel_err(t.grad.cpu().numpy(), g) <= 1e-12
+    # and the second state against dense FP64 autograd (compression error)
+    Xt, lt, st = leaf(P2), leaf(0.3), leaf(0.7)
+    fd = (torch.tensor(y) * dense_reference("MATERN52", lt, st, Xt, torch.tensor(x))).sum()
+    fd.backward()
+    assert abs(f2.item() - fd.item()) / abs(fd.item()) < 1e-4
+    assert abs(b[1].grad.item() - lt.grad.item()) / abs(lt.grad.item()) < 1e-3
+    assert rel_err(b[3].grad.cpu().numpy(), Xt.grad.numpy()) < 1e-3

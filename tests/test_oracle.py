@@ -1,5 +1,5 @@
 """The oracle against the reference's own known-answer checks: the transfer
-identity (compute_cluster_bases_impl.h:150-171, asserted < 1e-13 by
+identity (compute_cluster_bases_impl.h:59-80, asserted < 1e-13 by
 tests/test_H2Matrix.cpp:46-49) and the H2-vs-dense compression error the way
 tests/test_H2Matrix.cpp:59-74 measures it."""
 from __future__ import annotations
@@ -74,3 +74,30 @@ def test_kernel_formulas():
         b = np.sqrt(5) / 0.5 * r
         assert oracle.kernel(2, 0.5, r) == pytest.approx((1 + b + b * b / 3) * np.exp(-b), rel=1e-14)
         assert oracle.kernel(3, 0.5, r) == pytest.approx(np.exp(-0.5 * r * r / 0.25), rel=1e-15)
+
+
+@pytest.mark.parametrize("nparts", [2, 8])
+def test_action_parts_reproduce_the_full_product(nparts):
+    """oracle_action_part (the bounded samples of the timed CPU baseline):
+    every part's rows equal the full product's rows bit for bit, and the
+    parts' pair counts add up to the full product's (up to the blocks of the
+    levels above the parts, which every part redoes)."""
+    P = np.random.default_rng(3).random((3, 12000))
+    X = np.random.default_rng(4).standard_normal((12000, 3))
+    O = oracle.OraclePlan(P, None, 3, 0.8, 64)
+    O.set_keep(True)
+    Y, (dp, lp) = O.action(1, 0.5, X)
+    perm = O.perm(0)
+    Yp = np.full_like(Y, np.nan, order="F")
+    seen = np.zeros(12000, dtype=bool)
+    tot = np.zeros(2)
+    for k in range(nparts):
+        (b, n), work = O.action_part(1, 0.5, X, Yp, k, nparts)
+        rows = perm[b:b + n]
+        assert not seen[rows].any()
+        seen[rows] = True
+        assert np.array_equal(Yp[rows], Y[rows])
+        tot += work
+    assert seen.all()
+    assert tot[0] >= dp and tot[1] >= lp
+    assert tot[0] + tot[1] <= 1.02 * (dp + lp)

@@ -115,6 +115,82 @@ def test_malformed_files_are_refused(tmp_path):
         H2Matrix.load(tmp_path / "missing.bin", CovarianceKernel("MATERN32", 0.5))
 
 
+# record index of every matrix in a plan file of one cloud: header, eta, the
+# two point clouds, the two trees (11 records each), then the block lists,
+# leaves, transfer data, nodes and cloud offsets
+ROW_TREE = dict(zip(["perm", "begin", "size", "level", "parent", "son0", "nsons", "bbmin",
+                     "bbmax", "bbext", "level_ptr"], range(4, 15)))
+LISTS = dict(zip(["far_row", "far_col", "near_row", "near_col", "far_ptr", "far_idx",
+                  "near_ptr", "near_ivl", "row_leaves", "col_leaves", "row_E", "col_E",
+                  "row_nodes", "col_nodes", "cloud_offsets"], range(26, 41)))
+DTYPES = {"perm": np.uint32, "begin": np.uint32, "size": np.uint32, "near_ivl": np.uint32,
+          "row_E": np.float64, "col_E": np.float64, "cloud_offsets": np.int64}
+
+
+def write_print2bin(path, recs):
+    with open(path, "wb") as f:
+        for size, rows, cols, data in recs:
+            f.write(np.array([size, 0, rows, cols], dtype=np.uint64).tobytes())
+            f.write(data)
+
+
+def corrupted(recs, field, edit):
+    """recs with the array of `field` replaced by edit(copy of the array)."""
+    k = ROW_TREE.get(field, LISTS.get(field))
+    dt = DTYPES.get(field, np.int32)
+    a = edit(np.frombuffer(recs[k][3], dtype=dt).copy())
+    out = list(recs)
+    out[k] = (np.dtype(dt).itemsize, a.size, 1, a.astype(dt).tobytes())
+    return out
+
+
+def test_corrupted_structure_fields_are_refused(tmp_path):
+    """Every structural array of a plan file is checked before it reaches the
+    device: levels, parents, sons, level offsets, CSR offsets, intervals,
+    leaves, transfer data sizes and cloud offsets."""
+    P = uniform_cloud(3000, 3, seed=7)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 3, 0.8)
+    f = tmp_path / "plan.bin"
+    H.save(f)
+    recs = read_print2bin(f)
+    C = H.info["row_clusters"]
+
+    def setv(i, v):
+        def e(a):
+            a[i] = v
+            return a
+        return e
+
+    def swap_first_interval(a):
+        a[0] = a[1] + 1
+        return a
+
+    cases = {
+        "perm": lambda a: setv(1, a[0])(a),             # an index twice
+        "level": setv(5, 99),                            # level past the last one
+        "parent": setv(3, C + 7),                        # parent out of range
+        "son0": setv(0, C - 1),                          # sons past the last cluster
+        "nsons": setv(0, 10**6),
+        "level_ptr": setv(1, 10**6),                     # offsets not monotone
+        "far_ptr": setv(0, 1),                           # CSR not starting at 0
+        "near_ptr": setv(1, -1),                         # CSR not monotone
+        "near_ivl": swap_first_interval,                 # interval with begin > end
+        "row_leaves": setv(0, 0),                        # the root as a leaf
+        "row_E": lambda a: a[:-1],                       # transfer data one short
+        "cloud_offsets": lambda a: np.array([0, 5], dtype=np.int64),
+    }
+    for field, edit in cases.items():
+        g = tmp_path / f"bad_{field}.bin"
+        write_print2bin(g, corrupted(recs, field, edit))
+        with pytest.raises(FmcaError) as e:
+            H2Matrix.load(g, CovarianceKernel("MATERN32", 0.5))
+        assert e.value.status == ERR["FMCA_ERR_INVALID_ARGUMENT"], field
+    # the untouched records still load
+    g = tmp_path / "same.bin"
+    write_print2bin(g, recs)
+    same_plan(H, H2Matrix.load(g, CovarianceKernel("MATERN32", 0.5)))
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("interp", ["tensor", "total_degree"])
 def test_loaded_plan_gives_the_same_product(cuda_device, tmp_path, interp):

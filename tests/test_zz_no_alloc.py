@@ -5,7 +5,10 @@ synchronisation of cudaMalloc / cudaFree).  It runs the same product as
 fmca_matvec with its scratch in a fixed 64 MiB device array of the library.
 
 Called here through the C ABI and compared with fmca_matvec, within the
-tolerances of the other GPU tests, on two calls in a row.  This file is
+tolerances of the other GPU tests, on two calls in a row.  Around the second
+call (the first one looked up the array's device address) the GPU's free
+memory and the plan's own device memory must stay exactly the same: the
+call allocates nothing, neither itself nor through the plan's workspace.  This file is
 collected last so that a run stopping at its first failure has run every
 other test already; it also passes on its own in a fresh process."""
 from __future__ import annotations
@@ -33,6 +36,12 @@ def static_matvec(H, cov, prec, x, y, stream):
         C.c_void_p(y.data_ptr()), y.stride(0), y.stride(1), C.c_void_p(stream.cuda_stream))
 
 
+def plan_device_bytes(H):
+    n = C.c_size_t(0)
+    assert _lib.load().fmca_plan_device_bytes(H.handle, C.byref(n)) == _lib.FMCA_OK
+    return n.value
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32", "mixed"])
 def test_static_scratch_matches_matvec(cuda_device, prec):
     import torch
@@ -43,10 +52,15 @@ def test_static_scratch_matches_matvec(cuda_device, prec):
     x = torch.tensor(X, device=cuda_device)
     y_ref = H.matvec(x, precision=prec)          # fmca_matvec; makes the plan resident
     stream = torch.cuda.current_stream(cuda_device)
-    for _ in range(2):                             # two calls in a row share the scratch
+    for call in range(2):                          # two calls in a row share the scratch
         y = torch.full_like(y_ref, float("nan"))
+        torch.cuda.synchronize(cuda_device)
+        free0, held0 = torch.cuda.mem_get_info(cuda_device)[0], plan_device_bytes(H)
         assert static_matvec(H, cov, prec, x, y, stream) == _lib.FMCA_OK
         torch.cuda.synchronize(cuda_device)
+        if call == 1:
+            assert torch.cuda.mem_get_info(cuda_device)[0] == free0
+            assert plan_device_bytes(H) == held0
         assert torch.isfinite(y).all()
         assert rel_err(y.cpu().numpy(), y_ref.cpu().numpy()) < TOL[prec]
     H.check_device_error()
