@@ -245,6 +245,8 @@ def run_c3(args, torch, dev):
     N, R = B.rows(), 8
     X = torch.tensor(rng.standard_normal((N, R)), dtype=torch.float32, device=dev)
     Y = torch.empty_like(X)
+    B.set_autotune(not args.no_autotune)
+    B.matvec(X, Y)  # tunes (outside the graph capture)
     g = B.graph(X, Y)
     for _ in range(args.warmup):
         g.launch()
@@ -252,6 +254,8 @@ def run_c3(args, torch, dev):
     singles = [H2Matrix(cov, P, P, 3, 0.8, precision="mixed") for P in clouds]
     xs = [X[B.offsets[i]:B.offsets[i + 1]] for i in range(64)]
     ys = [torch.empty_like(x) for x in xs]
+    for S in singles:
+        S.set_autotune(not args.no_autotune)
 
     def each():
         for S, x, y in zip(singles, xs, ys):
@@ -261,13 +265,27 @@ def run_c3(args, torch, dev):
     ms_each = _events_ms(torch, each, args.steps)
     err = max(float((torch.linalg.norm(Y[B.offsets[i]:B.offsets[i + 1]] - ys[i]) /
                      torch.linalg.norm(ys[i])).item()) for i in range(64))
+    # the batched result against the FP64 oracle, cloud by cloud, on the
+    # eight smallest clouds (a reduced batch the CPU finishes in seconds)
+    import oracle
+    small = sorted(range(64), key=lambda i: clouds[i].shape[1])[:8]
+    Yh, Xh = Y.double().cpu().numpy(), X.double().cpu().numpy()
+    err_or = 0.0
+    for i in small:
+        a, b = B.offsets[i], B.offsets[i + 1]
+        Yo, _ = oracle.OraclePlan(clouds[i], None, 3, 0.8, 0).action(3, 0.2, Xh[a:b])
+        err_or = max(err_or, float(np.linalg.norm(Yh[a:b] - Yo) / np.linalg.norm(Yo)))
     return {
         "metric": "batched H2 matvecs/sec (n·RHS/s), 64 clouds, one CUDA-graph launch",
         "value": N * R / (ms_graph * 1e-3), "unit": UNIT, "ms_per_step": ms_graph,
         "per_instance": {"value": N * R / (ms_each * 1e-3), "ms_per_step": ms_each,
                          "launch": "64 plans, one matvec each, back to back"},
         "speedup_graph_vs_per_instance": ms_each / ms_graph,
-        "max_rel_diff_batched_vs_single": err, "dtype": "f32", "data": "synthetic",
+        "max_rel_diff_batched_vs_single": err,
+        "max_rel_err_vs_fp64_oracle": {"value": err_or, "clouds": [int(clouds[i].shape[1])
+                                                                  for i in small]},
+        "dtype": "f32", "data": "synthetic",
+        "autotune": B.tuned_config(R),
         "config": {"workload": "C3: 64 clouds, n log-uniform [2e3, 2e5], Gaussian mixture, "
                                "GAUSSIAN l=0.2, p=3, eta=0.8, R=8, float32",
                    "total_points": int(N), "far_blocks": B.info["far_blocks"],
@@ -291,6 +309,9 @@ def run_c4(args, torch, dev):
     x64, y64 = torch.tensor(x, device=dev), torch.tensor(y, device=dev)
     x32, y32 = x64.float(), y64.float()
     ref = H.adjoint(x64, y64, precision="fp64")
+    # the adjoint uses the launch shapes a matvec of its key tuned
+    H.set_autotune(not args.no_autotune)
+    H.matvec(x32, precision="mixed")
     for _ in range(args.warmup):
         H.adjoint(x32, y32, precision="mixed")
     ms_mixed = _events_ms(torch, lambda: H.adjoint(x32, y32, precision="mixed"), args.steps)
@@ -328,7 +349,7 @@ def run_c4(args, torch, dev):
                                   "df_dsigma2": abs(v32[2] - v64[2]) / abs(v64[2]),
                                   "df_dX": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))},
         "fp64_vs_central_differences_h1e-4": {"max_rel_err": max(fd_err), "checks": fd_err},
-        "dtype": "f32", "data": "synthetic",
+        "dtype": "f32", "data": "synthetic", "autotune": H.tuned_config(1, "mixed"),
         "config": {"workload": "C4: n=2e5 on S^2, MATERN52 l=0.3 sigma2=1, p=4, eta=0.8, "
                                "leaf 96 (125 effective), x,y ~ N(0,1) float32",
                    "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"]},
@@ -354,6 +375,8 @@ def run_c5(args, torch, dev):
 
     def step(zz, prec):
         return H.adjoint(zz, zz, precision=prec, want_dX=False, want_Kx=True)
+    H.set_autotune(not args.no_autotune)
+    H.matvec(z32, precision="mixed")  # tunes the key the adjoint uses
     for _ in range(args.warmup):
         step(z32, "mixed")
     ms_mixed = _events_ms(torch, lambda: step(z32, "mixed"), args.steps)
@@ -368,6 +391,7 @@ def run_c5(args, torch, dev):
         "value": n * 64 / (ms_mixed * 1e-3), "unit": UNIT, "ms_per_step": ms_mixed,
         "fp64": {"ms_per_step": ms_fp64, "value": n * 64 / (ms_fp64 * 1e-3),
                  "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed},
+        "autotune": H.tuned_config(64, "mixed"),
         "mixed_rel_err_vs_fp64": {"Kz": kz_err,
                                   "zKz": abs(va[0] - vb[0]) / abs(vb[0]),
                                   "z_dKdl_z": abs(va[1] - vb[1]) / abs(vb[1])},
@@ -404,6 +428,8 @@ def main():
     ap.add_argument("--rhs", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="default launch shapes instead of the autotuner's")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2 (default): the headline workload; c3 batching, c4 gradients, "
                          "c5 GP step (one JSON line each, not the headline)")
@@ -437,16 +463,20 @@ def main():
     Xd = torch.tensor(X, device=dev)  # FP64, n x R row-major
     Y = torch.empty_like(Xd)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    # the autotuner measures the launch shapes on the first warm-up matvec
+    # (untimed) and every later matvec reuses them
+    H.set_autotune(not args.no_autotune)
 
     def barrier():
         torch.cuda.synchronize(dev)
         if dist is not None:
             dist.barrier()
 
-    # warm-up (also uploads the plan)
+    # warm-up (also uploads the plan and tunes)
     for _ in range(args.warmup):
         H.matvec(Xd, Y)
     barrier()
+    tuned = H.tuned_config(args.rhs)
     H.set_profiling(True)
     sampler = ClockSampler(gpu_smi_id(torch, dev))
     sampler.start()
@@ -579,7 +609,7 @@ def main():
                     "ms_per_step": e2e_ms},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "fp64_gpu": fp64,
-            "vs_fp64_oracle": vs_oracle,
+            "vs_fp64_oracle": vs_oracle, "autotune": tuned,
             "plan": {"build_s": t_plan, "far_blocks": info["far_blocks"],
                      "near_blocks": info["near_blocks"], "near_pairs": info["near_pairs"],
                      "clusters": info["row_clusters"]},

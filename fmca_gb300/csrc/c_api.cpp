@@ -71,10 +71,13 @@ gpu::KernelDesc to_desc(const fmca_kernel_desc* k) {
   return d;
 }
 
-gpu::KernelDesc to_desc(const fmca_plan* p, const fmca_kernel_desc* k) {
-  gpu::KernelDesc d = to_desc(k);
-  d.wait_ns = p->wait_ns.load();
-  return d;
+gpu::CallOpts call_opts(const fmca_plan* p) {
+  gpu::CallOpts o;
+  o.profile = p->profile.load();
+  o.wait_ns = p->wait_ns.load();
+  o.stall = p->stall.load();
+  o.autotune = p->autotune.load();
+  return o;
 }
 
 fmca_status check_matvec_args(const fmca_plan* p, const fmca_kernel_desc* kernel,
@@ -395,10 +398,10 @@ fmca_status fmca_matvec(fmca_plan* p, const fmca_kernel_desc* kernel,
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
-  st = fmca::gpu::matvec(p->plan, p->dev, to_desc(p, kernel), precision, dtype, order,
+  st = fmca::gpu::matvec(p->plan, p->dev, to_desc(kernel), precision, dtype, order,
                          nrhs, x, x_stride_i, x_stride_r, y, y_stride_i, y_stride_r,
                          workspace, workspace_bytes, (cudaStream_t)stream, &err,
-                         p->profile.load());
+                         fmca::capi::call_opts(p));
   if (st != FMCA_OK) return fail((fmca_status)st, err);
   return ok();
 }
@@ -473,10 +476,10 @@ fmca_status fmca_matvec_adjoint(fmca_plan* p, const fmca_kernel_desc* kernel, in
   std::string err;
   int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
   if (st != FMCA_OK) return fail((fmca_status)st, err);
-  st = fmca::gpu::adjoint(p->plan, p->dev, to_desc(p, kernel), precision, dtype, nrhs, x,
+  st = fmca::gpu::adjoint(p->plan, p->dev, to_desc(kernel), precision, dtype, nrhs, x,
                           x_stride_i, x_stride_r, y, y_stride_i, y_stride_r, values, dX,
                           dX_stride_i, dX_stride_d, Kx, Ky, workspace, workspace_bytes,
-                          (cudaStream_t)stream, &err, p->profile.load());
+                          (cudaStream_t)stream, &err, fmca::capi::call_opts(p));
   if (st != FMCA_OK) return fail((fmca_status)st, err);
   return ok();
 }
@@ -596,6 +599,26 @@ fmca_status fmca_plan_set_profiling(fmca_plan* p, int enable) {
 fmca_status fmca_plan_set_wait_limit(fmca_plan* p, uint64_t ns) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   p->wait_ns = ns;
+  return ok();
+}
+
+fmca_status fmca_plan_set_autotune(fmca_plan* p, int enable) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->autotune = enable != 0;
+  return ok();
+}
+
+fmca_status fmca_plan_tuned_config(fmca_plan* p, int precision, int kernel_type, int nrhs,
+                                   int32_t out[FMCA_TUNE_COUNT]) {
+  if (!p || !out) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "nrhs must be >= 1");
+  fmca::gpu::tuned_config(p->dev, precision, kernel_type, nrhs, out);
+  return ok();
+}
+
+fmca_status fmca_plan_set_stalled_wait(fmca_plan* p, int on) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->stall = on != 0;
   return ok();
 }
 

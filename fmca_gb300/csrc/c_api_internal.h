@@ -23,6 +23,9 @@ struct fmca_plan {
   std::atomic<bool> profile{false};
   // limit of the kernel sums' bounded waits in ns (0: the default of 2 s)
   std::atomic<uint64_t> wait_ns{0};
+  // test hook of fmca_plan_set_stalled_wait
+  std::atomic<int> stall{0};
+  std::atomic<bool> autotune{false};
 };
 
 namespace fmca {
@@ -34,7 +37,8 @@ fmca_status check_matvec_args(const fmca_plan* p, const fmca_kernel_desc* kernel
                               int precision, int dtype, int order, int nrhs,
                               const void* x, const void* y);
 gpu::KernelDesc to_desc(const fmca_kernel_desc* k);
-// the same with the plan's settings (wait limit)
-gpu::KernelDesc to_desc(const fmca_plan* p, const fmca_kernel_desc* k);
+// the options of a call on plan p: its settings (profiling, wait limit,
+// stalled-wait hook, autotuner)
+gpu::CallOpts call_opts(const fmca_plan* p);
 }  // namespace capi
 }  // namespace fmca

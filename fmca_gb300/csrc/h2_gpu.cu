@@ -1,5 +1,6 @@
 // Device plan and matvec driver.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -69,12 +70,50 @@ struct GroupList {
   int maxcount = 0;
 };
 
+// Launch shapes of the kernel sums (stages of the copy ring, tiles per
+// accumulation unit).
+struct UmCfg {
+  int nst, F;
+};
+// Transfer level thresholds (cluster counts): levels with fewer than
+// wide_below clusters run the sum-factorised transfer with 8 warps per
+// cluster, levels with fewer than slice_below clusters split the
+// right-hand sides over blockIdx.y in slices of 8.
+struct TrCfg {
+  int wide_below, slice_below;
+};
+// Every launch-shape choice of one matvec: the defaults (measured fastest at
+// n = 1e6, 3-D, p = 4, 32 right-hand sides) or what the autotuner measured
+// fastest on a plan for one (precision, kernel, right-hand sides) key.
+struct TuneCfg {
+  UmCfg near{um_stages(2), 2};       // near field, two target halves
+  UmCfg far_grid{um_stages(2), 2};   // far field on sibling-paired tensor grids
+  UmCfg far_nodes{um_stages(1), 1};  // far field on interpolation nodes
+  int far_pairs = 1;  // 3-D plans of degree kGridP1 - 1: paired grids (1) or nodes (0)
+  TrCfg tr{4 * 152, 2 * 152};
+  int small_tc = 0;   // mixed precision, nrhs <= 16: tensor cores (1) or FP32 CUDA cores (0)
+  int tuned = 0;      // 1 if the autotuner chose these values
+  float tune_ms = 0;  // time the tuning took
+  static TuneCfg defaults(int sms) {
+    TuneCfg c;
+    c.tr = TrCfg{4 * sms, 2 * sms};
+    return c;
+  }
+};
+
 }  // namespace
 
 struct DevPlan {
   int device = -1;
+  int sms = 152;  // multiprocessors of the device (read at upload)
   std::vector<void*> allocs;
   size_t alloc_bytes = 0;  // sum of the sizes of allocs
+  // launch shapes of the current call, and those the autotuner chose per
+  // (precision, kernel, right-hand sides) key
+  TuneCfg cfg;
+  bool autotune = false;
+  std::map<uint64_t, TuneCfg> tuned;
+  int64_t tunings = 0;  // tuning runs on this plan
   DevSet<double> d;
   DevSet<float> f;
   int* midx = nullptr;
@@ -96,7 +135,9 @@ struct DevPlan {
   void* ws = nullptr;
   size_t ws_bytes = 0;
   std::mutex mu;
-  // stage profiling: events recorded at stage boundaries of the last matvec
+  // options of the current call; stage profiling: events recorded at stage
+  // boundaries of the last matvec
+  CallOpts opts;
   bool profile = false;
   std::vector<cudaEvent_t> events;
   std::vector<int> event_stage;
@@ -456,7 +497,7 @@ size_t ws_layout(const Plan& plan, int nrhs, void* base, Workspace<T>* w) {
 }
 
 template <typename T>
-KParams<T> make_kparams(const KernelDesc& k) {
+KParams<T> make_kparams(const KernelDesc& k, const CallOpts& opts = CallOpts()) {
   KParams<T> kp;
   const double l = k.l, log2e = 1.4426950408889634;
   double a = 0, e2 = 0;
@@ -513,7 +554,8 @@ KParams<T> make_kparams(const KernelDesc& k) {
       break;
   }
   kp.g = (T)g;
-  kp.wait_ns = k.wait_ns ? k.wait_ns : kWaitLimitNs;
+  kp.wait_ns = opts.wait_ns ? opts.wait_ns : kWaitLimitNs;
+  kp.stall = opts.stall;
   return kp;
 }
 
@@ -605,19 +647,22 @@ cudaError_t launch_ksum(int rb, const GroupList& gl, const Pt4<T>* tgt,
 }
 
 // one transfer level (M2M when UP, else L2L) over the nb clusters of list.
-// A level with fewer than two clusters per SM splits the right-hand sides
-// over blockIdx.y in slices of 8, so that it still spreads over the GPU.
+// A level with fewer than tc.slice_below clusters (default: two per SM)
+// splits the right-hand sides over blockIdx.y in slices of 8, so that it
+// still spreads over the GPU; the sum-factorised kernel runs 8 warps per
+// cluster on levels with fewer than tc.wide_below clusters (default: four
+// per SM).
 template <int DIM, int P, bool UP>
 void launch_transfer_sf(int nb, const int32_t* list, const int32_t* son0,
                         const int32_t* nsons, const int32_t* parent, const float* E,
                         const int* midx, float* buf, int ld, int rofs, int rcount,
-                        cudaStream_t st) {
+                        const TrCfg& tc, cudaStream_t st) {
   constexpr int Q = DIM == 2 ? P * P : P * P * P;
   auto kern = transfer_sf_kernel<DIM, P, UP>;
   const size_t smem = (size_t)(3 * Q * 32 + Q + DIM * P * P) * sizeof(float);
   ensure_smem(kern, smem);
   // levels with few clusters: 8 warps per cluster shorten its latency chain
-  const int threads = nb < 4 * 152 ? 256 : 128;
+  const int threads = nb < tc.wide_below ? 256 : 128;
   kern<<<nb, threads, smem, st>>>(list, son0, nsons, parent, E, midx, buf, ld, rofs, rcount);
 }
 
@@ -628,12 +673,12 @@ template <bool UP>
 bool launch_transfer_sf_any(int nb, const int32_t* list, const int32_t* son0,
                             const int32_t* nsons, const int32_t* parent, const float* E,
                             const int* midx, const InterpDev<float>& ip, float* buf, int ld,
-                            int rofs, int rcount, cudaStream_t st) {
+                            int rofs, int rcount, const TrCfg& tc, cudaStream_t st) {
   if (rcount > 32) return false;
 #define FMCA_SF(D, P)                                                                    \
   case D * 16 + P:                                                                       \
     launch_transfer_sf<D, P, UP>(nb, list, son0, nsons, parent, E, midx, buf, ld, rofs, \
-                                 rcount, st);                                            \
+                                 rcount, tc, st);                                        \
     return true;
   switch (ip.dim * 16 + ip.p1) {
     FMCA_SF(2, 4)
@@ -654,12 +699,12 @@ template <typename T, int RB, bool UP>
 void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
                      const int32_t* nsons, const int32_t* parent, const T* E,
                      const int* midx, const InterpDev<T>& ip, T* buf, int ld,
-                     int rofs, int rcount, cudaStream_t st) {
+                     int rofs, int rcount, const TrCfg& tc, cudaStream_t st) {
   if (ip.kind == kInterpTotalDegree) {
     // dense E per cluster; levels with few clusters split the right-hand
     // sides in slices of 8
     const int q = ip.q;
-    if (nb < 2 * 152 && rcount > 8 && RB > 8) {
+    if (nb < tc.slice_below && rcount > 8 && RB > 8) {
       auto kern = transfer_dense_kernel<T, 8, UP>;
       const size_t smem = (dense_pad(q) + (size_t)q * 8) * sizeof(T);
       ensure_smem(kern, smem);
@@ -676,12 +721,12 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
   }
   if constexpr (std::is_same<T, float>::value && RB == 32) {
     if (launch_transfer_sf_any<UP>(nb, list, son0, nsons, parent, E, midx, ip, buf, ld, rofs,
-                                   rcount, st))
+                                   rcount, tc, st))
       return;
   }
   const size_t tail = (size_t)ip.q * sizeof(int);
   if constexpr (RB > 8) {
-    if (nb < 2 * 152 && rcount > 8) {
+    if (nb < tc.slice_below && rcount > 8) {
       constexpr int RS = 8;
       auto kern = transfer_kernel<T, RS, UP>;
       const size_t smem = (192 + kTransferChunk * RS) * sizeof(T) + tail;
@@ -745,7 +790,7 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     if (nb) {
       launch_transfer<T, RB, true>(nb, dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
                                    dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip, w.t, ld,
-                                   rofs, rcount, st);
+                                   rofs, rcount, dp->cfg.tr, st);
       ++dp->launches;
     }
   }
@@ -766,7 +811,7 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     if (nb) {
       launch_transfer<T, RB, false>(nb, dp->l2l_list + dp->l2l_ptr[l], nullptr, nullptr,
                                     dp->parent_r, S.E_r, dp->midx, S.ip, w.s, ld, rofs,
-                                    rcount, st);
+                                    rcount, dp->cfg.tr, st);
       ++dp->launches;
     }
   }
@@ -854,13 +899,13 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
   }
   dp->reset_marks();
   dp->mark(-1, st);
-  const KParams<T> kp = make_kparams<T>(k);
+  const KParams<T> kp = make_kparams<T>(k, dp->opts);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
   const uint32_t* pr = order == FMCA_ORDER_NATURAL ? dp->perm_r : nullptr;
   const int nthr = 256;
   auto blocks = [&](int64_t total) {
     int64_t b = (total + nthr - 1) / nthr;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)dp->sms * 32));
   };
   if (dtype == FMCA_DTYPE_F64)
     gather_kernel<double, T><<<blocks((int64_t)plan.cols.n * ld * nchunks_for(nrhs)), nthr, 0,
@@ -954,26 +999,33 @@ size_t tc_ws_layout(const Plan& plan, int nrhs, void* base, TcWorkspace* w) {
 
 // kernels whose values lie in [0, 1] (the FP16 split needs a bounded range):
 // the six covariance kernels and l * dk/dl of the first four
-bool tc_supported(int type, int nrhs) {
-  const bool bounded = (type >= FMCA_KERNEL_EXPONENTIAL && type <= FMCA_KERNEL_MATERN92) ||
-                       (type >= K_DL_EXPONENTIAL && type <= K_DL_GAUSSIAN);
-  return bounded && nrhs > 16;
+// fewer than 17 right-hand sides take the CUDA-core FP32 path unless the
+// autotuner found the tensor-core path (columns padded to 32) faster
+bool tc_bounded(int type) {
+  return (type >= FMCA_KERNEL_EXPONENTIAL && type <= FMCA_KERNEL_MATERN92) ||
+         (type >= K_DL_EXPONENTIAL && type <= K_DL_GAUSSIAN);
+}
+bool tc_supported(int type, int nrhs, int small_tc) {
+  return tc_bounded(type) && (nrhs > 16 || small_tc);
 }
 
 // Tensor-core kernel sum over a group list: H target halves of 128 per
 // CTA (groups of up to 128 H targets). q > 0: the sources are
 // interpolation nodes (q per cluster) weighted by their cluster's moment
 // exponent; q = 0: points of weight 1. grid: nodes on tensor grids
-// (tscale_grid_kernel layout).
+// (tscale_grid_kernel layout). uc: stages and tiles per accumulation unit.
+
 template <int KT, int H, bool REL, bool GRID>
 cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
-                        const KParams<float>& kp, int q, int* errf, cudaStream_t st) {
+                        const KParams<float>& kp, int q, int* errf, cudaStream_t st,
+                        const UmCfg& uc) {
   auto kern = ksum_um_kernel<KT, H, REL, GRID>;
-  const size_t smem = um_smem_bytes(H);
+  const size_t smem = um_smem_bytes(H, kUmMaxStages);
   ensure_smem(kern, smem);
-  kern<<<gl.ngroups, kUmThreads, smem, st>>>(gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs,
-                                             rcount, kp, q, errf, gl.imask);
+  kern<<<gl.ngroups, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
+      gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf, gl.imask, uc.nst,
+      uc.F);
   return cudaGetLastError();
 }
 
@@ -981,22 +1033,26 @@ template <int KT, int H>
 cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        bool grid) {
+                        bool grid, const UmCfg& uc) {
   if constexpr (H == 2) {  // tensor grids: sibling row clusters as the two halves
     if (grid)
-      return launch_um_v<KT, 2, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
+      return launch_um_v<KT, 2, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st,
+                                            uc);
   }
   if (q > 0)
-    return launch_um_v<KT, H, true, false>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st);
-  return launch_um_v<KT, H, false, false>(gl, tgt, pairs, vals, out, rcount, kp, 0, errf, st);
+    return launch_um_v<KT, H, true, false>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st,
+                                           uc);
+  return launch_um_v<KT, H, false, false>(gl, tgt, pairs, vals, out, rcount, kp, 0, errf, st,
+                                          uc);
 }
 
 template <int H>
 cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        bool grid) {
-#define FMCA_UM(KT) launch_um_t<KT, H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid)
+                        bool grid, const UmCfg& uc) {
+#define FMCA_UM(KT) \
+  launch_um_t<KT, H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc)
   switch (kp.type) {
     case 0:
       return FMCA_UM(0);
@@ -1021,19 +1077,155 @@ cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4
 }
 
 // grid: the far field of a 3-D plan of degree kGridP1 - 1 (sources in the
-// tscale_grid_kernel layout)
+// tscale_grid_kernel layout). uc is checked here: 2 <= nst <= kUmMaxStages,
+// 1 <= F <= min(kUmMaxUnit, nst) (a unit's tiles must fit in the ring).
 template <int H>
 cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                       const __half* vals, float* out, int rcount,
                       const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                      bool grid = false) {
+                      bool grid, const UmCfg& uc) {
   if (gl.ngroups == 0) return cudaSuccess;
-  return launch_um_k<H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid);
+  if (uc.nst < 2 || uc.nst > kUmMaxStages || uc.F < 1 || uc.F > kUmMaxUnit || uc.F > uc.nst)
+    return cudaErrorInvalidValue;
+  return launch_um_k<H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc);
 }
 
 bool grid_far(const Plan& plan) {
   return plan.interp.kind == kInterpTensor && plan.interp.dim == 3 &&
          plan.interp.deg + 1 == kGridP1;
+}
+
+// The stages of one right-hand-side chunk (32 columns) of the mixed
+// precision matvec, each callable on its own (the autotuner times them one
+// by one with different launch shapes).  Every stage records its event and
+// counts its launches.
+struct TcChunk {
+  const Plan* plan;
+  DevPlan* dp;
+  DevSet<float>* S;
+  KParams<float> kp;
+  int rcount, q, Cc, Cr;
+  int64_t npc;
+  float *xc, *t, *s, *yfar, *ynear;
+  const __half* xv;
+  TcWorkspace w;
+  cudaStream_t st;
+
+  cudaError_t leafmom() {
+    constexpr int RB = kTcRhs;
+    auto kern = leafmom_kernel<float, RB>;
+    const size_t smem = leafmom_smem<float, RB>(q);
+    ensure_smem(kern, smem);
+    if (dp->nleaves_c) {
+      kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
+                                             S->bbmin_c, S->bbext_c, S->pts_c, xc, kTcRhs, 0,
+                                             rcount, dp->midx, S->ip, t);
+      ++dp->launches;
+    }
+    dp->mark(FMCA_STAGE_LEAFMOM, st);
+    return cudaGetLastError();
+  }
+  cudaError_t m2m(const TrCfg& tr) {
+    for (int l = plan->cols.nlevels() - 1; l >= 0; --l) {
+      const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
+      if (nb) {
+        launch_transfer<float, kTcRhs, true>(nb, dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
+                                             dp->nsons_c, nullptr, S->E_c, dp->midx, S->ip, t,
+                                             kTcRhs, 0, rcount, tr, st);
+        ++dp->launches;
+      }
+    }
+    dp->launches +=
+        launch_basis_change<float, kTcRhs>(S->ip, Cc, S->to_nodal, t, kTcRhs, 0, rcount, st);
+    dp->mark(FMCA_STAGE_M2M, st);
+    return cudaGetLastError();
+  }
+  // far field: moments scaled into the FP16 value layout, then the kernel
+  // sum, on the sibling-paired tensor grids (3-D plans of degree
+  // kGridP1 - 1, unless cfg.far_pairs is 0) or on interpolation nodes
+  cudaError_t far(const TuneCfg& cfg) {
+    const bool grid = grid_far(*plan) && cfg.far_pairs;
+    if (grid)
+      tscale_grid_kernel<<<Cc, 128, 0, st>>>(Cc, rcount, t, S->nodes_c, dp->midx, kp.g, w.tv,
+                                              reinterpret_cast<float*>(w.pairs_n));
+    else
+      tscale_kernel<<<Cc, 128, 0, st>>>(Cc, q, rcount, t, S->nodes_c, kp.g, w.tv,
+                                         reinterpret_cast<float*>(w.pairs_n));
+    ++dp->launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const GroupList& fl = grid ? dp->far_grid2 : dp->far_tc;
+    e = grid ? launch_um<2>(fl, S->nodes_r, w.pairs_n, w.tv, s, rcount, kp, q, dp->err_flag, st,
+                            true, cfg.far_grid)
+             : launch_um<1>(fl, S->nodes_r, w.pairs_n, w.tv, s, rcount, kp, q, dp->err_flag, st,
+                            false, cfg.far_nodes);
+    if (e != cudaSuccess) return e;
+    dp->launches += fl.ngroups ? 1 : 0;
+    dp->launches +=
+        launch_basis_change<float, kTcRhs>(S->ip, Cr, S->from_nodal, s, kTcRhs, 0, rcount, st);
+    dp->mark(FMCA_STAGE_FAR, st);
+    return cudaGetLastError();
+  }
+  cudaError_t l2l(const TrCfg& tr) {
+    for (int l = 1; l < plan->rows.nlevels(); ++l) {
+      const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
+      if (nb) {
+        launch_transfer<float, kTcRhs, false>(nb, dp->l2l_list + dp->l2l_ptr[l], nullptr,
+                                              nullptr, dp->parent_r, S->E_r, dp->midx, S->ip, s,
+                                              kTcRhs, 0, rcount, tr, st);
+        ++dp->launches;
+      }
+    }
+    dp->mark(FMCA_STAGE_L2L, st);
+    return cudaGetLastError();
+  }
+  cudaError_t leafgather() {
+    constexpr int RB = kTcRhs;
+    auto kern = leafgather_kernel<float, RB>;
+    const size_t smem = leafgather_smem<float, RB>(q);
+    ensure_smem(kern, smem);
+    if (dp->nleaves_r) {
+      kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
+                                             S->bbmin_r, S->bbext_r, S->pts_r, s, kTcRhs, 0,
+                                             rcount, dp->midx, S->ip, yfar);
+      ++dp->launches;
+    }
+    dp->mark(FMCA_STAGE_LEAFGATHER, st);
+    return cudaGetLastError();
+  }
+  cudaError_t near(const UmCfg& uc) {
+    cudaError_t e = launch_um<2>(dp->near, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0,
+                                 dp->err_flag, st, false, uc);
+    dp->launches += dp->near.ngroups ? 1 : 0;
+    dp->mark(FMCA_STAGE_NEAR, st);
+    return e;
+  }
+};
+
+TcChunk tc_chunk(const Plan& plan, DevPlan* dp, DevSet<float>& S, const TcWorkspace& w,
+                 const KParams<float>& kp, int nrhs, int ch, cudaStream_t st) {
+  const int RB = kTcRhs, ld = kTcRhs;
+  const int64_t nc = plan.cols.n, nr = plan.rows.n;
+  const size_t q = plan.interp.q;
+  TcChunk c;
+  c.plan = &plan;
+  c.dp = dp;
+  c.S = &S;
+  c.kp = kp;
+  c.rcount = std::min(RB, nrhs - ch * RB);
+  c.q = (int)q;
+  c.Cc = plan.cols.nclusters();
+  c.Cr = plan.rows.nclusters();
+  c.npc = (int64_t)um_padded(nc);
+  c.xc = w.xc + (size_t)ch * nc * ld;
+  c.t = w.t + (size_t)ch * c.Cc * q * ld;
+  c.s = w.s + (size_t)ch * c.Cr * q * ld;
+  c.yfar = w.yfar + (size_t)ch * nr * ld;
+  c.ynear = w.ynear + (size_t)ch * nr * ld;
+  c.xv = w.xv + (size_t)ch * c.npc * ld * 2;
+  c.w = w;
+  c.st = st;
+  return c;
 }
 
 int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc& k,
@@ -1057,13 +1249,13 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   }
   dp->reset_marks();
   dp->mark(-1, st);
-  const KParams<float> kp = make_kparams<float>(k);
+  const KParams<float> kp = make_kparams<float>(k, dp->opts);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
   const uint32_t* pr = order == FMCA_ORDER_NATURAL ? dp->perm_r : nullptr;
   const int nthr = 256;
   auto blocks = [&](int64_t total) {
     int64_t b = (total + nthr - 1) / nthr;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)dp->sms * 32));
   };
   const int64_t nc = plan.cols.n, nr = plan.rows.n;
   const int nch = (nrhs + RB - 1) / RB;
@@ -1073,10 +1265,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     const int ncol = std::min(kColChunk, nrhs - c0);
     const size_t smem = sizeof(unsigned int) * ncol;
     if (dtype == FMCA_DTYPE_F64)
-      colmax_kernel<double><<<152 * 4, nthr, smem, st>>>(
+      colmax_kernel<double><<<dp->sms * 4, nthr, smem, st>>>(
           nc, c0, ncol, static_cast<const double*>(x), sxi, sxr, w.cmax);
     else
-      colmax_kernel<float><<<152 * 4, nthr, smem, st>>>(
+      colmax_kernel<float><<<dp->sms * 4, nthr, smem, st>>>(
           nc, c0, ncol, static_cast<const float*>(x), sxi, sxr, w.cmax);
     ++dp->launches;
   }
@@ -1092,81 +1284,14 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   FMCA_CK(cudaGetLastError());
   dp->launches += 2;
   dp->mark(FMCA_STAGE_GATHER, st);
-  const size_t q = plan.interp.q;
-  const int Cc = plan.cols.nclusters(), Cr = plan.rows.nclusters();
   for (int ch = 0; ch < nch; ++ch) {
-    const int rcount = std::min(RB, nrhs - ch * RB);
-    float* xc = w.xc + (size_t)ch * nc * ld;
-    float* t = w.t + (size_t)ch * Cc * q * ld;
-    float* s = w.s + (size_t)ch * Cr * q * ld;
-    float* yfar = w.yfar + (size_t)ch * nr * ld;
-    {
-      auto kern = leafmom_kernel<float, RB>;
-      const size_t smem = leafmom_smem<float, RB>((int)q);
-      ensure_smem(kern, smem);
-      if (dp->nleaves_c) {
-        kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
-                                               S.bbmin_c, S.bbext_c, S.pts_c, xc, ld, 0,
-                                               rcount, dp->midx, S.ip, t);
-        ++dp->launches;
-      }
-      dp->mark(FMCA_STAGE_LEAFMOM, st);
-    }
-    for (int l = plan.cols.nlevels() - 1; l >= 0; --l) {
-      const int nb = dp->m2m_ptr[l + 1] - dp->m2m_ptr[l];
-      if (nb) {
-        launch_transfer<float, RB, true>(nb, dp->m2m_list + dp->m2m_ptr[l], dp->son0_c,
-                                         dp->nsons_c, nullptr, S.E_c, dp->midx, S.ip, t, ld,
-                                         0, rcount, st);
-        ++dp->launches;
-      }
-    }
-    dp->launches += launch_basis_change<float, RB>(S.ip, Cc, S.to_nodal, t, ld, 0, rcount, st);
-    dp->mark(FMCA_STAGE_M2M, st);
-    const bool grid = grid_far(plan);
-    if (grid)
-      tscale_grid_kernel<<<Cc, 128, 0, st>>>(Cc, rcount, t, S.nodes_c, dp->midx, kp.g, w.tv,
-                                              reinterpret_cast<float*>(w.pairs_n));
-    else
-      tscale_kernel<<<Cc, 128, 0, st>>>(Cc, (int)q, rcount, t, S.nodes_c, kp.g, w.tv,
-                                         reinterpret_cast<float*>(w.pairs_n));
-    ++dp->launches;
-    const GroupList& fl = grid ? dp->far_grid2 : dp->far_tc;
-    if (grid)
-      FMCA_CK(launch_um<2>(fl, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q, dp->err_flag, st,
-                           true));
-    else
-      FMCA_CK(launch_um<1>(fl, S.nodes_r, w.pairs_n, w.tv, s, rcount, kp, (int)q, dp->err_flag, st));
-    dp->launches += fl.ngroups ? 1 : 0;
-    dp->launches += launch_basis_change<float, RB>(S.ip, Cr, S.from_nodal, s, ld, 0, rcount, st);
-    dp->mark(FMCA_STAGE_FAR, st);
-    for (int l = 1; l < plan.rows.nlevels(); ++l) {
-      const int nb = dp->l2l_ptr[l + 1] - dp->l2l_ptr[l];
-      if (nb) {
-        launch_transfer<float, RB, false>(nb, dp->l2l_list + dp->l2l_ptr[l], nullptr,
-                                          nullptr, dp->parent_r, S.E_r, dp->midx, S.ip, s,
-                                          ld, 0, rcount, st);
-        ++dp->launches;
-      }
-    }
-    dp->mark(FMCA_STAGE_L2L, st);
-    {
-      auto kern = leafgather_kernel<float, RB>;
-      const size_t smem = leafgather_smem<float, RB>((int)q);
-      ensure_smem(kern, smem);
-      if (dp->nleaves_r) {
-        kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
-                                               S.bbmin_r, S.bbext_r, S.pts_r, s, ld, 0,
-                                               rcount, dp->midx, S.ip, yfar);
-        ++dp->launches;
-      }
-      dp->mark(FMCA_STAGE_LEAFGATHER, st);
-    }
-    FMCA_CK(launch_um<2>(dp->near, S.pts_r, w.pairs_c, w.xv + (size_t)ch * npc * ld * 2,
-                         w.ynear + (size_t)ch * nr * ld, rcount,
-                         kp, 0, dp->err_flag, st));
-    dp->launches += dp->near.ngroups ? 1 : 0;
-    dp->mark(FMCA_STAGE_NEAR, st);
+    TcChunk c = tc_chunk(plan, dp, S, w, kp, nrhs, ch, st);
+    FMCA_CK(c.leafmom());
+    FMCA_CK(c.m2m(dp->cfg.tr));
+    FMCA_CK(c.far(dp->cfg));
+    FMCA_CK(c.l2l(dp->cfg.tr));
+    FMCA_CK(c.leafgather());
+    FMCA_CK(c.near(dp->cfg.near));
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_scaled_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
@@ -1189,6 +1314,11 @@ int upload(const Plan& plan, int precision, DevPlan** dev, std::string* err) {
   if (!dp) {
     dp = new DevPlan();
     dp->device = cur;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur) == cudaSuccess &&
+        sms > 0)
+      dp->sms = sms;
+    dp->cfg = TuneCfg::defaults(dp->sms);
     int s = upload_common(plan, dp, err);
     if (s != FMCA_OK) {
       destroy(dp);
@@ -1223,26 +1353,231 @@ size_t workspace_bytes(const Plan& plan, int precision, int nrhs) {
   return std::max(f, tc_ws_layout(plan, nrhs, nullptr, nullptr));
 }
 
+namespace {
+
+uint64_t tune_key(int precision, int type, int nrhs) {
+  return (uint64_t)precision | ((uint64_t)type << 8) | ((uint64_t)std::min(nrhs, 33) << 16);
+}
+
+// the cached launch shapes of a key, or the defaults
+TuneCfg config_for(const DevPlan* dp, int precision, int type, int nrhs) {
+  auto it = dp->tuned.find(tune_key(precision, type, nrhs));
+  return it != dp->tuned.end() ? it->second : TuneCfg::defaults(dp->sms);
+}
+
+bool stream_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return true;
+  return cs != cudaStreamCaptureStatusNone;
+}
+
+// The autotuner: measures the launch shapes of the mixed-precision matvec on
+// this plan with CUDA events on the caller's stream and keeps the fastest in
+// dp->cfg.  Steps (each trial timed twice, the faster counts):
+//  1. fewer than 17 right-hand sides: one whole matvec on the FP32 CUDA
+//     cores against one on the tensor cores (columns padded to 32);
+//  2. on the tensor-core path, after one matvec with the defaults has
+//     filled the workspace, the stages of the first right-hand-side chunk
+//     one by one: the near-field kernel sum over stage counts 4..7 and
+//     units of 1..3 tiles; the far field (moment scaling + kernel sum) on
+//     paired tensor grids (stages 4..6, units 1..3) and on nodes (stages
+//     5..7, units 1..2); the upward and downward transfer passes over the
+//     level thresholds {0, 2, 4, 8} x SMs (8 warps per cluster) and
+//     {0, 1, 2, 4} x SMs (right-hand-side slices).
+// The trials overwrite the workspace; the caller runs the real matvec with
+// the chosen shapes afterwards.  Other precisions keep the defaults.
+int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int dtype,
+         int order, int nrhs, const void* x, int64_t sxi, int64_t sxr, void* y, int64_t syi,
+         int64_t syr, void* ws, size_t wsb, cudaStream_t st, std::string* err) {
+  const auto t_begin = std::chrono::steady_clock::now();
+  TuneCfg best = TuneCfg::defaults(dp->sms);
+  dp->cfg = best;
+  if (precision == FMCA_PREC_MIXED && tc_bounded(k.type)) {
+    cudaEvent_t e0, e1;
+    FMCA_CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      *err = "cudaEventCreate failed";
+      return FMCA_ERR_CUDA;
+    }
+    const bool prof = dp->profile;
+    dp->profile = false;  // no stage events inside the trials
+    int status = FMCA_OK;
+    // fastest of two runs of fn (ms); negative on a failure
+    auto timed = [&](auto&& fn) -> float {
+      float bestms = -1.f;
+      for (int r = 0; r < 2; ++r) {
+        if (cudaEventRecord(e0, st) != cudaSuccess) return -1.f;
+        if (fn() != FMCA_OK) return -1.f;
+        float ms = 0.f;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+          return -1.f;
+        if (bestms < 0.f || ms < bestms) bestms = ms;
+      }
+      return bestms;
+    };
+    auto run_tc = [&]() {
+      return matvec_tc(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi, syr, ws, wsb,
+                       st, err);
+    };
+    auto run_cc = [&]() {
+      return matvec_t<float>(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi, syr,
+                             ws, wsb, st, err);
+    };
+    auto ok_cuda = [](cudaError_t e) { return e == cudaSuccess ? FMCA_OK : FMCA_ERR_CUDA; };
+    bool use_tc = nrhs > 16;
+    if (!use_tc) {
+      dp->cfg.small_tc = 0;
+      const float t_cc = timed(run_cc);
+      dp->cfg.small_tc = 1;
+      const float t_tc = timed(run_tc);
+      if (t_cc < 0.f || t_tc < 0.f) status = FMCA_ERR_CUDA;
+      use_tc = t_tc < t_cc;
+      best.small_tc = use_tc ? 1 : 0;
+    }
+    if (status == FMCA_OK && use_tc) {
+      dp->cfg = best;
+      status = run_tc();
+      if (status == FMCA_OK) {
+        TcWorkspace w;
+        tc_ws_layout(plan, nrhs, ws ? ws : dp->ws, &w);
+        TcChunk c = tc_chunk(plan, dp, dp->f, w, make_kparams<float>(k, dp->opts), nrhs, 0, st);
+        float bt = -1.f;
+        for (int nst = 4; nst <= kUmMaxStages && status == FMCA_OK; ++nst)
+          for (int F = 1; F <= kUmMaxUnit; ++F) {
+            const UmCfg uc{nst, F};
+            const float ms = timed([&]() { return ok_cuda(c.near(uc)); });
+            if (ms < 0.f) {
+              status = FMCA_ERR_CUDA;
+              break;
+            }
+            if (bt < 0.f || ms < bt) {
+              bt = ms;
+              best.near = uc;
+            }
+          }
+        bt = -1.f;
+        const bool grid = grid_far(plan);
+        for (int pairs = grid ? 1 : 0; pairs >= 0 && status == FMCA_OK; --pairs)
+          for (int nst = pairs ? 4 : 5; nst <= (pairs ? 6 : 7); ++nst)
+            for (int F = 1; F <= (pairs ? 3 : 2); ++F) {
+              TuneCfg cand = best;
+              cand.far_pairs = pairs;
+              (pairs ? cand.far_grid : cand.far_nodes) = UmCfg{nst, F};
+              const float ms = timed([&]() { return ok_cuda(c.far(cand)); });
+              if (ms < 0.f) {
+                status = FMCA_ERR_CUDA;
+                break;
+              }
+              if (bt < 0.f || ms < bt) {
+                bt = ms;
+                best.far_pairs = cand.far_pairs;
+                best.far_grid = cand.far_grid;
+                best.far_nodes = cand.far_nodes;
+              }
+            }
+        bt = -1.f;
+        for (int wide : {0, 2, 4, 8})
+          for (int slice : {0, 1, 2, 4}) {
+            if (status != FMCA_OK) break;
+            const TrCfg tr{wide * dp->sms, slice * dp->sms};
+            const float ms = timed([&]() {
+              cudaError_t e = c.m2m(tr);
+              return ok_cuda(e == cudaSuccess ? c.l2l(tr) : e);
+            });
+            if (ms < 0.f) {
+              status = FMCA_ERR_CUDA;
+              break;
+            }
+            if (bt < 0.f || ms < bt) {
+              bt = ms;
+              best.tr = tr;
+            }
+          }
+      }
+    }
+    dp->profile = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != FMCA_OK) {
+      if (err->empty()) *err = std::string("autotuner: ") + cudaGetErrorString(cudaGetLastError());
+      return status;
+    }
+  }
+  best.tuned = 1;
+  best.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() -
+                                                          t_begin).count();
+  dp->tuned[tune_key(precision, k.type, nrhs)] = best;
+  ++dp->tunings;
+  dp->cfg = best;
+  return FMCA_OK;
+}
+
+// sets the call's options and launch shapes (tuning them first if the
+// autotuner is on and this key has none yet, outside stream captures)
+int prepare_call(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int dtype,
+                 int order, int nrhs, const void* x, int64_t sxi, int64_t sxr, void* y,
+                 int64_t syi, int64_t syr, void* ws, size_t wsb, cudaStream_t st,
+                 std::string* err, const CallOpts& opts, bool may_tune) {
+  dp->opts = opts;
+  dp->profile = opts.profile;
+  dp->cfg = config_for(dp, precision, k.type, nrhs);
+  if (may_tune && opts.autotune && !dp->cfg.tuned && !stream_capturing(st))
+    return tune(plan, dp, k, precision, dtype, order, nrhs, x, sxi, sxr, y, syi, syr, ws, wsb,
+                st, err);
+  return FMCA_OK;
+}
+
+}  // namespace
+
 int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
            int dtype, int order, int nrhs, const void* x, int64_t sxi,
            int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-           size_t ws_bytes, cudaStream_t st, std::string* err, bool profile) {
+           size_t ws_bytes, cudaStream_t st, std::string* err, const CallOpts& opts) {
   std::lock_guard<std::mutex> lock(dp->mu);
-  dp->profile = profile;
+  FMCA_TRY(prepare_call(plan, dp, k, precision, dtype, order, nrhs, x, sxi, sxr, y, syi, syr,
+                        ws, ws_bytes, st, err, opts, true));
   if (precision == FMCA_PREC_FP64)
     return matvec_t<double>(plan, dp, dp->d, k, dtype, order, nrhs, x, sxi, sxr, y,
                             syi, syr, ws, ws_bytes, st, err);
-  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs))
+  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs, dp->cfg.small_tc))
     return matvec_tc(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi, syr, ws,
                      ws_bytes, st, err);
   return matvec_t<float>(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi,
                          syr, ws, ws_bytes, st, err);
 }
 
+void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) {
+  for (int i = 0; i < FMCA_TUNE_COUNT; ++i) out[i] = 0;
+  TuneCfg c = TuneCfg::defaults(dp ? dp->sms : 152);
+  if (dp) {
+    std::lock_guard<std::mutex> lock(dp->mu);
+    c = config_for(dp, precision, type, nrhs);
+    out[FMCA_TUNE_TUNINGS] = (int32_t)dp->tunings;
+  }
+  const bool pairs = c.far_pairs != 0;
+  out[FMCA_TUNE_TUNED] = c.tuned;
+  out[FMCA_TUNE_NEAR_STAGES] = c.near.nst;
+  out[FMCA_TUNE_NEAR_UNIT] = c.near.F;
+  out[FMCA_TUNE_FAR_PAIRS] = c.far_pairs;
+  out[FMCA_TUNE_FAR_GRID_STAGES] = c.far_grid.nst;
+  out[FMCA_TUNE_FAR_GRID_UNIT] = c.far_grid.F;
+  out[FMCA_TUNE_FAR_NODE_STAGES] = c.far_nodes.nst;
+  out[FMCA_TUNE_FAR_NODE_UNIT] = c.far_nodes.F;
+  out[FMCA_TUNE_WIDE_BELOW] = c.tr.wide_below;
+  out[FMCA_TUNE_SLICE_BELOW] = c.tr.slice_below;
+  out[FMCA_TUNE_SMALL_R_TENSOR] = c.small_tc;
+  out[FMCA_TUNE_US] = (int32_t)(c.tune_ms * 1000.f);
+  (void)pairs;
+}
+
 // ---------------------------------------------------------------------------
 // adjoint
 namespace {
 
+// blocks of the dot-product reduction (its partial sums live in the
+// workspace, so the count is fixed: 4 per SM of a 152-SM GB300)
 constexpr int kDotBlocks = 152 * 4;
 
 // z (contiguous n_r x R column-major, dtype of x) = K x
@@ -1253,7 +1588,7 @@ int matvec_state(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precisi
   if (precision == FMCA_PREC_FP64)
     return matvec_t<double>(plan, dp, dp->d, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr,
                             z, 1, nr, ws, wsb, st, err, state);
-  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs))
+  if (precision == FMCA_PREC_MIXED && tc_supported(k.type, nrhs, dp->cfg.small_tc))
     return matvec_tc(plan, dp, dp->f, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr, z, 1, nr,
                      ws, wsb, st, err, state);
   return matvec_t<float>(plan, dp, dp->f, k, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr, z,
@@ -1407,9 +1742,12 @@ size_t adjoint_workspace_bytes(const Plan& plan, int precision, int nrhs) {
 int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int dtype,
             int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
             int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx, void* Ky,
-            void* ws, size_t wsb, cudaStream_t st, std::string* err, bool profile) {
+            void* ws, size_t wsb, cudaStream_t st, std::string* err, const CallOpts& opts) {
   std::lock_guard<std::mutex> lock(dp->mu);
-  dp->profile = profile;
+  // launch shapes: those tuned for this key by matvecs, if any (the adjoint
+  // does not tune)
+  FMCA_TRY(prepare_call(plan, dp, k, precision, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr,
+                        nullptr, 0, 0, ws, wsb, st, err, opts, false));
   const bool base_kernel = k.type >= FMCA_KERNEL_EXPONENTIAL && k.type <= FMCA_KERNEL_GAUSSIAN;
   if ((dX || Ky) && !plan.same_tree) {
     *err = "gradients w.r.t. the points and K^T y need one point cloud (Pr == Pc)";
@@ -1429,7 +1767,7 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
   const int nthr = 256;
   auto blocks = [&](int64_t total) {
     int64_t b = (total + nthr - 1) / nthr;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)dp->sms * 32));
   };
   MatvecState A, B;
   // z = K x with unit variance; f = sigma2 * y . z, df/dsigma2 = y . z
@@ -1549,7 +1887,11 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
   FMCA_CK(cudaMemcpy(dr, PR, sizeof(double) * dim * nr, cudaMemcpyHostToDevice));
   FMCA_CK(cudaMemcpy(dc, PC, sizeof(double) * dim * nc, cudaMemcpyHostToDevice));
   const KParams<double> kp = make_kparams<double>(k);
-  dense_eval_kernel<<<152 * 16, 256>>>(dim, dr, nr, dc, nc, kp, output_scale(k), dout);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 152;
+  dense_eval_kernel<<<sms * 16, 256>>>(dim, dr, nr, dc, nc, kp, output_scale(k), dout);
   FMCA_CK(cudaGetLastError());
   FMCA_CK(cudaMemcpy(out, dout, sizeof(double) * nr * nc, cudaMemcpyDeviceToHost));
   cudaFree(dr);

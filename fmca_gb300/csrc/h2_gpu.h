@@ -17,20 +17,25 @@ struct DevPlan;
 struct KernelDesc {
   int type;
   double l, c, nu, sigma2;
-  // limit of every bounded wait of the kernel sums in ns (0: the default)
-  uint64_t wait_ns = 0;
 };
 
-// status codes are the fmca_status values of include/fmca_gb300.h.
-// profile: record stage events for fmca_plan_profile during this call (set
-// on the device plan under its mutex, so concurrent calls do not race on it)
+// Options of one call, set on the device plan under its mutex (so that
+// concurrent calls on one plan do not race on them).
+struct CallOpts {
+  bool profile = false;  // stage events for fmca_plan_profile
+  uint64_t wait_ns = 0;  // limit of the kernel sums' bounded waits (0: 2 s)
+  int stall = 0;         // test hook: the kernel sums' first wait runs out
+  bool autotune = false; // tune launch shapes on the first call of a key
+};
+
+// status codes are the fmca_status values of include/fmca_gb300.h
 int upload(const Plan& plan, int precision, DevPlan** dev, std::string* err);
 void destroy(DevPlan* dev);
 size_t workspace_bytes(const Plan& plan, int precision, int nrhs);
 int matvec(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision,
            int dtype, int order, int nrhs, const void* x, int64_t sxi,
            int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
-           size_t ws_bytes, cudaStream_t stream, std::string* err, bool profile);
+           size_t ws_bytes, cudaStream_t stream, std::string* err, const CallOpts& opts);
 int check_device_error(DevPlan* dev, std::string* err);
 int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
                const double* PC, int64_t nc, double* out, std::string* err);
@@ -44,7 +49,10 @@ int adjoint(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision, 
             int nrhs, const void* x, int64_t sxi, int64_t sxr, const void* y, int64_t syi,
             int64_t syr, double* values, void* dX, int64_t sdi, int64_t sdd, void* Kx,
             void* Ky, void* ws, size_t ws_bytes, cudaStream_t stream, std::string* err,
-            bool profile);
+            const CallOpts& opts);
+// Launch shapes for (precision, kernel type, nrhs): out[FMCA_TUNE_*] (see
+// include/fmca_gb300.h); the defaults if the autotuner has not run for it.
+void tuned_config(DevPlan* dev, int precision, int type, int nrhs, int32_t* out);
 // re-uploads the point coordinates held by the plan (tree and boxes fixed)
 int update_points(const Plan& plan, DevPlan* dev, std::string* err);
 // true if the plan's device data for this precision lives on the current

@@ -62,6 +62,9 @@ struct KParams {
   T il;  // 1 / l
   T g;   // coordinate scale of the tensor-core path (1 for generic kernels)
   unsigned long long wait_ns;  // limit of the kernel sums' bounded waits
+  // test hook (fmca_plan_set_stalled_wait): the first wait of every
+  // kernel-sum CTA is on a barrier that nothing completes, so it runs out
+  int stall;
 };
 
 // kind 0: Chebyshev tensor product (Lagrange factors from xi, w); kind 1:
@@ -376,8 +379,11 @@ __global__ void ksum_kernel(const KGroup* __restrict__ groups,
   for (int i = g.ivl_begin; i < g.ivl_end; ++i)
     ntiles += (int)((ivl[2 * i + 1] - ivl[2 * i] + TS - 1) / TS);
 
+  // a barrier nothing arrives on (the stalled-wait test hook waits on it)
+  uint64_t* never = reinterpret_cast<uint64_t*>(smem_raw + 64);
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    mbar_init(never, 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -411,7 +417,8 @@ __global__ void ksum_kernel(const KGroup* __restrict__ groups,
   for (int k = 0; k < ntiles; ++k) {
     const int stage = k % STAGES;
     const uint32_t parity = (uint32_t)((k / STAGES) & 1);
-    const bool ok = mbar_wait_bounded(&bars[stage], parity, kp.wait_ns);
+    const bool ok =
+        mbar_wait_bounded((kp.stall && k == 0) ? never : &bars[stage], parity, kp.wait_ns);
     if (ok) {
       const int cnt = scnt[stage];
       const Pt4<T>* P = spts + stage * TS;

@@ -90,13 +90,17 @@ extern "C" fmca_status fmca_matvec_static_scratch(
   void* scratch = nullptr;
   s = scratch_address(&scratch);
   if (s != FMCA_OK) return s;
-  // no stage events (profile = false): they would be created, that is
-  // allocated, on first use
+  // no stage events (they would be created, that is allocated, on first
+  // use) and no tuning (its events are allocated too): the launch shapes
+  // tuned earlier for this key by fmca_matvec, if any, else the defaults
+  fmca::gpu::CallOpts opts = fmca::capi::call_opts(p);
+  opts.profile = false;
+  opts.autotune = false;
   std::string err;
-  const int st = fmca::gpu::matvec(p->plan, p->dev, fmca::capi::to_desc(p, kernel), precision,
+  const int st = fmca::gpu::matvec(p->plan, p->dev, fmca::capi::to_desc(kernel), precision,
                                    dtype, order, nrhs, x, x_stride_i, x_stride_r, y,
                                    y_stride_i, y_stride_r, scratch, kStaticScratchBytes,
-                                   (cudaStream_t)stream, &err, false);
+                                   (cudaStream_t)stream, &err, opts);
   if (st != FMCA_OK) return fmca::capi::fail((fmca_status)st, err);
   return FMCA_OK;
 }

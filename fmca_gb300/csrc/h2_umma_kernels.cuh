@@ -74,14 +74,18 @@ constexpr int kUmThreads = 32 * (3 + 4 * kUmSets + kUmFlushWarps);
 // floats per target row of the running total: 32 columns and a pad of 4,
 // so that a quarter warp's 16-byte accesses to 8 rows hit 32 banks
 constexpr int kUmTotStride = kTcRhs + 4;
-// stages, and the shared memory of a CTA: header, stages, running total
-// [target][column]. Either size leaves no room for a second CTA on the SM,
-// which matters as each CTA allocates all 512 tensor-memory columns.
+// stages (a launch parameter from 2 to kUmMaxStages; the defaults were the
+// fastest at n = 1e6), and the shared memory of a CTA: header, stages,
+// running total [target][column]. Every size leaves no room for a second
+// CTA on the SM, which matters as each CTA allocates all 512 tensor-memory
+// columns.
+constexpr int kUmMaxStages = 7;
 __host__ __device__ constexpr int um_stages(int H) { return H == 2 ? 5 : 6; }
-__host__ __device__ constexpr size_t um_smem_bytes(int H) {
-  return kUmHeader + (size_t)um_stages(H) * kUmStageBytes +
-         (size_t)128 * H * kUmTotStride * sizeof(float);
+__host__ __device__ constexpr size_t um_smem_bytes(int H, int nst) {
+  return kUmHeader + (size_t)nst * kUmStageBytes + (size_t)128 * H * kUmTotStride * sizeof(float);
 }
+// tiles per accumulation unit: at most 3 (4 starved the stage ring)
+constexpr int kUmMaxUnit = 3;
 constexpr uint32_t kUmCols = 512;
 
 __device__ __forceinline__ void mbar_expect_tx_only(uint64_t* bar, uint32_t bytes) {
@@ -204,18 +208,21 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // exponent, else points of weight 1; GRID (with REL, H = 1, 3-D, q =
 // kGridP1^3): every tile is one source cluster on its tensor grid
 // (tscale_grid_kernel layout; `pairs` holds the clusters' 64-byte grid-line
-// records). F: tiles per accumulation unit (the tensor cores accumulate F
-// tiles before a flush adds them into a running total): 2 on tensor grids
-// and with two target halves. 256 sources per flush made the far field 5 %
-// and the near field 2 % faster, and the far field's rounding error 1.5x
-// larger (5e-7 relative at n = 1e6, measured against FP64).
-template <int KT, int H, bool REL, bool GRID, int F = ((GRID || H == 2) ? 2 : 1)>
+// records). nst: stages of the ring (2 .. kUmMaxStages). F: tiles per
+// accumulation unit (1 .. min(kUmMaxUnit, nst); the tensor cores
+// accumulate F tiles before a flush adds them into a running total): 2 by
+// default on tensor grids and with two target halves. 256 sources per flush
+// made the far field 5 % and the near field 2 % faster, and the far field's
+// rounding error 1.5x larger (5e-7 relative at n = 1e6, measured against
+// FP64). Both are chosen per plan by the autotuner when it is enabled.
+template <int KT, int H, bool REL, bool GRID>
 __global__ void __launch_bounds__(kUmThreads, 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
                    const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
-                   KParams<float> kp, int q, int* err, const uint32_t* __restrict__ imask) {
-  constexpr int NST = um_stages(H);
+                   KParams<float> kp, int q, int* err, const uint32_t* __restrict__ imask,
+                   int nst, int F) {
+  const int NST = nst;
   constexpr int NSETS = kUmSets, NEVAL = 4 * NSETS;
   constexpr int NT = 128 * H;  // targets of a group
   // tensor-memory columns: accumulators [buffer][thread] x 64 (0..31: the
@@ -232,7 +239,6 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // every half is one row cluster of q nodes; imask[interval] holds the
   // halves a source cluster serves)
   const int HS = GRID ? q : 128;
-  static_assert(F >= 1 && F <= NST, "accumulation unit: at most the stage ring");
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -247,10 +253,12 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   uint64_t* accf = aempty + NPS;                             // [4]
   uint64_t* acce = accf + 4;                                 // [2]
   uint64_t* done = acce + 2;                                 // [2]
-  static_assert(8 * (2 * NST + 2 * NPS + 4 + 2 + 2) <= 512, "barrier area");
+  uint64_t* never = done + 2;  // nothing arrives (the stalled-wait test hook)
+  static_assert(8 * (2 * kUmMaxStages + 2 * NPS + 4 + 2 + 2 + 1) <= 512, "barrier area");
+  static_assert(528 + 16 * kUmMaxStages <= 640, "stage masks");
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 512);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 516);
-  uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 528);  // [NST][4]
+  uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 528);  // [kUmMaxStages][4]
   float* ered = reinterpret_cast<float*>(smem_raw + 640);          // [NEVAL][H]
   unsigned char* stages = smem_raw + kUmHeader;
   float* tot = reinterpret_cast<float*>(stages + (size_t)NST * kUmStageBytes);
@@ -275,7 +283,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // and the totals; the proxy fence orders these writes before the copies
   {
     uint4* z = reinterpret_cast<uint4*>(stages);
-    const int n16 = (int)((um_smem_bytes(H) - kUmHeader) / 16);
+    const int n16 = (int)((um_smem_bytes(H, NST) - kUmHeader) / 16);
     for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -292,6 +300,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     for (int b = 0; b < 2; ++b) mbar_init(&acce[b], 4);
     mbar_init(&done[0], 1);
     mbar_init(&done[1], 1);
+    mbar_init(never, 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -310,8 +319,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       int pi = g.ivl_begin;
       uint32_t pos = 0xffffffffu;  // next source inside interval pi (none yet)
       int issued = 0;
-      bool ok = true;
-      for (int k = 0; k < ntiles; ++k) {
+      bool ok = !kp.stall || um_wait(never, 0, abort_flag, wlim);
+      for (int k = 0; k < ntiles && ok; ++k) {
         const int stage = k % NST;
         if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag, wlim)) {
           ok = false;

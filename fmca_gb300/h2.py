@@ -438,6 +438,25 @@ class H2Matrix:
         following matvecs (fmca_plan_set_wait_limit); 0: the default 2 s."""
         check(_lib.load().fmca_plan_set_wait_limit(self._h, int(ns)))
 
+    def set_autotune(self, enable: bool = True) -> None:
+        """Autotuner on or off (fmca_plan_set_autotune): the first
+        mixed-precision matvec of each (precision, kernel, nrhs) key measures
+        the launch shapes and later calls of that key reuse the fastest."""
+        check(_lib.load().fmca_plan_set_autotune(self._h, 1 if enable else 0))
+
+    def tuned_config(self, nrhs: int, precision: Optional[str] = None, cov=None) -> dict:
+        """Launch shapes a matvec of this key uses now (fmca_plan_tuned_config)."""
+        cov = cov or self.cov
+        out = (C.c_int32 * len(_lib.TUNE_KEYS))()
+        check(_lib.load().fmca_plan_tuned_config(self._h, _PREC[precision or self.precision],
+                                                 cov.desc().type, int(nrhs), out))
+        return dict(zip(_lib.TUNE_KEYS, [int(v) for v in out]))
+
+    def set_stalled_wait(self, on: bool) -> None:
+        """Test hook (fmca_plan_set_stalled_wait): while on, the first wait of
+        every kernel-sum CTA runs out after the wait limit."""
+        check(_lib.load().fmca_plan_set_stalled_wait(self._h, 1 if on else 0))
+
     def device_bytes(self) -> int:
         """Device memory the plan holds now (fmca_plan_device_bytes)."""
         n = C.c_size_t(0)

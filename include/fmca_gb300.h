@@ -325,9 +325,56 @@ fmca_status fmca_plan_check_device_error(fmca_plan* plan);
    error flag (FMCA_ERR_TIMEOUT from fmca_plan_check_device_error), drains
    its own copies and tensor-core products under a fixed limit, frees its
    tensor memory and returns; the results of that call are undefined and
-   the GPU context stays usable.  A short limit is how a test makes a wait
-   run out.  No counterpart in the reference (which has no GPU waits). */
+   the GPU context stays usable.  No counterpart in the reference (which has no GPU waits). */
 fmca_status fmca_plan_set_wait_limit(fmca_plan* plan, uint64_t ns);
+/* Test hook for the timeout path (no reference counterpart): while on,
+   the first wait of every kernel-sum CTA of this plan's matvecs is on a
+   barrier that nothing completes, so it runs out after the wait limit and
+   the call ends with FMCA_ERR_TIMEOUT as described above, without a GPU
+   fault.  Off by default; results of calls made while it is on are
+   undefined. */
+fmca_status fmca_plan_set_stalled_wait(fmca_plan* plan, int on);
+
+/* Autotuner (no counterpart in the reference, whose column-bucket loop,
+   H2MatrixBase.h:127-148, has no launch shapes to choose).  While enabled,
+   the first mixed-precision matvec of each (precision, kernel type, nrhs)
+   key on this plan measures the launch shapes below with CUDA events on the
+   caller's stream and keeps the fastest for every later call of that key:
+     - nrhs <= 16: FP32 CUDA-core kernel sums, or tensor-core kernel sums
+       with the right-hand sides padded to 32 columns;
+     - the near-field kernel sum's copy-ring stages (4..7) and tiles per
+       accumulation unit (1..3);
+     - the far field on sibling-paired tensor grids or on interpolation
+       nodes (3-D plans of degree 4), with its stages and units;
+     - the transfer passes' level thresholds for 8 warps per cluster and
+       for splitting the right-hand sides into slices of 8.
+   That first call takes longer (about 20 kernel-sum runs) and gives the
+   same result as a call with the chosen shapes.  Calls made inside a CUDA
+   stream capture, adjoints and FP64 / FP32 matvecs do not tune (they use the
+   tuned shapes of their key if there are any, else the defaults).  Off by
+   default. */
+fmca_status fmca_plan_set_autotune(fmca_plan* plan, int enable);
+/* Indices of fmca_plan_tuned_config's output. */
+enum {
+  FMCA_TUNE_TUNED = 0,            /* 1: chosen by the autotuner, 0: defaults */
+  FMCA_TUNE_NEAR_STAGES = 1,      /* near field: copy-ring stages */
+  FMCA_TUNE_NEAR_UNIT = 2,        /* near field: tiles per accumulation unit */
+  FMCA_TUNE_FAR_PAIRS = 3,        /* 1: paired tensor grids, 0: nodes */
+  FMCA_TUNE_FAR_GRID_STAGES = 4,  /* far field on paired grids: stages */
+  FMCA_TUNE_FAR_GRID_UNIT = 5,    /*   and tiles per unit */
+  FMCA_TUNE_FAR_NODE_STAGES = 6,  /* far field on nodes: stages */
+  FMCA_TUNE_FAR_NODE_UNIT = 7,    /*   and tiles per unit */
+  FMCA_TUNE_WIDE_BELOW = 8,       /* transfer levels with fewer clusters: 8 warps each */
+  FMCA_TUNE_SLICE_BELOW = 9,      /* transfer levels with fewer clusters: RHS slices of 8 */
+  FMCA_TUNE_SMALL_R_TENSOR = 10,  /* nrhs <= 16: 1 tensor cores, 0 CUDA cores */
+  FMCA_TUNE_US = 11,              /* time the tuning took, microseconds */
+  FMCA_TUNE_TUNINGS = 12,         /* tuning runs on this plan so far */
+  FMCA_TUNE_COUNT = 13
+};
+/* The launch shapes a matvec of this key uses now: the tuned ones, or the
+   defaults (FMCA_TUNE_TUNED = 0). */
+fmca_status fmca_plan_tuned_config(fmca_plan* plan, int precision, int kernel_type, int nrhs,
+                                   int32_t out[FMCA_TUNE_COUNT]);
 
 /* Stages of one matvec, indices of fmca_plan_profile's output. */
 enum {

@@ -205,3 +205,19 @@ def test_model_detects_a_ring_of_partial_tiles():
     # share a slot while the sets run a tile apart
     bad = [simulate(n, 2, s, NPS=3) for s in range(40) for n in (5, 9)]
     assert "early" in bad
+
+
+# the launch shapes the autotuner may choose: 2..7 stages, units of 1..3
+# tiles (at most the stage count), one or two target halves
+SHAPES = [(H, NST, F) for H in (1, 2) for NST in range(2, 8) for F in (1, 2, 3) if F <= NST]
+
+
+@pytest.mark.parametrize("H,NST,F", SHAPES)
+def test_protocol_over_tuned_launch_shapes(H, NST, F):
+    for seed in range(12):
+        for ntiles in (1, 2, 3, 5, 8, 13, 21):
+            assert simulate(ntiles, H, seed, F=F, NST=NST) == "ok", (ntiles, seed)
+    for b in ({"done": 0.05}, {0: 50.0, "done": 0.1}, {4: 0.05}, {3: 20.0, "done": 0.2}):
+        for seed in range(6):
+            rnd = BiasedRandom(seed, b)
+            assert simulate(13, H, seed, F=F, NST=NST, rnd=rnd) == "ok", (b, seed)

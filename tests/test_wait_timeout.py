@@ -1,13 +1,15 @@
 """Bounded waits running out on the GPU, without a fault.
 
 Every wait of the kernel sums (near and far field, tensor-core and CUDA-core
-versions) is bounded.  fmca_plan_set_wait_limit shortens that bound to 1 ns
-for one matvec, so the waits give up at their first unfinished test: the
-kernels raise the plan's error flag, drain their own copies and products
-under their fixed drain limit, free tensor memory and return.  The test
-checks that the host reads FMCA_ERR_TIMEOUT from
-fmca_plan_check_device_error, and that the next matvec with the default
-limit, on the same plan and GPU context, again equals the FP64 oracle."""
+versions) is bounded.  For one matvec the test shortens that bound to 1 ms
+(fmca_plan_set_wait_limit) and turns on the stalled-wait hook
+(fmca_plan_set_stalled_wait): the first wait of every kernel-sum CTA is then
+on a barrier that nothing completes.  The kernels raise the plan's error
+flag, drain their own copies and products under their fixed drain limit,
+free tensor memory and return.  The test checks that the host reads
+FMCA_ERR_TIMEOUT from fmca_plan_check_device_error, and that the next
+matvecs with the default limit, on the same plan and GPU context, again
+equal the FP64 oracle."""
 from __future__ import annotations
 
 import numpy as np
@@ -33,12 +35,14 @@ def test_wait_limit_runs_out_and_the_context_stays_usable(cuda_device, prec):
     x = torch.tensor(X, device=cuda_device)
     H.matvec(x)
     H.check_device_error()
-    H.set_wait_limit(1)
+    H.set_wait_limit(1_000_000)
+    H.set_stalled_wait(True)
     H.matvec(x)
     with pytest.raises(FmcaError) as e:
         H.check_device_error()
     assert e.value.status == ERR["FMCA_ERR_TIMEOUT"]
     H.check_device_error()  # the flag was cleared
+    H.set_stalled_wait(False)
     H.set_wait_limit(0)
     for _ in range(2):
         Y = H.matvec(x)
