@@ -52,7 +52,7 @@ EXPORTED = [
     "fmca_graph_destroy", "fmca_plan_create_ex", "fmca_plan_interpolator",
     "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets", "fmca_plan_device_bytes",
     "fmca_plan_set_wait_limit", "fmca_plan_set_stalled_wait", "fmca_plan_set_autotune",
-    "fmca_plan_tuned_config",
+    "fmca_plan_tuned_config", "fmca_plan_create_gpu",
 ]
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
@@ -95,6 +95,8 @@ def load() -> C.CDLL:
                                      C.POINTER(vp)]
     lib.fmca_plan_create_ex.argtypes = [dp, i32, i64, dp, i64, i32, i32, C.c_double, i64,
                                         C.POINTER(vp)]
+    lib.fmca_plan_create_gpu.argtypes = [dp, i32, i64, dp, i64, i32, i32, C.c_double, i64,
+                                         C.POINTER(C.c_int), C.POINTER(vp)]
     lib.fmca_plan_interpolator.argtypes = [vp, dp, dp]
     lib.fmca_plan_save.argtypes = [vp, C.c_char_p]
     lib.fmca_plan_load.argtypes = [C.c_char_p, C.POINTER(vp)]

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <new>
 #include <string>
 #include <thread>
@@ -123,9 +124,12 @@ fmca_status fmca_plan_create(const double* P_rows, int dim, int64_t n_rows,
                              FMCA_INTERP_TENSOR_PRODUCT, degree, eta, min_leaf, out);
 }
 
-fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
-                                const double* P_cols, int64_t n_cols, int interpolator,
-                                int degree, double eta, int64_t min_leaf, fmca_plan** out) {
+namespace {
+// fmca_plan_create_ex, with the trees' level sorts on `sorter` if given
+fmca_status create_plan(const double* P_rows, int dim, int64_t n_rows, const double* P_cols,
+                        int64_t n_cols, int interpolator, int degree, double eta,
+                        int64_t min_leaf, fmca::LevelSorter* sorter, int* sorted_elsewhere,
+                        fmca_plan** out) {
   if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!P_rows) return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows is NULL");
@@ -161,7 +165,9 @@ fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
     p->plan.build(P_rows, (uint32_t)n_rows, same ? P_rows : P_cols,
                   (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same,
                   interpolator == FMCA_INTERP_TOTAL_DEGREE ? fmca::kInterpTotalDegree
-                                                           : fmca::kInterpTensor);
+                                                           : fmca::kInterpTensor,
+                  sorter);
+    if (sorted_elsewhere) *sorted_elsewhere = p->plan.trees_sorted_elsewhere;
     *out = p;
   } catch (const std::bad_alloc&) {
     return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
@@ -169,6 +175,24 @@ fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
     return fail(FMCA_ERR_INTERNAL, e.what());
   }
   return ok();
+}
+}  // namespace
+
+fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
+                                const double* P_cols, int64_t n_cols, int interpolator,
+                                int degree, double eta, int64_t min_leaf, fmca_plan** out) {
+  return create_plan(P_rows, dim, n_rows, P_cols, n_cols, interpolator, degree, eta, min_leaf,
+                     nullptr, nullptr, out);
+}
+
+fmca_status fmca_plan_create_gpu(const double* P_rows, int dim, int64_t n_rows,
+                                 const double* P_cols, int64_t n_cols, int interpolator,
+                                 int degree, double eta, int64_t min_leaf, int* trees_on_gpu,
+                                 fmca_plan** out) {
+  if (trees_on_gpu) *trees_on_gpu = 0;
+  std::unique_ptr<fmca::LevelSorter> sorter = fmca::gpu::make_gpu_level_sorter();
+  return create_plan(P_rows, dim, n_rows, P_cols, n_cols, interpolator, degree, eta, min_leaf,
+                     sorter.get(), trees_on_gpu, out);
 }
 
 fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_points,

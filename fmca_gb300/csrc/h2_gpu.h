@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <string>
 
 #include "h2_plan.h"
@@ -61,6 +62,10 @@ bool resident(const DevPlan* dev, int precision);
 // device bytes the plan holds: uploaded data plus the workspace it owns
 size_t device_bytes(const DevPlan* dev);
 int profile(DevPlan* dev, double* stage_ms, int64_t* launches, std::string* err);
+// The level sorter of Tree::build_with on the current device
+// (h2_tree_gpu.cu): every level of a cluster tree as one segmented radix
+// sort.
+std::unique_ptr<LevelSorter> make_gpu_level_sorter();
 
 }  // namespace gpu
 }  // namespace fmca

@@ -303,16 +303,21 @@ struct TreeBuilder {
   // range along the longest edge of its (propagated) box and halves it.
   // Reads nodes[me] and writes only its own index range and sons, so nodes
   // of one level split concurrently. False: the node is a leaf.
+  // longest edge of a (propagated) box, first maximum
+  int longest_edge(const TmpNode& f) const {
+    int longest = 0;
+    for (int d = 1; d < dim; ++d)
+      if (f.bb[2 * dim + d] > f.bb[2 * dim + longest]) longest = d;
+    return longest;
+  }
+
   bool split(int me, TmpNode* sons) const {
     const TmpNode& f = nodes[me];
     if (f.size <= split_threshold) return false;
     TmpNode s0 = f, s1 = f;
     s0.level = s1.level = f.level + 1;
     s0.nsons = s1.nsons = 0;
-    // longest edge of the (propagated) father box, first maximum
-    int longest = 0;
-    for (int d = 1; d < dim; ++d)
-      if (s0.bb[2 * dim + d] > s0.bb[2 * dim + longest]) longest = d;
+    const int longest = longest_edge(f);
     // std::sort of the index range by the coordinate, done on (coordinate,
     // index) records: the algorithm makes the same comparisons and moves
     // whatever the element type, so the index order is that of sorting the
@@ -392,6 +397,54 @@ struct TreeBuilder {
     }
   }
 
+  // refine_all with every level's sorts done by a LevelSorter: the same
+  // splits (a sorted range is unique when its coordinates are distinct),
+  // the son boxes from the coordinates the sorter returns at the split.
+  // false: a sorted range held equal coordinates, or the sorter failed.
+  bool refine_with(LevelSorter* so) {
+    std::vector<int> cur{0};
+    std::vector<SortSegment> segs;
+    std::vector<int> who;
+    std::vector<double> cut;
+    while (!cur.empty()) {
+      segs.clear();
+      who.clear();
+      for (int c : cur) {
+        const TmpNode& f = nodes[c];
+        if (f.size <= split_threshold) continue;
+        segs.push_back(SortSegment{f.begin, f.size, longest_edge(f)});
+        who.push_back(c);
+      }
+      if (segs.empty()) break;
+      bool ties = false;
+      if (!so->sort_level(segs, &cut, &ties) || ties) return false;
+      std::vector<int> nxt;
+      for (size_t i = 0; i < who.size(); ++i) {
+        const int longest = segs[i].coord;
+        TmpNode s0 = nodes[who[i]], s1 = nodes[who[i]];
+        s0.level = s1.level = nodes[who[i]].level + 1;
+        s0.nsons = s1.nsons = 0;
+        s0.size /= 2;
+        s1.size -= s0.size;
+        s1.begin += s0.size;
+        s0.bb[dim + longest] = cut[2 * i];
+        s0.bb[2 * dim + longest] = s0.bb[dim + longest] - s0.bb[longest];
+        s1.bb[longest] = cut[2 * i + 1];
+        s1.bb[2 * dim + longest] = s1.bb[dim + longest] - s1.bb[longest];
+        const int i0 = (int)nodes.size();
+        nodes.push_back(std::move(s0));
+        nodes.push_back(std::move(s1));
+        nodes[who[i]].sons[0] = i0;
+        nodes[who[i]].sons[1] = i0 + 1;
+        nodes[who[i]].nsons = 2;
+        nxt.push_back(i0);
+        nxt.push_back(i0 + 1);
+      }
+      cur.swap(nxt);
+    }
+    return so->finish(idx);
+  }
+
   // shrinkToFit_impl (ClusterTreeInitializer_ClusterTree.h:88-132)
   void shrink(int me) {
     std::vector<double> bb(3 * dim);
@@ -433,18 +486,18 @@ struct TreeBuilder {
     nodes[me].bb = std::move(bb);
   }
 };
-}  // namespace
 
-void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize, int threads) {
-  dim = dim_;
-  n = n_;
-  perm.resize(n);
-  std::iota(perm.begin(), perm.end(), 0u);
-  TreeBuilder tb;
-  tb.P = P;
-  tb.dim = dim;
-  tb.split_threshold = min_csize >= 1 ? (2 * min_csize - 1) : 1;
-  tb.idx = &perm;
+// init_BoundingBox_impl and the root of the refinement
+void start_builder(TreeBuilder* tb, Tree* t, const double* P, int dim, uint32_t n,
+                   uint32_t min_csize) {
+  t->dim = dim;
+  t->n = n;
+  t->perm.resize(n);
+  std::iota(t->perm.begin(), t->perm.end(), 0u);
+  tb->P = P;
+  tb->dim = dim;
+  tb->split_threshold = min_csize >= 1 ? (2 * min_csize - 1) : 1;
+  tb->idx = &t->perm;
   TmpNode root;
   root.begin = 0;
   root.size = n;
@@ -464,10 +517,23 @@ void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize, int
     root.bb[dim + d] = hi;
     root.bb[2 * dim + d] = hi - lo;
   }
-  tb.nodes.reserve(2 * (n / std::max<uint32_t>(1, min_csize)) + 8);
-  tb.nodes.push_back(std::move(root));
-  if (threads <= 0) threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  tb.refine_all(threads);
+  tb->nodes.reserve(2 * (n / std::max<uint32_t>(1, min_csize)) + 8);
+  tb->nodes.push_back(std::move(root));
+}
+
+// shrinkToFit and the level-order numbering of a refined tree
+void finish_tree(TreeBuilder& tb, Tree* t) {
+  const int dim = t->dim;
+  std::vector<uint32_t>& begin = t->begin;
+  std::vector<uint32_t>& size = t->size;
+  std::vector<int32_t>& level = t->level;
+  std::vector<int32_t>& parent = t->parent;
+  std::vector<int32_t>& son0 = t->son0;
+  std::vector<int32_t>& nsons = t->nsons;
+  std::vector<double>& bbmin = t->bbmin;
+  std::vector<double>& bbmax = t->bbmax;
+  std::vector<double>& bbext = t->bbext;
+  std::vector<int32_t>& level_ptr = t->level_ptr;
   tb.shrink(0);
   // level-order numbering (IDDFSForwardIterator): breadth first, sons in order
   const int C = (int)tb.nodes.size();
@@ -510,6 +576,27 @@ void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize, int
   for (int i = 0; i < C; ++i) level_ptr[level[i] + 1] = i + 1;
   for (int l = 1; l <= maxlev + 1; ++l)
     level_ptr[l] = std::max(level_ptr[l], level_ptr[l - 1]);
+}
+}  // namespace
+
+void Tree::build(const double* P, int dim_, uint32_t n_, uint32_t min_csize, int threads) {
+  TreeBuilder tb;
+  start_builder(&tb, this, P, dim_, n_, min_csize);
+  if (threads <= 0) threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  tb.refine_all(threads);
+  finish_tree(tb, this);
+}
+
+bool Tree::build_with(LevelSorter* sorter, const double* P, int dim_, uint32_t n_,
+                      uint32_t min_csize) {
+  TreeBuilder tb;
+  start_builder(&tb, this, P, dim_, n_, min_csize);
+  if (!sorter->start(P, dim_, n_) || !tb.refine_with(sorter)) {
+    *this = Tree();
+    return false;
+  }
+  finish_tree(tb, this);
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -617,7 +704,7 @@ Adm compare(const Tree& r, int i, const Tree& c, int j, double eta) {
 
 void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
                  int dim, int deg, double eta_, uint32_t min_leaf, bool same,
-                 int interp_kind) {
+                 int interp_kind, LevelSorter* sorter) {
   interp.init(dim, deg, interp_kind);
   eta = eta_;
   points_r.assign(Pr, Pr + (size_t)dim * nr);
@@ -628,11 +715,20 @@ void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
   same_tree = same;
   const uint32_t mincsize =
       min_leaf > (uint32_t)interp.q ? min_leaf : (uint32_t)interp.q;
-  rows.build(Pr, dim, nr, mincsize, build_threads);
+  // trees: level sorts on the sorter when one is given, else (and when a
+  // sorted range holds equal coordinates) on the host
+  trees_sorted_elsewhere = 0;
+  auto make_tree = [&](Tree* t, const double* P, uint32_t n) {
+    if (sorter && t->build_with(sorter, P, dim, n, mincsize))
+      ++trees_sorted_elsewhere;
+    else
+      t->build(P, dim, n, mincsize, build_threads);
+  };
+  make_tree(&rows, Pr, nr);
   if (same)
     cols = rows;
   else
-    cols.build(Pc, dim, nc, mincsize, build_threads);
+    make_tree(&cols, Pc, nc);
   compute_transfer_factors(rows, interp, &row_E);
   compute_node_coords(rows, interp, &row_nodes);
   if (same) {

@@ -89,6 +89,31 @@ struct Interp {
   void poly(const double* u, double* out) const;
 };
 
+// The splits of one tree level done elsewhere (the GPU level sorter of
+// h2_tree_gpu.cu): every segment is the index range of one cluster that
+// splits, sorted by one coordinate.
+struct SortSegment {
+  uint32_t begin, size;
+  int coord;
+};
+class LevelSorter {
+ public:
+  virtual ~LevelSorter() {}
+  // Uploads the points (dim x n, natural order) and the identity
+  // permutation; false on failure.
+  virtual bool start(const double* P, int dim, uint32_t n) = 0;
+  // Sorts every segment's range of the permutation by its coordinate
+  // (ascending) and returns per segment the coordinates at offsets
+  // size / 2 - 1 and size / 2 of the sorted range (split[2 s], split[2 s +
+  // 1]). *ties: some segment holds equal coordinates (whose order the
+  // reference's std::sort decides); the result is then not used.  false on
+  // failure.
+  virtual bool sort_level(const std::vector<SortSegment>& segs, std::vector<double>* split,
+                          bool* ties) = 0;
+  // Copies the permutation back; false on failure.
+  virtual bool finish(std::vector<uint32_t>* perm) = 0;
+};
+
 // Cluster tree in level order.  Cluster c owns cluster-ordered points
 // [begin[c], begin[c] + size[c]); perm maps cluster order to natural order
 // (ClusterTreeBase::indices()).
@@ -107,6 +132,11 @@ struct Tree {
   // one level split on up to `threads` host threads (0: one per core, at
   // most 16); the result does not depend on the thread count.
   void build(const double* P, int dim, uint32_t n, uint32_t min_csize, int threads = 0);
+  // The same tree with every level's sorts done by `sorter` (one call per
+  // level). Returns false, leaving the tree empty, when a sorted range held
+  // equal coordinates or the sorter failed: the caller then builds on the
+  // host, where std::sort orders equal keys as the reference does.
+  bool build_with(LevelSorter* sorter, const double* P, int dim, uint32_t n, uint32_t min_csize);
 };
 
 // Row-owned block lists.
@@ -140,7 +170,10 @@ struct Plan {
 
   void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
              int dim, int deg, double eta, uint32_t min_leaf, bool same,
-             int interp_kind = kInterpTensor);
+             int interp_kind = kInterpTensor, LevelSorter* sorter = nullptr);
+  // trees whose sorts ran on the sorter (0, 1 or 2); the others were built
+  // on the host
+  int trees_sorted_elsewhere = 0;
   int build_threads = 0;  // host threads of the tree builds (0: one per core)
   // Block-diagonal plan of independent point clouds: trees, bases and block
   // lists of the parts concatenated (cluster ids, point indices and node

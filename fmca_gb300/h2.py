@@ -77,15 +77,17 @@ class H2Matrix:
     Mirrors pyH2Matrix(ker, Pr, Pc, p=3, eta=0.8) (py/FMCA.cpp:209-220).
     Keywords: ``min_leaf`` (minimum cluster size; the effective value is
     max(min_leaf, q) like H2ClusterTree::init), ``precision`` ("fp64",
-    "fp32" or "mixed"; the default of ``action``) and ``interpolator``
+    "fp32" or "mixed"; the default of ``action``), ``interpolator``
     ("tensor": Chebyshev tensor product, q = (p+1)^dim; "total_degree":
     TotalDegreeInterpolator, q = binom(p+dim, dim), as the reference module
-    builds it). ``fmca_gb300.FMCA`` gives the reference module's defaults.
+    builds it) and ``build`` ("host", or "gpu": the cluster trees' sorts on
+    the current CUDA device, fmca_plan_create_gpu, the same plan;
+    ``trees_on_gpu`` tells how many trees were sorted there). ``fmca_gb300.FMCA`` gives the reference module's defaults.
     """
 
     def __init__(self, cov: CovarianceKernel, Pr, Pc=None, p: int = 3,
                  eta: float = 0.8, min_leaf: int = 0, precision: str = "mixed",
-                 interpolator: str = "tensor"):
+                 interpolator: str = "tensor", build: str = "host"):
         lib = _lib.load()
         self.cov = cov
         self.p = int(p)
@@ -109,9 +111,19 @@ class H2Matrix:
         handle = C.c_void_p()
         Pcp = None if same else _dptr(Pc)
         nc = Pr.shape[1] if same else Pc.shape[1]
-        check(lib.fmca_plan_create_ex(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
-                                      _lib.INTERPOLATORS[interpolator], self.p, self.eta,
-                                      int(min_leaf), C.byref(handle)))
+        if build == "host":
+            check(lib.fmca_plan_create_ex(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
+                                          _lib.INTERPOLATORS[interpolator], self.p, self.eta,
+                                          int(min_leaf), C.byref(handle)))
+            self.trees_on_gpu = 0
+        elif build == "gpu":
+            ng = C.c_int(0)
+            check(lib.fmca_plan_create_gpu(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
+                                           _lib.INTERPOLATORS[interpolator], self.p, self.eta,
+                                           int(min_leaf), C.byref(ng), C.byref(handle)))
+            self.trees_on_gpu = ng.value
+        else:
+            raise ValueError("build must be 'host' or 'gpu'")
         self._h = handle
         info = (C.c_int64 * _lib.INFO_COUNT)()
         check(lib.fmca_plan_info(self._h, info))
