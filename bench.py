@@ -225,6 +225,23 @@ def _events_ms(torch, fn, steps, flush=None):
     return sum(times) / len(times)
 
 
+def plan_build_on_gpu(H, P, p, eta, leaf, dev):
+    """The same plan with the cluster tree sorted on the GPU
+    (fmca_plan_create_gpu): its build time (two runs, the second counts; the
+    first warms up the device) and whether it equals the host-built plan."""
+    import torch
+    from fmca_gb300 import H2Matrix
+    torch.cuda.synchronize(dev)
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        G = H2Matrix(H.cov, P, P, p, eta, min_leaf=leaf, precision="mixed", build="gpu")
+        times.append(time.perf_counter() - t0)
+    same = (G.info == H.info and np.array_equal(G.rindices(), H.rindices()) and
+            all(np.array_equal(a, b) for k in (0, 1) for a, b in zip(G.blocks(k), H.blocks(k))))
+    return {"build_s": times[-1], "trees_on_gpu": G.trees_on_gpu, "equals_host_plan": bool(same)}
+
+
 def run_c3(args, torch, dev):
     """Batching: 64 clouds, n log-uniform in [2e3, 2e5], 3-D Gaussian mixture
     (8 components, sigma 0.05, centres U[0,1]^3 per cloud), GAUSSIAN l = 0.2,
@@ -370,6 +387,7 @@ def run_c5(args, torch, dev):
     t0 = time.perf_counter()
     H = H2Matrix(CovarianceKernel("EXPONENTIAL", 0.1), P, P, 5, 0.6, min_leaf=128)
     t_plan = time.perf_counter() - t0
+    gpu_build = plan_build_on_gpu(H, P, 5, 0.6, 128, dev)
     z32 = torch.tensor(z, dtype=torch.float32, device=dev)
     z64 = z32.double()
 
@@ -399,7 +417,7 @@ def run_c5(args, torch, dev):
         "config": {"workload": "C5: n=2e6 in [0,4]x[0,1], EXPONENTIAL l=0.1, p=5 (q=36), "
                                "eta=0.6, leaf 128, 64 Rademacher probes",
                    "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"],
-                   "plan_build_s": t_plan},
+                   "plan_build_s": t_plan, "gpu_tree_build": gpu_build},
     }
 
 
@@ -460,6 +478,7 @@ def main():
                  precision="mixed")
     t_plan = time.perf_counter() - t0
     info = H.info
+    gpu_build = plan_build_on_gpu(H, P, 4, 0.8, 128, dev)
     Xd = torch.tensor(X, device=dev)  # FP64, n x R row-major
     Y = torch.empty_like(Xd)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -610,7 +629,8 @@ def main():
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "fp64_gpu": fp64,
             "vs_fp64_oracle": vs_oracle, "autotune": tuned,
-            "plan": {"build_s": t_plan, "far_blocks": info["far_blocks"],
+            "plan": {"build_s": t_plan, "gpu_tree_build": gpu_build,
+                     "far_blocks": info["far_blocks"],
                      "near_blocks": info["near_blocks"], "near_pairs": info["near_pairs"],
                      "clusters": info["row_clusters"]},
         }

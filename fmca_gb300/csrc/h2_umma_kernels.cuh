@@ -320,9 +320,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       uint32_t pos = 0xffffffffu;  // next source inside interval pi (none yet)
       int issued = 0;
       bool ok = !kp.stall || um_wait(never, 0, abort_flag, wlim);
+      // ring position of tile k: stage = k % NST, phase = (k / NST) & 1,
+      // kept as counters (NST is a launch parameter; no divisions per tile)
+      int stage = -1;
+      uint32_t ph = 1;
       for (int k = 0; k < ntiles && ok; ++k) {
-        const int stage = k % NST;
-        if (k >= NST && !um_wait(&empty[stage], (uint32_t)((k / NST - 1) & 1), abort_flag, wlim)) {
+        if (++stage == NST) stage = 0;
+        if (stage == 0) ph ^= 1u;
+        if (k >= NST && !um_wait(&empty[stage], ph ^ 1u, abort_flag, wlim)) {
           ok = false;
           break;
         }
@@ -394,10 +399,20 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     if (lane == 0) {
       bool ok = true;
       const int h = H == 2 ? j : 0;
+      // ring position (stage, ph) and accumulation unit (u, tile kin of
+      // the unit) of tile k, kept as counters
+      int stage = -1, u = 0, kin = -1;
+      uint32_t ph = 1;
       for (int k = 0; k < ntiles && ok; ++k) {
-        const int stage = k % NST, u = k / F, b = u & 1;
-        const bool first = k % F == 0;
-        if (!um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag, wlim) ||
+        if (++stage == NST) stage = 0;
+        if (stage == 0) ph ^= 1u;
+        if (++kin == F) {
+          kin = 0;
+          ++u;
+        }
+        const int b = u & 1;
+        const bool first = kin == 0;
+        if (!um_wait(&full[stage], ph, abort_flag, wlim) ||
             (first && u >= 2 &&
              !um_wait(&acce[b], (uint32_t)(((u >> 1) - 1) & 1), abort_flag, wlim))) {
           ok = false;
@@ -426,7 +441,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
           umma_commit(&aempty[slot]);
         }
         if (!ok) break;
-        if (k % F == F - 1 || k == ntiles - 1) umma_commit(&accf[u % 4]);
+        if (kin == F - 1 || k == ntiles - 1) umma_commit(&accf[u % 4]);
       }
       if (!ok) {
         atomicExch(err, 1);
@@ -499,9 +514,12 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       }
     }
     bool ok = true;
+    int stage = -1;  // k % NST and (k / NST) & 1, kept as counters
+    uint32_t ph = 1;
     for (int k = 0; k < ntiles && ok; ++k) {
-      const int stage = k % NST;
-      if (!__all_sync(0xffffffffu, um_wait(&full[stage], (uint32_t)((k / NST) & 1), abort_flag, wlim))) {
+      if (++stage == NST) stage = 0;
+      if (stage == 0) ph ^= 1u;
+      if (!__all_sync(0xffffffffu, um_wait(&full[stage], ph, abort_flag, wlim))) {
         ok = false;
         break;
       }
@@ -616,6 +634,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     float* mytot = tot + (size_t)row * kUmTotStride;
     bool ok = true;
     const int nunits = (ntiles + F - 1) / F;
+    int fstage = 0;  // stage of the first tile of unit u
     for (int u = 0; u < nunits; ++u) {
       const int b = u & 1;
       if (!__all_sync(0xffffffffu, um_wait(&accf[u % 4], (uint32_t)((u / 4) & 1), abort_flag, wlim))) {
@@ -662,8 +681,13 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       if (lane == 0) {
         mbar_arrive1(&acce[b]);
         if ((warp & 3) == 0)
-          for (int t = u * F; t < u * F + F && t < ntiles; ++t) mbar_arrive1(&empty[t % NST]);
+          for (int t = u * F, st = fstage; t < u * F + F && t < ntiles; ++t) {
+            mbar_arrive1(&empty[st]);
+            if (++st == NST) st = 0;
+          }
       }
+      fstage += F;
+      if (fstage >= NST) fstage -= NST;
     }
     if (!ok) atomicExch(err, 1);
     if (ok && !*abort_flag) {
