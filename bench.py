@@ -226,9 +226,10 @@ def _events_ms(torch, fn, steps, flush=None):
 
 
 def plan_build_on_gpu(H, P, p, eta, leaf, dev):
-    """The same plan with the cluster tree sorted on the GPU
-    (fmca_plan_create_gpu): its build time (two runs, the second counts; the
-    first warms up the device) and whether it equals the host-built plan."""
+    """The same plan with the cluster tree sorted and the block pattern built
+    on the GPU (fmca_plan_create_gpu): its build time (two runs, the second
+    counts; the first warms up the device) and whether it equals the
+    host-built plan."""
     import torch
     from fmca_gb300 import H2Matrix
     torch.cuda.synchronize(dev)
@@ -239,7 +240,8 @@ def plan_build_on_gpu(H, P, p, eta, leaf, dev):
         times.append(time.perf_counter() - t0)
     same = (G.info == H.info and np.array_equal(G.rindices(), H.rindices()) and
             all(np.array_equal(a, b) for k in (0, 1) for a, b in zip(G.blocks(k), H.blocks(k))))
-    return {"build_s": times[-1], "trees_on_gpu": G.trees_on_gpu, "equals_host_plan": bool(same)}
+    return {"build_s": times[-1], "trees_on_gpu": G.trees_on_gpu,
+            "pattern_on_gpu": G.pattern_on_gpu, "equals_host_plan": bool(same)}
 
 
 def run_c3(args, torch, dev):

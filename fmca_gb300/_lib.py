@@ -96,7 +96,7 @@ def load() -> C.CDLL:
     lib.fmca_plan_create_ex.argtypes = [dp, i32, i64, dp, i64, i32, i32, C.c_double, i64,
                                         C.POINTER(vp)]
     lib.fmca_plan_create_gpu.argtypes = [dp, i32, i64, dp, i64, i32, i32, C.c_double, i64,
-                                         C.POINTER(C.c_int), C.POINTER(vp)]
+                                         C.POINTER(C.c_int), C.POINTER(vp)]  # gpu_parts[2]
     lib.fmca_plan_interpolator.argtypes = [vp, dp, dp]
     lib.fmca_plan_save.argtypes = [vp, C.c_char_p]
     lib.fmca_plan_load.argtypes = [C.c_char_p, C.POINTER(vp)]

@@ -128,8 +128,9 @@ namespace {
 // fmca_plan_create_ex, with the trees' level sorts on `sorter` if given
 fmca_status create_plan(const double* P_rows, int dim, int64_t n_rows, const double* P_cols,
                         int64_t n_cols, int interpolator, int degree, double eta,
-                        int64_t min_leaf, fmca::LevelSorter* sorter, int* sorted_elsewhere,
-                        fmca_plan** out) {
+                        int64_t min_leaf, fmca::LevelSorter* sorter,
+                        fmca::PatternBuilder* pattern_builder, int* sorted_elsewhere,
+                        int* pattern_elsewhere, fmca_plan** out) {
   if (!out) return fail(FMCA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!P_rows) return fail(FMCA_ERR_INVALID_ARGUMENT, "P_rows is NULL");
@@ -166,8 +167,9 @@ fmca_status create_plan(const double* P_rows, int dim, int64_t n_rows, const dou
                   (uint32_t)n_cols, dim, degree, eta, (uint32_t)min_leaf, same,
                   interpolator == FMCA_INTERP_TOTAL_DEGREE ? fmca::kInterpTotalDegree
                                                            : fmca::kInterpTensor,
-                  sorter);
+                  sorter, pattern_builder);
     if (sorted_elsewhere) *sorted_elsewhere = p->plan.trees_sorted_elsewhere;
+    if (pattern_elsewhere) *pattern_elsewhere = p->plan.pattern_built_elsewhere;
     *out = p;
   } catch (const std::bad_alloc&) {
     return fail(FMCA_ERR_OUT_OF_MEMORY, "host allocation failed while building the plan");
@@ -182,17 +184,24 @@ fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
                                 const double* P_cols, int64_t n_cols, int interpolator,
                                 int degree, double eta, int64_t min_leaf, fmca_plan** out) {
   return create_plan(P_rows, dim, n_rows, P_cols, n_cols, interpolator, degree, eta, min_leaf,
-                     nullptr, nullptr, out);
+                     nullptr, nullptr, nullptr, nullptr, out);
 }
 
 fmca_status fmca_plan_create_gpu(const double* P_rows, int dim, int64_t n_rows,
                                  const double* P_cols, int64_t n_cols, int interpolator,
-                                 int degree, double eta, int64_t min_leaf, int* trees_on_gpu,
+                                 int degree, double eta, int64_t min_leaf, int* gpu_parts,
                                  fmca_plan** out) {
-  if (trees_on_gpu) *trees_on_gpu = 0;
+  if (gpu_parts) gpu_parts[0] = gpu_parts[1] = 0;
   std::unique_ptr<fmca::LevelSorter> sorter = fmca::gpu::make_gpu_level_sorter();
-  return create_plan(P_rows, dim, n_rows, P_cols, n_cols, interpolator, degree, eta, min_leaf,
-                     sorter.get(), trees_on_gpu, out);
+  std::unique_ptr<fmca::PatternBuilder> pb = fmca::gpu::make_gpu_pattern_builder();
+  int trees = 0, pattern = 0;
+  const fmca_status s = create_plan(P_rows, dim, n_rows, P_cols, n_cols, interpolator, degree,
+                                    eta, min_leaf, sorter.get(), pb.get(), &trees, &pattern, out);
+  if (gpu_parts) {
+    gpu_parts[0] = trees;
+    gpu_parts[1] = pattern;
+  }
+  return s;
 }
 
 fmca_status fmca_plan_create_batched(const double* const* P, const int64_t* n_points,

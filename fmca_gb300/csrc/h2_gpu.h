@@ -66,6 +66,10 @@ int profile(DevPlan* dev, double* stage_ms, int64_t* launches, std::string* err)
 // (h2_tree_gpu.cu): every level of a cluster tree as one segmented radix
 // sort.
 std::unique_ptr<LevelSorter> make_gpu_level_sorter();
+// The block-pattern builder of Plan::build on the current device
+// (h2_tree_gpu.cu): the block tree level by level, leaves sorted into the
+// reference's depth-first order.
+std::unique_ptr<PatternBuilder> make_gpu_pattern_builder();
 
 }  // namespace gpu
 }  // namespace fmca

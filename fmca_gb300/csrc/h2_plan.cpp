@@ -704,7 +704,7 @@ Adm compare(const Tree& r, int i, const Tree& c, int j, double eta) {
 
 void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
                  int dim, int deg, double eta_, uint32_t min_leaf, bool same,
-                 int interp_kind, LevelSorter* sorter) {
+                 int interp_kind, LevelSorter* sorter, PatternBuilder* pattern_builder) {
   interp.init(dim, deg, interp_kind);
   eta = eta_;
   points_r.assign(Pr, Pr + (size_t)dim * nr);
@@ -750,12 +750,19 @@ void Plan::build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
   leaves_of(rows, &row_leaves);
   leaves_of(cols, &col_leaves);
 
-  // pattern: depth-first stack over cluster pairs (H2MatrixBase.h:160-191)
+  // pattern: depth-first stack over cluster pairs (H2MatrixBase.h:160-191),
+  // or the same leaves in the same order from the pattern builder
   Pattern& P = pat;
   P = Pattern();
   const uint32_t qq = (uint32_t)interp.q * (uint32_t)interp.q;  // Index arithmetic
+  pattern_built_elsewhere = 0;
+  if (pattern_builder && pattern_builder->build(rows, cols, qq, eta, &P.far_row, &P.far_col,
+                                                &P.near_row, &P.near_col))
+    pattern_built_elsewhere = 1;
+  else
+    P = Pattern();
   std::vector<std::pair<int32_t, int32_t>> stack;
-  stack.emplace_back(0, 0);
+  if (!pattern_built_elsewhere) stack.emplace_back(0, 0);
   while (!stack.empty()) {
     const auto blk = stack.back();
     stack.pop_back();
@@ -870,7 +877,7 @@ void Plan::merge(const std::vector<const Plan*>& parts) {
   for (const Plan* p : parts) {
     same_tree = same_tree && p->same_tree;
     const int32_t rco = rows.nclusters(), cco = cols.nclusters();
-    const uint32_t rpo = rows.n, cpo = cols.n;
+    const uint32_t cpo = cols.n;
     // block lists
     for (size_t b = 0; b < p->pat.far_row.size(); ++b) {
       pat.far_row.push_back(p->pat.far_row[b] + rco);

@@ -114,10 +114,25 @@ class LevelSorter {
   virtual bool finish(std::vector<uint32_t>* perm) = 0;
 };
 
+class Tree;
+// The leaves of the block tree of H2MatrixBase::computePattern
+// (H2MatrixBase.h:160-191) built elsewhere (the GPU pattern builder of
+// h2_tree_gpu.cu): far (low-rank) and near (dense) (row, column) cluster
+// pairs in the order of the reference's depth-first recursion.  false: not
+// built; the host recursion runs instead.
+class PatternBuilder {
+ public:
+  virtual ~PatternBuilder() {}
+  virtual bool build(const Tree& rows, const Tree& cols, uint32_t qq, double eta,
+                     std::vector<int32_t>* far_row, std::vector<int32_t>* far_col,
+                     std::vector<int32_t>* near_row, std::vector<int32_t>* near_col) = 0;
+};
+
 // Cluster tree in level order.  Cluster c owns cluster-ordered points
 // [begin[c], begin[c] + size[c]); perm maps cluster order to natural order
 // (ClusterTreeBase::indices()).
-struct Tree {
+class Tree {
+ public:
   int dim = 0;
   uint32_t n = 0;
   std::vector<uint32_t> perm;
@@ -170,10 +185,13 @@ struct Plan {
 
   void build(const double* Pr, uint32_t nr, const double* Pc, uint32_t nc,
              int dim, int deg, double eta, uint32_t min_leaf, bool same,
-             int interp_kind = kInterpTensor, LevelSorter* sorter = nullptr);
+             int interp_kind = kInterpTensor, LevelSorter* sorter = nullptr,
+             PatternBuilder* pattern_builder = nullptr);
   // trees whose sorts ran on the sorter (0, 1 or 2); the others were built
   // on the host
   int trees_sorted_elsewhere = 0;
+  // 1 if the pattern builder built the block lists, 0 if the host did
+  int pattern_built_elsewhere = 0;
   int build_threads = 0;  // host threads of the tree builds (0: one per core)
   // Block-diagonal plan of independent point clouds: trees, bases and block
   // lists of the parts concatenated (cluster ids, point indices and node

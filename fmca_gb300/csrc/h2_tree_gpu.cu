@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -212,6 +213,85 @@ __global__ void split_values_kernel(const SegDev* __restrict__ segs, int m,
   }
 }
 
+// Stable LSD radix sort of (key, val, sid) records on one stream: ping-pong
+// buffers of a fixed capacity; sort() runs 8-bit passes over the low
+// key_bits of the key, then over the low sid_bits of sid, and leaves the
+// sorted records in buffer cur.
+struct RecordSort {
+  cudaStream_t st = nullptr;
+  size_t cap = 0;
+  uint64_t* k[2] = {nullptr, nullptr};
+  uint32_t* v[2] = {nullptr, nullptr};
+  uint32_t* s[2] = {nullptr, nullptr};
+  uint32_t* hist = nullptr;
+  int cur = 0;
+
+  void release() {
+    for (int b = 0; b < 2; ++b) {
+      cudaFree(k[b]);
+      cudaFree(v[b]);
+      cudaFree(s[b]);
+      k[b] = nullptr;
+      v[b] = nullptr;
+      s[b] = nullptr;
+    }
+    cudaFree(hist);
+    hist = nullptr;
+    cap = 0;
+  }
+  // capacity for n records (buffer cur keeps its first `keep` records)
+  bool reserve(size_t n, size_t keep = 0) {
+    if (n <= cap) return true;
+    size_t nc = std::max<size_t>(n, cap * 2);
+    uint64_t* nk[2] = {nullptr, nullptr};
+    uint32_t* nv[2] = {nullptr, nullptr};
+    uint32_t* ns[2] = {nullptr, nullptr};
+    uint32_t* nh = nullptr;
+    bool ok = true;
+    for (int b = 0; b < 2; ++b)
+      ok = ok && cudaMalloc(&nk[b], nc * 8) == cudaSuccess &&
+           cudaMalloc(&nv[b], nc * 4) == cudaSuccess && cudaMalloc(&ns[b], nc * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&nh, (size_t)256 * 4 * ((nc + kRxTile - 1) / kRxTile + 1)) == cudaSuccess;
+    if (ok && keep)
+      ok = cudaMemcpyAsync(nk[0], k[cur], keep * 8, cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+           cudaMemcpyAsync(nv[0], v[cur], keep * 4, cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+           cudaMemcpyAsync(ns[0], s[cur], keep * 4, cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+           cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) {
+      for (int b = 0; b < 2; ++b) {
+        cudaFree(nk[b]);
+        cudaFree(nv[b]);
+        cudaFree(ns[b]);
+      }
+      cudaFree(nh);
+      return false;
+    }
+    release();
+    for (int b = 0; b < 2; ++b) {
+      k[b] = nk[b];
+      v[b] = nv[b];
+      s[b] = ns[b];
+    }
+    hist = nh;
+    cap = nc;
+    cur = 0;
+    return true;
+  }
+  void sort(uint32_t n, int key_bits, int sid_bits) {
+    if (n == 0) return;
+    const int nb = (int)((n + kRxTile - 1) / kRxTile);
+    auto pass = [&](int shift, int on_seg) {
+      rx_hist_kernel<<<nb, kRxThreads, 0, st>>>(k[cur], s[cur], n, shift, on_seg, hist);
+      rx_scan_kernel<<<1, 1024, 0, st>>>(hist, (uint32_t)(256 * nb));
+      rx_scatter_kernel<<<nb, kRxThreads, 0, st>>>(k[cur], v[cur], s[cur], k[cur ^ 1], v[cur ^ 1],
+                                                   s[cur ^ 1], n, hist, shift, on_seg);
+      cur ^= 1;
+    };
+    for (int shift = 0; shift < key_bits; shift += 8) pass(shift, 0);
+    for (int shift = 0; shift < sid_bits; shift += 8) pass(shift, 1);
+  }
+};
+
 class GpuLevelSorter final : public LevelSorter {
  public:
   GpuLevelSorter() = default;
@@ -222,6 +302,7 @@ class GpuLevelSorter final : public LevelSorter {
     for (void* p : bufs_) cudaFree(p);
     if (segdev_) cudaFree(segdev_);
     if (cut_) cudaFree(cut_);
+    rs_.release();
     if (st_) cudaStreamDestroy(st_);
   }
 
@@ -229,10 +310,9 @@ class GpuLevelSorter final : public LevelSorter {
     dim_ = dim;
     n_ = n;
     if (cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess) return false;
-    const uint32_t nb = std::max<uint32_t>(1, (n + kRxTile - 1) / kRxTile);
-    if (!alloc(&P_, (size_t)dim * n) || !alloc(&idx_, n) || !alloc(&k_[0], n) ||
-        !alloc(&k_[1], n) || !alloc(&v_[0], n) || !alloc(&v_[1], n) || !alloc(&s_[0], n) ||
-        !alloc(&s_[1], n) || !alloc(&hist_, (size_t)256 * nb) || !alloc(&ties_, 1))
+    rs_.st = st_;
+    if (!alloc(&P_, (size_t)dim * n) || !alloc(&idx_, n) || !alloc(&ties_, 1) ||
+        !rs_.reserve(std::max<uint32_t>(1, n)))
       return false;
     std::vector<uint32_t> iota(n);
     for (uint32_t i = 0; i < n; ++i) iota[i] = i;
@@ -268,28 +348,21 @@ class GpuLevelSorter final : public LevelSorter {
         return false;
       seg_cap_ = m;
     }
-    const int nb = (int)((total + kRxTile - 1) / kRxTile);
     const int grid = std::min<int>(4096, (int)((total + 255) / 256));
     bool ok = cudaMemcpyAsync(segdev_, hs.data(), sizeof(SegDev) * m, cudaMemcpyHostToDevice,
                               st_) == cudaSuccess &&
               cudaMemsetAsync(ties_, 0, sizeof(int), st_) == cudaSuccess;
     if (!ok) return false;
-    gather_records_kernel<<<grid, 256, 0, st_>>>(segdev_, m, total, idx_, P_, dim_, k_[0], v_[0],
-                                                 s_[0]);
-    int cur = 0;
-    auto pass = [&](int shift, int on_seg) {
-      rx_hist_kernel<<<nb, kRxThreads, 0, st_>>>(k_[cur], s_[cur], total, shift, on_seg, hist_);
-      rx_scan_kernel<<<1, 1024, 0, st_>>>(hist_, (uint32_t)(256 * nb));
-      rx_scatter_kernel<<<nb, kRxThreads, 0, st_>>>(k_[cur], v_[cur], s_[cur], k_[cur ^ 1],
-                                                    v_[cur ^ 1], s_[cur ^ 1], total, hist_, shift,
-                                                    on_seg);
-      cur ^= 1;
-    };
-    for (int shift = 0; shift < 64; shift += 8) pass(shift, 0);
-    for (int shift = 0; m > 1 && ((uint32_t)(m - 1) >> shift) != 0; shift += 8) pass(shift, 1);
-    scatter_back_kernel<<<grid, 256, 0, st_>>>(segdev_, total, v_[cur], s_[cur], P_, dim_, idx_,
-                                               ties_);
-    split_values_kernel<<<(m + 255) / 256, 256, 0, st_>>>(segdev_, m, v_[cur], P_, dim_, cut_);
+    rs_.cur = 0;
+    gather_records_kernel<<<grid, 256, 0, st_>>>(segdev_, m, total, idx_, P_, dim_, rs_.k[0],
+                                                 rs_.v[0], rs_.s[0]);
+    int sid_bits = 0;
+    while (m > 1 && ((uint32_t)(m - 1) >> sid_bits) != 0) sid_bits += 8;
+    rs_.sort(total, 64, sid_bits);
+    const int c = rs_.cur;
+    scatter_back_kernel<<<grid, 256, 0, st_>>>(segdev_, total, rs_.v[c], rs_.s[c], P_, dim_,
+                                               idx_, ties_);
+    split_values_kernel<<<(m + 255) / 256, 256, 0, st_>>>(segdev_, m, rs_.v[c], P_, dim_, cut_);
     if (cudaGetLastError() != cudaSuccess) return false;
     cut->resize(2 * (size_t)m);
     int t = 0;
@@ -324,20 +397,277 @@ class GpuLevelSorter final : public LevelSorter {
   std::vector<void*> bufs_;
   double* P_ = nullptr;
   uint32_t* idx_ = nullptr;
-  uint64_t* k_[2] = {nullptr, nullptr};
-  uint32_t* v_[2] = {nullptr, nullptr};
-  uint32_t* s_[2] = {nullptr, nullptr};
-  uint32_t* hist_ = nullptr;
+  RecordSort rs_;
   int* ties_ = nullptr;
   SegDev* segdev_ = nullptr;
   double* cut_ = nullptr;
   size_t seg_cap_ = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Block pattern (H2MatrixBase::computePattern, H2MatrixBase.h:160-191) level
+// by level: every pair of the current level is compared
+// (Admissibility.h:19-29,95-115, in the reference's FP64 operation order
+// with rounded operations only, so that every decision equals the host's)
+// and becomes a far leaf (low-rank and cheaper than dense, 32-bit unsigned
+// products like the reference's Index), a near leaf, or four son pairs of
+// the next level.  Every pair carries its path from the root, two bits per
+// level: the rank of the son pair in the order the reference's stack pops
+// them (the last pushed, sons (1, 1), first).  Sorting the leaves by the
+// left-aligned path gives exactly the order of the depth-first recursion.
+struct TreeDev {
+  const double *bbmin, *bbmax, *radius;
+  const uint32_t* size;
+  const int32_t *son0, *nsons;
+};
+
+struct PairList {
+  uint64_t* key;
+  int32_t *i, *j;
+};
+
+__global__ void pattern_level_kernel(const uint64_t* __restrict__ fkey,
+                                     const int32_t* __restrict__ fi,
+                                     const int32_t* __restrict__ fj, uint32_t nf, int depth,
+                                     TreeDev R, TreeDev Cl, int dim, double eta, uint32_t qq,
+                                     PairList far, PairList near, PairList next,
+                                     unsigned int* __restrict__ counts) {
+  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    const int i = fi[f], j = fj[f];
+    const uint64_t key = fkey[f];
+    double s2 = 0.0;
+    for (int d = 0; d < dim; ++d) {
+      double a = __dsub_rn(R.bbmin[(size_t)i * dim + d], Cl.bbmin[(size_t)j * dim + d]);
+      a = __dadd_rn(a, R.bbmax[(size_t)i * dim + d]);
+      a = __dsub_rn(a, Cl.bbmax[(size_t)j * dim + d]);
+      const double v = __dmul_rn(0.5, a);
+      const double sq = __dmul_rn(v, v);
+      s2 = d == 0 ? sq : __dadd_rn(s2, sq);
+    }
+    const double r1 = R.radius[i], r2 = Cl.radius[j];
+    double dist = __dsub_rn(__dsub_rn(__dsqrt_rn(s2), r1), r2);
+    dist = dist > 0 ? dist : 0;
+    const double radius = r1 > r2 ? r1 : r2;
+    if (radius > __dmul_rn(eta, dist)) {
+      const int ni = R.nsons[i], nj = Cl.nsons[j];
+      if (!ni || !nj) {
+        const unsigned int o = atomicAdd(&counts[1], 1u);
+        near.key[o] = key;
+        near.i[o] = i;
+        near.j[o] = j;
+      } else {
+        const unsigned int o = atomicAdd(&counts[2], (unsigned int)(ni * nj));
+        const int shift = 62 - 2 * depth;
+        for (int b = 0; b < nj; ++b)
+          for (int a = 0; a < ni; ++a) {
+            const int t = b * ni + a;  // push index
+            const uint64_t rank = (uint64_t)(ni * nj - 1 - t);
+            next.key[o + t] = key | (rank << shift);
+            next.i[o + t] = R.son0[i] + a;
+            next.j[o + t] = Cl.son0[j] + b;
+          }
+      }
+    } else {
+      const uint32_t dense = R.size[i] * Cl.size[j];
+      const int which = qq < dense ? 0 : 1;
+      const unsigned int o = atomicAdd(&counts[which], 1u);
+      PairList& out = which ? near : far;
+      out.key[o] = key;
+      out.i[o] = i;
+      out.j[o] = j;
+    }
+  }
+}
+
+// leaves packed as sort records (key, i, j)
+__global__ void pack_leaves_kernel(const uint64_t* __restrict__ key, const int32_t* __restrict__ i,
+                                   const int32_t* __restrict__ j, uint32_t n,
+                                   uint64_t* __restrict__ k, uint32_t* __restrict__ v,
+                                   uint32_t* __restrict__ s) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    k[p] = key[p];
+    v[p] = (uint32_t)i[p];
+    s[p] = (uint32_t)j[p];
+  }
+}
+
+// device buffer of one array type with a host-side capacity
+template <typename V>
+struct DevBuf {
+  V* p = nullptr;
+  size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { cudaFree(p); }
+  void swap(DevBuf& o) {
+    std::swap(p, o.p);
+    std::swap(cap, o.cap);
+  }
+  // grows to n elements, keeping the first `keep`
+  bool reserve(size_t n, size_t keep, cudaStream_t st) {
+    if (n <= cap) return true;
+    const size_t nc = std::max(n, cap * 2);
+    V* q = nullptr;
+    if (cudaMalloc(&q, nc * sizeof(V)) != cudaSuccess) return false;
+    if (keep && (cudaMemcpyAsync(q, p, keep * sizeof(V), cudaMemcpyDeviceToDevice, st) !=
+                     cudaSuccess ||
+                 cudaStreamSynchronize(st) != cudaSuccess)) {
+      cudaFree(q);
+      return false;
+    }
+    cudaFree(p);
+    p = q;
+    cap = nc;
+    return true;
+  }
+};
+
+struct PairBufs {
+  DevBuf<uint64_t> key;
+  DevBuf<int32_t> i, j;
+  bool reserve(size_t n, size_t keep, cudaStream_t st) {
+    return key.reserve(n, keep, st) && i.reserve(n, keep, st) && j.reserve(n, keep, st);
+  }
+  PairList list() { return PairList{key.p, i.p, j.p}; }
+  void swap(PairBufs& o) {
+    key.swap(o.key);
+    i.swap(o.i);
+    j.swap(o.j);
+  }
+};
+
+class GpuPatternBuilder final : public PatternBuilder {
+ public:
+  GpuPatternBuilder() = default;
+  GpuPatternBuilder(const GpuPatternBuilder&) = delete;
+  GpuPatternBuilder& operator=(const GpuPatternBuilder&) = delete;
+  ~GpuPatternBuilder() override {
+    if (st_) cudaStreamSynchronize(st_);
+    for (void* p : bufs_) cudaFree(p);
+    rs_.release();
+    if (st_) cudaStreamDestroy(st_);
+  }
+
+  bool build(const Tree& rows, const Tree& cols, uint32_t qq, double eta,
+             std::vector<int32_t>* far_row, std::vector<int32_t>* far_col,
+             std::vector<int32_t>* near_row, std::vector<int32_t>* near_col) override {
+    const int dim = rows.dim;
+    if (cols.dim != dim || rows.nclusters() < 1 || cols.nclusters() < 1) return false;
+    // binary trees of at most 32 levels: two bits of path per level
+    for (const Tree* t : {&rows, &cols}) {
+      if (t->nlevels() > 32) return false;
+      for (int32_t ns : t->nsons)
+        if (ns != 0 && ns != 2) return false;
+    }
+    if (!st_) {
+      if (cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess) return false;
+      rs_.st = st_;
+    }
+    TreeDev R, Cl;
+    if (!upload_tree(rows, &R) || !upload_tree(cols, &Cl)) return false;
+    unsigned int* counts = nullptr;
+    if (!alloc(&counts, 3)) return false;
+    PairBufs cur, nxt, far, near;
+    const uint64_t zero = 0;
+    const int32_t root = 0;
+    if (!cur.reserve(1, 0, st_) ||
+        cudaMemcpyAsync(cur.key.p, &zero, 8, cudaMemcpyHostToDevice, st_) != cudaSuccess ||
+        cudaMemcpyAsync(cur.i.p, &root, 4, cudaMemcpyHostToDevice, st_) != cudaSuccess ||
+        cudaMemcpyAsync(cur.j.p, &root, 4, cudaMemcpyHostToDevice, st_) != cudaSuccess)
+      return false;
+    unsigned int h[3] = {0, 0, 0};
+    uint32_t nf = 1;
+    for (int depth = 0; nf > 0; ++depth) {
+      if (depth > 31) return false;
+      if (!far.reserve((size_t)h[0] + nf, h[0], st_) ||
+          !near.reserve((size_t)h[1] + nf, h[1], st_) || !nxt.reserve((size_t)4 * nf, 0, st_))
+        return false;
+      unsigned int c3[3] = {h[0], h[1], 0};
+      if (cudaMemcpyAsync(counts, c3, sizeof(c3), cudaMemcpyHostToDevice, st_) != cudaSuccess)
+        return false;
+      const int grid = (int)std::min<uint32_t>(4096, (nf + 255) / 256);
+      pattern_level_kernel<<<grid, 256, 0, st_>>>(cur.key.p, cur.i.p, cur.j.p, nf, depth, R, Cl,
+                                                  dim, eta, qq, far.list(), near.list(),
+                                                  nxt.list(), counts);
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st_) != cudaSuccess ||
+          cudaStreamSynchronize(st_) != cudaSuccess)
+        return false;
+      nf = h[2];
+      cur.swap(nxt);
+    }
+    return sorted(far, h[0], far_row, far_col) && sorted(near, h[1], near_row, near_col);
+  }
+
+ private:
+  // the leaves in depth-first order: sorted by their left-aligned paths
+  bool sorted(PairBufs& b, uint32_t n, std::vector<int32_t>* ri, std::vector<int32_t>* rj) {
+    ri->resize(n);
+    rj->resize(n);
+    if (n == 0) return true;
+    if (!rs_.reserve(n)) return false;
+    rs_.cur = 0;
+    const int grid = (int)std::min<uint32_t>(4096, (n + 255) / 256);
+    pack_leaves_kernel<<<grid, 256, 0, st_>>>(b.key.p, b.i.p, b.j.p, n, rs_.k[0], rs_.v[0],
+                                              rs_.s[0]);
+    rs_.sort(n, 64, 0);
+    return cudaGetLastError() == cudaSuccess &&
+           cudaMemcpyAsync(ri->data(), rs_.v[rs_.cur], 4 * (size_t)n, cudaMemcpyDeviceToHost,
+                           st_) == cudaSuccess &&
+           cudaMemcpyAsync(rj->data(), rs_.s[rs_.cur], 4 * (size_t)n, cudaMemcpyDeviceToHost,
+                           st_) == cudaSuccess &&
+           cudaStreamSynchronize(st_) == cudaSuccess;
+  }
+
+  bool upload_tree(const Tree& t, TreeDev* d) {
+    const int C = t.nclusters(), dim = t.dim;
+    // cluster radii as the host compare forms them: 0.5 * |extent|, the
+    // squares summed in dimension order
+    std::vector<double> rad(C);
+    for (int c = 0; c < C; ++c) {
+      const double* e = t.bbext.data() + (size_t)c * dim;
+      double s2 = e[0] * e[0];
+      for (int k = 1; k < dim; ++k) s2 += e[k] * e[k];
+      rad[c] = 0.5 * std::sqrt(s2);
+    }
+    double *bmin, *bmax, *r;
+    uint32_t* sz;
+    int32_t *s0, *ns;
+    if (!put(&bmin, t.bbmin) || !put(&bmax, t.bbmax) || !put(&r, rad) || !put(&sz, t.size) ||
+        !put(&s0, t.son0) || !put(&ns, t.nsons))
+      return false;
+    *d = TreeDev{bmin, bmax, r, sz, s0, ns};
+    return true;
+  }
+  template <typename V>
+  bool alloc(V** p, size_t count) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, std::max<size_t>(1, count) * sizeof(V)) != cudaSuccess) return false;
+    bufs_.push_back(q);
+    *p = static_cast<V*>(q);
+    return true;
+  }
+  template <typename V>
+  bool put(V** p, const std::vector<V>& h) {
+    return alloc(p, h.size()) &&
+           cudaMemcpyAsync(*p, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice, st_) ==
+               cudaSuccess;
+  }
+
+  cudaStream_t st_ = nullptr;
+  std::vector<void*> bufs_;
+  RecordSort rs_;
+};
+
 }  // namespace
 
 std::unique_ptr<LevelSorter> make_gpu_level_sorter() {
   return std::unique_ptr<LevelSorter>(new GpuLevelSorter());
+}
+
+std::unique_ptr<PatternBuilder> make_gpu_pattern_builder() {
+  return std::unique_ptr<PatternBuilder>(new GpuPatternBuilder());
 }
 
 }  // namespace gpu

@@ -80,9 +80,10 @@ class H2Matrix:
     "fp32" or "mixed"; the default of ``action``), ``interpolator``
     ("tensor": Chebyshev tensor product, q = (p+1)^dim; "total_degree":
     TotalDegreeInterpolator, q = binom(p+dim, dim), as the reference module
-    builds it) and ``build`` ("host", or "gpu": the cluster trees' sorts on
-    the current CUDA device, fmca_plan_create_gpu, the same plan;
-    ``trees_on_gpu`` tells how many trees were sorted there). ``fmca_gb300.FMCA`` gives the reference module's defaults.
+    builds it) and ``build`` ("host", or "gpu": the cluster trees' sorts and
+    the block pattern on the current CUDA device, fmca_plan_create_gpu, the
+    same plan; ``trees_on_gpu`` and ``pattern_on_gpu`` tell what ran
+    there). ``fmca_gb300.FMCA`` gives the reference module's defaults.
     """
 
     def __init__(self, cov: CovarianceKernel, Pr, Pc=None, p: int = 3,
@@ -115,13 +116,13 @@ class H2Matrix:
             check(lib.fmca_plan_create_ex(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
                                           _lib.INTERPOLATORS[interpolator], self.p, self.eta,
                                           int(min_leaf), C.byref(handle)))
-            self.trees_on_gpu = 0
+            self.trees_on_gpu = self.pattern_on_gpu = 0
         elif build == "gpu":
-            ng = C.c_int(0)
+            parts = (C.c_int * 2)()
             check(lib.fmca_plan_create_gpu(_dptr(Pr), self.dim, Pr.shape[1], Pcp, nc,
                                            _lib.INTERPOLATORS[interpolator], self.p, self.eta,
-                                           int(min_leaf), C.byref(ng), C.byref(handle)))
-            self.trees_on_gpu = ng.value
+                                           int(min_leaf), parts, C.byref(handle)))
+            self.trees_on_gpu, self.pattern_on_gpu = parts[0], parts[1]
         else:
             raise ValueError("build must be 'host' or 'gpu'")
         self._h = handle

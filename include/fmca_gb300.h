@@ -165,21 +165,26 @@ fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
                                 const double* P_cols, int64_t n_cols, int interpolator,
                                 int degree, double eta, int64_t min_leaf, fmca_plan** out);
 
-/* fmca_plan_create_ex with the cluster trees built on the GPU (current
-   device): every level of a tree is one segmented radix sort of the index
-   ranges of the clusters that split, in place of the reference's std::sort
-   per cluster (ClusterTreeSplitter.h:60-81 called by
-   ClusterTreeInitializer_ClusterTree.h:56-86).  The plan is identical to
-   fmca_plan_create_ex's: where a sorted range holds equal coordinates,
-   whose order is decided by the reference's std::sort, that tree is built
-   on the host instead.  *trees_on_gpu (may be NULL) receives how many trees
-   were sorted on the GPU (0, 1, or 2 for two point clouds).  The block
-   pattern and the interpolation data are built on the host as for
-   fmca_plan_create_ex.  Synchronous; uses its own stream and frees its
-   device memory before returning. */
+/* fmca_plan_create_ex with the plan's structure built on the GPU (current
+   device), giving the identical plan:
+   - cluster trees: every level of a tree is one segmented radix sort of the
+     index ranges of the clusters that split, in place of the reference's
+     std::sort per cluster (ClusterTreeSplitter.h:60-81 called by
+     ClusterTreeInitializer_ClusterTree.h:56-86).  Where a sorted range holds
+     equal coordinates, whose order the reference's std::sort decides, that
+     tree is built on the host instead;
+   - block pattern: the block tree of computePattern (H2MatrixBase.h:
+     160-191) level by level, the same admissibility decisions in the same
+     FP64 operation order, the leaves sorted into the reference's
+     depth-first order.
+   gpu_parts (may be NULL) receives two ints: the number of trees sorted on
+   the GPU (0, 1, or 2 for two point clouds) and 1 if the block lists were
+   built there.  Bounding boxes, interpolation data and the derived GPU
+   lists are built on the host as for fmca_plan_create_ex.  Synchronous;
+   uses its own stream and frees its device memory before returning. */
 fmca_status fmca_plan_create_gpu(const double* P_rows, int dim, int64_t n_rows,
                                  const double* P_cols, int64_t n_cols, int interpolator,
-                                 int degree, double eta, int64_t min_leaf, int* trees_on_gpu,
+                                 int degree, double eta, int64_t min_leaf, int* gpu_parts,
                                  fmca_plan** out);
 
 /* One plan for many independent point clouds (batching): cloud i has

@@ -1,5 +1,5 @@
-"""Cluster trees built with a level sorter (Tree::build_with), the path of
-fmca_plan_create_gpu.
+"""Plans built with a level sorter (Tree::build_with) and a block-pattern
+builder, the path of fmca_plan_create_gpu.
 
 CPU: h2_plan.cpp compiled with g++ together with a host level sorter that
 sorts every segment with std::stable_sort (any sort gives the same order of
@@ -7,8 +7,13 @@ distinct keys) and reports equal neighbours like the GPU sorter.  On clouds
 without equal coordinates the tree equals Tree::build's (permutation,
 ranges, levels, links, boxes); with equal coordinates build_with refuses.
 
-GPU: fmca_plan_create_gpu (one segmented radix sort per tree level on the
-device) gives exactly the plan of fmca_plan_create_ex (permutations,
+The pattern builder's ordering argument (leaves of a level-by-level
+expansion sorted by their paths are in depth-first order) is restated on
+the CPU against the host's block lists.
+
+GPU: fmca_plan_create_gpu (one segmented radix sort per tree level, the block
+tree level by level on the device) gives exactly the plan of
+fmca_plan_create_ex (permutations,
 clusters, block lists, statistics, nodes, products) on tie-free clouds, and
 falls back to the host build, with the same plan, on clouds with equal
 coordinates."""
@@ -136,6 +141,60 @@ def test_level_sorter_refuses_equal_coordinates(prog):
     assert run(prog, P, 16)[0] == "refused"
 
 
+def test_path_keys_give_the_depth_first_order():
+    """The ordering argument of the GPU pattern builder, restated on the CPU:
+    expanding the block tree level by level and sorting its leaves by their
+    left-aligned paths (two bits per level, the rank of a son pair in the
+    order the reference's stack pops them) reproduces the raw block lists
+    of the host's depth-first recursion exactly."""
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    for P, p, eta in ((uniform_cloud(6000, 3, seed=31), 3, 0.8),
+                      (sphere_cloud(4000, seed=32), 2, 0.5),
+                      (uniform_cloud(5000, 2, seed=33), 4, 1.2)):
+        H = H2Matrix(CovarianceKernel("EXPONENTIAL", 1.0), P, P, p, eta)
+        meta, bb = H.clusters(0)
+        C, dim = meta.shape[0], P.shape[0]
+        sons = [[] for _ in range(C)]
+        for c in range(1, C):
+            sons[meta[c, 3]].append(c)
+        bmin, bmax, bext = bb[:, 0, :], bb[:, 1, :], bb[:, 2, :]
+
+        def norm(v):
+            s = v[0] * v[0]
+            for k in range(1, len(v)):
+                s = s + v[k] * v[k]
+            return np.sqrt(s)
+        rad = [0.5 * norm(bext[c]) for c in range(C)]
+        qq = np.uint32(H.info["q"]) * np.uint32(H.info["q"])
+        far, near, cur = [], [], [(0, 0, 0)]
+        for depth in range(40):
+            nxt = []
+            for key, i, j in cur:
+                v = [0.5 * (((bmin[i, d] - bmin[j, d]) + bmax[i, d]) - bmax[j, d])
+                     for d in range(dim)]
+                dist = max((norm(v) - rad[i]) - rad[j], 0.0)
+                if max(rad[i], rad[j]) > eta * dist:
+                    if not sons[i] or not sons[j]:
+                        near.append((key, i, j))
+                        continue
+                    for b, sj in enumerate(sons[j]):
+                        for a, si in enumerate(sons[i]):
+                            rank = 3 - (2 * b + a)
+                            nxt.append((key | (rank << (62 - 2 * depth)), si, sj))
+                elif qq < np.uint32(meta[i, 1]) * np.uint32(meta[j, 1]):
+                    far.append((key, i, j))
+                else:
+                    near.append((key, i, j))
+            cur = nxt
+            if not cur:
+                break
+        for kind, leaves in ((0, far), (1, near)):
+            r, c = H.blocks(kind)
+            leaves.sort()
+            assert np.array_equal(r, [x[1] for x in leaves])
+            assert np.array_equal(c, [x[2] for x in leaves])
+
+
 # ---------------------------------------------------------------------------
 # GPU: fmca_plan_create_gpu against fmca_plan_create_ex
 
@@ -174,7 +233,7 @@ def test_gpu_built_plan_equals_host_plan(cuda_device, case):
     Pc_ = Pr if Pc is None else Pc
     A = H2Matrix(cov, Pr, Pc_, p, 0.8, min_leaf=leaf, precision="fp64")
     B = H2Matrix(cov, Pr, Pc_, p, 0.8, min_leaf=leaf, precision="fp64", build="gpu")
-    assert B.trees_on_gpu == (1 if Pc is None else 2)
+    assert B.trees_on_gpu == (1 if Pc is None else 2) and B.pattern_on_gpu == 1
     same_plans(A, B)
     x = np.random.default_rng(1).standard_normal((Pc_.shape[1], 2))
     assert rel_err(B.action(x), A.action(x)) == 0.0
@@ -188,5 +247,5 @@ def test_gpu_build_falls_back_on_equal_coordinates(cuda_device):
     cov = CovarianceKernel("EXPONENTIAL", 1.0)
     A = H2Matrix(cov, P, P, 3, 0.8, precision="fp64")
     B = H2Matrix(cov, P, P, 3, 0.8, precision="fp64", build="gpu")
-    assert B.trees_on_gpu == 0
+    assert B.trees_on_gpu == 0 and B.pattern_on_gpu == 1
     same_plans(A, B)
