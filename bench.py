@@ -369,6 +369,8 @@ def run_c4(args, torch, dev):
                                   "df_dX": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))},
         "fp64_vs_central_differences_h1e-4": {"max_rel_err": max(fd_err), "checks": fd_err},
         "dtype": "f32", "data": "synthetic", "autotune": H.tuned_config(1, "mixed"),
+        "adjoint_path": "kernel sums on the FP32 CUDA cores (adjoints with fewer than 17 "
+                        "right-hand sides do not take the padded tensor-core path)",
         "config": {"workload": "C4: n=2e5 on S^2, MATERN52 l=0.3 sigma2=1, p=4, eta=0.8, "
                                "leaf 96 (125 effective), x,y ~ N(0,1) float32",
                    "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"]},
@@ -389,7 +391,7 @@ def run_c5(args, torch, dev):
     t0 = time.perf_counter()
     H = H2Matrix(CovarianceKernel("EXPONENTIAL", 0.1), P, P, 5, 0.6, min_leaf=128)
     t_plan = time.perf_counter() - t0
-    gpu_build = plan_build_on_gpu(H, P, 5, 0.6, 128, dev)
+    gpu_build = None if args.no_gpu_build else plan_build_on_gpu(H, P, 5, 0.6, 128, dev)
     z32 = torch.tensor(z, dtype=torch.float32, device=dev)
     z64 = z32.double()
 
@@ -450,6 +452,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="default launch shapes instead of the autotuner's")
+    ap.add_argument("--no-gpu-build", action="store_true",
+                    help="skip timing the plan build on the GPU")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2 (default): the headline workload; c3 batching, c4 gradients, "
                          "c5 GP step (one JSON line each, not the headline)")
@@ -480,7 +484,7 @@ def main():
                  precision="mixed")
     t_plan = time.perf_counter() - t0
     info = H.info
-    gpu_build = plan_build_on_gpu(H, P, 4, 0.8, 128, dev)
+    gpu_build = None if args.no_gpu_build else plan_build_on_gpu(H, P, 4, 0.8, 128, dev)
     Xd = torch.tensor(X, device=dev)  # FP64, n x R row-major
     Y = torch.empty_like(Xd)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)

@@ -52,11 +52,11 @@ EXPORTED = [
     "fmca_graph_destroy", "fmca_plan_create_ex", "fmca_plan_interpolator",
     "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets", "fmca_plan_device_bytes",
     "fmca_plan_set_wait_limit", "fmca_plan_set_stalled_wait", "fmca_plan_set_autotune",
-    "fmca_plan_tuned_config", "fmca_plan_create_gpu",
+    "fmca_plan_tuned_config", "fmca_plan_create_gpu", "fmca_plan_set_tuned_config",
 ]
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
-             "small_r_tensor", "tune_us", "tunings"]
+             "small_r_tensor", "near_halves", "tune_us", "tunings"]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
 
@@ -134,6 +134,7 @@ def load() -> C.CDLL:
     lib.fmca_plan_set_stalled_wait.argtypes = [vp, i32]
     lib.fmca_plan_set_autotune.argtypes = [vp, i32]
     lib.fmca_plan_tuned_config.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_int32)]
+    lib.fmca_plan_set_tuned_config.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_int32)]
     for name in EXPORTED:
         if name not in ("fmca_last_error", "fmca_version"):
             getattr(lib, name).restype = C.c_int

@@ -649,6 +649,19 @@ fmca_status fmca_plan_tuned_config(fmca_plan* p, int precision, int kernel_type,
   return ok();
 }
 
+fmca_status fmca_plan_set_tuned_config(fmca_plan* p, int precision, int kernel_type, int nrhs,
+                                       const int32_t cfg[FMCA_TUNE_COUNT]) {
+  if (!p || !cfg) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "nrhs must be >= 1");
+  if (!fmca::gpu::resident(p->dev, precision))
+    return fail(FMCA_ERR_INVALID_ARGUMENT,
+                "the plan is not resident on the current device for this precision");
+  std::string err;
+  const int st = fmca::gpu::set_tuned_config(p->dev, precision, kernel_type, nrhs, cfg, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
 fmca_status fmca_plan_set_stalled_wait(fmca_plan* p, int on) {
   if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
   p->stall = on != 0;

@@ -86,7 +86,8 @@ struct TrCfg {
 // n = 1e6, 3-D, p = 4, 32 right-hand sides) or what the autotuner measured
 // fastest on a plan for one (precision, kernel, right-hand sides) key.
 struct TuneCfg {
-  UmCfg near{um_stages(2), 2};       // near field, two target halves
+  UmCfg near{um_stages(2), 2};       // near field
+  int near_halves = 2;  // near field: target groups of two halves (256) or one (128)
   UmCfg far_grid{um_stages(2), 2};   // far field on sibling-paired tensor grids
   UmCfg far_nodes{um_stages(1), 1};  // far field on interpolation nodes
   int far_pairs = 1;  // 3-D plans of degree kGridP1 - 1: paired grids (1) or nodes (0)
@@ -129,6 +130,7 @@ struct DevPlan {
   int32_t* l2l_list = nullptr;  // row clusters of level >= 1, by level
   std::vector<int> l2l_ptr;
   GroupList far, near;  // chunked to kGroupCap targets (near: also the tensor-core list)
+  GroupList near_h1;    // near field chunked to kTcGroupCap targets (one target half)
   GroupList far_tc;     // chunked to kTcGroupCap targets
   GroupList far_grid2;  // tensor grids: sibling row clusters paired as two target halves
   int* err_flag = nullptr;
@@ -429,18 +431,20 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
   }
   // near groups: targets = points of every row leaf, sources = merged
   // column point intervals; kGroupCap = 256 targets suits both the CUDA-core
-  // kernel sum and the tensor-core one (two halves of 128)
-  {
+  // kernel sum and the tensor-core one with two halves of 128, kTcGroupCap
+  // = 128 the tensor-core one with one half (small leaves; an autotuner
+  // choice)
+  for (int pass = 0; pass < 2; ++pass) {
     HostGroups hg;
     const Pattern& P = plan.pat;
     hg.ivl = P.near_ivl;
     for (size_t l = 0; l < plan.row_leaves.size(); ++l) {
       const int c = plan.row_leaves[l];
       add_target_range(&hg, plan.rows.begin[c], plan.rows.size[c], P.near_ptr[l],
-                       P.near_ptr[l + 1], kGroupCap);
+                       P.near_ptr[l + 1], pass == 0 ? kGroupCap : kTcGroupCap);
     }
     sort_groups(&hg);
-    FMCA_TRY(upload_groups(dp, hg, &dp->near, err));
+    FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->near : &dp->near_h1, err));
   }
   {
     void* p = nullptr;
@@ -545,7 +549,11 @@ KParams<T> make_kparams(const KernelDesc& k, const CallOpts& opts = CallOpts()) 
       break;
     case FMCA_KERNEL_MATERN32:
     case FMCA_KERNEL_MATERN52:
+    case FMCA_KERNEL_MATERN72:
       g = log2e * a;
+      break;
+    case FMCA_KERNEL_MATERN92:
+      g = log2e * 3. / l;
       break;
     case FMCA_KERNEL_GAUSSIAN:
       g = std::sqrt(0.5 * log2e) / l;
@@ -1062,6 +1070,10 @@ cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4
       return FMCA_UM(2);
     case 3:
       return FMCA_UM(3);
+    case 4:
+      return FMCA_UM(4);
+    case 5:
+      return FMCA_UM(5);
     case K_DL_EXPONENTIAL:
       return FMCA_UM(K_DL_EXPONENTIAL);
     case K_DL_EXPONENTIAL + 1:
@@ -1193,10 +1205,17 @@ struct TcChunk {
     dp->mark(FMCA_STAGE_LEAFGATHER, st);
     return cudaGetLastError();
   }
-  cudaError_t near(const UmCfg& uc) {
-    cudaError_t e = launch_um<2>(dp->near, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0,
-                                 dp->err_flag, st, false, uc);
-    dp->launches += dp->near.ngroups ? 1 : 0;
+  // near field: groups of up to 256 targets as two halves of 128, or of up
+  // to 128 targets as one half (halves = 1)
+  cudaError_t near(const UmCfg& uc, int halves) {
+    const GroupList& gl = halves == 1 ? dp->near_h1 : dp->near;
+    cudaError_t e =
+        halves == 1
+            ? launch_um<1>(gl, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0, dp->err_flag, st,
+                           false, uc)
+            : launch_um<2>(gl, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0, dp->err_flag, st,
+                           false, uc);
+    dp->launches += gl.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);
     return e;
   }
@@ -1291,7 +1310,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     FMCA_CK(c.far(dp->cfg));
     FMCA_CK(c.l2l(dp->cfg.tr));
     FMCA_CK(c.leafgather());
-    FMCA_CK(c.near(dp->cfg.near));
+    FMCA_CK(c.near(dp->cfg.near, dp->cfg.near_halves));
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_scaled_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
@@ -1378,8 +1397,9 @@ bool stream_capturing(cudaStream_t st) {
 //     cores against one on the tensor cores (columns padded to 32);
 //  2. on the tensor-core path, after one matvec with the defaults has
 //     filled the workspace, the stages of the first right-hand-side chunk
-//     one by one: the near-field kernel sum over stage counts 4..7 and
-//     units of 1..3 tiles; the far field (moment scaling + kernel sum) on
+//     one by one: the near-field kernel sum with two target halves over
+//     stage counts 4..7 and units of 1..3 tiles and with one half over 5..7
+//     and 1..2; the far field (moment scaling + kernel sum) on
 //     paired tensor grids (stages 4..6, units 1..3) and on nodes (stages
 //     5..7, units 1..2); the upward and downward transfer passes over the
 //     level thresholds {0, 2, 4, 8} x SMs (8 warps per cluster) and
@@ -1444,19 +1464,21 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
         tc_ws_layout(plan, nrhs, ws ? ws : dp->ws, &w);
         TcChunk c = tc_chunk(plan, dp, dp->f, w, make_kparams<float>(k, dp->opts), nrhs, 0, st);
         float bt = -1.f;
-        for (int nst = 4; nst <= kUmMaxStages && status == FMCA_OK; ++nst)
-          for (int F = 1; F <= kUmMaxUnit; ++F) {
-            const UmCfg uc{nst, F};
-            const float ms = timed([&]() { return ok_cuda(c.near(uc)); });
-            if (ms < 0.f) {
-              status = FMCA_ERR_CUDA;
-              break;
+        for (int halves = 2; halves >= 1 && status == FMCA_OK; --halves)
+          for (int nst = halves == 2 ? 4 : 5; nst <= kUmMaxStages && status == FMCA_OK; ++nst)
+            for (int F = 1; F <= (halves == 2 ? kUmMaxUnit : 2); ++F) {
+              const UmCfg uc{nst, F};
+              const float ms = timed([&]() { return ok_cuda(c.near(uc, halves)); });
+              if (ms < 0.f) {
+                status = FMCA_ERR_CUDA;
+                break;
+              }
+              if (bt < 0.f || ms < bt) {
+                bt = ms;
+                best.near = uc;
+                best.near_halves = halves;
+              }
             }
-            if (bt < 0.f || ms < bt) {
-              bt = ms;
-              best.near = uc;
-            }
-          }
         bt = -1.f;
         const bool grid = grid_far(plan);
         for (int pairs = grid ? 1 : 0; pairs >= 0 && status == FMCA_OK; --pairs)
@@ -1568,8 +1590,39 @@ void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) 
   out[FMCA_TUNE_WIDE_BELOW] = c.tr.wide_below;
   out[FMCA_TUNE_SLICE_BELOW] = c.tr.slice_below;
   out[FMCA_TUNE_SMALL_R_TENSOR] = c.small_tc;
+  out[FMCA_TUNE_NEAR_HALVES] = c.near_halves;
   out[FMCA_TUNE_US] = (int32_t)(c.tune_ms * 1000.f);
   (void)pairs;
+}
+
+int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32_t* in,
+                     std::string* err) {
+  auto um_ok = [](int nst, int F) {
+    return nst >= 2 && nst <= kUmMaxStages && F >= 1 && F <= kUmMaxUnit && F <= nst;
+  };
+  if (!um_ok(in[FMCA_TUNE_NEAR_STAGES], in[FMCA_TUNE_NEAR_UNIT]) ||
+      !um_ok(in[FMCA_TUNE_FAR_GRID_STAGES], in[FMCA_TUNE_FAR_GRID_UNIT]) ||
+      !um_ok(in[FMCA_TUNE_FAR_NODE_STAGES], in[FMCA_TUNE_FAR_NODE_UNIT]) ||
+      (in[FMCA_TUNE_FAR_PAIRS] != 0 && in[FMCA_TUNE_FAR_PAIRS] != 1) ||
+      (in[FMCA_TUNE_SMALL_R_TENSOR] != 0 && in[FMCA_TUNE_SMALL_R_TENSOR] != 1) ||
+      (in[FMCA_TUNE_NEAR_HALVES] != 1 && in[FMCA_TUNE_NEAR_HALVES] != 2) ||
+      in[FMCA_TUNE_WIDE_BELOW] < 0 || in[FMCA_TUNE_SLICE_BELOW] < 0) {
+    *err = "launch shapes out of range (stages 2..7, units 1..min(3, stages), flags 0/1, "
+           "halves 1/2, thresholds >= 0)";
+    return FMCA_ERR_INVALID_ARGUMENT;
+  }
+  TuneCfg c = TuneCfg::defaults(dp->sms);
+  c.near = UmCfg{in[FMCA_TUNE_NEAR_STAGES], in[FMCA_TUNE_NEAR_UNIT]};
+  c.near_halves = in[FMCA_TUNE_NEAR_HALVES];
+  c.far_pairs = in[FMCA_TUNE_FAR_PAIRS];
+  c.far_grid = UmCfg{in[FMCA_TUNE_FAR_GRID_STAGES], in[FMCA_TUNE_FAR_GRID_UNIT]};
+  c.far_nodes = UmCfg{in[FMCA_TUNE_FAR_NODE_STAGES], in[FMCA_TUNE_FAR_NODE_UNIT]};
+  c.tr = TrCfg{in[FMCA_TUNE_WIDE_BELOW], in[FMCA_TUNE_SLICE_BELOW]};
+  c.small_tc = in[FMCA_TUNE_SMALL_R_TENSOR];
+  c.tuned = 1;
+  std::lock_guard<std::mutex> lock(dp->mu);
+  dp->tuned[tune_key(precision, type, nrhs)] = c;
+  return FMCA_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1748,6 +1801,10 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
   // does not tune)
   FMCA_TRY(prepare_call(plan, dp, k, precision, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr,
                         nullptr, 0, 0, ws, wsb, st, err, opts, false));
+  // fewer than 17 right-hand sides stay on the CUDA cores: the gradient
+  // terms run over the stored layout of the product, and the tensor-core
+  // layout pads every right-hand-side block to 32 columns
+  dp->cfg.small_tc = 0;
   const bool base_kernel = k.type >= FMCA_KERNEL_EXPONENTIAL && k.type <= FMCA_KERNEL_GAUSSIAN;
   if ((dX || Ky) && !plan.same_tree) {
     *err = "gradients w.r.t. the points and K^T y need one point cloud (Pr == Pc)";

@@ -54,6 +54,10 @@ int adjoint(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision, 
 // Launch shapes for (precision, kernel type, nrhs): out[FMCA_TUNE_*] (see
 // include/fmca_gb300.h); the defaults if the autotuner has not run for it.
 void tuned_config(DevPlan* dev, int precision, int type, int nrhs, int32_t* out);
+// Stores launch shapes for (precision, kernel type, nrhs) as if tuned
+// (validated; FMCA_ERR_INVALID_ARGUMENT when out of range).
+int set_tuned_config(DevPlan* dev, int precision, int type, int nrhs, const int32_t* in,
+                     std::string* err);
 // re-uploads the point coordinates held by the plan (tree and boxes fixed)
 int update_points(const Plan& plan, DevPlan* dev, std::string* err);
 // true if the plan's device data for this precision lives on the current

@@ -45,8 +45,9 @@ __device__ __forceinline__ float pow2i(float e) {
 }
 
 // a = k * 2^w of two squared distances in the coordinates scaled by g
-// (make_kparams: g = log2(e) / l for EXPONENTIAL, log2(e) sqrt(3) / l and
-// log2(e) sqrt(5) / l for MATERN32 / 52, so that r' = sqrt(r2) is the
+// (make_kparams: g = log2(e) / l for EXPONENTIAL, log2(e) sqrt(3) / l,
+// log2(e) sqrt(5) / l, log2(e) sqrt(7) / l and 3 log2(e) / l for MATERN32 /
+// 52 / 72 / 92, so that r' = sqrt(r2) is the
 // kernel argument times log2(e) and e^-argument = 2^-r'). FP32x2
 // arithmetic, the square root and exponential per element on the SFU;
 // sqrt(0) = 0, so coincident points need no guard. ZEROW: w = 0 (point
@@ -62,7 +63,8 @@ __device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<fl
     const float2 u = ZEROW ? f2(-r2.x, -r2.y) : __ffma2_rn(r2, f2(-1.f, -1.f), w);
     const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
     return __fmul2_rn(__fmul2_rn(r2, f2(2.f * kLn2, 2.f * kLn2)), e);
-  } else if constexpr (KT == 0 || KT == 1 || KT == 2 || KT == 10 || KT == 11 || KT == 12) {
+  } else if constexpr (KT == 0 || KT == 1 || KT == 2 || KT == 4 || KT == 5 || KT == 10 ||
+                       KT == 11 || KT == 12) {
     const float2 r = f2(sqrt_approx(r2.x), sqrt_approx(r2.y));
     const float2 u = ZEROW ? f2(-r.x, -r.y) : __ffma2_rn(r, f2(-1.f, -1.f), w);
     const float2 e = f2(ex2_approx(u.x), ex2_approx(u.y));
@@ -73,6 +75,19 @@ __device__ __forceinline__ float2 kscaled2(float2 r2, float2 w, const KParams<fl
     } else if constexpr (KT == 2) {  // MATERN52: (1 + t + t^2 / 3) e^-t
       const float2 p = __ffma2_rn(__ffma2_rn(r, f2(c2 / 3.f, c2 / 3.f), f2(c1, c1)), r,
                                   f2(1.f, 1.f));
+      return __fmul2_rn(p, e);
+    } else if constexpr (KT == 4) {  // MATERN72: (1 + t + 2 t^2 / 5 + t^3 / 15) e^-t
+      constexpr float k2 = 0.4f * c2, k3 = c2 * c1 / 15.f;
+      const float2 p = __ffma2_rn(__ffma2_rn(__ffma2_rn(r, f2(k3, k3), f2(k2, k2)), r,
+                                             f2(c1, c1)),
+                                  r, f2(1.f, 1.f));
+      return __fmul2_rn(p, e);
+    } else if constexpr (KT == 5) {  // MATERN92: (1 + t + 3 t^2 / 7 + 2 t^3 / 21 + t^4 / 105) e^-t
+      constexpr float k2 = 3.f / 7.f * c2, k3 = 2.f / 21.f * c2 * c1, k4 = c2 * c2 / 105.f;
+      const float2 p = __ffma2_rn(
+          __ffma2_rn(__ffma2_rn(__ffma2_rn(r, f2(k4, k4), f2(k3, k3)), r, f2(k2, k2)), r,
+                     f2(c1, c1)),
+          r, f2(1.f, 1.f));
       return __fmul2_rn(p, e);
     } else if constexpr (KT == 10) {  // l dk/dl of EXPONENTIAL: t e^-t
       return __fmul2_rn(__fmul2_rn(r, f2(c1, c1)), e);

@@ -465,6 +465,16 @@ class H2Matrix:
                                                  cov.desc().type, int(nrhs), out))
         return dict(zip(_lib.TUNE_KEYS, [int(v) for v in out]))
 
+    def set_tuned_config(self, nrhs: int, cfg: dict, precision: Optional[str] = None,
+                         cov=None) -> None:
+        """Launch shapes for a key as if tuned (fmca_plan_set_tuned_config),
+        e.g. a dict returned by ``tuned_config`` in an earlier run; the plan
+        must have run a matvec on this device."""
+        cov = cov or self.cov
+        arr = (C.c_int32 * len(_lib.TUNE_KEYS))(*[int(cfg.get(k, 0)) for k in _lib.TUNE_KEYS])
+        check(_lib.load().fmca_plan_set_tuned_config(self._h, _PREC[precision or self.precision],
+                                                     cov.desc().type, int(nrhs), arr))
+
     def set_stalled_wait(self, on: bool) -> None:
         """Test hook (fmca_plan_set_stalled_wait): while on, the first wait of
         every kernel-sum CTA runs out after the wait limit."""

@@ -85,7 +85,9 @@ enum {
      significant bits) and FP32 accumulation; transfers, leaf moments and the
      leaf gather in FP32; final near + far combination in FP64.  Kernels that
      are not bounded by 1 (MULTIQUADRIC, INVMULTIQUADRIC, BIHARMONIC3D,
-     TRIHARMONIC3D) and fewer than 17 right-hand sides use FMCA_PREC_FP32. */
+     TRIHARMONIC3D) use FMCA_PREC_FP32, and so do fewer than 17 right-hand
+     sides unless the autotuner (fmca_plan_set_autotune) measured the
+     tensor-core path, with the columns padded to 32, faster. */
   FMCA_PREC_MIXED = 1,
   /* every stage in FP32 on CUDA cores with FP32 accumulation, final
      combination in FP64 */
@@ -365,7 +367,8 @@ fmca_status fmca_plan_set_stalled_wait(fmca_plan* plan, int on);
      - nrhs <= 16: FP32 CUDA-core kernel sums, or tensor-core kernel sums
        with the right-hand sides padded to 32 columns;
      - the near-field kernel sum's copy-ring stages (4..7) and tiles per
-       accumulation unit (1..3);
+       accumulation unit (1..3), with target groups of two halves of 128 or
+       of one (small leaves);
      - the far field on sibling-paired tensor grids or on interpolation
        nodes (3-D plans of degree 4), with its stages and units;
      - the transfer passes' level thresholds for 8 warps per cluster and
@@ -389,14 +392,23 @@ enum {
   FMCA_TUNE_WIDE_BELOW = 8,       /* transfer levels with fewer clusters: 8 warps each */
   FMCA_TUNE_SLICE_BELOW = 9,      /* transfer levels with fewer clusters: RHS slices of 8 */
   FMCA_TUNE_SMALL_R_TENSOR = 10,  /* nrhs <= 16: 1 tensor cores, 0 CUDA cores */
-  FMCA_TUNE_US = 11,              /* time the tuning took, microseconds */
-  FMCA_TUNE_TUNINGS = 12,         /* tuning runs on this plan so far */
-  FMCA_TUNE_COUNT = 13
+  FMCA_TUNE_NEAR_HALVES = 11,     /* near field: groups of 2 x 128 or 1 x 128 targets */
+  FMCA_TUNE_US = 12,              /* time the tuning took, microseconds */
+  FMCA_TUNE_TUNINGS = 13,         /* tuning runs on this plan so far */
+  FMCA_TUNE_COUNT = 14
 };
 /* The launch shapes a matvec of this key uses now: the tuned ones, or the
    defaults (FMCA_TUNE_TUNED = 0). */
 fmca_status fmca_plan_tuned_config(fmca_plan* plan, int precision, int kernel_type, int nrhs,
                                    int32_t out[FMCA_TUNE_COUNT]);
+/* Sets the launch shapes of a key as if the autotuner had chosen them
+   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_NEAR_HALVES of cfg; the others
+   are ignored): for reusing shapes tuned earlier, for instance in another
+   process on the same plan.  The plan must be resident on the current
+   device (after one matvec).  Out-of-range shapes give
+   FMCA_ERR_INVALID_ARGUMENT. */
+fmca_status fmca_plan_set_tuned_config(fmca_plan* plan, int precision, int kernel_type,
+                                       int nrhs, const int32_t cfg[FMCA_TUNE_COUNT]);
 
 /* Stages of one matvec, indices of fmca_plan_profile's output. */
 enum {

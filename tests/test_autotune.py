@@ -57,3 +57,76 @@ def test_tuned_shapes_are_cached_and_give_the_same_product(cuda_device, dim, p, 
     assert H.tuned_config(R) == {**cfg, "tunings": 2}
     # the defaults of an untuned plan are unaffected
     assert D.tuned_config(R)["tuned"] == 0
+
+
+SHAPES = [
+    # near field with one target half (groups of up to 128 targets)
+    dict(near_halves=1, near_stages=5, near_unit=1),
+    dict(near_halves=1, near_stages=7, near_unit=2),
+    # two halves at the ends of the tuned ranges
+    dict(near_halves=2, near_stages=4, near_unit=3, far_grid_stages=4, far_grid_unit=3),
+    dict(near_halves=2, near_stages=7, near_unit=1, far_grid_stages=6, far_grid_unit=1),
+    # the far field on nodes instead of paired tensor grids
+    dict(far_pairs=0, far_node_stages=7, far_node_unit=2),
+    dict(far_pairs=0, far_node_stages=5, far_node_unit=1, wide_below=0, slice_below=0),
+    # transfers: 8 warps and right-hand-side slices on every level
+    dict(wide_below=1 << 30, slice_below=1 << 30),
+]
+
+
+@pytest.mark.parametrize("leaf", [64, 200])
+@pytest.mark.parametrize("shape", range(len(SHAPES)))
+def test_set_shapes_match_the_oracle(cuda_device, shape, leaf):
+    """Every launch shape the autotuner may choose, set through
+    fmca_plan_set_tuned_config, gives the FP64 oracle's product within 1e-5
+    (3-D, degree 4: paired tensor-grid far field available; leaves of 64..127
+    and of 200..399 points, so one-half near groups hold one leaf or part of
+    one)."""
+    import torch
+    n, R = 25000, 32
+    P = uniform_cloud(n, 3, seed=22)
+    X = np.random.default_rng(22).standard_normal((n, R))
+    Y_ref, _ = oracle.OraclePlan(P, None, 4, 0.8, leaf).action(1, 0.45, X)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.45), P, P, 4, 0.8, min_leaf=leaf,
+                 precision="mixed")
+    x = torch.tensor(X, device=cuda_device)
+    H.matvec(x)  # resident
+    cfg = {**H.tuned_config(R), **SHAPES[shape]}
+    H.set_tuned_config(R, cfg)
+    got = H.tuned_config(R)
+    assert got["tuned"] == 1 and all(got[k] == v for k, v in SHAPES[shape].items())
+    for _ in range(2):
+        y = H.matvec(x).cpu().numpy()
+        H.check_device_error()
+        assert rel_err(y, Y_ref) < 1e-5
+
+
+def test_small_r_on_padded_tensor_cores(cuda_device):
+    # 8 right-hand sides on the tensor cores (columns padded to 32)
+    import torch
+    n, R = 20000, 8
+    P = uniform_cloud(n, 3, seed=23)
+    X = np.random.default_rng(23).standard_normal((n, R))
+    Y_ref, _ = oracle.OraclePlan(P, None, 3, 0.8, 64).action(3, 0.3, X)
+    H = H2Matrix(CovarianceKernel("GAUSSIAN", 0.3), P, P, 3, 0.8, min_leaf=64, precision="mixed")
+    x = torch.tensor(X, device=cuda_device)
+    H.matvec(x)
+    H.set_tuned_config(R, {**H.tuned_config(R), "small_r_tensor": 1, "near_halves": 1})
+    y = H.matvec(x).cpu().numpy()
+    H.check_device_error()
+    assert rel_err(y, Y_ref) < 1e-5
+
+
+def test_set_shapes_are_validated(cuda_device):
+    import torch
+    from fmca_gb300 import FmcaError
+    P = uniform_cloud(3000, 3, seed=24)
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 3, 0.8, precision="mixed")
+    with pytest.raises(FmcaError):  # not resident yet
+        H.set_tuned_config(32, H.tuned_config(32))
+    H.matvec(torch.zeros((3000, 32), dtype=torch.float64, device=cuda_device))
+    for bad in (dict(near_stages=8), dict(near_stages=2, near_unit=3), dict(near_halves=3),
+                dict(far_pairs=2), dict(near_unit=0), dict(wide_below=-1)):
+        with pytest.raises(FmcaError):
+            H.set_tuned_config(32, {**H.tuned_config(32), **bad})
+    assert H.tuned_config(32)["tuned"] == 0

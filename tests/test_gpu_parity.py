@@ -69,6 +69,19 @@ def test_all_kernels(cuda_device, kname, precision):
     assert rel_err(H.action(X), Y_ref) < TOL[precision]
 
 
+@pytest.mark.parametrize("kname", ["EXPONENTIAL", "MATERN52", "MATERN72", "MATERN92", "GAUSSIAN"])
+def test_kernels_on_tensor_grids(cuda_device, kname):
+    # 3-D, degree 4, 32 right-hand sides: the compile-time kernel values of
+    # the tensor-core kernel sums, near field and sibling-paired grid far
+    # field
+    P = uniform_cloud(20000, 3, seed=12)
+    X = np.random.default_rng(12).standard_normal((20000, 32))
+    kt = KNAMES.index(kname)
+    Y_ref, _ = oracle.OraclePlan(P, None, 4, 0.8, 128).action(kt, 0.4, X)
+    H = H2Matrix(CovarianceKernel(kname, 0.4), P, P, 4, 0.8, min_leaf=128, precision="mixed")
+    assert rel_err(H.action(X), Y_ref) < TOL["mixed"]
+
+
 @pytest.mark.parametrize("R", [1, 2, 7, 8, 9, 16, 17, 32, 33, 64, 70])
 @pytest.mark.parametrize("precision", PRECS)
 def test_rhs_counts(cuda_device, R, precision):
