@@ -369,8 +369,7 @@ def run_c4(args, torch, dev):
                                   "df_dX": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))},
         "fp64_vs_central_differences_h1e-4": {"max_rel_err": max(fd_err), "checks": fd_err},
         "dtype": "f32", "data": "synthetic", "autotune": H.tuned_config(1, "mixed"),
-        "adjoint_path": "kernel sums on the FP32 CUDA cores (adjoints with fewer than 17 "
-                        "right-hand sides do not take the padded tensor-core path)",
+
         "config": {"workload": "C4: n=2e5 on S^2, MATERN52 l=0.3 sigma2=1, p=4, eta=0.8, "
                                "leaf 96 (125 effective), x,y ~ N(0,1) float32",
                    "far_blocks": H.info["far_blocks"], "near_pairs": H.info["near_pairs"]},

@@ -1262,7 +1262,9 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     state->s = w.s;
     state->cmax = w.cmax;
     state->ld = ld;
-    state->rb = RB;
+    // up to 8 right-hand sides (tensor cores chosen by the autotuner): the
+    // gradient terms read only the occupied columns of the 32-column layout
+    state->rb = nrhs <= 8 ? rhs_block(nrhs) : RB;
     state->nch = (nrhs + RB - 1) / RB;
     state->fp64 = false;
   }
@@ -1801,10 +1803,6 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
   // does not tune)
   FMCA_TRY(prepare_call(plan, dp, k, precision, dtype, FMCA_ORDER_NATURAL, nrhs, x, sxi, sxr,
                         nullptr, 0, 0, ws, wsb, st, err, opts, false));
-  // fewer than 17 right-hand sides stay on the CUDA cores: the gradient
-  // terms run over the stored layout of the product, and the tensor-core
-  // layout pads every right-hand-side block to 32 columns
-  dp->cfg.small_tc = 0;
   const bool base_kernel = k.type >= FMCA_KERNEL_EXPONENTIAL && k.type <= FMCA_KERNEL_GAUSSIAN;
   if ((dX || Ky) && !plan.same_tree) {
     *err = "gradients w.r.t. the points and K^T y need one point cloud (Pr == Pc)";

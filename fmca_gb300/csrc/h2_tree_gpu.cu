@@ -14,8 +14,9 @@
 //   2. a stable least-significant-digit radix sort of the records, eight
 //      8-bit passes on the key, then one or two passes on the segment (so the
 //      ranges come out whole, each in coordinate order); every pass is a
-//      block histogram, one scan over [digit][block] and a scatter that ranks
-//      equal digits of a warp with __match_any_sync in position order;
+//      block histogram, one scan over the [block][digit] counts and a
+//      scatter that ranks equal digits of a warp with __match_any_sync in
+//      position order;
 //   3. scatter back into the permutation, the coordinates at the split
 //      (offsets size / 2 - 1 and size / 2) per segment, and a scan for equal
 //      neighbouring coordinates (compared as doubles, as std::sort's
@@ -89,7 +90,7 @@ __device__ __forceinline__ uint32_t rx_digit(const uint64_t* keys, const uint32_
   return on_seg ? (sid[p] >> shift) & 255u : (uint32_t)(keys[p] >> shift) & 255u;
 }
 
-// hist[d * nblocks + b] = records of block b with digit d
+// hist[b * 256 + d] = records of block b with digit d
 __global__ void rx_hist_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ sid,
                                uint32_t n, int shift, int on_seg, uint32_t* __restrict__ hist) {
   __shared__ uint32_t cnt[256];
@@ -100,34 +101,37 @@ __global__ void rx_hist_kernel(const uint64_t* __restrict__ keys, const uint32_t
   for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x)
     atomicAdd(&cnt[rx_digit(keys, sid, p, shift, on_seg)], 1u);
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = cnt[d];
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)blockIdx.x * 256 + d] = cnt[d];
 }
 
-// exclusive scan of len entries in place, one block of 1024 threads
-__global__ void rx_scan_kernel(uint32_t* __restrict__ a, uint32_t len) {
-  __shared__ uint32_t part[1024];
-  const uint32_t per = (len + blockDim.x - 1) / blockDim.x;
-  const uint32_t b0 = threadIdx.x * per, b1 = min(len, b0 + per);
-  uint32_t s = 0;
-  for (uint32_t i = b0; i < b1; ++i) s += a[i];
-  part[threadIdx.x] = s;
+// in place: hist[b * 256 + d] = (records of digits < d in all blocks) +
+// (records of digit d in blocks < b), the start of block b's digit-d
+// records after the pass.  One block of 256 threads, thread d walks its
+// digit over the blocks (consecutive threads read consecutive words).
+__global__ void rx_scan_kernel(uint32_t* __restrict__ hist, int nblocks) {
+  __shared__ uint32_t base[256];
+  const int d = threadIdx.x;
+  uint32_t run = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    const uint32_t c = hist[(size_t)b * 256 + d];
+    hist[(size_t)b * 256 + d] = run;
+    run += c;
+  }
+  base[d] = run;
   __syncthreads();
-  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-    const uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+  // exclusive scan of the digit totals (Hillis-Steele over 256 entries)
+  for (int o = 1; o < 256; o <<= 1) {
+    const uint32_t v = d >= o ? base[d - o] : 0u;
     __syncthreads();
-    part[threadIdx.x] += v;
+    base[d] += v;
     __syncthreads();
   }
-  uint32_t run = part[threadIdx.x] - s;  // exclusive prefix of this thread's chunk
-  for (uint32_t i = b0; i < b1; ++i) {
-    const uint32_t v = a[i];
-    a[i] = run;
-    run += v;
-  }
+  const uint32_t off = base[d] - run;
+  for (int b = 0; b < nblocks; ++b) hist[(size_t)b * 256 + d] += off;
 }
 
 // stable scatter of one radix pass: records of block b with digit d go to
-// offs[d * nblocks + b] + their rank among the block's digit-d records in
+// offs[b * 256 + d] + their rank among the block's digit-d records in
 // position order (warps own consecutive runs of 512 records; in every round
 // of 32 the lanes with equal digits rank by __match_any_sync)
 __global__ void rx_scatter_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
@@ -171,7 +175,7 @@ __global__ void rx_scatter_kernel(const uint64_t* __restrict__ kin, const uint32
       d = rx_digit(kin, sin, p, shift, on_seg);
       peers = __match_any_sync(act, d);
       const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-      const uint32_t dst = offs[(size_t)d * gridDim.x + blockIdx.x] + cnt[warp][d] + rank;
+      const uint32_t dst = offs[(size_t)blockIdx.x * 256 + d] + cnt[warp][d] + rank;
       kout[dst] = kin[p];
       vout[dst] = vin[p];
       sout[dst] = sin[p];
@@ -282,7 +286,7 @@ struct RecordSort {
     const int nb = (int)((n + kRxTile - 1) / kRxTile);
     auto pass = [&](int shift, int on_seg) {
       rx_hist_kernel<<<nb, kRxThreads, 0, st>>>(k[cur], s[cur], n, shift, on_seg, hist);
-      rx_scan_kernel<<<1, 1024, 0, st>>>(hist, (uint32_t)(256 * nb));
+      rx_scan_kernel<<<1, 256, 0, st>>>(hist, nb);
       rx_scatter_kernel<<<nb, kRxThreads, 0, st>>>(k[cur], v[cur], s[cur], k[cur ^ 1], v[cur ^ 1],
                                                    s[cur ^ 1], n, hist, shift, on_seg);
       cur ^= 1;

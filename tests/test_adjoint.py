@@ -132,6 +132,27 @@ def test_gpu_adjoint_mixed_tensor_core_path(cuda_device):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("R", [1, 5])
+def test_gpu_adjoint_few_rhs_on_padded_tensor_cores(cuda_device, R):
+    # fewer than 17 right-hand sides with the tensor-core path set for the
+    # key (as the autotuner may choose it): the products run on 32 padded
+    # columns and the gradient terms read only the R occupied ones
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    P, x, y = _problem(8000, R, seed=13, sphere=True)
+    O = oracle.OraclePlan(P, None, 4, 0.8, 0)
+    vals_ref, dX_ref = oracle.adjoint(O, 2, 0.3, x, y, sigma2=1.0)
+    H = H2Matrix(CovarianceKernel("MATERN52", 0.3), P, P, 4, 0.8)
+    xt, yt = torch.tensor(x, device=cuda_device), torch.tensor(y, device=cuda_device)
+    H.matvec(xt)  # resident
+    H.set_tuned_config(R, {**H.tuned_config(R), "small_r_tensor": 1})
+    out = H.adjoint(xt, yt, precision="mixed")
+    H.check_device_error()
+    assert np.allclose(out["values"].cpu().numpy(), vals_ref, rtol=1e-5, atol=0)
+    assert rel_err(out["dX"].cpu().numpy(), dX_ref) < 1e-4
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kname", ["MATERN32", "MATERN52", "GAUSSIAN"])
 def test_gpu_adjoint_against_finite_differences(cuda_device, kname):
     # central differences (h = 1e-4) of the GPU FP64 product with the tree,
