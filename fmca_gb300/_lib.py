@@ -56,7 +56,8 @@ EXPORTED = [
 ]
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
-             "small_r_tensor", "near_halves", "tune_us", "tunings"]
+             "small_r_tensor", "near_halves", "near_persist", "far_persist", "tune_us",
+             "tunings"]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
 

@@ -74,6 +74,7 @@ struct GroupList {
 // accumulation unit).
 struct UmCfg {
   int nst, F;
+  int persist = 0;  // 1: one CTA per SM running groups in turn; 0: one CTA per group
 };
 // Transfer level thresholds (cluster counts): levels with fewer than
 // wide_below clusters run the sum-factorised transfer with 8 warps per
@@ -131,6 +132,7 @@ struct DevPlan {
   std::vector<int> l2l_ptr;
   GroupList far, near;  // chunked to kGroupCap targets (near: also the tensor-core list)
   GroupList near_h1;    // near field chunked to kTcGroupCap targets (one target half)
+  float* gexp = nullptr;  // per far group and target half: the moment exponent E
   GroupList far_tc;     // chunked to kTcGroupCap targets
   GroupList far_grid2;  // tensor grids: sibling row clusters paired as two target halves
   int* err_flag = nullptr;
@@ -453,6 +455,15 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     dp->alloc_bytes += sizeof(int);
     FMCA_CK(cudaMemset(p, 0, sizeof(int)));
     dp->err_flag = static_cast<int*>(p);
+  }
+  {
+    const size_t ng = std::max<size_t>({(size_t)1, (size_t)dp->far_tc.ngroups,
+                                        (size_t)dp->far_grid2.ngroups});
+    void* p = nullptr;
+    FMCA_CK(cudaMalloc(&p, sizeof(float) * 2 * ng));
+    dp->allocs.push_back(p);
+    dp->alloc_bytes += sizeof(float) * 2 * ng;
+    dp->gexp = static_cast<float*>(p);
   }
   return FMCA_OK;
 }
@@ -1027,13 +1038,14 @@ template <int KT, int H, bool REL, bool GRID>
 cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        const UmCfg& uc) {
+                        const UmCfg& uc, const float* gexp, int sms) {
   auto kern = ksum_um_kernel<KT, H, REL, GRID>;
   const size_t smem = um_smem_bytes(H, kUmMaxStages);
   ensure_smem(kern, smem);
-  kern<<<gl.ngroups, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
-      gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf, gl.imask, uc.nst,
-      uc.F);
+  const int grid = uc.persist ? std::min(gl.ngroups, sms) : gl.ngroups;
+  kern<<<grid, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
+      gl.groups, gl.ngroups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf,
+      gl.imask, gexp, uc.nst, uc.F);
   return cudaGetLastError();
 }
 
@@ -1041,26 +1053,36 @@ template <int KT, int H>
 cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        bool grid, const UmCfg& uc) {
+                        bool grid, const UmCfg& uc, float* gexp, int sms) {
+  // node sources: the groups' moment exponents first
+  if (q > 0) {
+    const int blocks = (gl.ngroups * 32 + 255) / 256;
+    if (grid)
+      group_exponents_kernel<true, H><<<blocks, 256, 0, st>>>(gl.groups, gl.ngroups, gl.ivl,
+                                                              pairs, q, gl.imask, gexp);
+    else
+      group_exponents_kernel<false, H><<<blocks, 256, 0, st>>>(gl.groups, gl.ngroups, gl.ivl,
+                                                               pairs, q, gl.imask, gexp);
+  }
   if constexpr (H == 2) {  // tensor grids: sibling row clusters as the two halves
     if (grid)
       return launch_um_v<KT, 2, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st,
-                                            uc);
+                                            uc, gexp, sms);
   }
   if (q > 0)
     return launch_um_v<KT, H, true, false>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st,
-                                           uc);
+                                           uc, gexp, sms);
   return launch_um_v<KT, H, false, false>(gl, tgt, pairs, vals, out, rcount, kp, 0, errf, st,
-                                          uc);
+                                          uc, nullptr, sms);
 }
 
 template <int H>
 cudaError_t launch_um_k(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        bool grid, const UmCfg& uc) {
+                        bool grid, const UmCfg& uc, float* gexp, int sms) {
 #define FMCA_UM(KT) \
-  launch_um_t<KT, H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc)
+  launch_um_t<KT, H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc, gexp, sms)
   switch (kp.type) {
     case 0:
       return FMCA_UM(0);
@@ -1095,11 +1117,11 @@ template <int H>
 cudaError_t launch_um(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                       const __half* vals, float* out, int rcount,
                       const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                      bool grid, const UmCfg& uc) {
+                      bool grid, const UmCfg& uc, float* gexp, int sms) {
   if (gl.ngroups == 0) return cudaSuccess;
   if (uc.nst < 2 || uc.nst > kUmMaxStages || uc.F < 1 || uc.F > kUmMaxUnit || uc.F > uc.nst)
     return cudaErrorInvalidValue;
-  return launch_um_k<H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc);
+  return launch_um_k<H>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st, grid, uc, gexp, sms);
 }
 
 bool grid_far(const Plan& plan) {
@@ -1168,11 +1190,11 @@ struct TcChunk {
     if (e != cudaSuccess) return e;
     const GroupList& fl = grid ? dp->far_grid2 : dp->far_tc;
     e = grid ? launch_um<2>(fl, S->nodes_r, w.pairs_n, w.tv, s, rcount, kp, q, dp->err_flag, st,
-                            true, cfg.far_grid)
+                            true, cfg.far_grid, dp->gexp, dp->sms)
              : launch_um<1>(fl, S->nodes_r, w.pairs_n, w.tv, s, rcount, kp, q, dp->err_flag, st,
-                            false, cfg.far_nodes);
+                            false, cfg.far_nodes, dp->gexp, dp->sms);
     if (e != cudaSuccess) return e;
-    dp->launches += fl.ngroups ? 1 : 0;
+    dp->launches += fl.ngroups ? 2 : 0;  // exponents + kernel sum
     dp->launches +=
         launch_basis_change<float, kTcRhs>(S->ip, Cr, S->from_nodal, s, kTcRhs, 0, rcount, st);
     dp->mark(FMCA_STAGE_FAR, st);
@@ -1212,9 +1234,9 @@ struct TcChunk {
     cudaError_t e =
         halves == 1
             ? launch_um<1>(gl, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0, dp->err_flag, st,
-                           false, uc)
+                           false, uc, nullptr, dp->sms)
             : launch_um<2>(gl, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0, dp->err_flag, st,
-                           false, uc);
+                           false, uc, nullptr, dp->sms);
     dp->launches += gl.ngroups ? 1 : 0;
     dp->mark(FMCA_STAGE_NEAR, st);
     return e;
@@ -1481,6 +1503,15 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
                 best.near_halves = halves;
               }
             }
+        if (status == FMCA_OK) {  // the fastest shape as a persistent launch
+          UmCfg uc = best.near;
+          uc.persist = 1;
+          const float ms = timed([&]() { return ok_cuda(c.near(uc, best.near_halves)); });
+          if (ms < 0.f)
+            status = FMCA_ERR_CUDA;
+          else if (ms < bt)
+            best.near = uc;
+        }
         bt = -1.f;
         const bool grid = grid_far(plan);
         for (int pairs = grid ? 1 : 0; pairs >= 0 && status == FMCA_OK; --pairs)
@@ -1501,6 +1532,17 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
                 best.far_nodes = cand.far_nodes;
               }
             }
+        if (status == FMCA_OK) {  // the fastest shape as a persistent launch
+          TuneCfg cand = best;
+          (cand.far_pairs && grid ? cand.far_grid : cand.far_nodes).persist = 1;
+          const float ms = timed([&]() { return ok_cuda(c.far(cand)); });
+          if (ms < 0.f) {
+            status = FMCA_ERR_CUDA;
+          } else if (ms < bt) {
+            best.far_grid = cand.far_grid;
+            best.far_nodes = cand.far_nodes;
+          }
+        }
         bt = -1.f;
         for (int wide : {0, 2, 4, 8})
           for (int slice : {0, 1, 2, 4}) {
@@ -1593,6 +1635,9 @@ void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) 
   out[FMCA_TUNE_SLICE_BELOW] = c.tr.slice_below;
   out[FMCA_TUNE_SMALL_R_TENSOR] = c.small_tc;
   out[FMCA_TUNE_NEAR_HALVES] = c.near_halves;
+  out[FMCA_TUNE_NEAR_PERSIST] = c.near.persist;
+  // the tuner sets it on the far-field form the plan uses
+  out[FMCA_TUNE_FAR_PERSIST] = c.far_grid.persist | c.far_nodes.persist;
   out[FMCA_TUNE_US] = (int32_t)(c.tune_ms * 1000.f);
   (void)pairs;
 }
@@ -1608,17 +1653,21 @@ int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32
       (in[FMCA_TUNE_FAR_PAIRS] != 0 && in[FMCA_TUNE_FAR_PAIRS] != 1) ||
       (in[FMCA_TUNE_SMALL_R_TENSOR] != 0 && in[FMCA_TUNE_SMALL_R_TENSOR] != 1) ||
       (in[FMCA_TUNE_NEAR_HALVES] != 1 && in[FMCA_TUNE_NEAR_HALVES] != 2) ||
+      (in[FMCA_TUNE_NEAR_PERSIST] != 0 && in[FMCA_TUNE_NEAR_PERSIST] != 1) ||
+      (in[FMCA_TUNE_FAR_PERSIST] != 0 && in[FMCA_TUNE_FAR_PERSIST] != 1) ||
       in[FMCA_TUNE_WIDE_BELOW] < 0 || in[FMCA_TUNE_SLICE_BELOW] < 0) {
     *err = "launch shapes out of range (stages 2..7, units 1..min(3, stages), flags 0/1, "
            "halves 1/2, thresholds >= 0)";
     return FMCA_ERR_INVALID_ARGUMENT;
   }
   TuneCfg c = TuneCfg::defaults(dp->sms);
-  c.near = UmCfg{in[FMCA_TUNE_NEAR_STAGES], in[FMCA_TUNE_NEAR_UNIT]};
+  c.near = UmCfg{in[FMCA_TUNE_NEAR_STAGES], in[FMCA_TUNE_NEAR_UNIT], in[FMCA_TUNE_NEAR_PERSIST]};
   c.near_halves = in[FMCA_TUNE_NEAR_HALVES];
   c.far_pairs = in[FMCA_TUNE_FAR_PAIRS];
-  c.far_grid = UmCfg{in[FMCA_TUNE_FAR_GRID_STAGES], in[FMCA_TUNE_FAR_GRID_UNIT]};
-  c.far_nodes = UmCfg{in[FMCA_TUNE_FAR_NODE_STAGES], in[FMCA_TUNE_FAR_NODE_UNIT]};
+  c.far_grid = UmCfg{in[FMCA_TUNE_FAR_GRID_STAGES], in[FMCA_TUNE_FAR_GRID_UNIT],
+                     in[FMCA_TUNE_FAR_PERSIST]};
+  c.far_nodes = UmCfg{in[FMCA_TUNE_FAR_NODE_STAGES], in[FMCA_TUNE_FAR_NODE_UNIT],
+                      in[FMCA_TUNE_FAR_PERSIST]};
   c.tr = TrCfg{in[FMCA_TUNE_WIDE_BELOW], in[FMCA_TUNE_SLICE_BELOW]};
   c.small_tc = in[FMCA_TUNE_SMALL_R_TENSOR];
   c.tuned = 1;

@@ -368,9 +368,11 @@ fmca_status fmca_plan_set_stalled_wait(fmca_plan* plan, int on);
        with the right-hand sides padded to 32 columns;
      - the near-field kernel sum's copy-ring stages (4..7) and tiles per
        accumulation unit (1..3), with target groups of two halves of 128 or
-       of one (small leaves);
+       of one (small leaves), launched with one CTA per group or as a
+       persistent grid of one CTA per SM that runs the groups in turn;
      - the far field on sibling-paired tensor grids or on interpolation
-       nodes (3-D plans of degree 4), with its stages and units;
+       nodes (3-D plans of degree 4), with its stages, units and launch
+       form;
      - the transfer passes' level thresholds for 8 warps per cluster and
        for splitting the right-hand sides into slices of 8.
    That first call takes longer (about 20 kernel-sum runs) and gives the
@@ -393,16 +395,18 @@ enum {
   FMCA_TUNE_SLICE_BELOW = 9,      /* transfer levels with fewer clusters: RHS slices of 8 */
   FMCA_TUNE_SMALL_R_TENSOR = 10,  /* nrhs <= 16: 1 tensor cores, 0 CUDA cores */
   FMCA_TUNE_NEAR_HALVES = 11,     /* near field: groups of 2 x 128 or 1 x 128 targets */
-  FMCA_TUNE_US = 12,              /* time the tuning took, microseconds */
-  FMCA_TUNE_TUNINGS = 13,         /* tuning runs on this plan so far */
-  FMCA_TUNE_COUNT = 14
+  FMCA_TUNE_NEAR_PERSIST = 12,    /* near field: 1 one CTA per SM running groups in turn */
+  FMCA_TUNE_FAR_PERSIST = 13,     /* far field: the same */
+  FMCA_TUNE_US = 14,              /* time the tuning took, microseconds */
+  FMCA_TUNE_TUNINGS = 15,         /* tuning runs on this plan so far */
+  FMCA_TUNE_COUNT = 16
 };
 /* The launch shapes a matvec of this key uses now: the tuned ones, or the
    defaults (FMCA_TUNE_TUNED = 0). */
 fmca_status fmca_plan_tuned_config(fmca_plan* plan, int precision, int kernel_type, int nrhs,
                                    int32_t out[FMCA_TUNE_COUNT]);
 /* Sets the launch shapes of a key as if the autotuner had chosen them
-   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_NEAR_HALVES of cfg; the others
+   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_FAR_PERSIST of cfg; the others
    are ignored): for reusing shapes tuned earlier, for instance in another
    process on the same plan.  The plan must be resident on the current
    device (after one matvec).  Out-of-range shapes give

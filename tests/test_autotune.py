@@ -71,14 +71,21 @@ SHAPES = [
     dict(far_pairs=0, far_node_stages=5, far_node_unit=1, wide_below=0, slice_below=0),
     # transfers: 8 warps and right-hand-side slices on every level
     dict(wide_below=1 << 30, slice_below=1 << 30),
+    # persistent launches: one CTA per SM running the groups in turn
+    dict(near_persist=1, far_persist=1),
+    dict(near_persist=1, far_persist=1, near_halves=1, near_stages=6, near_unit=2,
+         far_pairs=0, far_node_stages=6, far_node_unit=2),
+    dict(near_persist=1, far_persist=1, near_stages=4, near_unit=3, far_grid_stages=4,
+         far_grid_unit=3),
 ]
 
 
 @pytest.mark.parametrize("leaf", [64, 200])
 @pytest.mark.parametrize("shape", range(len(SHAPES)))
 def test_set_shapes_match_the_oracle(cuda_device, shape, leaf):
-    """Every launch shape the autotuner may choose, set through
-    fmca_plan_set_tuned_config, gives the FP64 oracle's product within 1e-5
+    """Every launch shape the autotuner may choose (persistent launches
+    included), set through fmca_plan_set_tuned_config, gives the FP64
+    oracle's product within 1e-5
     (3-D, degree 4: paired tensor-grid far field available; leaves of 64..127
     and of 200..399 points, so one-half near groups hold one leaf or part of
     one)."""
@@ -126,7 +133,8 @@ def test_set_shapes_are_validated(cuda_device):
         H.set_tuned_config(32, H.tuned_config(32))
     H.matvec(torch.zeros((3000, 32), dtype=torch.float64, device=cuda_device))
     for bad in (dict(near_stages=8), dict(near_stages=2, near_unit=3), dict(near_halves=3),
-                dict(far_pairs=2), dict(near_unit=0), dict(wide_below=-1)):
+                dict(far_pairs=2), dict(near_unit=0), dict(wide_below=-1),
+                dict(near_persist=2), dict(far_persist=-1)):
         with pytest.raises(FmcaError):
             H.set_tuned_config(32, {**H.tuned_config(32), **bad})
     assert H.tuned_config(32)["tuned"] == 0

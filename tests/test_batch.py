@@ -3,7 +3,9 @@ matvecs recorded into CUDA graphs.
 
 CPU: the batched plan holds every cloud's own tree and block lists, offset.
 GPU: one batched matvec (all clouds per launch) against the oracle run cloud
-by cloud, in every precision; a graph replay against the direct call."""
+by cloud, in every precision; a graph replay against the direct call; the
+persistent kernel sums (one CTA per SM over the groups of every cloud) in a
+graph against the oracle."""
 from __future__ import annotations
 
 import numpy as np
@@ -119,3 +121,31 @@ def test_batched_adjoint_values(cuda_device):
         ref += v
         assert rel_err(dX[o:e], d) < 1e-10, i
     assert np.allclose(vals, ref, rtol=1e-10, atol=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deg", [3, 4])
+def test_persistent_kernel_sums_over_all_clouds(cuda_device, deg):
+    # one persistent launch per kernel sum: one CTA per SM runs the groups of
+    # every cloud (the flattened near and far group lists) in turn, recorded
+    # into a CUDA graph; against the oracle cloud by cloud
+    import torch
+    clouds = mixture_clouds(12, seed=10)
+    R = 32
+    cov = CovarianceKernel("GAUSSIAN", 0.2)
+    B = H2Matrix.batched(cov, clouds, deg, 0.8, precision="mixed")
+    X = torch.tensor(np.random.default_rng(11).standard_normal((B.rows(), R)), device=cuda_device)
+    B.matvec(X)  # resident
+    B.set_tuned_config(R, {**B.tuned_config(R), "near_persist": 1, "far_persist": 1})
+    Y = torch.empty_like(X)
+    g = B.graph(X, Y)
+    for _ in range(2):
+        g.launch()
+        torch.cuda.synchronize()
+        B.check_device_error()
+        Yh, Xh = Y.cpu().numpy(), X.cpu().numpy()
+        for i, P in enumerate(clouds):
+            o, e = B.offsets[i], B.offsets[i + 1]
+            Yi, _ = oracle.OraclePlan(P, None, deg, 0.8, 0).action(3, 0.2, Xh[o:e])
+            assert rel_err(Yh[o:e], Yi) < TOL["mixed"], i
+    del g

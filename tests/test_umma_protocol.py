@@ -15,6 +15,9 @@ Roles and barriers follow the kernel:
 - Four flush warps (one per tensor-memory lane quarter) take the units in
   order: each waits for unit u (accf[u % 4]) and releases its accumulator
   buffer (acce[u & 1]); the first also frees the unit's stages.
+- A persistent CTA runs the tiles of several groups through the same ring,
+  pair slots and accumulator buffers: the counters run on, and the last
+  unit of every group closes early (units never span two groups).
 
 mbarrier waits are parity waits: they pass when the barrier's current phase
 has the other parity, which is the intended phase only while the waiter is
@@ -54,41 +57,62 @@ def npair_slots(H, cols=512):
     return (cols - 256) // (H * 32)
 
 
+def units_of(items, F):
+    """(first tile, tile count) of every accumulation unit: units of F tiles
+    that never span two items (a CTA of the persistent kernel sum runs its
+    items' tiles through one ring, closing the last unit of every item)."""
+    out, k = [], 0
+    for n in items:
+        for t in range(0, n, F):
+            out.append((k + t, min(F, n - t)))
+        k += n
+    return out
+
+
 def simulate(ntiles, H, seed, F=1, NST=None, NPS=None, nbars=4, rnd=None):
-    """'ok', 'deadlock' or 'early' for one random schedule."""
+    """'ok', 'deadlock' or 'early' for one random schedule.  ntiles: the
+    tile count of one group, or a list of the tile counts of the items one
+    persistent CTA processes in turn."""
     rnd = rnd or random.Random(seed)
     NST = NST or nstages(H)
     NPS = NPS or npair_slots(H)
+    items = list(ntiles) if isinstance(ntiles, (list, tuple)) else [ntiles]
+    units = units_of(items, F)
+    total = sum(items)
+    unit_of = {}
+    for u, (t0, c) in enumerate(units):
+        for t in range(t0, t0 + c):
+            unit_of[t] = u
     full = [Bar(1) for _ in range(NST)]
     empty = [Bar(1) for _ in range(NST)]
     afull = [Bar(4) for _ in range(NPS)]
     aempty = [Bar(2 if H == 2 else 1) for _ in range(NPS)]
     accf = [Bar(2) for _ in range(nbars)]
     acce = [Bar(4) for _ in range(2)]
-    nunits = (ntiles + F - 1) // F
 
     def producer():
-        for k in range(ntiles):
+        for k in range(total):
             st = k % NST
             if k >= NST:
                 yield ("wait", empty[st], k // NST - 1)
             yield ("arrive", full[st])
 
     def products(j):
-        for k in range(ntiles):
-            st, u = k % NST, k // F
+        for k in range(total):
+            st, u = k % NST, unit_of[k]
+            t0, c = units[u]
             yield ("wait", full[st], k // NST)
-            if k % F == 0 and u >= 2:
+            if k == t0 and u >= 2:
                 yield ("wait", acce[u & 1], (u >> 1) - 1)
             for s in (range(4) if H == 2 else (j, j + 2)):
                 p = 4 * k + s
                 yield ("wait", afull[p % NPS], p // NPS)
                 yield ("commit", aempty[p % NPS])
-            if k % F == F - 1 or k == ntiles - 1:
+            if k == t0 + c - 1:
                 yield ("commit", accf[u % nbars])
 
     def evaluation(s, w):
-        for k in range(ntiles):
+        for k in range(total):
             yield ("wait", full[k % NST], k // NST)
             p = 4 * k + s
             if p >= NPS:
@@ -96,11 +120,11 @@ def simulate(ntiles, H, seed, F=1, NST=None, NPS=None, nbars=4, rnd=None):
             yield ("arrive", afull[p % NPS])
 
     def flusher(w):
-        for u in range(nunits):
+        for u, (t0, c) in enumerate(units):
             yield ("wait", accf[u % nbars], u // nbars)
             yield ("arrive", acce[u & 1])
             if w == 0:
-                for t in range(u * F, min(ntiles, u * F + F)):
+                for t in range(t0, t0 + c):
                     yield ("arrive", empty[t % NST])
 
     roles = ([producer(), products(0), products(1)] +
@@ -221,3 +245,21 @@ def test_protocol_over_tuned_launch_shapes(H, NST, F):
         for seed in range(6):
             rnd = BiasedRandom(seed, b)
             assert simulate(13, H, seed, F=F, NST=NST, rnd=rnd) == "ok", (b, seed)
+
+
+# items of a persistent CTA: tile counts of consecutive groups (empty groups
+# included), the units closing at every group's end
+ITEMS = [[3, 1, 4], [1, 1, 1, 1, 1], [0, 5, 0, 2], [7, 0, 0, 6, 1], [2, 9, 3, 3]]
+
+
+@pytest.mark.parametrize("H,NST,F", [(1, 6, 1), (2, 5, 2), (2, 4, 3), (1, 5, 2), (2, 7, 3),
+                                     (2, 2, 2), (1, 3, 3)])
+def test_protocol_over_items_of_a_persistent_cta(H, NST, F):
+    for seed in range(25):
+        for items in ITEMS:
+            assert simulate(items, H, seed, F=F, NST=NST) == "ok", (items, seed)
+    for b in ({"done": 0.05}, {0: 50.0, "done": 0.1}, {4: 0.05}, {3: 20.0, "done": 0.2}):
+        for seed in range(8):
+            for items in ITEMS:
+                rnd = BiasedRandom(seed, b)
+                assert simulate(items, H, seed, F=F, NST=NST, rnd=rnd) == "ok", (b, items, seed)
