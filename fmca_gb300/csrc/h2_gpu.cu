@@ -14,6 +14,7 @@
 #include "h2_gpu_kernels.cuh"
 #include "h2_tc_kernels.cuh"
 #include "h2_umma_kernels.cuh"
+#include "h2_umma_persistent.h"
 
 namespace fmca {
 namespace gpu {
@@ -1038,14 +1039,17 @@ template <int KT, int H, bool REL, bool GRID>
 cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4* pairs,
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
-                        const UmCfg& uc, const float* gexp, int sms) {
+                        const UmCfg& uc, float* gexp, int sms) {
+  if (uc.persist)
+    return launch_um_persistent(KT, H, REL, GRID, gl.groups, gl.ngroups, gl.ivl, gl.imask, tgt,
+                                pairs, vals, out, rcount, kp, q, errf, gexp, uc.nst, uc.F, sms,
+                                st);
   auto kern = ksum_um_kernel<KT, H, REL, GRID>;
   const size_t smem = um_smem_bytes(H, kUmMaxStages);
   ensure_smem(kern, smem);
-  const int grid = uc.persist ? std::min(gl.ngroups, sms) : gl.ngroups;
-  kern<<<grid, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
-      gl.groups, gl.ngroups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf,
-      gl.imask, gexp, uc.nst, uc.F);
+  kern<<<gl.ngroups, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
+      gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf, gl.imask, uc.nst,
+      uc.F);
   return cudaGetLastError();
 }
 
@@ -1054,16 +1058,6 @@ cudaError_t launch_um_t(const GroupList& gl, const Pt4<float>* tgt, const float4
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                         bool grid, const UmCfg& uc, float* gexp, int sms) {
-  // node sources: the groups' moment exponents first
-  if (q > 0) {
-    const int blocks = (gl.ngroups * 32 + 255) / 256;
-    if (grid)
-      group_exponents_kernel<true, H><<<blocks, 256, 0, st>>>(gl.groups, gl.ngroups, gl.ivl,
-                                                              pairs, q, gl.imask, gexp);
-    else
-      group_exponents_kernel<false, H><<<blocks, 256, 0, st>>>(gl.groups, gl.ngroups, gl.ivl,
-                                                               pairs, q, gl.imask, gexp);
-  }
   if constexpr (H == 2) {  // tensor grids: sibling row clusters as the two halves
     if (grid)
       return launch_um_v<KT, 2, true, true>(gl, tgt, pairs, vals, out, rcount, kp, q, errf, st,
@@ -1194,7 +1188,9 @@ struct TcChunk {
              : launch_um<1>(fl, S->nodes_r, w.pairs_n, w.tv, s, rcount, kp, q, dp->err_flag, st,
                             false, cfg.far_nodes, dp->gexp, dp->sms);
     if (e != cudaSuccess) return e;
-    dp->launches += fl.ngroups ? 2 : 0;  // exponents + kernel sum
+    // the persistent form computes the groups' exponents in a launch first
+    const bool persist = grid ? cfg.far_grid.persist : cfg.far_nodes.persist;
+    dp->launches += fl.ngroups ? (persist ? 2 : 1) : 0;
     dp->launches +=
         launch_basis_change<float, kTcRhs>(S->ip, Cr, S->from_nodal, s, kTcRhs, 0, rcount, st);
     dp->mark(FMCA_STAGE_FAR, st);

@@ -1064,7 +1064,7 @@ __global__ void scatter_kernel(const uint32_t* __restrict__ perm, int64_t n,
 }
 
 // dense FP64 kernel matrix (CovarianceKernel::eval), column-major n_r x n_c
-__global__ void dense_eval_kernel(int dim, const double* __restrict__ PR,
+static __global__ void dense_eval_kernel(int dim, const double* __restrict__ PR,
                                   int64_t nr, const double* __restrict__ PC,
                                   int64_t nc, KParams<double> kp, double sigma2,
                                   double* __restrict__ out) {

@@ -227,7 +227,7 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
 
 // pair records of n points (cluster order), coordinates multiplied by -g,
 // w = 0; zero records up to um_padded(n)
-__global__ void point_pairs_kernel(int64_t n, const Pt4<float>* __restrict__ pts, float g,
+static __global__ void point_pairs_kernel(int64_t n, const Pt4<float>* __restrict__ pts, float g,
                                    float4* __restrict__ pairs) {
   const int64_t np = (int64_t)um_padded(n) / 2;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
@@ -246,7 +246,7 @@ __global__ void point_pairs_kernel(int64_t n, const Pt4<float>* __restrict__ pts
 // the pair-record entries of the cluster's q nodes with coordinates
 // multiplied by -g and w = e (-1000 for a cluster without moments). The
 // last block also zeroes the padding after node C q.
-__global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict__ t,
+static __global__ void tscale_kernel(int C, int q, int rcount, const float* __restrict__ t,
                               const Pt4<float>* __restrict__ nodes, float g,
                               __half* __restrict__ tv, float* __restrict__ pairs) {
   const int c = blockIdx.x;
@@ -309,7 +309,7 @@ constexpr int kGridRows = 128;
 
 // per column cluster c (one block each, q = kGridP1^3 nodes): moments t in
 // the plan's node order, midx = digits of each node (3 per node)
-__global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ t,
+static __global__ void tscale_grid_kernel(int C, int rcount, const float* __restrict__ t,
                                    const Pt4<float>* __restrict__ nodes,
                                    const int* __restrict__ midx, float g,
                                    __half* __restrict__ tv, float* __restrict__ rec) {
