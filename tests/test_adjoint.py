@@ -148,7 +148,10 @@ def test_gpu_adjoint_few_rhs_on_padded_tensor_cores(cuda_device, R):
     H.set_tuned_config(R, {**H.tuned_config(R), "small_r_tensor": 1})
     out = H.adjoint(xt, yt, precision="mixed")
     H.check_device_error()
-    assert np.allclose(out["values"].cpu().numpy(), vals_ref, rtol=1e-5, atol=0)
+    # f and its derivatives are single scalars summed over few columns: the
+    # mixed path's ~1e-6 relative error of the products grows by their
+    # cancellation (df/dl 3e-5 here at R = 1, the CUDA-core path alike)
+    assert np.allclose(out["values"].cpu().numpy(), vals_ref, rtol=1e-4, atol=0)
     assert rel_err(out["dX"].cpu().numpy(), dX_ref) < 1e-4
 
 
