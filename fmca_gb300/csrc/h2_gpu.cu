@@ -61,7 +61,29 @@ struct DevSet {
   T* to_nodal = nullptr;    // total degree: invV^T (row-major q x q)
   T* from_nodal = nullptr;  // total degree: invV
   InterpDev<T> ip;
+  // centre of the box of both point clouds (the near field's dot-product
+  // distance form measures coordinates from it)
+  float ctr[3] = {0.f, 0.f, 0.f};
 };
+
+// midpoint of the bounding box of the row and column points (dim <= 3)
+void cloud_centre(const Plan& plan, float ctr[3]) {
+  const int dim = plan.interp.dim;
+  for (int d = 0; d < 3; ++d) {
+    double lo = 0, hi = 0;
+    bool any = false;
+    for (const std::vector<double>* P : {&plan.points_r, &plan.points_c}) {
+      for (size_t i = 0; d < dim && i + dim <= P->size(); i += dim) {
+        const double v = (*P)[i + d];
+        if (!std::isfinite(v)) continue;
+        if (!any || v < lo) lo = v;
+        if (!any || v > hi) hi = v;
+        any = true;
+      }
+    }
+    ctr[d] = any ? (float)(0.5 * (lo + hi)) : 0.f;
+  }
+}
 
 struct GroupList {
   KGroup* groups = nullptr;
@@ -272,6 +294,7 @@ int upload_set(const Plan& plan, DevPlan* dp, DevSet<T>* s, std::string* err) {
   };
   std::vector<Pt4<T>> hp;
   std::vector<T> hv;
+  cloud_centre(plan, s->ctr);
   make_pts(plan.points_r, plan.rows, &hp);
   FMCA_TRY(to_device(dp, hp.data(), hp.size(), &s->pts_r, err));
   make_pts(plan.points_c, plan.cols, &hp);
@@ -518,7 +541,7 @@ KParams<T> make_kparams(const KernelDesc& k, const CallOpts& opts = CallOpts()) 
   const double l = k.l, log2e = 1.4426950408889634;
   double a = 0, e2 = 0;
   // the length-scale derivative kernels share the constants of their kernel
-  const int base = k.type >= K_DL_EXPONENTIAL ? k.type - K_DL_EXPONENTIAL : k.type;
+  const int base = is_dl_kernel(k.type) ? k.type - K_DL_EXPONENTIAL : k.type;
   switch (base) {
     case FMCA_KERNEL_EXPONENTIAL:
       e2 = -log2e / l;
@@ -579,10 +602,20 @@ KParams<T> make_kparams(const KernelDesc& k, const CallOpts& opts = CallOpts()) 
   return kp;
 }
 
+// kernel parameters of the tensor-core path: with the centre of the set's
+// point clouds for the near field's dot-product distance form
+KParams<float> tc_kparams(const DevSet<float>& S, const KernelDesc& k, const CallOpts& opts) {
+  KParams<float> kp = make_kparams<float>(k, opts);
+  kp.cx = S.ctr[0];
+  kp.cy = S.ctr[1];
+  kp.cz = S.ctr[2];
+  return kp;
+}
+
 // scale applied to the assembled product: sigma2, divided by l for the
 // length-scale derivative kernels (their device values are l * dk/dl)
 double output_scale(const KernelDesc& k) {
-  return k.type >= K_DL_EXPONENTIAL ? k.sigma2 / k.l : k.sigma2;
+  return is_dl_kernel(k.type) ? k.sigma2 / k.l : k.sigma2;
 }
 
 // Raises a kernel's dynamic shared-memory limit once per (kernel, device):
@@ -1288,7 +1321,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   }
   dp->reset_marks();
   dp->mark(-1, st);
-  const KParams<float> kp = make_kparams<float>(k, dp->opts);
+  const KParams<float> kp = tc_kparams(S, k, dp->opts);
   const uint32_t* pc = order == FMCA_ORDER_NATURAL ? dp->perm_c : nullptr;
   const uint32_t* pr = order == FMCA_ORDER_NATURAL ? dp->perm_r : nullptr;
   const int nthr = 256;
@@ -1319,7 +1352,10 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
   else
     gather_split_kernel<float><<<ggrid, nthr, 0, st>>>(
         pc, nc, nrhs, static_cast<const float*>(x), sxi, sxr, w.cmax, w.xc, w.xv);
-  point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
+  if (um_near_dot(kp.type))
+    point_pairs_dot_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp, w.pairs_c);
+  else
+    point_pairs_kernel<<<blocks(npc / 2), nthr, 0, st>>>(nc, S.pts_c, kp.g, w.pairs_c);
   FMCA_CK(cudaGetLastError());
   dp->launches += 2;
   dp->mark(FMCA_STAGE_GATHER, st);
@@ -1482,7 +1518,7 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
       if (status == FMCA_OK) {
         TcWorkspace w;
         tc_ws_layout(plan, nrhs, ws ? ws : dp->ws, &w);
-        TcChunk c = tc_chunk(plan, dp, dp->f, w, make_kparams<float>(k, dp->opts), nrhs, 0, st);
+        TcChunk c = tc_chunk(plan, dp, dp->f, w, tc_kparams(dp->f, k, dp->opts), nrhs, 0, st);
         float bt = -1.f;
         for (int halves = 2; halves >= 1 && status == FMCA_OK; --halves)
           for (int nst = halves == 2 ? 4 : 5; nst <= kUmMaxStages && status == FMCA_OK; ++nst)
@@ -1953,6 +1989,7 @@ int update_points(const Plan& plan, DevPlan* dp, std::string* err) {
       FMCA_CK(cudaMemcpy(side == 0 ? S.pts_r : S.pts_c, hp.data(), sizeof(Pt4<T>) * t.n,
                          cudaMemcpyHostToDevice));
     }
+    cloud_centre(plan, S.ctr);
     return FMCA_OK;
   };
   std::lock_guard<std::mutex> lock(dp->mu);

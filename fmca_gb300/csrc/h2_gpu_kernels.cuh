@@ -61,6 +61,9 @@ struct KParams {
   T e2;  // scale of the exponent in base 2 (FP32 path)
   T il;  // 1 / l
   T g;   // coordinate scale of the tensor-core path (1 for generic kernels)
+  // centre subtracted from every coordinate before the scaling by g in the
+  // near field's dot-product distance form (um_near_dot)
+  T cx = 0, cy = 0, cz = 0;
   unsigned long long wait_ns;  // limit of the kernel sums' bounded waits
   // test hook (fmca_plan_set_stalled_wait): the first wait of every
   // kernel-sum CTA is on a barrier that nothing completes, so it runs out
@@ -90,6 +93,12 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kLn2f = 0.693147180559945309f;
 __device__ __forceinline__ float rsqrt_approx(float x) {
   float y;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -202,6 +211,10 @@ __device__ __forceinline__ double keval_ref(int type, double r2,
       const double t2 = r2 / (l * l);
       return t2 * exp(-0.5 * t2);
     }
+    case 14:  // BIHARMONIC2D, 0 below r = DBL_EPSILON
+      return r < 2.220446049250313e-16 ? 0. : log(r / l) * (r / l) * (r / l);
+    case 15:  // TPS2D
+      return r > 0. ? r * r * log(r) : 0.;
   }
   return 0.;
 }
@@ -277,6 +290,13 @@ __device__ __forceinline__ float keval_fast(int type, float r2,
     }
     case 13:
       return r2 * kp.il * kp.il * ex2_approx(r2 * kp.e2);
+    // thin-plate kernels from r^2: t^2 log t = (ln 2 / 2) t^2 log2(t^2)
+    case 14: {
+      const float t2 = r2 * (kp.il * kp.il);
+      return t2 > 0.f ? (0.5f * kLn2f) * t2 * lg2_approx(t2) : 0.f;
+    }
+    case 15:
+      return r2 > 0.f ? (0.5f * kLn2f) * r2 * lg2_approx(r2) : 0.f;
   }
   return 0.f;
 }

@@ -28,7 +28,8 @@ int kernel_type_from_name(const std::string& name) {
                                 "GAUSSIAN",        "MATERN72",       "MATERN92",
                                 "INVMULTIQUADRIC", "MULTIQUADRIC",   "BIHARMONIC3D",
                                 "TRIHARMONIC3D",   "DL_EXPONENTIAL", "DL_MATERN32",
-                                "DL_MATERN52",     "DL_GAUSSIAN"};
+                                "DL_MATERN52",     "DL_GAUSSIAN",    "BIHARMONIC2D",
+                                "TPS2D"};
   for (int i = 0; i < K_NUM_KERNELS; ++i)
     if (s == names[i]) return i;
   return -1;
@@ -39,11 +40,12 @@ const char* kernel_type_name(int type) {
                                 "GAUSSIAN",        "MATERN72",       "MATERN92",
                                 "INVMULTIQUADRIC", "MULTIQUADRIC",   "BIHARMONIC3D",
                                 "TRIHARMONIC3D",   "DL_EXPONENTIAL", "DL_MATERN32",
-                                "DL_MATERN52",     "DL_GAUSSIAN"};
+                                "DL_MATERN52",     "DL_GAUSSIAN",    "BIHARMONIC2D",
+                                "TPS2D"};
   return (type >= 0 && type < K_NUM_KERNELS) ? names[type] : "UNKNOWN";
 }
 
-// Expression order follows FMCA/src/CovarianceKernel/CovarianceKernel.h:56-116.
+// Expression order follows FMCA/src/CovarianceKernel/CovarianceKernel.h:56-118.
 double kernel_eval_host(int type, double l, double c, double r) {
   switch (type) {
     case K_EXPONENTIAL:
@@ -83,6 +85,10 @@ double kernel_eval_host(int type, double l, double c, double r) {
     }
     case K_DL_GAUSSIAN:  // (r^2 / l^3) exp(-r^2 / (2 l^2))
       return r * r / (l * l * l) * std::exp(-0.5 * r * r / (l * l));
+    case K_BIHARMONIC2D:
+      return r < std::numeric_limits<double>::epsilon() ? 0. : std::log(r / l) * (r / l) * (r / l);
+    case K_TPS2D:
+      return r > 0 ? r * r * std::log(r) : 0.;
   }
   return std::numeric_limits<double>::quiet_NaN();
 }

@@ -51,8 +51,14 @@ enum KernelType : int {
   K_DL_MATERN32 = 11,
   K_DL_MATERN52 = 12,
   K_DL_GAUSSIAN = 13,
-  K_NUM_KERNELS = 14
+  // the thin-plate kernels of CovarianceKernel.h:56-59 and 117-118
+  K_BIHARMONIC2D = 14,
+  K_TPS2D = 15,
+  K_NUM_KERNELS = 16
 };
+
+// true for the length-scale derivative kernels K_DL_*
+inline bool is_dl_kernel(int type) { return type >= K_DL_EXPONENTIAL && type <= K_DL_GAUSSIAN; }
 
 // Parses an FMCA kernel name (case-insensitive, like CovarianceKernel.h:54).
 // Returns -1 for names that are not supported.

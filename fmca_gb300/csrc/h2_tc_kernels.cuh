@@ -227,6 +227,51 @@ __global__ void gather_split_kernel(const uint32_t* __restrict__ perm, int64_t n
 
 // pair records of n points (cluster order), coordinates multiplied by -g,
 // w = 0; zero records up to um_padded(n)
+// Kernels whose near field takes the squared distance in the dot-product
+// form r^2 = (|t|^2 + |s|^2) - 2 t.s (four FP32x2 instructions per two
+// sources instead of six). Its rounding error, a few ulp of |t|^2 + |s|^2
+// in coordinates centred on the clouds' box, enters k through dk/d(r^2),
+// which is bounded at r = 0 for these kernels (MATERN32..92, GAUSSIAN and
+// their l dk/dl). EXPONENTIAL and its l dk/dl have dk/dr = -1/l at r = 0:
+// there an error of d in r^2 moves k by about sqrt(d), so they keep the
+// difference form.
+__host__ __device__ constexpr bool um_near_dot(int kt) {
+  return kt == 1 || kt == 2 || kt == 3 || kt == 4 || kt == 5 || kt == 11 || kt == 12 ||
+         kt == 13;
+}
+
+// FP32 coordinate u of a point in the dot form: g (x - c), with the same
+// two rounded operations for targets and sources
+__device__ __forceinline__ float um_dot_coord(float x, float c, float g) {
+  return __fmul_rn(g, __fsub_rn(x, c));
+}
+__device__ __forceinline__ float um_dot_norm(float ux, float uy, float uz) {
+  return (float)((double)ux * ux + (double)uy * uy + (double)uz * uz);
+}
+
+// Point sources in the dot form: record p = sources 2p, 2p + 1 as
+// (2 u_x0, 2 u_x1, 2 u_y0, 2 u_y1), (2 u_z0, 2 u_z1, |u_0|^2, |u_1|^2),
+// u = g (x - c); zero records of padding
+static __global__ void point_pairs_dot_kernel(int64_t n, const Pt4<float>* __restrict__ pts,
+                                              KParams<float> kp, float4* __restrict__ pairs) {
+  const int64_t np = (int64_t)um_padded(n) / 2;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float u[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}, nn[2] = {0.f, 0.f};
+    for (int k = 0; k < 2; ++k) {
+      const int64_t s = 2 * p + k;
+      if (s >= n) continue;
+      const Pt4<float> a = pts[s];
+      u[k][0] = um_dot_coord(a.x, kp.cx, kp.g);
+      u[k][1] = um_dot_coord(a.y, kp.cy, kp.g);
+      u[k][2] = um_dot_coord(a.z, kp.cz, kp.g);
+      nn[k] = um_dot_norm(u[k][0], u[k][1], u[k][2]);
+    }
+    pairs[2 * p] = make_float4(2.f * u[0][0], 2.f * u[1][0], 2.f * u[0][1], 2.f * u[1][1]);
+    pairs[2 * p + 1] = make_float4(2.f * u[0][2], 2.f * u[1][2], nn[0], nn[1]);
+  }
+}
+
 static __global__ void point_pairs_kernel(int64_t n, const Pt4<float>* __restrict__ pts, float g,
                                    float4* __restrict__ pairs) {
   const int64_t np = (int64_t)um_padded(n) / 2;

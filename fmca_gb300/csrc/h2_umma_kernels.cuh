@@ -150,6 +150,78 @@ __device__ __forceinline__ void um_eval_chunk(const float4* __restrict__ rec, ui
   }
 }
 
+// The near field in the dot form (um_near_dot): records from
+// point_pairs_dot_kernel, targets as nx = (-u_x, -u_x), ... and tn = |u|^2
+// (um_targets), so r^2 = tn + |s|^2 - 2 u.s in four FP32x2 instructions.
+// Masked rows get w = -inf (a = 0). Kernels with a square root take it of
+// |r^2|: rounding can leave r^2 slightly below 0 for coincident points.
+template <int KT, int H, bool MASKED>
+__device__ __forceinline__ void um_eval_chunk_dot(const float4* __restrict__ rec, uint32_t m16,
+                                                  const float2 (&nx)[H], const float2 (&ny)[H],
+                                                  const float2 (&nz)[H], const float2 (&tn)[H],
+                                                  const KParams<float>& kp, uint32_t (&hi)[H][8],
+                                                  uint32_t (&lo)[H][8]) {
+  constexpr bool kSqrt = KT != 3 && KT != 13;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 a = rec[2 * j], b = rec[2 * j + 1];
+    const float2 sx = f2(a.x, a.y), sy = f2(a.z, a.w), sz = f2(b.x, b.y), sn = f2(b.z, b.w);
+    float2 sw = f2(0.f, 0.f);
+    if constexpr (MASKED) {
+      if (!((m16 >> (2 * j)) & 1u)) sw.x = -CUDART_INF_F;
+      if (!((m16 >> (2 * j + 1)) & 1u)) sw.y = -CUDART_INF_F;
+    }
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      float2 r2 = __ffma2_rn(nx[h], sx, __ffma2_rn(ny[h], sy,
+                                                   __ffma2_rn(nz[h], sz, __fadd2_rn(tn[h], sn))));
+      if constexpr (kSqrt) r2 = f2(fabsf(r2.x), fabsf(r2.y));
+      const float2 av = kscaled2<KT, !MASKED>(r2, sw, kp);
+      const float2 hv = f2(__uint_as_float(__float_as_uint(av.x) & 0xffffe000u),
+                           __uint_as_float(__float_as_uint(av.y) & 0xffffe000u));
+      const float2 lv = __ffma2_rn(hv, f2(-1.f, -1.f), av);
+      hi[h][j] = h2_bits(__floats2half2_rn(hv.x, hv.y));
+      lo[h][j] = h2_bits(__floats2half2_rn(lv.x, lv.y));
+    }
+  }
+}
+
+// The evaluation warps' target registers for the H halves of group g (row
+// = tensor-memory lane, HS targets per half): (g t, g t) per coordinate, or
+// in the near field's dot form (-u, -u) with u = g (t - c) and tn = |u|^2.
+// Lanes without a target get zeros.
+template <int H, bool DOT>
+__device__ __forceinline__ void um_targets(const Pt4<float>* __restrict__ tgt, const KGroup& g,
+                                           int row, int HS, const KParams<float>& kp,
+                                           float2 (&tx)[H], float2 (&ty)[H], float2 (&tz)[H],
+                                           float2 (&tn)[H]) {
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const uint32_t i = (uint32_t)(h * HS + row);
+    float px = 0.f, py = 0.f, pz = 0.f, pn = 0.f;
+    if (row < HS && i < g.tcount) {
+      const Pt4<float> pt = tgt[g.tbegin + i];
+      if constexpr (DOT) {
+        const float ux = um_dot_coord(pt.x, kp.cx, kp.g);
+        const float uy = um_dot_coord(pt.y, kp.cy, kp.g);
+        const float uz = um_dot_coord(pt.z, kp.cz, kp.g);
+        pn = um_dot_norm(ux, uy, uz);
+        px = -ux;
+        py = -uy;
+        pz = -uz;
+      } else {
+        px = kp.g * pt.x;
+        py = kp.g * pt.y;
+        pz = kp.g * pt.z;
+      }
+    }
+    tx[h] = f2(px, px);
+    ty[h] = f2(py, py);
+    tz[h] = f2(pz, pz);
+    tn[h] = f2(pn, pn);
+  }
+}
+
 // Tensor-grid sources (one column cluster per tile, nodes in grid order):
 // kernel values of the chunks 2 S and 2 S + 1 (grid rows 32 S .. 32 S + 31)
 // for target (tx, ty, tz) (scaled by g). With the grid lines X (scaled by
@@ -243,6 +315,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // every half is one row cluster of q nodes; imask[interval] holds the
   // halves a source cluster serves)
   const int HS = GRID ? q : 128;
+  // point sources of a kernel smooth at r = 0: the dot-product distance form
+  constexpr bool DOT = !REL && !GRID && um_near_dot(KT);
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -460,22 +534,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int ew = warp - 3, set = ew >> 2;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
     const int row = (warp & 3) * 32 + lane;
-    const float gs = kp.g;
-    float2 tx[H], ty[H], tz[H];
-#pragma unroll
-    for (int h = 0; h < H; ++h) {
-      const uint32_t i = (uint32_t)(h * HS + row);
-      float px = 0.f, py = 0.f, pz = 0.f;
-      if (row < HS && i < g.tcount) {
-        const Pt4<float> pt = tgt[g.tbegin + i];
-        px = gs * pt.x;
-        py = gs * pt.y;
-        pz = gs * pt.z;
-      }
-      tx[h] = f2(px, px);
-      ty[h] = f2(py, py);
-      tz[h] = f2(pz, pz);
-    }
+    float2 tx[H], ty[H], tz[H], tn[H];
+    um_targets<H, DOT>(tgt, g, row, HS, kp, tx, ty, tz, tn);
     // largest moment exponent E of the group's source clusters
     // largest moment exponent E of the group's source clusters, per target
     // half (Eh: over the intervals that serve the half) and overall (E)
@@ -589,14 +649,20 @@ __global__ void __launch_bounds__(kUmThreads, 1)
           const uint32_t m16 = (masks[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
           uint32_t hi[H][8], lo[H][8];
           if (m16 == 0xffffu) {
-            um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+            if constexpr (DOT)
+              um_eval_chunk_dot<KT, H, false>(R4 + kk * 16, m16, tx, ty, tz, tn, kp, hi, lo);
+            else
+              um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
           } else if (m16 == 0u) {
 #pragma unroll
             for (int h = 0; h < H; ++h)
 #pragma unroll
               for (int i = 0; i < 8; ++i) hi[h][i] = lo[h][i] = 0u;
           } else {
-            um_eval_chunk<KT, H, true, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+            if constexpr (DOT)
+              um_eval_chunk_dot<KT, H, true>(R4 + kk * 16, m16, tx, ty, tz, tn, kp, hi, lo);
+            else
+              um_eval_chunk<KT, H, true, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
           }
           if (cc == 0) {
             if (!slot_free()) {

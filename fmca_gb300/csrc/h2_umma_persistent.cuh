@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // every half is one row cluster of q nodes; imask[interval] holds the
   // halves a source cluster serves)
   const int HS = GRID ? q : 128;
+  constexpr bool DOT = !REL && !GRID && um_near_dot(KT);  // near-field distance form
 
   if (*reinterpret_cast<volatile int*>(err)) return;
 
@@ -314,28 +315,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int ew = warp - 3, set = ew >> 2;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
     const int row = (warp & 3) * 32 + lane;
-    const float gs = kp.g;
     bool ok = true;
     int stage = -1, k = 0;  // k % NST and (k / NST) & 1, kept as counters
     uint32_t ph = 1;
     for (int gi = g0; gi < ngroups && ok; gi += gstep) {
     const KGroup g = groups[gi];
     const int ntiles = group_tiles(g);
-    float2 tx[H], ty[H], tz[H];
-#pragma unroll
-    for (int h = 0; h < H; ++h) {
-      const uint32_t i = (uint32_t)(h * HS + row);
-      float px = 0.f, py = 0.f, pz = 0.f;
-      if (row < HS && i < g.tcount) {
-        const Pt4<float> pt = tgt[g.tbegin + i];
-        px = gs * pt.x;
-        py = gs * pt.y;
-        pz = gs * pt.z;
-      }
-      tx[h] = f2(px, px);
-      ty[h] = f2(py, py);
-      tz[h] = f2(pz, pz);
-    }
+    float2 tx[H], ty[H], tz[H], tn[H];
+    um_targets<H, DOT>(tgt, g, row, HS, kp, tx, ty, tz, tn);
     // largest moment exponent of the group's source clusters per target half
     // (Eh, over the intervals that serve the half: group_exponents_kernel)
     // and overall (E)
@@ -419,14 +406,20 @@ __global__ void __launch_bounds__(kUmThreads, 1)
           const uint32_t m16 = (masks[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
           uint32_t hi[H][8], lo[H][8];
           if (m16 == 0xffffu) {
-            um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+            if constexpr (DOT)
+              um_eval_chunk_dot<KT, H, false>(R4 + kk * 16, m16, tx, ty, tz, tn, kp, hi, lo);
+            else
+              um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
           } else if (m16 == 0u) {
 #pragma unroll
             for (int h = 0; h < H; ++h)
 #pragma unroll
               for (int i = 0; i < 8; ++i) hi[h][i] = lo[h][i] = 0u;
           } else {
-            um_eval_chunk<KT, H, true, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
+            if constexpr (DOT)
+              um_eval_chunk_dot<KT, H, true>(R4 + kk * 16, m16, tx, ty, tz, tn, kp, hi, lo);
+            else
+              um_eval_chunk<KT, H, true, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
           }
           if (cc == 0) {
             if (!slot_free()) {

@@ -73,7 +73,11 @@ enum {
   FMCA_KERNEL_DL_EXPONENTIAL = 10,
   FMCA_KERNEL_DL_MATERN32 = 11,
   FMCA_KERNEL_DL_MATERN52 = 12,
-  FMCA_KERNEL_DL_GAUSSIAN = 13
+  FMCA_KERNEL_DL_GAUSSIAN = 13,
+  /* (r/l)^2 log(r/l), 0 below r = DBL_EPSILON (CovarianceKernel.h:56-59) */
+  FMCA_KERNEL_BIHARMONIC2D = 14,
+  /* r^2 log(r), 0 at r = 0; l is not used (CovarianceKernel.h:117-118) */
+  FMCA_KERNEL_TPS2D = 15
 };
 
 /* Arithmetic of the matvec. */
@@ -84,8 +88,8 @@ enum {
      tensor cores with FP16 hi/lo split operands (three products, about 22
      significant bits) and FP32 accumulation; transfers, leaf moments and the
      leaf gather in FP32; final near + far combination in FP64.  Kernels that
-     are not bounded by 1 (MULTIQUADRIC, INVMULTIQUADRIC, BIHARMONIC3D,
-     TRIHARMONIC3D) use FMCA_PREC_FP32, and so do fewer than 17 right-hand
+     are not bounded by 1 (MULTIQUADRIC, INVMULTIQUADRIC, BIHARMONIC2D/3D,
+     TRIHARMONIC3D, TPS2D) use FMCA_PREC_FP32, and so do fewer than 17 right-hand
      sides unless the autotuner (fmca_plan_set_autotune) measured the
      tensor-core path, with the columns padded to 32, faster. */
   FMCA_PREC_MIXED = 1,

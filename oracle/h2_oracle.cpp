@@ -512,6 +512,12 @@ KernelFn make_kernel(int type, Scalar l, Scalar c) {
         return a * a * r * r / (3. * l) * (1. + a * r) * std::exp(-a * r);
       };
     case 13: return [l](Scalar r) { return r * r / (l * l * l) * std::exp(-0.5 * r * r / (l * l)); };
+    // BIHARMONIC2D and TPS2D (CovarianceKernel.h:56-59, 117-118)
+    case 14:
+      return [l](Scalar r) {
+        return r < std::numeric_limits<Scalar>::epsilon() ? 0 : std::log(r / l) * (r / l) * (r / l);
+      };
+    case 15: return [](Scalar r) { return r > 0 ? r * r * std::log(r) : 0; };
   }
   return [](Scalar) { return std::numeric_limits<Scalar>::quiet_NaN(); };
 }

@@ -21,6 +21,8 @@ TOL = {"fp64": 1e-12, "fp32": 1e-5, "mixed": 1e-5}
 PRECS = ["fp64", "fp32", "mixed"]
 KNAMES = ["EXPONENTIAL", "MATERN32", "MATERN52", "GAUSSIAN", "MATERN72", "MATERN92",
           "INVMULTIQUADRIC", "MULTIQUADRIC", "BIHARMONIC3D", "TRIHARMONIC3D"]
+# kernel codes of the C ABI (FMCA_KERNEL_*)
+KCODE = {**{k: i for i, k in enumerate(KNAMES)}, "BIHARMONIC2D": 14, "TPS2D": 15}
 
 
 @pytest.fixture(scope="module")
@@ -67,6 +69,20 @@ def test_all_kernels(cuda_device, kname, precision):
     H = H2Matrix(CovarianceKernel(kname, 0.7, 0.9), P, P, 3, 0.8, min_leaf=32,
                  precision=precision)
     assert rel_err(H.action(X), Y_ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("kname", ["BIHARMONIC2D", "TPS2D"])
+@pytest.mark.parametrize("precision", PRECS)
+def test_thin_plate_kernels_in_2d(cuda_device, kname, precision):
+    # the thin-plate kernels of CovarianceKernel.h:56-59 and 117-118 (unbounded:
+    # the mixed precision takes the FP32 CUDA-core path), 2-D, 24 right-hand
+    # sides; tps: r^2 log r changes sign at r = 1, so the cloud spans [0, 3]^2
+    P = uniform_cloud(8000, 2, seed=13) * 3.0
+    X = np.random.default_rng(13).standard_normal((8000, 24))
+    Y_ref, _ = oracle.OraclePlan(P, None, 5, 0.8, 32).action(KCODE[kname], 0.7, X)
+    H = H2Matrix(CovarianceKernel(kname, 0.7), P, P, 5, 0.8, min_leaf=32, precision=precision)
+    assert rel_err(H.action(X), Y_ref) < TOL[precision]
+    H.check_device_error()
 
 
 @pytest.mark.parametrize("kname", ["EXPONENTIAL", "MATERN52", "MATERN72", "MATERN92", "GAUSSIAN"])
@@ -181,7 +197,7 @@ def test_torch_device_api(cuda_device):
 def test_dense_kernel_eval(cuda_device):
     rng = np.random.default_rng(0)
     PR, PC = rng.random((3, 50)), rng.random((3, 40))
-    for kt, kname in enumerate(KNAMES):
+    for kname, kt in KCODE.items():
         K = CovarianceKernel(kname, 0.6, 0.8).eval(PR, PC)
         r = np.linalg.norm(PR[:, :, None] - PC[:, None, :], axis=0)
         ref = np.vectorize(lambda t: oracle.kernel(kt, 0.6, t, c=0.8))(r)

@@ -74,6 +74,13 @@ def test_kernel_formulas():
         b = np.sqrt(5) / 0.5 * r
         assert oracle.kernel(2, 0.5, r) == pytest.approx((1 + b + b * b / 3) * np.exp(-b), rel=1e-14)
         assert oracle.kernel(3, 0.5, r) == pytest.approx(np.exp(-0.5 * r * r / 0.25), rel=1e-15)
+    # BIHARMONIC2D (CovarianceKernel.h:56-59) and TPS2D (:117-118), zero at r = 0
+    for r in (0.3, 1.0, 1.7):
+        t = r / 0.5
+        assert oracle.kernel(14, 0.5, r) == pytest.approx(np.log(t) * t * t, rel=1e-15)
+        assert oracle.kernel(15, 0.5, r) == pytest.approx(r * r * np.log(r), rel=1e-15, abs=0)
+    assert oracle.kernel(14, 0.5, 0.0) == 0.0 and oracle.kernel(14, 0.5, 1e-17) == 0.0
+    assert oracle.kernel(15, 0.5, 0.0) == 0.0
 
 
 @pytest.mark.parametrize("nparts", [2, 8])
