@@ -47,7 +47,7 @@ SFU_PAIRS_PER_CLK = 32.0 / 3.0
 # DRAM bytes (read + write) of one near-field kernel-sum launch of the default
 # workload: a fixed figure from one ncu capture of the current kernel
 # (dram__bytes_read.sum + dram__bytes_write.sum), not measured by this script
-NEAR_DRAM_BYTES_PER_LAUNCH = 2.644428e9 + 0.149038e9
+NEAR_DRAM_BYTES_PER_LAUNCH = 2.671359e9 + 0.151429e9
 # parts of the CPU reference's product per timed step (a level of the
 # cluster tree with this many clusters)
 REF_PARTS = 16
