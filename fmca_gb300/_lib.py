@@ -53,6 +53,8 @@ EXPORTED = [
     "fmca_plan_save", "fmca_plan_load", "fmca_plan_cloud_offsets", "fmca_plan_device_bytes",
     "fmca_plan_set_wait_limit", "fmca_plan_set_stalled_wait", "fmca_plan_set_autotune",
     "fmca_plan_tuned_config", "fmca_plan_create_gpu", "fmca_plan_set_tuned_config",
+    "fmca_plan_assembled_size", "fmca_plan_assemble", "fmca_matvec_assembled",
+    "fmca_plan_release_assembled",
 ]
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
@@ -136,6 +138,11 @@ def load() -> C.CDLL:
     lib.fmca_plan_set_autotune.argtypes = [vp, i32]
     lib.fmca_plan_tuned_config.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_int32)]
     lib.fmca_plan_set_tuned_config.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_int32)]
+    lib.fmca_plan_assembled_size.argtypes = [vp, i32, C.POINTER(C.c_size_t)]
+    lib.fmca_plan_assemble.argtypes = [vp, C.POINTER(KernelDesc), i32, vp]
+    lib.fmca_matvec_assembled.argtypes = [vp, i32, i32, i32, i32, vp, i64, i64, vp, i64, i64,
+                                          vp, C.c_size_t, vp]
+    lib.fmca_plan_release_assembled.argtypes = [vp]
     for name in EXPORTED:
         if name not in ("fmca_last_error", "fmca_version"):
             getattr(lib, name).restype = C.c_int

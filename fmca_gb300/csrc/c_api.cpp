@@ -439,6 +439,66 @@ fmca_status fmca_matvec(fmca_plan* p, const fmca_kernel_desc* kernel,
   return ok();
 }
 
+fmca_status fmca_plan_assembled_size(const fmca_plan* p, int precision, size_t* bytes) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  if (!bytes) return fail(FMCA_ERR_INVALID_ARGUMENT, "bytes is NULL");
+  *bytes = fmca::gpu::assembled_bytes(p->plan, precision);
+  return ok();
+}
+
+fmca_status fmca_plan_assemble(fmca_plan* p, const fmca_kernel_desc* kernel, int precision,
+                               void* stream) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  s = check_kernel(kernel);
+  if (s != FMCA_OK) return s;
+  std::string err;
+  int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  st = fmca::gpu::assemble(p->plan, p->dev, to_desc(kernel), precision, (cudaStream_t)stream,
+                           &err, fmca::capi::call_opts(p));
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_matvec_assembled(fmca_plan* p, int precision, int dtype, int order, int nrhs,
+                                  const void* x, int64_t x_stride_i, int64_t x_stride_r,
+                                  void* y, int64_t y_stride_i, int64_t y_stride_r,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+  fmca_status s = check_gpu_plan(p, precision);
+  if (s != FMCA_OK) return s;
+  if (dtype != FMCA_DTYPE_F64 && dtype != FMCA_DTYPE_F32)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown dtype");
+  if (order != FMCA_ORDER_NATURAL && order != FMCA_ORDER_CLUSTER)
+    return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown order");
+  if (nrhs < 1) return fail(FMCA_ERR_INVALID_ARGUMENT, "nrhs must be >= 1");
+  if (!x || !y) return fail(FMCA_ERR_INVALID_ARGUMENT, "x or y is NULL");
+  const int ap = p->dev ? fmca::gpu::assembled_precision(p->dev) : -1;
+  if (ap < 0)
+    return fail(FMCA_ERR_INVALID_ARGUMENT,
+                "the plan holds no assembled blocks (fmca_plan_assemble)");
+  if ((ap == FMCA_PREC_FP64) != (precision == FMCA_PREC_FP64))
+    return fail(FMCA_ERR_INVALID_ARGUMENT,
+                "the plan's blocks were assembled in another precision (FP64 blocks serve "
+                "FMCA_PREC_FP64, FP32 blocks FMCA_PREC_FP32 and FMCA_PREC_MIXED)");
+  std::string err;
+  int st = fmca::gpu::upload(p->plan, precision, &p->dev, &err);
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  st = fmca::gpu::matvec_assembled(p->plan, p->dev, precision, dtype, order, nrhs, x,
+                                   x_stride_i, x_stride_r, y, y_stride_i, y_stride_r,
+                                   workspace, workspace_bytes, (cudaStream_t)stream, &err,
+                                   fmca::capi::call_opts(p));
+  if (st != FMCA_OK) return fail((fmca_status)st, err);
+  return ok();
+}
+
+fmca_status fmca_plan_release_assembled(fmca_plan* p) {
+  if (!p) return fail(FMCA_ERR_INVALID_ARGUMENT, "plan is NULL");
+  fmca::gpu::release_assembled(p->dev);
+  return ok();
+}
+
 fmca_status fmca_matvec_host(fmca_plan* p, const fmca_kernel_desc* kernel,
                              int precision, int order, int nrhs, const double* x,
                              double* y) {

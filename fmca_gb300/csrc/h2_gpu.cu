@@ -11,6 +11,7 @@
 #include "../../include/fmca_gb300.h"
 #include "h2_gpu.h"
 #include "h2_adjoint_kernels.cuh"
+#include "h2_assembled.h"
 #include "h2_gpu_kernels.cuh"
 #include "h2_tc_kernels.cuh"
 #include "h2_umma_kernels.cuh"
@@ -126,6 +127,26 @@ struct TuneCfg {
   }
 };
 
+// Stored far- and near-field blocks of an assembled plan
+// (fmca_plan_assemble): FP64 values for FMCA_PREC_FP64, FP32 values
+// otherwise, one block per group of the CUDA-core group lists dp->far and
+// dp->near at the per-group element offsets far_off / near_off.
+struct AsmStore {
+  int precision = -1;  // -1: not assembled
+  KernelDesc k{};
+  void* far = nullptr;
+  void* near = nullptr;
+  uint64_t* far_off = nullptr;
+  uint64_t* near_off = nullptr;
+  size_t bytes = 0;  // device bytes of the four arrays
+};
+
+void release_store(AsmStore* a) {
+  for (void* p : {a->far, a->near, (void*)a->far_off, (void*)a->near_off})
+    if (p) cudaFree(p);
+  *a = AsmStore();
+}
+
 }  // namespace
 
 struct DevPlan {
@@ -161,6 +182,7 @@ struct DevPlan {
   int* err_flag = nullptr;
   void* ws = nullptr;
   size_t ws_bytes = 0;
+  AsmStore as;  // stored blocks of fmca_plan_assemble
   std::mutex mu;
   // options of the current call; stage profiling: events recorded at stage
   // boundaries of the last matvec
@@ -820,10 +842,13 @@ size_t leafgather_smem(int q) {
   return ((size_t)128 * 24 + (size_t)q * RB) * sizeof(T) + (size_t)q * sizeof(int);
 }
 
+// as: stored blocks of an assembled plan (the far field streams them instead
+// of evaluating the kernel), or null
 template <typename T, int RB>
 cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
                             Workspace<T>& w, int ld, int rofs, int rcount,
-                            const KParams<T>& kp, cudaStream_t st) {
+                            const KParams<T>& kp, cudaStream_t st,
+                            const AsmStore* as = nullptr) {
   const int q = plan.interp.q;
   // upward pass: leaf moments
   {
@@ -851,8 +876,12 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
                                              rofs, rcount, st);
   dp->mark(FMCA_STAGE_M2M, st);
   // far-field coupling
-  cudaError_t e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s,
-                                 rofs, rcount, kp, 0, dp->err_flag, st);
+  cudaError_t e =
+      as ? launch_kstream<T>(RB, dp->far.groups, dp->far.ngroups, dp->far.maxcount, dp->far.ivl,
+                             as->far_off, static_cast<const T*>(as->far), w.t, ld, w.s, rofs,
+                             rcount, kp.wait_ns, kp.stall, dp->err_flag, st)
+         : launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s, rofs, rcount, kp, 0,
+                          dp->err_flag, st);
   if (e != cudaSuccess) return e;
   dp->launches += dp->far.ngroups ? 1 : 0;
   dp->launches += launch_basis_change<T, RB>(S.ip, plan.rows.nclusters(), S.from_nodal, w.s,
@@ -889,9 +918,13 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
 // chain on a second stream gained nothing at n = 1e6)
 template <typename T, int RB>
 cudaError_t run_near(DevPlan* dp, DevSet<T>& S, Workspace<T>& w, int ld, int rcount,
-                     const KParams<T>& kp, cudaStream_t st) {
-  cudaError_t e = launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, 0,
-                                 rcount, kp, 0, dp->err_flag, st);
+                     const KParams<T>& kp, cudaStream_t st, const AsmStore* as = nullptr) {
+  cudaError_t e =
+      as ? launch_kstream<T>(RB, dp->near.groups, dp->near.ngroups, dp->near.maxcount,
+                             dp->near.ivl, as->near_off, static_cast<const T*>(as->near), w.xc,
+                             ld, w.ynear, 0, rcount, kp.wait_ns, kp.stall, dp->err_flag, st)
+         : launch_ksum<T>(RB, dp->near, S.pts_r, S.pts_c, w.xc, ld, w.ynear, 0, rcount, kp, 0,
+                          dp->err_flag, st);
   dp->launches += dp->near.ngroups ? 1 : 0;
   dp->mark(FMCA_STAGE_NEAR, st);
   return e;
@@ -934,7 +967,7 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
              int dtype, int order, int nrhs, const void* x, int64_t sxi,
              int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
              size_t wsb, cudaStream_t st, std::string* err,
-             MatvecState* state = nullptr) {
+             MatvecState* state = nullptr, const AsmStore* as = nullptr) {
   const int ld = ld_for<T>(nrhs);
   const int rb = rhs_block(nrhs);
   const size_t need = ws_layout<T>(plan, nrhs, nullptr, nullptr);
@@ -983,16 +1016,16 @@ int matvec_t(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     cudaError_t e;
     switch (rb) {
       case 1:
-        e = run_tree_stages<T, 1>(plan, dp, S, wc, ld, 0, rcount, kp, st);
-        if (e == cudaSuccess) e = run_near<T, 1>(dp, S, wc, ld, rcount, kp, st);
+        e = run_tree_stages<T, 1>(plan, dp, S, wc, ld, 0, rcount, kp, st, as);
+        if (e == cudaSuccess) e = run_near<T, 1>(dp, S, wc, ld, rcount, kp, st, as);
         break;
       case 8:
-        e = run_tree_stages<T, 8>(plan, dp, S, wc, ld, 0, rcount, kp, st);
-        if (e == cudaSuccess) e = run_near<T, 8>(dp, S, wc, ld, rcount, kp, st);
+        e = run_tree_stages<T, 8>(plan, dp, S, wc, ld, 0, rcount, kp, st, as);
+        if (e == cudaSuccess) e = run_near<T, 8>(dp, S, wc, ld, rcount, kp, st, as);
         break;
       default:
-        e = run_tree_stages<T, 32>(plan, dp, S, wc, ld, 0, rcount, kp, st);
-        if (e == cudaSuccess) e = run_near<T, 32>(dp, S, wc, ld, rcount, kp, st);
+        e = run_tree_stages<T, 32>(plan, dp, S, wc, ld, 0, rcount, kp, st, as);
+        if (e == cudaSuccess) e = run_near<T, 32>(dp, S, wc, ld, rcount, kp, st, as);
         break;
     }
     FMCA_CK(e);
@@ -1415,6 +1448,7 @@ void destroy(DevPlan* dp) {
   cudaGetDevice(&cur);
   if (dp->device >= 0 && dp->device != cur) cudaSetDevice(dp->device);
   for (void* p : dp->allocs) cudaFree(p);
+  release_store(&dp->as);
   for (cudaEvent_t e : dp->events) cudaEventDestroy(e);
   if (dp->ws) cudaFree(dp->ws);
   if (dp->device >= 0 && dp->device != cur && cur >= 0) cudaSetDevice(cur);
@@ -1644,6 +1678,171 @@ int matvec(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
                      ws_bytes, st, err);
   return matvec_t<float>(plan, dp, dp->f, k, dtype, order, nrhs, x, sxi, sxr, y, syi,
                          syr, ws, ws_bytes, st, err);
+}
+
+// ---------------------------------------------------------------------------
+// assembled plans (fmca_plan_assemble, fmca_matvec_assembled)
+namespace {
+
+// Stored elements and groups of the assembled blocks, from the host plan:
+// the groups of the CUDA-core lists (far: the nodes of every row cluster,
+// near: the points of every row leaf, both chunked to kGroupCap targets),
+// each a block of (its sources) x (its targets rounded up to 4).
+void asm_counts(const Plan& plan, uint64_t* elems, uint64_t* groups) {
+  auto chunks = [](uint32_t tc, uint64_t* ng) {
+    uint64_t rows = 0;
+    for (uint32_t o = 0; o < tc; o += kGroupCap) {
+      rows += asm_row_stride(std::min<uint32_t>(kGroupCap, tc - o));
+      ++*ng;
+    }
+    return rows;
+  };
+  const Pattern& P = plan.pat;
+  const uint64_t q = plan.interp.q;
+  uint64_t e = 0, ng = 0;
+  for (int c = 0; c < plan.rows.nclusters(); ++c)
+    e += (uint64_t)(P.far_ptr[c + 1] - P.far_ptr[c]) * q * chunks((uint32_t)q, &ng);
+  for (size_t l = 0; l < plan.row_leaves.size(); ++l) {
+    uint64_t ns = 0;
+    for (int k = P.near_ptr[l]; k < P.near_ptr[l + 1]; ++k)
+      ns += P.near_ivl[2 * k + 1] - P.near_ivl[2 * k];
+    e += ns * chunks(plan.rows.size[plan.row_leaves[l]], &ng);
+  }
+  *elems = e;
+  *groups = ng;
+}
+
+// per-group element offsets of one device group list's blocks and their sum
+int asm_offsets(const GroupList& gl, std::vector<uint64_t>* off, uint64_t* total,
+                std::string* err) {
+  off->assign(gl.ngroups, 0);
+  *total = 0;
+  if (!gl.ngroups) return FMCA_OK;
+  std::vector<KGroup> g(gl.ngroups);
+  FMCA_CK(cudaMemcpy(g.data(), gl.groups, sizeof(KGroup) * g.size(), cudaMemcpyDeviceToHost));
+  int nivl = 0;
+  for (const KGroup& x : g) nivl = std::max(nivl, x.ivl_end);
+  std::vector<uint32_t> iv((size_t)2 * nivl);
+  if (nivl)
+    FMCA_CK(cudaMemcpy(iv.data(), gl.ivl, sizeof(uint32_t) * iv.size(), cudaMemcpyDeviceToHost));
+  uint64_t o = 0;
+  for (int i = 0; i < gl.ngroups; ++i) {
+    uint64_t ns = 0;
+    for (int k = g[i].ivl_begin; k < g[i].ivl_end; ++k) ns += iv[2 * k + 1] - iv[2 * k];
+    (*off)[i] = o;
+    o += ns * asm_row_stride(g[i].tcount);
+  }
+  *total = o;
+  return FMCA_OK;
+}
+
+template <typename T>
+int assemble_t(DevPlan* dp, DevSet<T>& S, const KernelDesc& k, int precision,
+               cudaStream_t st, std::string* err) {
+  std::vector<uint64_t> foff, noff;
+  uint64_t fe = 0, ne = 0;
+  FMCA_TRY(asm_offsets(dp->far, &foff, &fe, err));
+  FMCA_TRY(asm_offsets(dp->near, &noff, &ne, err));
+  AsmStore& a = dp->as;
+  auto grab = [&](size_t bytes, void** out) -> int {
+    *out = nullptr;
+    if (!bytes) return FMCA_OK;
+    FMCA_CK(cudaMalloc(out, bytes));
+    a.bytes += bytes;
+    return FMCA_OK;
+  };
+  int s = grab(fe * sizeof(T), &a.far);
+  if (s == FMCA_OK) s = grab(ne * sizeof(T), &a.near);
+  if (s == FMCA_OK) s = grab(foff.size() * sizeof(uint64_t), (void**)&a.far_off);
+  if (s == FMCA_OK) s = grab(noff.size() * sizeof(uint64_t), (void**)&a.near_off);
+  if (s == FMCA_OK && !foff.empty() &&
+      cudaMemcpy(a.far_off, foff.data(), foff.size() * sizeof(uint64_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    s = FMCA_ERR_CUDA;
+  if (s == FMCA_OK && !noff.empty() &&
+      cudaMemcpy(a.near_off, noff.data(), noff.size() * sizeof(uint64_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    s = FMCA_ERR_CUDA;
+  const KParams<T> kp = make_kparams<T>(k, dp->opts);
+  cudaError_t e = cudaSuccess;
+  if (s == FMCA_OK)
+    e = launch_kstore<T>(dp->far.groups, dp->far.ngroups, dp->far.ivl, a.far_off, S.nodes_r,
+                         S.nodes_c, kp, static_cast<T*>(a.far), st);
+  if (s == FMCA_OK && e == cudaSuccess)
+    e = launch_kstore<T>(dp->near.groups, dp->near.ngroups, dp->near.ivl, a.near_off, S.pts_r,
+                         S.pts_c, kp, static_cast<T*>(a.near), st);
+  if (s == FMCA_OK && e != cudaSuccess) {
+    *err = std::string("storing the blocks failed: ") + cudaGetErrorString(e);
+    s = FMCA_ERR_CUDA;
+  }
+  if (s != FMCA_OK) {
+    if (err->empty()) *err = "assembling the plan failed (device memory)";
+    release_store(&dp->as);
+    return s;
+  }
+  dp->launches = (dp->far.ngroups ? 1 : 0) + (dp->near.ngroups ? 1 : 0);
+  a.precision = precision;
+  a.k = k;
+  return FMCA_OK;
+}
+
+}  // namespace
+
+size_t assembled_bytes(const Plan& plan, int precision) {
+  uint64_t e = 0, g = 0;
+  asm_counts(plan, &e, &g);
+  return (size_t)(e * (precision == FMCA_PREC_FP64 ? 8 : 4) + g * sizeof(uint64_t));
+}
+
+int assemble(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision,
+             cudaStream_t st, std::string* err, const CallOpts& opts) {
+  (void)plan;
+  std::lock_guard<std::mutex> lock(dp->mu);
+  if (dp->far.maxcount > kAsmMaxTargets || dp->near.maxcount > kAsmMaxTargets) {
+    *err = "group larger than the assembled stream supports";
+    return FMCA_ERR_UNSUPPORTED;
+  }
+  release_store(&dp->as);
+  dp->opts = opts;
+  dp->profile = false;
+  if (precision == FMCA_PREC_FP64) return assemble_t<double>(dp, dp->d, k, precision, st, err);
+  return assemble_t<float>(dp, dp->f, k, precision, st, err);
+}
+
+void release_assembled(DevPlan* dp) {
+  if (!dp) return;
+  std::lock_guard<std::mutex> lock(dp->mu);
+  release_store(&dp->as);
+}
+
+int assembled_precision(DevPlan* dp) {
+  if (!dp) return -1;
+  std::lock_guard<std::mutex> lock(dp->mu);
+  return dp->as.precision;
+}
+
+int matvec_assembled(const Plan& plan, DevPlan* dp, int precision, int dtype, int order,
+                     int nrhs, const void* x, int64_t sxi, int64_t sxr, void* y, int64_t syi,
+                     int64_t syr, void* ws, size_t ws_bytes, cudaStream_t st, std::string* err,
+                     const CallOpts& opts) {
+  std::lock_guard<std::mutex> lock(dp->mu);
+  if (dp->as.precision < 0) {
+    *err = "the plan holds no assembled blocks (fmca_plan_assemble)";
+    return FMCA_ERR_INVALID_ARGUMENT;
+  }
+  if ((precision == FMCA_PREC_FP64) != (dp->as.precision == FMCA_PREC_FP64)) {
+    *err = "the plan's blocks were assembled in another precision (FP64 blocks serve "
+           "FMCA_PREC_FP64, FP32 blocks FMCA_PREC_FP32 and FMCA_PREC_MIXED)";
+    return FMCA_ERR_INVALID_ARGUMENT;
+  }
+  dp->opts = opts;
+  dp->profile = opts.profile;
+  dp->cfg = TuneCfg::defaults(dp->sms);
+  if (precision == FMCA_PREC_FP64)
+    return matvec_t<double>(plan, dp, dp->d, dp->as.k, dtype, order, nrhs, x, sxi, sxr, y, syi,
+                            syr, ws, ws_bytes, st, err, nullptr, &dp->as);
+  return matvec_t<float>(plan, dp, dp->f, dp->as.k, dtype, order, nrhs, x, sxi, sxr, y, syi,
+                         syr, ws, ws_bytes, st, err, nullptr, &dp->as);
 }
 
 void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) {
@@ -2040,7 +2239,7 @@ int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
 int device_of(const DevPlan* dp) { return dp ? dp->device : -1; }
 
 size_t device_bytes(const DevPlan* dp) {
-  return dp ? dp->alloc_bytes + dp->ws_bytes : 0;
+  return dp ? dp->alloc_bytes + dp->ws_bytes + dp->as.bytes : 0;
 }
 
 bool resident(const DevPlan* dp, int precision) {

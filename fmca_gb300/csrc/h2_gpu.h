@@ -38,6 +38,19 @@ int matvec(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision,
            int64_t sxr, void* y, int64_t syi, int64_t syr, void* ws,
            size_t ws_bytes, cudaStream_t stream, std::string* err, const CallOpts& opts);
 int check_device_error(DevPlan* dev, std::string* err);
+// Assembled plans: device bytes the stored blocks take (host count, no
+// device needed); storing them for kernel k (FP64 values for
+// FMCA_PREC_FP64, FP32 otherwise; replaces earlier ones); their release; the
+// precision they were assembled in (-1: none); the matvec that streams them.
+size_t assembled_bytes(const Plan& plan, int precision);
+int assemble(const Plan& plan, DevPlan* dev, const KernelDesc& k, int precision,
+             cudaStream_t stream, std::string* err, const CallOpts& opts);
+void release_assembled(DevPlan* dev);
+int assembled_precision(DevPlan* dev);
+int matvec_assembled(const Plan& plan, DevPlan* dev, int precision, int dtype, int order,
+                     int nrhs, const void* x, int64_t sxi, int64_t sxr, void* y, int64_t syi,
+                     int64_t syr, void* ws, size_t ws_bytes, cudaStream_t stream,
+                     std::string* err, const CallOpts& opts);
 int dense_eval(const KernelDesc& k, int dim, const double* PR, int64_t nr,
                const double* PC, int64_t nc, double* out, std::string* err);
 // device the plan lives on (-1 if not uploaded)

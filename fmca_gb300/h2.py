@@ -489,6 +489,124 @@ class H2Matrix:
     def check_device_error(self) -> None:
         check(_lib.load().fmca_plan_check_device_error(self._h))
 
+    # -- assembled H2 matrix (stored blocks) -------------------------------
+    def assembled_bytes(self, precision: Optional[str] = None) -> int:
+        """Device bytes the stored blocks of ``computeH2Matrix`` take
+        (fmca_plan_assembled_size; FP64 values for "fp64", FP32 otherwise)."""
+        n = C.c_size_t(0)
+        check(_lib.load().fmca_plan_assembled_size(self._h, _PREC[precision or self.precision],
+                                                   C.byref(n)))
+        return int(n.value)
+
+    def computeH2Matrix(self, precision: Optional[str] = None, cov=None,  # noqa: N802
+                        stream=None) -> None:
+        """Evaluates and stores every far-field coupling block and dense
+        near-field block on the current CUDA device (H2MatrixBase::
+        computeH2Matrix, H2MatrixBase.h:222-255) for the kernel ``cov``
+        (default: the matrix's kernel); later products ``H * x`` stream the
+        stored blocks instead of evaluating the kernel.  Needs
+        ``assembled_bytes(precision)`` of free device memory."""
+        import torch
+        prec = precision or self.precision
+        cov = cov or self.cov
+        d = cov.desc()
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        check(_lib.load().fmca_plan_assemble(self._h, C.byref(d), _PREC[prec],
+                                             C.c_void_p(stream.cuda_stream)))
+        self._asm_prec = prec
+
+    def release_assembled(self) -> None:
+        """Frees the stored blocks (fmca_plan_release_assembled)."""
+        check(_lib.load().fmca_plan_release_assembled(self._h))
+        self._asm_prec = None
+
+    @property
+    def assembled(self) -> Optional[str]:
+        """Precision the stored blocks serve ("fp64", or "fp32" / "mixed"),
+        None without stored blocks."""
+        return getattr(self, "_asm_prec", None)
+
+    def mul(self, x, y=None, precision: Optional[str] = None, order: str = "natural",
+            stream=None, workspace=None):
+        """Device product with the stored blocks (fmca_matvec_assembled) on
+        torch CUDA tensors, arguments as for ``matvec``; the precision
+        defaults to the one the blocks were assembled in."""
+        import torch
+        prec_name = precision or self.assembled or self.precision
+        prec = _PREC[prec_name]
+        if x.dim() == 1:
+            return self.mul(x.unsqueeze(1), None if y is None else y.unsqueeze(1),
+                            precision, order, stream, workspace).squeeze(1)
+        if x.dtype not in (torch.float64, torch.float32):
+            raise TypeError("x must be float64 or float32")
+        if x.shape[0] != self.cols():
+            raise ValueError(f"x must have {self.cols()} rows")
+        R = x.shape[1]
+        dev = x.device
+        if y is None:
+            y = torch.empty((self.rows(), R), dtype=x.dtype, device=dev)
+        if y.dtype != x.dtype or y.shape != (self.rows(), R) or y.device != dev:
+            raise ValueError("y must match x in dtype and device and be n_rows x R")
+        dt = _lib.DTYPE_F64 if x.dtype == torch.float64 else _lib.DTYPE_F32
+        with torch.cuda.device(dev):
+            if stream is None:
+                stream = torch.cuda.current_stream(dev)
+            if workspace is None:
+                key = (prec, R, dev.index)
+                need = self.workspace_bytes(R, prec_name)
+                ws = self._ws.get(key)
+                if ws is None or ws.numel() < need:
+                    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+                    self._ws[key] = ws
+                workspace = ws
+            check(_lib.load().fmca_matvec_assembled(
+                self._h, prec, dt,
+                _lib.ORDER_NATURAL if order == "natural" else _lib.ORDER_CLUSTER, R,
+                C.c_void_p(x.data_ptr()), x.stride(0), x.stride(1),
+                C.c_void_p(y.data_ptr()), y.stride(0), y.stride(1),
+                C.c_void_p(workspace.data_ptr()), workspace.numel(),
+                C.c_void_p(stream.cuda_stream)))
+        return y
+
+    def __mul__(self, rhs):
+        """H * rhs with the stored blocks (H2MatrixBase::operator*,
+        H2MatrixBase.h:107-109): natural order; CUDA tensors stay on the
+        device, numpy arrays and CPU tensors are copied in and out (FP64)."""
+        import torch
+        if self.assembled is None:
+            raise _lib.FmcaError(1, "the matrix holds no assembled blocks: call "
+                                    "computeH2Matrix() first")
+        if isinstance(rhs, torch.Tensor) and rhs.is_cuda:
+            return self.mul(rhs)
+        host = torch.as_tensor(np.asarray(rhs, dtype=np.float64))
+        vec = host.dim() == 1
+        x = host.reshape(-1, 1) if vec else host
+        dev = torch.device("cuda", torch.cuda.current_device())
+        y = self.mul(x.to(dev))
+        y = y.cpu().numpy()
+        if isinstance(rhs, torch.Tensor):
+            y = torch.from_numpy(y)
+        return y[:, 0] if vec else y
+
+    def full(self, precision: Optional[str] = None, block: int = 64) -> np.ndarray:
+        """The H2 matrix as a dense FP64 array (n_rows x n_cols, natural
+        order): H * I, in blocks of ``block`` identity columns, like
+        H2MatrixBase::full (H2MatrixBase.h:155-158).  Uses the stored blocks
+        when the matrix is assembled, else the matrix-free product."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        nc = self.cols()
+        out = np.empty((self.rows(), nc), dtype=np.float64, order="F")
+        for c0 in range(0, nc, block):
+            c1 = min(nc, c0 + block)
+            e = torch.zeros((nc, c1 - c0), dtype=torch.float64, device=dev)
+            e[torch.arange(c0, c1, device=dev), torch.arange(c1 - c0, device=dev)] = 1.0
+            y = self.mul(e, precision=precision) if self.assembled else \
+                self.matvec(e, precision=precision)
+            out[:, c0:c1] = y.cpu().numpy()
+        return out
+
 
 class MatvecGraph:
     """A matvec recorded into a CUDA graph (fmca_matvec_graph_create); each

@@ -310,6 +310,48 @@ fmca_status fmca_matvec_host(fmca_plan* plan, const fmca_kernel_desc* kernel,
                              int precision, int order, int nrhs,
                              const double* x, double* y);
 
+/* Assembled H2 matrix: the far-field coupling blocks S (kernel at the
+   interpolation nodes, q x q per admissible block) and the dense near-field
+   blocks evaluated once and kept in device memory, traded for the kernel
+   evaluations of every later product (repeated products with one kernel:
+   iterative solvers, trace estimation, the FP64 residual of a mixed solve).
+
+   fmca_plan_assembled_size: device bytes the stored blocks take for this
+   precision (FP64 values for FMCA_PREC_FP64, FP32 values for FMCA_PREC_FP32
+   and FMCA_PREC_MIXED), counted on the host; no device is needed.
+   Replaces nothing in the reference (its H2MatrixBase::statistics,
+   H2MatrixBase.h:70-105, estimates the storage of an assembled FP64 matrix).
+
+   fmca_plan_assemble: H2MatrixBase::computeH2Matrix (H2MatrixBase.h:222-255;
+   the H2Matrix(CT, mat_eval, eta) constructor, H2Matrix.h:53-66): evaluates
+   and stores every block for this kernel on the current device, replacing
+   blocks stored earlier.  The kernel evaluations run asynchronously on
+   stream; the allocation and the block offsets are synchronous.
+   FMCA_ERR_OUT_OF_MEMORY leaves the plan without stored blocks.
+
+   fmca_matvec_assembled: H2MatrixBase::operator* (H2MatrixBase.h:107-109,
+   matrix_vector_product_impl.h:17-98): y = K_H2 x from the stored blocks,
+   with the upward and downward passes of fmca_matvec.  The kernel is the
+   one the blocks were assembled with; precision must be FMCA_PREC_FP64 for
+   FP64 blocks and FMCA_PREC_FP32 or FMCA_PREC_MIXED for FP32 blocks (the
+   stored blocks are contracted on the FP32 CUDA cores), otherwise
+   FMCA_ERR_INVALID_ARGUMENT, as without stored blocks.  Arguments, workspace
+   (fmca_matvec_workspace_size of the same precision suffices) and stream as
+   for fmca_matvec.
+
+   fmca_plan_release_assembled: frees the stored blocks (no-op without). */
+fmca_status fmca_plan_assembled_size(const fmca_plan* plan, int precision,
+                                     size_t* bytes);
+fmca_status fmca_plan_assemble(fmca_plan* plan, const fmca_kernel_desc* kernel,
+                               int precision, void* stream);
+fmca_status fmca_matvec_assembled(fmca_plan* plan, int precision, int dtype,
+                                  int order, int nrhs, const void* x,
+                                  int64_t x_stride_i, int64_t x_stride_r,
+                                  void* y, int64_t y_stride_i,
+                                  int64_t y_stride_r, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+fmca_status fmca_plan_release_assembled(fmca_plan* plan);
+
 /* Adjoint of the H2 product (no counterpart in the reference, which has no
    derivatives).  For f = sum_r y_r^T K x_r with K = sigma2 * H2[k] (cluster
    tree, boxes and interpolation nodes held fixed), it computes on the device:
