@@ -53,15 +53,16 @@ NEAR_DRAM_BYTES_PER_LAUNCH = 2.671359e9 + 0.151429e9
 REF_PARTS = 16
 
 
-def _measured_bf16_tflops():
+def _measured_peak(key, fallback):
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["bf16_tflops"])
+            return float(json.load(f)[key]), "of measured"
     except (OSError, KeyError, ValueError):
-        return 1900.0  # fallback figure of an earlier GB300 measurement
+        return fallback, "of fallback"  # figures of an earlier GB300 measurement
 
 
-BF16_TFLOPS = _measured_bf16_tflops()
+BF16_TFLOPS, BF16_SOURCE = _measured_peak("bf16_tflops", 1900.0)
+HBM_GBS, HBM_SOURCE = _measured_peak("hbm_gbs", 6800.0)
 
 
 def workload_config(args):
@@ -453,6 +454,8 @@ def main():
                     help="default launch shapes instead of the autotuner's")
     ap.add_argument("--no-gpu-build", action="store_true",
                     help="skip timing the plan build on the GPU")
+    ap.add_argument("--no-assembled", action="store_true",
+                    help="skip the assembled (stored-block) product of the workload")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2 (default): the headline workload; c3 batching, c4 gradients, "
                          "c5 GP step (one JSON line each, not the headline)")
@@ -561,6 +564,57 @@ def main():
         fp64 = {"ms_per_step": ms64, "value": args.n * args.rhs / (ms64 * 1e-3),
                 "mixed_rel_err_vs_fp64": err, "speedup_mixed_vs_fp64": ms64 / ms}
 
+    # the assembled H2 matrix of the workload (computeH2Matrix): FP32 blocks
+    # stored in HBM and streamed by every product (fmca_matvec_assembled);
+    # with one right-hand side the stream is bound by HBM bandwidth
+    asm = None
+    if not args.no_assembled:
+        need = H.assembled_bytes("fp32")
+        free = torch.cuda.mem_get_info(dev)[0]
+        if need + (8 << 30) > free:
+            asm = {"skipped": f"{need / 1e9:.1f} GB of stored blocks do not fit next to "
+                              f"the {free / 1e9:.1f} GB free"}
+        else:
+            barrier()
+            t0 = time.perf_counter()
+            H.computeH2Matrix("fp32")
+            barrier()
+            t_asm = time.perf_counter() - t0
+            Ya = torch.empty_like(Xd)
+            x1 = Xd[:, :1].contiguous()
+            y1 = torch.empty_like(x1)
+
+            def timed(fn, reps=5):
+                fn()
+                out = []
+                for _ in range(reps):
+                    flush.zero_()
+                    e0, e1 = (torch.cuda.Event(enable_timing=True),
+                              torch.cuda.Event(enable_timing=True))
+                    e0.record()
+                    fn()
+                    e1.record()
+                    torch.cuda.synchronize(dev)
+                    out.append(e0.elapsed_time(e1))
+                return statistics.median(out)
+
+            ms_a32 = timed(lambda: H.mul(Xd, Ya))
+            ms_a1 = timed(lambda: H.mul(x1, y1))
+            H.check_device_error()
+            ref = Y64 if fp64 is not None else Y
+            err = float((torch.linalg.norm(Ya - ref) / torch.linalg.norm(ref)).item())
+            asm = {"precision": "fp32", "stored_bytes": need, "assemble_s": t_asm,
+                   "ms_per_step": ms_a32, "value": args.n * args.rhs / (ms_a32 * 1e-3),
+                   "rel_err_vs_fp64" if fp64 is not None else "rel_err_vs_mixed": err,
+                   "r1_ms_per_step": ms_a1,
+                   "r1_roofline": {"bound": "hbm", "achieved": need / (ms_a1 * 1e-3) / 1e9,
+                                   "peak": HBM_GBS, "unit": "GB/s",
+                                   "frac": need / (ms_a1 * 1e-3) / 1e9 / HBM_GBS,
+                                   "peak_source": f"MEASURED_PEAKS.json hbm_gbs, {HBM_SOURCE}",
+                                   "work": "every stored block value read once per product"}}
+            del Ya, x1, y1
+            H.release_assembled()
+
     # roofline of the dominant kernel, the near-field kernel sum (ksum_um_kernel):
     # every point pair costs one square root and one exponential on
     # the special-function unit, the busiest unit of the kernel; the tensor
@@ -589,7 +643,7 @@ def main():
         "tensor": {"achieved": tensor_flops / t_near / 1e12, "peak": BF16_TFLOPS,
                    "unit": "TFLOP/s", "frac": tensor_flops / t_near / 1e12 / BF16_TFLOPS,
                    "work": "192 executed FP16 tensor flops per pair (3 products x 32 columns x 2)",
-                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst), of measured"},
+                   "peak_source": f"MEASURED_PEAKS.json bf16_tflops (cuBLAS burst), {BF16_SOURCE}"},
         "stage_ms": stage_ms,
     }
 
@@ -633,7 +687,7 @@ def main():
                     "ms_per_step": e2e_ms},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "fp64_gpu": fp64,
-            "vs_fp64_oracle": vs_oracle, "autotune": tuned,
+            "vs_fp64_oracle": vs_oracle, "autotune": tuned, "assembled": asm,
             "plan": {"build_s": t_plan, "gpu_tree_build": gpu_build,
                      "far_blocks": info["far_blocks"],
                      "near_blocks": info["near_blocks"], "near_pairs": info["near_pairs"],
