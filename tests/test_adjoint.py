@@ -259,3 +259,69 @@ def test_autograd_two_forwards_before_their_backwards(cuda_device):
     assert abs(f2.item() - fd.item()) / abs(fd.item()) < 1e-4
     assert abs(b[1].grad.item() - lt.grad.item()) / abs(lt.grad.item()) < 1e-3
     assert rel_err(b[3].grad.cpu().numpy(), Xt.grad.numpy()) < 1e-3
+
+
+@pytest.mark.gpu
+def test_c4_small_case_against_dense_autograd_and_differences(cuda_device):
+    # the gradient workload's own checks at its reduced size: n = 5000 points
+    # on S^2, MATERN52 l = 0.3, sigma2 = 1, p = 4, eta = 0.8, leaf 96
+    # (effective 125), x, y ~ N(0, 1) drawn in float32.  The GPU gradients
+    # (FP64 and mixed) against dense FP64 torch autograd of y^T K x (up to
+    # the H2 compression error, 7e-6 in f and 2e-5 in dX here) and the FP64
+    # ones against central differences with h = 1e-4 (1e-6)
+    import torch
+    from fmca_gb300 import CovarianceKernel, H2Matrix
+    from fmca_gb300.autograd import dense_reference
+    n, l = 5000, 0.3
+    P = sphere_cloud(n, seed=0)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((n, 1)).astype(np.float32)
+    y = rng.standard_normal((n, 1)).astype(np.float32)
+    Xt = torch.tensor(P, device=cuda_device, requires_grad=True)
+    lt = torch.tensor(l, dtype=torch.float64, device=cuda_device, requires_grad=True)
+    st = torch.tensor(1.0, dtype=torch.float64, device=cuda_device, requires_grad=True)
+    fd_ = (torch.tensor(y, dtype=torch.float64, device=cuda_device) *
+           dense_reference("MATERN52", lt, st, Xt,
+                           torch.tensor(x, dtype=torch.float64, device=cuda_device))).sum()
+    fd_.backward()
+    dense = {"f": fd_.item(), "dl": lt.grad.item(), "ds": st.grad.item(),
+             "dX": Xt.grad.cpu().numpy().T}
+    H = H2Matrix(CovarianceKernel("MATERN52", l), P, P, 4, 0.8, min_leaf=96, precision="fp64")
+    assert H.info["far_blocks"] > 0
+    got = {}
+    for prec, dt in (("fp64", torch.float64), ("mixed", torch.float32)):
+        out = H.adjoint(torch.tensor(x, dtype=dt, device=cuda_device),
+                        torch.tensor(y, dtype=dt, device=cuda_device), precision=prec)
+        v = out["values"].cpu().numpy()
+        got[prec] = {"f": v[0], "dl": v[1], "ds": v[2],
+                     "dX": out["dX"].double().cpu().numpy()}
+        H.check_device_error()
+    bound = {"fp64": {"f": 2e-5, "dl": 4e-5, "ds": 2e-5, "dX": 6e-5},
+             "mixed": {"f": 1e-4, "dl": 1e-4, "ds": 1e-4, "dX": 1e-4}}
+    for prec in ("fp64", "mixed"):
+        for k in ("f", "dl", "ds"):
+            assert abs(got[prec][k] - dense[k]) / abs(dense[k]) < bound[prec][k], (prec, k)
+        assert rel_err(got[prec]["dX"], dense["dX"]) < bound[prec]["dX"], prec
+    # central differences of the GPU FP64 product (tree, boxes, nodes frozen)
+    xt = torch.tensor(x, dtype=torch.float64, device=cuda_device)
+    yt = torch.tensor(y, dtype=torch.float64, device=cuda_device)
+
+    def f(cov_l=l, P_=None):
+        if P_ is not None:
+            H.update_points(P_)
+        H.cov.l = cov_l
+        v = float((yt * H.matvec(xt)).sum())
+        H.cov.l = l
+        return v
+
+    h = 1e-4
+    fd_l = (f(l * (1 + h)) - f(l * (1 - h))) / (2 * l * h)
+    assert abs(got["fp64"]["dl"] - fd_l) / abs(fd_l) < 1e-6
+    for _ in range(4):
+        i, d = int(rng.integers(0, n)), int(rng.integers(0, 3))
+        Pp, Pm = P.copy(), P.copy()
+        Pp[d, i] += h
+        Pm[d, i] -= h
+        fd = (f(P_=Pp) - f(P_=Pm)) / (2 * h)
+        H.update_points(P)
+        assert abs(got["fp64"]["dX"][i, d] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, d)
