@@ -6,6 +6,6 @@ by hand-written sm_103a CUDA kernels behind the C ABI of
 ``include/fmca_gb300.h``.
 """
 from ._lib import FmcaError, load  # noqa: F401
-from .h2 import CovarianceKernel, H2Matrix  # noqa: F401
+from .h2 import CovarianceKernel, H2Matrix, MultipoleFunctionEvaluator  # noqa: F401
 
-__all__ = ["CovarianceKernel", "H2Matrix", "FmcaError", "load"]
+__all__ = ["CovarianceKernel", "H2Matrix", "MultipoleFunctionEvaluator", "FmcaError", "load"]

@@ -54,8 +54,12 @@ fmca_status check_gpu_plan(const fmca_plan* p, int precision) {
     return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown precision mode");
   if (p->plan.interp.dim > 3)
     return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports dim <= 3");
-  if (p->plan.interp.deg > 7)
-    return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports degree <= 7");
+  if (p->plan.interp.kind == fmca::kInterpTensor && p->plan.interp.deg > 7)
+    return fail(FMCA_ERR_UNSUPPORTED, "the GPU path supports tensor-product degree <= 7");
+  if (p->plan.interp.kind == fmca::kInterpTotalDegree &&
+      (p->plan.interp.deg > 15 || p->plan.interp.q > 120))
+    return fail(FMCA_ERR_UNSUPPORTED,
+                "the GPU path supports total degree <= 15 with at most 120 nodes");
   return FMCA_OK;
 }
 }  // namespace
@@ -146,9 +150,16 @@ fmca_status create_plan(const double* P_rows, int dim, int64_t n_rows, const dou
   if (interpolator != FMCA_INTERP_TENSOR_PRODUCT && interpolator != FMCA_INTERP_TOTAL_DEGREE)
     return fail(FMCA_ERR_INVALID_ARGUMENT, "unknown interpolator");
   // the total-degree nodes come from Halton sequences in the first three
-  // prime bases, and the GPU passes take at most 8 polynomial factors
-  if (interpolator == FMCA_INTERP_TOTAL_DEGREE && (dim > 3 || degree > 7))
-    return fail(FMCA_ERR_UNSUPPORTED, "total-degree interpolation needs dim <= 3, degree <= 7");
+  // prime bases; the GPU passes take at most 16 polynomial factors per
+  // dimension and dense transfer matrices of at most 120 x 120
+  if (interpolator == FMCA_INTERP_TOTAL_DEGREE) {
+    int64_t q = 1;
+    for (int i = 1; i <= dim && dim <= 3; ++i) q = q * (degree + i) / i;  // binom(degree + dim, dim)
+    if (dim > 3 || degree > 15 || q > 120)
+      return fail(FMCA_ERR_UNSUPPORTED,
+                  "total-degree interpolation needs dim <= 3, degree <= 15 and at most 120 "
+                  "nodes (degree <= 7 in 3-D, <= 14 in 2-D)");
+  }
   if (!(eta >= 0) || !std::isfinite(eta))
     return fail(FMCA_ERR_INVALID_ARGUMENT, "eta must be finite and >= 0");
   if (min_leaf < 0 || min_leaf > (int64_t)0x7FFFFFFF)

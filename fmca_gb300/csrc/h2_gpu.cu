@@ -833,13 +833,53 @@ bool launch_basis_change(const InterpDev<T>& ip, int ncl, const T* M, T* buf, in
   return true;
 }
 
-template <typename T, int RB>
+template <typename T, int RB, int FS>
 size_t leafmom_smem(int q) {
-  return (size_t)kLeafChunk * (24 + RB) * sizeof(T) + (size_t)q * sizeof(int);
+  return (size_t)kLeafChunk * (3 * FS + RB) * sizeof(T) + (size_t)q * sizeof(int);
+}
+template <typename T, int RB, int FS>
+size_t leafgather_smem(int q) {
+  return ((size_t)128 * 3 * FS + (size_t)q * RB) * sizeof(T) + (size_t)q * sizeof(int);
+}
+
+// The leaf passes (upward: moments of the column leaves into t; downward:
+// the row leaves' far-field values from s) with 8 factor slots per
+// dimension, or 16 for the total-degree bases of degree 8 and above.
+template <typename T, int RB, int FS>
+cudaError_t leafmom_fs(int nb, const DevPlan* dp, const DevSet<T>& S, const T* xc, int ld,
+                       int rofs, int rcount, T* t, cudaStream_t st) {
+  auto kern = leafmom_kernel<T, RB, FS>;
+  const size_t smem = leafmom_smem<T, RB, FS>(S.ip.q);
+  ensure_smem(kern, smem);
+  kern<<<nb, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c, S.bbmin_c, S.bbext_c,
+                              S.pts_c, xc, ld, rofs, rcount, dp->midx, S.ip, t);
+  return cudaGetLastError();
 }
 template <typename T, int RB>
-size_t leafgather_smem(int q) {
-  return ((size_t)128 * 24 + (size_t)q * RB) * sizeof(T) + (size_t)q * sizeof(int);
+cudaError_t launch_leafmom(const DevPlan* dp, const DevSet<T>& S, const T* xc, int ld, int rofs,
+                           int rcount, T* t, cudaStream_t st) {
+  if (!dp->nleaves_c) return cudaSuccess;
+  if (S.ip.p1 > 8)
+    return leafmom_fs<T, RB, 16>(dp->nleaves_c, dp, S, xc, ld, rofs, rcount, t, st);
+  return leafmom_fs<T, RB, 8>(dp->nleaves_c, dp, S, xc, ld, rofs, rcount, t, st);
+}
+template <typename T, int RB, int FS>
+cudaError_t leafgather_fs(int nb, const DevPlan* dp, const DevSet<T>& S, const T* s, int ld,
+                          int rofs, int rcount, T* y, cudaStream_t st) {
+  auto kern = leafgather_kernel<T, RB, FS>;
+  const size_t smem = leafgather_smem<T, RB, FS>(S.ip.q);
+  ensure_smem(kern, smem);
+  kern<<<nb, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r, S.bbmin_r, S.bbext_r,
+                              S.pts_r, s, ld, rofs, rcount, dp->midx, S.ip, y);
+  return cudaGetLastError();
+}
+template <typename T, int RB>
+cudaError_t launch_leafgather(const DevPlan* dp, const DevSet<T>& S, const T* s, int ld,
+                              int rofs, int rcount, T* y, cudaStream_t st) {
+  if (!dp->nleaves_r) return cudaSuccess;
+  if (S.ip.p1 > 8)
+    return leafgather_fs<T, RB, 16>(dp->nleaves_r, dp, S, s, ld, rofs, rcount, y, st);
+  return leafgather_fs<T, RB, 8>(dp->nleaves_r, dp, S, s, ld, rofs, rcount, y, st);
 }
 
 // as: stored blocks of an assembled plan (the far field streams them instead
@@ -853,13 +893,8 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
   // upward pass: leaf moments
   {
     dp->launches += dp->nleaves_c ? 1 : 0;
-    auto kern = leafmom_kernel<T, RB>;
-    const size_t smem = leafmom_smem<T, RB>(q);
-    ensure_smem(kern, smem);
-    if (dp->nleaves_c)
-      kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
-                                             S.bbmin_c, S.bbext_c, S.pts_c, w.xc, ld,
-                                             rofs, rcount, dp->midx, S.ip, w.t);
+    cudaError_t e = launch_leafmom<T, RB>(dp, S, w.xc, ld, rofs, rcount, w.t, st);
+    if (e != cudaSuccess) return e;
     dp->mark(FMCA_STAGE_LEAFMOM, st);
   }
   // M2M, bottom-up
@@ -900,13 +935,8 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
   dp->mark(FMCA_STAGE_L2L, st);
   // leaf gather
   {
-    auto kern = leafgather_kernel<T, RB>;
-    const size_t smem = leafgather_smem<T, RB>(q);
-    ensure_smem(kern, smem);
-    if (dp->nleaves_r)
-      kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
-                                             S.bbmin_r, S.bbext_r, S.pts_r, w.s, ld,
-                                             rofs, rcount, dp->midx, S.ip, w.yfar);
+    cudaError_t eg = launch_leafgather<T, RB>(dp, S, w.s, ld, rofs, rcount, w.yfar, st);
+    if (eg != cudaSuccess) return eg;
     dp->launches += dp->nleaves_r ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFGATHER, st);
   }
@@ -1206,16 +1236,9 @@ struct TcChunk {
   cudaStream_t st;
 
   cudaError_t leafmom() {
-    constexpr int RB = kTcRhs;
-    auto kern = leafmom_kernel<float, RB>;
-    const size_t smem = leafmom_smem<float, RB>(q);
-    ensure_smem(kern, smem);
-    if (dp->nleaves_c) {
-      kern<<<dp->nleaves_c, 128, smem, st>>>(dp->leaves_c, dp->cbegin_c, dp->csize_c,
-                                             S->bbmin_c, S->bbext_c, S->pts_c, xc, kTcRhs, 0,
-                                             rcount, dp->midx, S->ip, t);
-      ++dp->launches;
-    }
+    cudaError_t e = launch_leafmom<float, kTcRhs>(dp, *S, xc, kTcRhs, 0, rcount, t, st);
+    if (e != cudaSuccess) return e;
+    dp->launches += dp->nleaves_c ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFMOM, st);
     return cudaGetLastError();
   }
@@ -1276,16 +1299,9 @@ struct TcChunk {
     return cudaGetLastError();
   }
   cudaError_t leafgather() {
-    constexpr int RB = kTcRhs;
-    auto kern = leafgather_kernel<float, RB>;
-    const size_t smem = leafgather_smem<float, RB>(q);
-    ensure_smem(kern, smem);
-    if (dp->nleaves_r) {
-      kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r,
-                                             S->bbmin_r, S->bbext_r, S->pts_r, s, kTcRhs, 0,
-                                             rcount, dp->midx, S->ip, yfar);
-      ++dp->launches;
-    }
+    cudaError_t e = launch_leafgather<float, kTcRhs>(dp, *S, s, kTcRhs, 0, rcount, yfar, st);
+    if (e != cudaSuccess) return e;
+    dp->launches += dp->nleaves_r ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFGATHER, st);
     return cudaGetLastError();
   }

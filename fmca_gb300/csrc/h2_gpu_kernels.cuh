@@ -548,7 +548,7 @@ __device__ __forceinline__ void basis1d(const InterpDev<T>& ip, T x, T* f, int s
   }
 }
 
-// multi-index k -> (k0, k1, k2) packed as k0 | k1 << 8 | k2 << 16 (digits < 8)
+// multi-index k -> (k0, k1, k2) packed as k0 | k1 << 8 | k2 << 16 (digits < 256)
 __device__ __forceinline__ void pack_digits(const int* __restrict__ midx_g, int q,
                                             int* __restrict__ pk) {
   for (int i = threadIdx.x; i < q; i += blockDim.x)
@@ -636,8 +636,10 @@ __device__ __forceinline__ void store_row(T* o, const T (&acc)[RB], int rc) {
 }
 
 // leaf moments: t[c][k][r] = sum_i V_c[k][i] x[i][r]
-// blockDim 128; shared: F[CH][3][8], X[CH][RB], packed digits q ints
-template <typename T, int RB>
+// blockDim 128; shared: F[CH][3][FS], X[CH][RB], packed digits q ints.  FS:
+// slots for the 1-D factors of one dimension, 8 (degree <= 7) or 16 (the
+// total-degree bases of higher degree)
+template <typename T, int RB, int FS = 8>
 __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
                                const uint32_t* __restrict__ cbegin,
                                const uint32_t* __restrict__ csize,
@@ -649,8 +651,8 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
                                InterpDev<T> ip, T* __restrict__ tout) {
   constexpr int CH = kLeafChunk;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  T* F = reinterpret_cast<T*>(smem_raw);  // CH x 3 x 8
-  T* X = F + CH * 24;                     // CH x RB
+  T* F = reinterpret_cast<T*>(smem_raw);  // CH x 3 x FS
+  T* X = F + CH * 3 * FS;                 // CH x RB
   int* pk = reinterpret_cast<int*>(X + CH * RB);
   const int c = leaves[blockIdx.x];
   const uint32_t b = cbegin[c], n = csize[c];
@@ -666,7 +668,7 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
     const bool valid = k < q;
     __syncthreads();
     const int kd = valid ? pk[k] : 0;
-    const int m0 = kd & 255, m1 = 8 + ((kd >> 8) & 255), m2 = kd >> 16;
+    const int m0 = kd & 255, m1 = FS + ((kd >> 8) & 255), m2 = kd >> 16;
     T acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = T(0);
@@ -674,7 +676,7 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
       const int cnt = (int)((n - i0) < (uint32_t)CH ? (n - i0) : CH);
       for (int t = tid; t < cnt * 3; t += nthr) {
         const int i = t / 3, d = t - 3 * i;
-        T* f = F + t * 8;
+        T* f = F + t * FS;
         if (d < ip.dim) {
           const T x = reinterpret_cast<const T*>(pts + b + i0 + i)[d];
           const T lod = d == 0 ? lo[0] : (d == 1 ? lo[1] : lo[2]);
@@ -688,8 +690,8 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
       __syncthreads();
       if (valid) {
         for (int i = 0; i < cnt; ++i) {
-          const T* f = F + i * 24;
-          const T v = f[m0] * f[m1] * f[16 + m2];
+          const T* f = F + i * 3 * FS;
+          const T v = f[m0] * f[m1] * f[2 * FS + m2];
 #pragma unroll
           for (int r = 0; r < RB; ++r) acc[r] += v * X[i * RB + r];
         }
@@ -970,8 +972,9 @@ __global__ void __launch_bounds__(256)
 
 // leaf gather: yfar[i][r] = sum_k V_c[k][i] s[c][k][r] for row leaves; in
 // FP32 the sum over k is compensated (compensated_sum.h)
-// shared: F[24][blockDim] (one column per thread), S[q][RB], packed digits q ints
-template <typename T, int RB>
+// shared: F[3 FS][blockDim] (one column per thread), S[q][RB], packed digits
+// q ints; FS as for leafmom_kernel
+template <typename T, int RB, int FS = 8>
 __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
                                   const uint32_t* __restrict__ cbegin,
                                   const uint32_t* __restrict__ csize,
@@ -983,8 +986,8 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
                                   InterpDev<T> ip, T* __restrict__ yout) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int q = ip.q, tid = threadIdx.x, nthr = blockDim.x;
-  T* F = reinterpret_cast<T*>(smem_raw);  // 24 x blockDim
-  T* S = F + nthr * 24;                   // q x RB
+  T* F = reinterpret_cast<T*>(smem_raw);  // 3 FS x blockDim
+  T* S = F + nthr * 3 * FS;               // q x RB
   int* pk = reinterpret_cast<int*>(S + (size_t)q * RB);
   const int c = leaves[blockIdx.x];
   const uint32_t b = cbegin[c], n = csize[c];
@@ -1003,9 +1006,9 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
     const T pc[3] = {p.x, p.y, p.z};
     for (int d = 0; d < 3; ++d) {
       if (d < ip.dim)
-        basis1d(ip, (pc[d] - lo[d]) / ex[d], f + d * 8 * nthr, nthr);
+        basis1d(ip, (pc[d] - lo[d]) / ex[d], f + d * FS * nthr, nthr);
       else
-        f[d * 8 * nthr] = T(1);
+        f[d * FS * nthr] = T(1);
     }
     T acc[RB];
 #pragma unroll
@@ -1023,8 +1026,8 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
         for (int r = 0; r < RB; ++r) part[r] = T(0);
         for (int k = k0; k < k1; ++k) {
           const int kd = pk[k];
-          const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
-                      f[(16 + (kd >> 16)) * nthr];
+          const T v = f[(kd & 255) * nthr] * f[(FS + ((kd >> 8) & 255)) * nthr] *
+                      f[(2 * FS + (kd >> 16)) * nthr];
 #pragma unroll
           for (int r = 0; r < RB; ++r) part[r] += v * S[k * RB + r];
         }
@@ -1034,8 +1037,8 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
     } else {
       for (int k = 0; k < q; ++k) {
         const int kd = pk[k];
-        const T v = f[(kd & 255) * nthr] * f[(8 + ((kd >> 8) & 255)) * nthr] *
-                    f[(16 + (kd >> 16)) * nthr];
+        const T v = f[(kd & 255) * nthr] * f[(FS + ((kd >> 8) & 255)) * nthr] *
+                    f[(2 * FS + (kd >> 16)) * nthr];
 #pragma unroll
         for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
       }

@@ -608,6 +608,49 @@ class H2Matrix:
         return out
 
 
+class MultipoleFunctionEvaluator:
+    """Evaluation of a kernel expansion f(y) = sum_j k(y, p_j) c_j at many
+    points through an H2 matrix: FMCA's MultipoleFunctionEvaluator
+    (FMCA/src/KernelInterpolation/MultipoleFunctionEvaluator.h:17-62), with
+    its interpolator (total degree), its defaults (eta = 0, degree 3, minimum
+    cluster size 0) and the evaluation points as rows, the data points as
+    columns.  ``precision`` chooses the GPU product (FP64 by default, as the
+    reference computes)."""
+
+    def __init__(self, kernel: Optional[CovarianceKernel] = None, P=None, Peval=None,
+                 eta: float = 0.0, mpole_deg: int = 3, precision: str = "fp64"):
+        self.H = None
+        if kernel is not None:
+            self.init(kernel, P, Peval, eta, mpole_deg, precision)
+
+    def init(self, kernel: CovarianceKernel, P, Peval, eta: float = 0.0, mpole_deg: int = 3,
+             precision: str = "fp64") -> None:
+        """Trees of both point sets and the block pattern (init, :24-38)."""
+        self.eta = float(eta) if eta >= 0 else 0.0
+        self.mpole_deg = int(mpole_deg)
+        self._P = np.array(P, dtype=np.float64, order="F", copy=True)
+        self._Peval = np.array(Peval, dtype=np.float64, order="F", copy=True)
+        self.H = H2Matrix(kernel, self._Peval, self._P, self.mpole_deg, self.eta, min_leaf=0,
+                          precision=precision, interpolator="total_degree")
+
+    def evaluate(self, P, Peval, C) -> np.ndarray:
+        """f at Peval for the coefficients C (n_P x R, natural order), as
+        evaluate (:52-58).  Points other than those of ``init`` are moved
+        into the trees, boxes and nodes built at ``init``."""
+        if self.H is None:
+            raise RuntimeError("MultipoleFunctionEvaluator: call init() first")
+        P = np.asarray(P, dtype=np.float64)
+        Peval = np.asarray(Peval, dtype=np.float64)
+        if not (np.array_equal(P, self._P) and np.array_equal(Peval, self._Peval)):
+            self.H.update_points(Peval, P)
+            self._P = np.array(P, order="F", copy=True)
+            self._Peval = np.array(Peval, order="F", copy=True)
+        return self.H.action(C)
+
+    def statistics(self, verbose: bool = True) -> np.ndarray:
+        return self.H.statistics(verbose)
+
+
 class MatvecGraph:
     """A matvec recorded into a CUDA graph (fmca_matvec_graph_create); each
     ``launch`` replays the whole product with a single graph launch."""

@@ -165,8 +165,9 @@ enum { FMCA_INTERP_TENSOR_PRODUCT = 0, FMCA_INTERP_TOTAL_DEGREE = 1 };
    (FMCA/src/Interpolator/TotalDegreeInterpolator.h:26-47: q = binom(p+dim,
    dim) DeMarchi nodes, Legendre polynomials, coupling invV K invV^T), the
    interpolator the reference's Python module instantiates
-   (py/FMCA.cpp:37-40).  Total degree: dim <= 3, degree <= 7; the adjoint
-   and batched plans are tensor-product only (FMCA_ERR_UNSUPPORTED). */
+   (py/FMCA.cpp:37-40).  Total degree: dim <= 3, degree <= 15 and at most
+   120 nodes (degree <= 7 in 3-D, <= 14 in 2-D); the adjoint and batched
+   plans are tensor-product only (FMCA_ERR_UNSUPPORTED). */
 fmca_status fmca_plan_create_ex(const double* P_rows, int dim, int64_t n_rows,
                                 const double* P_cols, int64_t n_cols, int interpolator,
                                 int degree, double eta, int64_t min_leaf, fmca_plan** out);

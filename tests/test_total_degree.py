@@ -23,7 +23,7 @@ from fmca_gb300 import CovarianceKernel, H2Matrix, _lib
 
 ERR = {v: k for k, v in _lib.STATUS_NAMES.items()}
 
-CASES = [(1, 3), (2, 4), (2, 7), (3, 2), (3, 4), (3, 6)]
+CASES = [(1, 3), (2, 4), (2, 7), (3, 2), (3, 4), (3, 6), (2, 10), (2, 14), (1, 15)]
 
 
 @pytest.mark.parametrize("dim,p", CASES)
@@ -85,6 +85,18 @@ def test_out_of_range_total_degree_is_refused():
     P3 = np.asfortranarray(uniform_cloud(100, 3, seed=1))
     dp3 = P3.ctypes.data_as(C.POINTER(C.c_double))
     st = lib.fmca_plan_create_ex(dp3, 3, 100, None, 100, 1, 8, 0.8, 0, C.byref(h))
+    assert st == ERR["FMCA_ERR_UNSUPPORTED"]  # 165 nodes
+    P2 = np.asfortranarray(uniform_cloud(300, 2, seed=1))
+    dp2 = P2.ctypes.data_as(C.POINTER(C.c_double))
+    st = lib.fmca_plan_create_ex(dp2, 2, 300, None, 300, 1, 15, 0.8, 0, C.byref(h))
+    assert st == ERR["FMCA_ERR_UNSUPPORTED"]  # 136 nodes
+    assert lib.fmca_plan_create_ex(dp2, 2, 300, None, 300, 1, 14, 0.8, 0, C.byref(h)) == 0
+    lib.fmca_plan_destroy(h)
+    P1 = np.asfortranarray(uniform_cloud(300, 1, seed=1))
+    dp1 = P1.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.fmca_plan_create_ex(dp1, 1, 300, None, 300, 1, 15, 0.8, 0, C.byref(h)) == 0
+    lib.fmca_plan_destroy(h)
+    st = lib.fmca_plan_create_ex(dp1, 1, 300, None, 300, 1, 16, 0.8, 0, C.byref(h))
     assert st == ERR["FMCA_ERR_UNSUPPORTED"]
     st = lib.fmca_plan_create_ex(dp3, 3, 100, None, 100, 7, 3, 0.8, 0, C.byref(h))
     assert st == ERR["FMCA_ERR_INVALID_ARGUMENT"]
@@ -98,7 +110,9 @@ TOL = {"fp64": 1e-12, "fp32": 1e-5, "mixed": 1e-5}
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "mixed"])
 @pytest.mark.parametrize("dim,p,kname", [(3, 4, "MATERN32"), (3, 3, "GAUSSIAN"),
-                                         (2, 5, "EXPONENTIAL"), (3, 6, "MATERN52")])
+                                         (2, 5, "EXPONENTIAL"), (3, 6, "MATERN52"),
+                                         (2, 10, "EXPONENTIAL"), (2, 14, "MATERN32"),
+                                         (1, 15, "GAUSSIAN")])
 def test_gpu_matvec_against_oracle(cuda_device, precision, dim, p, kname):
     n = 20000
     P = uniform_cloud(n, dim, seed=p)
