@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "compensated_sum.h"
 
 namespace fmca {
@@ -443,8 +445,54 @@ __global__ void ksum_kernel(const KGroup* __restrict__ groups,
       const int cnt = scnt[stage];
       const Pt4<T>* P = spts + stage * TS;
       const T* V = svals + (size_t)stage * TS * ldv + rofs;
+      int j = 0;
+      if constexpr (sizeof(T) == 4 && RB % 4 == 0) {
+        // FP32: two sources per step in packed FP32x2 arithmetic (the
+        // squared distances of both, and every accumulator pair of
+        // columns (r, r + 1) updated by one FFMA2 per source); the same
+        // operations per element as the scalar loop below
+        for (; j + 1 < cnt; j += 2) {
+          const Pt4<T> s0 = P[j], s1 = P[j + 1];
+          const float2 sx = make_float2(s0.x, s1.x), sy = make_float2(s0.y, s1.y),
+                       sz = make_float2(s0.z, s1.z);
+          float2 ka[TPT], kb[TPT];
+#pragma unroll
+          for (int t = 0; t < TPT; ++t) {
+            const float2 m1 = make_float2(-1.f, -1.f);
+            const float2 dx = __ffma2_rn(sx, m1, make_float2(tx[t], tx[t]));
+            const float2 dy = __ffma2_rn(sy, m1, make_float2(ty[t], ty[t]));
+            const float2 dz = __ffma2_rn(sz, m1, make_float2(tz[t], tz[t]));
+            const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+            const T k0 = keval<T, KT>(r2.x, kp), k1 = keval<T, KT>(r2.y, kp);
+            ka[t] = make_float2(k0, k0);
+            kb[t] = make_float2(k1, k1);
+          }
+          const T* v0 = V + (size_t)j * ldv;
+          const T* v1 = v0 + ldv;
+#pragma unroll
+          for (int r = 0; r < RB; r += 4) {
+            const float4 a = *reinterpret_cast<const float4*>(v0 + r);
+            const float4 b = *reinterpret_cast<const float4*>(v1 + r);
+            const float2 a01 = make_float2(a.x, a.y), a23 = make_float2(a.z, a.w);
+            const float2 b01 = make_float2(b.x, b.y), b23 = make_float2(b.z, b.w);
+#pragma unroll
+            for (int t = 0; t < TPT; ++t) {
+              float2 p01 = make_float2(acc[t][r + 0], acc[t][r + 1]);
+              float2 p23 = make_float2(acc[t][r + 2], acc[t][r + 3]);
+              p01 = __ffma2_rn(ka[t], a01, p01);
+              p23 = __ffma2_rn(ka[t], a23, p23);
+              p01 = __ffma2_rn(kb[t], b01, p01);
+              p23 = __ffma2_rn(kb[t], b23, p23);
+              acc[t][r + 0] = p01.x;
+              acc[t][r + 1] = p01.y;
+              acc[t][r + 2] = p23.x;
+              acc[t][r + 3] = p23.y;
+            }
+          }
+        }
+      }
 #pragma unroll 2
-      for (int j = 0; j < cnt; ++j) {
+      for (; j < cnt; ++j) {
         const Pt4<T> s = P[j];
         T kv[TPT];
 #pragma unroll
