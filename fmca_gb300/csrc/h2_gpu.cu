@@ -1500,7 +1500,8 @@ bool stream_capturing(cudaStream_t st) {
 // this plan with CUDA events on the caller's stream and keeps the fastest in
 // dp->cfg.  Steps (each trial timed twice, the faster counts):
 //  1. fewer than 17 right-hand sides: one whole matvec on the FP32 CUDA
-//     cores against one on the tensor cores (columns padded to 32);
+//     cores against the faster of two on the tensor cores (columns padded
+//     to 32; near-field groups of two target halves and of one);
 //  2. on the tensor-core path, after one matvec with the defaults has
 //     filled the workspace, the stages of the first right-hand-side chunk
 //     one by one: the near-field kernel sum with two target halves over
@@ -1558,8 +1559,14 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
       const float t_cc = timed(run_cc);
       dp->cfg.small_tc = 1;
       const float t_tc = timed(run_tc);
-      if (t_cc < 0.f || t_tc < 0.f) status = FMCA_ERR_CUDA;
-      use_tc = t_tc < t_cc;
+      // the near field with one target half of 128 as well: leaves of up to
+      // 128 points fill a third of two halves
+      dp->cfg.near_halves = 1;
+      dp->cfg.near = UmCfg{um_stages(1), 1};
+      const float t_tc1 = timed(run_tc);
+      dp->cfg = best;
+      if (t_cc < 0.f || t_tc < 0.f || t_tc1 < 0.f) status = FMCA_ERR_CUDA;
+      use_tc = std::min(t_tc, t_tc1) < t_cc;
       best.small_tc = use_tc ? 1 : 0;
     }
     if (status == FMCA_OK && use_tc) {
