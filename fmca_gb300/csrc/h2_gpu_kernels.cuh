@@ -649,6 +649,30 @@ __device__ __forceinline__ void stage_rows(T* __restrict__ dst, const T* src, in
   }
 }
 
+// acc[r] += v * row[r] for r < RB; FP32 with RB a multiple of 4: packed
+// FP32x2 FMAs on column pairs fed by 16-byte loads (row 16-byte aligned),
+// the same rounding per element as the scalar loop
+template <typename T, int RB>
+__device__ __forceinline__ void axpy_row(T (&acc)[RB], T v, const T* __restrict__ row) {
+  if constexpr (sizeof(T) == 4 && RB % 4 == 0) {
+    const float2 vv = make_float2(v, v);
+#pragma unroll
+    for (int r = 0; r < RB; r += 4) {
+      const float4 x = *reinterpret_cast<const float4*>(row + r);
+      const float2 p01 = __ffma2_rn(vv, make_float2(x.x, x.y), make_float2(acc[r], acc[r + 1]));
+      const float2 p23 =
+          __ffma2_rn(vv, make_float2(x.z, x.w), make_float2(acc[r + 2], acc[r + 3]));
+      acc[r] = p01.x;
+      acc[r + 1] = p01.y;
+      acc[r + 2] = p23.x;
+      acc[r + 3] = p23.y;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = fma(v, row[r], acc[r]);
+  }
+}
+
 // o[r] = acc[r] (ADD: o[r] += acc[r]) for r < rc, as 16-byte vectors when the
 // row is full and aligned
 template <typename T, int RB, bool ADD>
@@ -740,8 +764,7 @@ __global__ void leafmom_kernel(const int32_t* __restrict__ leaves,
         for (int i = 0; i < cnt; ++i) {
           const T* f = F + i * 3 * FS;
           const T v = f[m0] * f[m1] * f[2 * FS + m2];
-#pragma unroll
-          for (int r = 0; r < RB; ++r) acc[r] += v * X[i * RB + r];
+          axpy_row<T, RB>(acc, v, X + i * RB);
         }
       }
       __syncthreads();
@@ -1076,8 +1099,7 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
           const int kd = pk[k];
           const T v = f[(kd & 255) * nthr] * f[(FS + ((kd >> 8) & 255)) * nthr] *
                       f[(2 * FS + (kd >> 16)) * nthr];
-#pragma unroll
-          for (int r = 0; r < RB; ++r) part[r] += v * S[k * RB + r];
+          axpy_row<T, RB>(part, v, S + k * RB);
         }
 #pragma unroll
         for (int r = 0; r < RB; ++r) kahan_add(acc[r], cmp[r], part[r]);
@@ -1087,8 +1109,7 @@ __global__ void leafgather_kernel(const int32_t* __restrict__ leaves,
         const int kd = pk[k];
         const T v = f[(kd & 255) * nthr] * f[(FS + ((kd >> 8) & 255)) * nthr] *
                     f[(2 * FS + (kd >> 16)) * nthr];
-#pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] += v * S[k * RB + r];
+        axpy_row<T, RB>(acc, v, S + k * RB);
       }
     }
     store_row<T, RB, false>(yout + (size_t)(b + i0 + tid) * ldv + rofs, acc, rcount);
