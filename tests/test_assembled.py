@@ -227,3 +227,20 @@ def test_assembled_stream_wait_runs_out(cuda_device, case):
     y = H.mul(x)
     H.check_device_error()
     assert rel_err(y.cpu().numpy(), Y_ref[:, :8]) < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,dim", [(1, 3), (2, 3), (17, 3), (500, 1), (3000, 2)])
+def test_assembled_small_and_low_dimensional(cuda_device, n, dim):
+    # single points, a leaf-only tree, one and two dimensions
+    import torch
+    P = uniform_cloud(n, dim, seed=n + dim)
+    X = np.random.default_rng(n).standard_normal((n, 3))
+    cov = CovarianceKernel("MATERN52", 0.5)
+    H = H2Matrix(cov, P, P, 3, 0.8, precision="fp64")
+    assert H.assembled_bytes("fp64") == expected_bytes(H, "fp64")
+    H.computeH2Matrix()
+    y = H.mul(torch.tensor(X, device=cuda_device)).cpu().numpy()
+    Y_ref, _ = oracle.OraclePlan(P, None, 3, 0.8, 0).action(2, 0.5, X)
+    assert rel_err(y, Y_ref) < 1e-12
+    H.check_device_error()
