@@ -118,6 +118,9 @@ struct TuneCfg {
   int far_pairs = 1;  // 3-D plans of degree kGridP1 - 1: paired grids (1) or nodes (0)
   TrCfg tr{4 * 152, 2 * 152};
   int small_tc = 0;   // mixed precision, nrhs <= 16: tensor cores (1) or FP32 CUDA cores (0)
+  // tensor-core path, GAUSSIAN on tensor-product nodes: the far field as
+  // Kronecker products on the CUDA cores (1) or the tensor-core kernel sum (0)
+  int far_kron = 1;
   int tuned = 0;      // 1 if the autotuner chose these values
   float tune_ms = 0;  // time the tuning took
   static TuneCfg defaults(int sms) {
@@ -818,6 +821,63 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
                               rcount);
 }
 
+// The far field of the GAUSSIAN kernel on tensor-product nodes as Kronecker
+// products (far_kron_kernel), for the grids it is instantiated for: 2-D with
+// 3..8 nodes per dimension, 3-D with 3..6.  false: not applicable (another
+// kernel, total degree, other grids); the caller runs the dense kernel sum.
+template <typename T>
+bool far_kron_ok(const DevPlan* dp, const DevSet<T>& S, int type, int rcount) {
+  const bool grid = (S.ip.dim == 2 && S.ip.p1 >= 3 && S.ip.p1 <= 8) ||
+                    (S.ip.dim == 3 && S.ip.p1 >= 3 && S.ip.p1 <= 6);
+  return type == FMCA_KERNEL_GAUSSIAN && S.ip.kind == kInterpTensor && rcount <= 32 && grid &&
+         dp->far.ngroups > 0 && dp->far.maxcount == S.ip.q;
+}
+template <typename T>
+bool launch_far_kron(const DevPlan* dp, const DevSet<T>& S, const KParams<T>& kp, const T* t,
+                     T* s, int ld, int rofs, int rcount, cudaStream_t st, cudaError_t* err) {
+  if (!far_kron_ok(dp, S, kp.type, rcount)) return false;
+  const T e = sizeof(T) == 4 ? kp.e2 : T(-0.5) / (kp.l * kp.l);
+  // columns per source-cluster slot: 32 / RW clusters contracted at once
+  const int rw = rcount <= 1 ? 1 : (rcount <= 8 ? 8 : 32);
+  auto go = [&](auto k1, auto k8, auto k32, int Q, int DIM, int P) {
+    const int sl = 32 / rw;
+    const size_t smem = ((size_t)3 * Q * 32 + DIM * P + (size_t)sl * DIM * P * P) * sizeof(T) +
+                        (size_t)(Q + sl) * sizeof(int);
+    auto launch = [&](auto kern) {
+      ensure_smem(kern, smem);
+      kern<<<dp->far.ngroups, 256, smem, st>>>(dp->far.groups, dp->far.ivl, S.nodes_r,
+                                               S.nodes_c, dp->midx, e, t, s, ld, rofs, rcount);
+    };
+    if (rw == 1)
+      launch(k1);
+    else if (rw == 8)
+      launch(k8);
+    else
+      launch(k32);
+    *err = cudaGetLastError();
+    return true;
+  };
+#define FMCA_KRON(D, P)                                                                       \
+  case D * 16 + P:                                                                            \
+    return go(far_kron_kernel<T, D, P, 1>, far_kron_kernel<T, D, P, 8>,                       \
+              far_kron_kernel<T, D, P, 32>, D == 2 ? P * P : P * P * P, D, P);
+  switch (S.ip.dim * 16 + S.ip.p1) {
+    FMCA_KRON(2, 3)
+    FMCA_KRON(2, 4)
+    FMCA_KRON(2, 5)
+    FMCA_KRON(2, 6)
+    FMCA_KRON(2, 7)
+    FMCA_KRON(2, 8)
+    FMCA_KRON(3, 3)
+    FMCA_KRON(3, 4)
+    FMCA_KRON(3, 5)
+    FMCA_KRON(3, 6)
+    default:
+      return false;
+  }
+#undef FMCA_KRON
+}
+
 // total degree: coefficients of clusters 0 .. ncl - 1 to (M = invV^T) or
 // from (M = invV) the nodal basis of the far field; one launch (or none for
 // the tensor product, whose basis is nodal already)
@@ -910,13 +970,16 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
   dp->launches += launch_basis_change<T, RB>(S.ip, plan.cols.nclusters(), S.to_nodal, w.t, ld,
                                              rofs, rcount, st);
   dp->mark(FMCA_STAGE_M2M, st);
-  // far-field coupling
-  cudaError_t e =
-      as ? launch_kstream<T>(RB, dp->far.groups, dp->far.ngroups, dp->far.maxcount, dp->far.ivl,
-                             as->far_off, static_cast<const T*>(as->far), w.t, ld, w.s, rofs,
-                             rcount, kp.wait_ns, kp.stall, dp->err_flag, st)
-         : launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s, rofs, rcount, kp, 0,
-                          dp->err_flag, st);
+  // far-field coupling: stored blocks, the Gaussian's Kronecker factors, or
+  // the kernel sum over the node pairs
+  cudaError_t e = cudaSuccess;
+  if (as)
+    e = launch_kstream<T>(RB, dp->far.groups, dp->far.ngroups, dp->far.maxcount, dp->far.ivl,
+                          as->far_off, static_cast<const T*>(as->far), w.t, ld, w.s, rofs,
+                          rcount, kp.wait_ns, kp.stall, dp->err_flag, st);
+  else if (!launch_far_kron<T>(dp, S, kp, w.t, w.s, ld, rofs, rcount, st, &e))
+    e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s, rofs, rcount, kp, 0,
+                       dp->err_flag, st);
   if (e != cudaSuccess) return e;
   dp->launches += dp->far.ngroups ? 1 : 0;
   dp->launches += launch_basis_change<T, RB>(S.ip, plan.rows.nclusters(), S.from_nodal, w.s,
@@ -1261,6 +1324,15 @@ struct TcChunk {
   // sum, on the sibling-paired tensor grids (3-D plans of degree
   // kGridP1 - 1, unless cfg.far_pairs is 0) or on interpolation nodes
   cudaError_t far(const TuneCfg& cfg) {
+    // the Gaussian's far field as Kronecker products (FP32 CUDA cores on the
+    // unscaled moments), when the grid is one it is compiled for
+    cudaError_t ek = cudaSuccess;
+    if (cfg.far_kron && launch_far_kron<float>(dp, *S, kp, t, s, kTcRhs, 0, rcount, st, &ek)) {
+      ++dp->launches;
+      if (ek != cudaSuccess) return ek;
+      dp->mark(FMCA_STAGE_FAR, st);
+      return cudaGetLastError();
+    }
     const bool grid = grid_far(*plan) && cfg.far_pairs;
     if (grid)
       tscale_grid_kernel<<<Cc, 128, 0, st>>>(Cc, rcount, t, S->nodes_c, dp->midx, kp.g, w.tv,
@@ -1602,11 +1674,26 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
             best.near = uc;
         }
         bt = -1.f;
+        // the Gaussian's Kronecker far field first (the default where it
+        // applies), then the tensor-core kernel sums
+        best.far_kron = 0;
+        if (far_kron_ok(dp, dp->f, k.type, std::min(nrhs, kTcRhs))) {
+          TuneCfg cand = best;
+          cand.far_kron = 1;
+          const float ms = timed([&]() { return ok_cuda(c.far(cand)); });
+          if (ms < 0.f)
+            status = FMCA_ERR_CUDA;
+          else {
+            bt = ms;
+            best.far_kron = 1;
+          }
+        }
         const bool grid = grid_far(plan);
         for (int pairs = grid ? 1 : 0; pairs >= 0 && status == FMCA_OK; --pairs)
           for (int nst = pairs ? 4 : 5; nst <= (pairs ? 6 : 7); ++nst)
             for (int F = 1; F <= (pairs ? 3 : 2); ++F) {
               TuneCfg cand = best;
+              cand.far_kron = 0;
               cand.far_pairs = pairs;
               (pairs ? cand.far_grid : cand.far_nodes) = UmCfg{nst, F};
               const float ms = timed([&]() { return ok_cuda(c.far(cand)); });
@@ -1616,12 +1703,13 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
               }
               if (bt < 0.f || ms < bt) {
                 bt = ms;
+                best.far_kron = 0;
                 best.far_pairs = cand.far_pairs;
                 best.far_grid = cand.far_grid;
                 best.far_nodes = cand.far_nodes;
               }
             }
-        if (status == FMCA_OK) {  // the fastest shape as a persistent launch
+        if (status == FMCA_OK && !best.far_kron) {  // the fastest shape as a persistent launch
           TuneCfg cand = best;
           (cand.far_pairs && grid ? cand.far_grid : cand.far_nodes).persist = 1;
           const float ms = timed([&]() { return ok_cuda(c.far(cand)); });
@@ -1893,6 +1981,7 @@ void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) 
   // the tuner sets it on the far-field form the plan uses
   out[FMCA_TUNE_FAR_PERSIST] = c.far_grid.persist | c.far_nodes.persist;
   out[FMCA_TUNE_US] = (int32_t)(c.tune_ms * 1000.f);
+  out[FMCA_TUNE_FAR_KRON] = c.far_kron;
   (void)pairs;
 }
 
@@ -1909,6 +1998,7 @@ int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32
       (in[FMCA_TUNE_NEAR_HALVES] != 1 && in[FMCA_TUNE_NEAR_HALVES] != 2) ||
       (in[FMCA_TUNE_NEAR_PERSIST] != 0 && in[FMCA_TUNE_NEAR_PERSIST] != 1) ||
       (in[FMCA_TUNE_FAR_PERSIST] != 0 && in[FMCA_TUNE_FAR_PERSIST] != 1) ||
+      (in[FMCA_TUNE_FAR_KRON] != 0 && in[FMCA_TUNE_FAR_KRON] != 1) ||
       in[FMCA_TUNE_WIDE_BELOW] < 0 || in[FMCA_TUNE_SLICE_BELOW] < 0) {
     *err = "launch shapes out of range (stages 2..7, units 1..min(3, stages), flags 0/1, "
            "halves 1/2, thresholds >= 0)";
@@ -1924,6 +2014,7 @@ int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32
                       in[FMCA_TUNE_FAR_PERSIST]};
   c.tr = TrCfg{in[FMCA_TUNE_WIDE_BELOW], in[FMCA_TUNE_SLICE_BELOW]};
   c.small_tc = in[FMCA_TUNE_SMALL_R_TENSOR];
+  c.far_kron = in[FMCA_TUNE_FAR_KRON];
   c.tuned = 1;
   std::lock_guard<std::mutex> lock(dp->mu);
   dp->tuned[tune_key(precision, type, nrhs)] = c;

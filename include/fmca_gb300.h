@@ -446,15 +446,17 @@ enum {
   FMCA_TUNE_FAR_PERSIST = 13,     /* far field: the same */
   FMCA_TUNE_US = 14,              /* time the tuning took, microseconds */
   FMCA_TUNE_TUNINGS = 15,         /* tuning runs on this plan so far */
-  FMCA_TUNE_COUNT = 16
+  FMCA_TUNE_FAR_KRON = 16,        /* GAUSSIAN on tensor-product nodes, mixed precision:
+                                     1 far field as Kronecker products, 0 kernel sums */
+  FMCA_TUNE_COUNT = 17
 };
 /* The launch shapes a matvec of this key uses now: the tuned ones, or the
    defaults (FMCA_TUNE_TUNED = 0). */
 fmca_status fmca_plan_tuned_config(fmca_plan* plan, int precision, int kernel_type, int nrhs,
                                    int32_t out[FMCA_TUNE_COUNT]);
 /* Sets the launch shapes of a key as if the autotuner had chosen them
-   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_FAR_PERSIST of cfg; the others
-   are ignored): for reusing shapes tuned earlier, for instance in another
+   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_FAR_PERSIST and
+   FMCA_TUNE_FAR_KRON of cfg; the others are ignored): for reusing shapes tuned earlier, for instance in another
    process on the same plan.  The plan must be resident on the current
    device (after one matvec).  Out-of-range shapes give
    FMCA_ERR_INVALID_ARGUMENT. */

@@ -47,12 +47,19 @@ def expected_bytes(H, precision):
     for c in range(H.info["row_clusters"]):
         elems += int(nfar[c]) * q * qr
         groups += qg
+    # dense blocks belong to the row leaves inside their row cluster (a dense
+    # block may pair a leaf with a larger cluster on either side)
+    is_leaf = np.ones(len(meta_r), bool)
+    is_leaf[meta_r[:, 3][meta_r[:, 3] >= 0]] = False
+    leaves = np.nonzero(is_leaf)[0]
     near_r, near_c = H.blocks(1)
     srcs = {}
     for r, c in zip(near_r, near_c):
-        srcs[r] = srcs.get(r, 0) + int(meta_c[c, 1])
-    for r, ns in srcs.items():
-        lr, lg = rows(int(meta_r[r, 1]))
+        b, e = meta_r[r, 0], meta_r[r, 0] + meta_r[r, 1]
+        for lf in leaves[(meta_r[leaves, 0] >= b) & (meta_r[leaves, 0] < e)]:
+            srcs[lf] = srcs.get(lf, 0) + int(meta_c[c, 1])
+    for lf, ns in srcs.items():
+        lr, lg = rows(int(meta_r[lf, 1]))
         elems += ns * lr
         groups += lg
     return elems * (8 if precision == "fp64" else 4) + groups * 8

@@ -279,3 +279,32 @@ def test_mixed_interpolation_orders(cuda_device, dim, p):
     H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, p, 0.8, precision="mixed")
     assert rel_err(H.action(X), Y_ref) < 1e-5
     H.check_device_error()
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("dim,p", [(2, 7), (3, 5), (2, 2), (3, 2), (3, 6)])
+def test_gaussian_far_field_as_kronecker_products(cuda_device, prec, dim, p):
+    # GAUSSIAN far fields on tensor-product nodes are Kronecker products of
+    # 1-D factors (grids of 3..8 nodes per dimension in 2-D, 3..6 in 3-D;
+    # p = 6 in 3-D, 7 nodes, takes the kernel sum); in mixed precision the
+    # tensor-core kernel sum stays a choice of the tuned configuration
+    import torch
+    n, R = 12000, 32
+    P = uniform_cloud(n, dim, seed=10 * dim + p)
+    X = np.random.default_rng(p).standard_normal((n, R))
+    O = oracle.OraclePlan(P, None, p, 0.8, 0)
+    assert O.n_far > 0
+    Y_ref, _ = O.action(3, 0.3, X)
+    H = H2Matrix(CovarianceKernel("GAUSSIAN", 0.3), P, P, p, 0.8, precision=prec)
+    x = torch.tensor(X, device=cuda_device)
+    y = H.matvec(x).cpu().numpy()
+    H.check_device_error()
+    assert rel_err(y, Y_ref) < TOL[prec]
+    if prec == "mixed":
+        cfg = H.tuned_config(R)
+        assert cfg["far_kron"] == 1
+        cfg["far_kron"] = 0
+        H.set_tuned_config(R, cfg)
+        y2 = H.matvec(x).cpu().numpy()
+        H.check_device_error()
+        assert rel_err(y2, Y_ref) < TOL[prec]
