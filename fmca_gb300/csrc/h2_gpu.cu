@@ -12,6 +12,7 @@
 #include "h2_gpu.h"
 #include "h2_adjoint_kernels.cuh"
 #include "h2_assembled.h"
+#include "h2_far_kron.h"
 #include "h2_gpu_kernels.cuh"
 #include "h2_tc_kernels.cuh"
 #include "h2_umma_kernels.cuh"
@@ -827,55 +828,18 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
 // kernel, total degree, other grids); the caller runs the dense kernel sum.
 template <typename T>
 bool far_kron_ok(const DevPlan* dp, const DevSet<T>& S, int type, int rcount) {
-  const bool grid = (S.ip.dim == 2 && S.ip.p1 >= 3 && S.ip.p1 <= 8) ||
-                    (S.ip.dim == 3 && S.ip.p1 >= 3 && S.ip.p1 <= 6);
-  return type == FMCA_KERNEL_GAUSSIAN && S.ip.kind == kInterpTensor && rcount <= 32 && grid &&
-         dp->far.ngroups > 0 && dp->far.maxcount == S.ip.q;
+  return type == FMCA_KERNEL_GAUSSIAN && S.ip.kind == kInterpTensor && rcount <= 32 &&
+         far_kron_grid(S.ip.dim, S.ip.p1) && dp->far.ngroups > 0 && dp->far.maxcount == S.ip.q;
 }
 template <typename T>
 bool launch_far_kron(const DevPlan* dp, const DevSet<T>& S, const KParams<T>& kp, const T* t,
                      T* s, int ld, int rofs, int rcount, cudaStream_t st, cudaError_t* err) {
   if (!far_kron_ok(dp, S, kp.type, rcount)) return false;
   const T e = sizeof(T) == 4 ? kp.e2 : T(-0.5) / (kp.l * kp.l);
-  // columns per source-cluster slot: 32 / RW clusters contracted at once
-  const int rw = rcount <= 1 ? 1 : (rcount <= 8 ? 8 : 32);
-  auto go = [&](auto k1, auto k8, auto k32, int Q, int DIM, int P) {
-    const int sl = 32 / rw;
-    const size_t smem = ((size_t)3 * Q * 32 + DIM * P + (size_t)sl * DIM * P * P) * sizeof(T) +
-                        (size_t)(Q + sl) * sizeof(int);
-    auto launch = [&](auto kern) {
-      ensure_smem(kern, smem);
-      kern<<<dp->far.ngroups, 256, smem, st>>>(dp->far.groups, dp->far.ivl, S.nodes_r,
-                                               S.nodes_c, dp->midx, e, t, s, ld, rofs, rcount);
-    };
-    if (rw == 1)
-      launch(k1);
-    else if (rw == 8)
-      launch(k8);
-    else
-      launch(k32);
-    *err = cudaGetLastError();
-    return true;
-  };
-#define FMCA_KRON(D, P)                                                                       \
-  case D * 16 + P:                                                                            \
-    return go(far_kron_kernel<T, D, P, 1>, far_kron_kernel<T, D, P, 8>,                       \
-              far_kron_kernel<T, D, P, 32>, D == 2 ? P * P : P * P * P, D, P);
-  switch (S.ip.dim * 16 + S.ip.p1) {
-    FMCA_KRON(2, 3)
-    FMCA_KRON(2, 4)
-    FMCA_KRON(2, 5)
-    FMCA_KRON(2, 6)
-    FMCA_KRON(2, 7)
-    FMCA_KRON(2, 8)
-    FMCA_KRON(3, 3)
-    FMCA_KRON(3, 4)
-    FMCA_KRON(3, 5)
-    FMCA_KRON(3, 6)
-    default:
-      return false;
-  }
-#undef FMCA_KRON
+  *err = launch_far_kron_kernel<T>(S.ip.dim, S.ip.p1, dp->far.groups, dp->far.ngroups,
+                                   dp->far.ivl, S.nodes_r, S.nodes_c, dp->midx, e, t, s, ld,
+                                   rofs, rcount, st);
+  return true;
 }
 
 // total degree: coefficients of clusters 0 .. ncl - 1 to (M = invV^T) or
