@@ -71,34 +71,47 @@ __device__ __forceinline__ float kgrad<float>(int type, float r2, const KParams<
 // Near-field gradient: G[t] += scale * sum_s c_ts g(|p_t - q_s|) (p_t - q_s)
 // (accumulated pair by pair from the differences),
 // c_ts = sum_r tval[t][r] * colscale[r] * sval[s][r] over the RHS chunk.
+// SYM (one point cloud, where every dense pair (t, s) is also one (s, t)):
+// c_ts also takes sum_r tval2[t][r] * colscale[r] * sval2[s][r], so that the
+// two sides of the adjoint (y_t x_s and x_t y_s) share one evaluation of g.
 // One thread per target; sources stream through shared memory like ksum.
-template <typename T, int RB, int TS, int STAGES>
+template <typename T, int RB, int TS, int STAGES, bool SYM = false>
 __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
                                  const uint32_t* __restrict__ ivl,
                                  const Pt4<T>* __restrict__ tgt, const Pt4<T>* __restrict__ src,
                                  const T* __restrict__ tval, const T* __restrict__ sval, int ld,
                                  const double* __restrict__ colscale, int rcount,
                                  KParams<T> kp, double scale, double* __restrict__ G,
-                                 int* err) {
+                                 int* err, const T* __restrict__ tval2 = nullptr,
+                                 const T* __restrict__ sval2 = nullptr) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
   int* scnt = reinterpret_cast<int*>(smem_raw + 8 * STAGES);
   Pt4<T>* spts = reinterpret_cast<Pt4<T>*>(smem_raw + 128);
   T* svals = reinterpret_cast<T*>(smem_raw + 128 + STAGES * TS * sizeof(Pt4<T>));
+  T* svals2 = svals + (size_t)STAGES * TS * ld;  // SYM only
 
   const KGroup g = groups[blockIdx.x];
   const int tid = threadIdx.x;
   const bool active = (uint32_t)tid < g.tcount;
   Pt4<T> p{T(0), T(0), T(0), T(0)};
-  T yv[RB];
+  T yv[RB], xv[SYM ? RB : 1];
 #pragma unroll
   for (int r = 0; r < RB; ++r) yv[r] = T(0);
+#pragma unroll
+  for (int r = 0; r < (SYM ? RB : 1); ++r) xv[r] = T(0);
   if (active) {
     p = tgt[g.tbegin + tid];
     const T* tv = tval + (size_t)(g.tbegin + tid) * ld;
 #pragma unroll
     for (int r = 0; r < RB; ++r)
       if (r < rcount) yv[r] = (T)((double)tv[r] * colscale[r]);
+    if constexpr (SYM) {
+      const T* tv2 = tval2 + (size_t)(g.tbegin + tid) * ld;
+#pragma unroll
+      for (int r = 0; r < RB; ++r)
+        if (r < rcount) xv[r] = (T)((double)tv2[r] * colscale[r]);
+    }
   }
   T ax = T(0), ay = T(0), az = T(0);
 
@@ -120,9 +133,11 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
     scnt[stage] = (int)cnt;
     const uint32_t bp = cnt * (uint32_t)sizeof(Pt4<T>);
     const uint32_t bv = cnt * (uint32_t)ld * (uint32_t)sizeof(T);
-    mbar_expect_tx(&bars[stage], bp + bv);
+    mbar_expect_tx(&bars[stage], bp + (SYM ? 2u : 1u) * bv);
     bulk_g2s(spts + stage * TS, src + s0, bp, &bars[stage]);
     bulk_g2s(svals + (size_t)stage * TS * ld, sval + (size_t)s0 * ld, bv, &bars[stage]);
+    if constexpr (SYM)
+      bulk_g2s(svals2 + (size_t)stage * TS * ld, sval2 + (size_t)s0 * ld, bv, &bars[stage]);
     poff += cnt;
     if (b + poff >= e) {
       ++pi;
@@ -140,12 +155,18 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
       const int cnt = scnt[stage];
       const Pt4<T>* P = spts + stage * TS;
       const T* V = svals + (size_t)stage * TS * ld;
+      const T* V2 = svals2 + (size_t)stage * TS * ld;
       for (int j = 0; j < cnt; ++j) {
         const Pt4<T> s = P[j];
         const T* v = V + (size_t)j * ld;
         T c = T(0);
 #pragma unroll
         for (int r = 0; r < RB; ++r) c += yv[r] * v[r];
+        if constexpr (SYM) {
+          const T* v2 = V2 + (size_t)j * ld;
+#pragma unroll
+          for (int r = 0; r < RB; ++r) c += xv[r] * v2[r];
+        }
         const T dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
         const T w = c * kgrad<T>(kp.type, dx * dx + dy * dy + dz * dz, kp);
         // accumulate w (p - q) directly: p sum(w) - sum(w q) cancels badly

@@ -2029,19 +2029,31 @@ __global__ void set_scalar_kernel(double* out, int idx, double v) {
   if (threadIdx.x == 0 && blockIdx.x == 0) out[idx] = v;
 }
 
+// tval2 / sval2 given: the symmetric form (both sides of the adjoint from one
+// evaluation per pair; one point cloud)
 template <typename T, int RB>
 cudaError_t launch_near_grad(const GroupList& gl, const Pt4<T>* tgt, const Pt4<T>* src,
                              const T* tval, const T* sval, int ld, const double* cs,
                              int rcount, const KParams<T>& kp, double scale, double* G,
-                             int* errf, cudaStream_t st) {
+                             int* errf, cudaStream_t st, const T* tval2 = nullptr,
+                             const T* sval2 = nullptr) {
   if (gl.ngroups == 0) return cudaSuccess;
   constexpr int TS = TileSize<T>::value;
-  auto kern = near_grad_kernel<T, RB, TS, kStages>;
-  const size_t smem = 128 + (size_t)kStages * TS * (sizeof(Pt4<T>) + (size_t)ld * sizeof(T));
-  ensure_smem(kern, smem);
+  const bool sym = tval2 && sval2;
+  const size_t smem =
+      128 + (size_t)kStages * TS * (sizeof(Pt4<T>) + (sym ? 2 : 1) * (size_t)ld * sizeof(T));
   const int threads = std::max(32, (gl.maxcount + 31) / 32 * 32);
-  kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
-                                          rcount, kp, scale, G, errf);
+  if (sym) {
+    auto kern = near_grad_kernel<T, RB, TS, kStages, true>;
+    ensure_smem(kern, smem);
+    kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
+                                            rcount, kp, scale, G, errf, tval2, sval2);
+  } else {
+    auto kern = near_grad_kernel<T, RB, TS, kStages, false>;
+    ensure_smem(kern, smem);
+    kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
+                                            rcount, kp, scale, G, errf, nullptr, nullptr);
+  }
   return cudaGetLastError();
 }
 
@@ -2079,33 +2091,30 @@ int grad_terms(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     cudaError_t e = cudaSuccess;
     switch (rb) {
       case 1:
+        // one point cloud (the adjoint refuses point gradients otherwise):
+        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 1>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                   scale, G, dp->err_flag, st);
-        if (e == cudaSuccess)
-          e = launch_near_grad<T, 1>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
-                                     scale, G, dp->err_flag, st);
+                                   scale, G, dp->err_flag, st, xa, yb);
         if (e == cudaSuccess)
           e = launch_far_grad<T, 1>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
         if (e == cudaSuccess)
           e = launch_far_grad<T, 1>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
         break;
       case 8:
+        // one point cloud (the adjoint refuses point gradients otherwise):
+        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 8>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                   scale, G, dp->err_flag, st);
-        if (e == cudaSuccess)
-          e = launch_near_grad<T, 8>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
-                                     scale, G, dp->err_flag, st);
+                                   scale, G, dp->err_flag, st, xa, yb);
         if (e == cudaSuccess)
           e = launch_far_grad<T, 8>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
         if (e == cudaSuccess)
           e = launch_far_grad<T, 8>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
         break;
       default:
+        // one point cloud (the adjoint refuses point gradients otherwise):
+        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 32>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                    scale, G, dp->err_flag, st);
-        if (e == cudaSuccess)
-          e = launch_near_grad<T, 32>(dp->near, S.pts_c, S.pts_r, xa, yb, ld, csc, rcount, kp,
-                                      scale, G, dp->err_flag, st);
+                                   scale, G, dp->err_flag, st, xa, yb);
         if (e == cudaSuccess)
           e = launch_far_grad<T, 32>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
         if (e == cudaSuccess)
