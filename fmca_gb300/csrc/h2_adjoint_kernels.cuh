@@ -74,6 +74,9 @@ __device__ __forceinline__ float kgrad<float>(int type, float r2, const KParams<
 // SYM (one point cloud, where every dense pair (t, s) is also one (s, t)):
 // c_ts also takes sum_r tval2[t][r] * colscale[r] * sval2[s][r], so that the
 // two sides of the adjoint (y_t x_s and x_t y_s) share one evaluation of g.
+// The values of a side start at a column offset of its rows (ofs: tval,
+// sval, tval2, sval2), so both sides may live in one buffer; sval2 ==
+// sval then stages the source rows once.
 // One thread per target; sources stream through shared memory like ksum.
 template <typename T, int RB, int TS, int STAGES, bool SYM = false>
 __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
@@ -83,13 +86,15 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
                                  const double* __restrict__ colscale, int rcount,
                                  KParams<T> kp, double scale, double* __restrict__ G,
                                  int* err, const T* __restrict__ tval2 = nullptr,
-                                 const T* __restrict__ sval2 = nullptr) {
+                                 const T* __restrict__ sval2 = nullptr, int4 ofs = {0, 0, 0, 0}) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
   int* scnt = reinterpret_cast<int*>(smem_raw + 8 * STAGES);
   Pt4<T>* spts = reinterpret_cast<Pt4<T>*>(smem_raw + 128);
   T* svals = reinterpret_cast<T*>(smem_raw + 128 + STAGES * TS * sizeof(Pt4<T>));
-  T* svals2 = svals + (size_t)STAGES * TS * ld;  // SYM only
+  // SYM with a second source buffer: its tiles after the first one's
+  const bool two = SYM && sval2 != sval;
+  T* svals2 = two ? svals + (size_t)STAGES * TS * ld : svals;
 
   const KGroup g = groups[blockIdx.x];
   const int tid = threadIdx.x;
@@ -102,12 +107,12 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
   for (int r = 0; r < (SYM ? RB : 1); ++r) xv[r] = T(0);
   if (active) {
     p = tgt[g.tbegin + tid];
-    const T* tv = tval + (size_t)(g.tbegin + tid) * ld;
+    const T* tv = tval + (size_t)(g.tbegin + tid) * ld + ofs.x;
 #pragma unroll
     for (int r = 0; r < RB; ++r)
       if (r < rcount) yv[r] = (T)((double)tv[r] * colscale[r]);
     if constexpr (SYM) {
-      const T* tv2 = tval2 + (size_t)(g.tbegin + tid) * ld;
+      const T* tv2 = tval2 + (size_t)(g.tbegin + tid) * ld + ofs.z;
 #pragma unroll
       for (int r = 0; r < RB; ++r)
         if (r < rcount) xv[r] = (T)((double)tv2[r] * colscale[r]);
@@ -133,10 +138,10 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
     scnt[stage] = (int)cnt;
     const uint32_t bp = cnt * (uint32_t)sizeof(Pt4<T>);
     const uint32_t bv = cnt * (uint32_t)ld * (uint32_t)sizeof(T);
-    mbar_expect_tx(&bars[stage], bp + (SYM ? 2u : 1u) * bv);
+    mbar_expect_tx(&bars[stage], bp + (two ? 2u : 1u) * bv);
     bulk_g2s(spts + stage * TS, src + s0, bp, &bars[stage]);
     bulk_g2s(svals + (size_t)stage * TS * ld, sval + (size_t)s0 * ld, bv, &bars[stage]);
-    if constexpr (SYM)
+    if (two)
       bulk_g2s(svals2 + (size_t)stage * TS * ld, sval2 + (size_t)s0 * ld, bv, &bars[stage]);
     poff += cnt;
     if (b + poff >= e) {
@@ -158,14 +163,18 @@ __global__ void near_grad_kernel(const KGroup* __restrict__ groups,
       const T* V2 = svals2 + (size_t)stage * TS * ld;
       for (int j = 0; j < cnt; ++j) {
         const Pt4<T> s = P[j];
-        const T* v = V + (size_t)j * ld;
+        // only the rcount columns from the offset are read: with a column
+        // offset, columns past them may lie beyond the row (and the stage)
+        const T* v = V + (size_t)j * ld + ofs.y;
         T c = T(0);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) c += yv[r] * v[r];
+        for (int r = 0; r < RB; ++r)
+          if (r < rcount) c += yv[r] * v[r];
         if constexpr (SYM) {
-          const T* v2 = V2 + (size_t)j * ld;
+          const T* v2 = V2 + (size_t)j * ld + ofs.w;
 #pragma unroll
-          for (int r = 0; r < RB; ++r) c += xv[r] * v2[r];
+          for (int r = 0; r < RB; ++r)
+            if (r < rcount) c += xv[r] * v2[r];
         }
         const T dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
         const T w = c * kgrad<T>(kp.type, dx * dx + dy * dy + dz * dz, kp);
@@ -246,13 +255,21 @@ __global__ void far_grad_kernel(const int32_t* __restrict__ leaves,
                                 const T* __restrict__ tval, int ld,
                                 const double* __restrict__ colscale, int rcount,
                                 const int* __restrict__ midx_g, InterpDev<T> ip,
-                                double scale, double* __restrict__ G) {
+                                double scale, double* __restrict__ G,
+                                const T* __restrict__ U2 = nullptr,
+                                const T* __restrict__ tval2 = nullptr,
+                                int4 ofs = {0, 0, 0, 0}) {
+  // U2 / tval2 given: the second side of the adjoint (its expansions U2 and
+  // point values tval2) with the same basis derivatives; ofs: column
+  // offsets of U, tval, U2, tval2 in their rows
   constexpr int KC = 64;
+  const bool sym = U2 != nullptr;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* F = reinterpret_cast<T*>(smem_raw);  // blockDim x 24
   T* D = F + blockDim.x * 24;             // blockDim x 24
   T* S = D + blockDim.x * 24;             // KC x RB
-  int* midx = reinterpret_cast<int*>(S + KC * RB);
+  T* S2 = S + KC * RB;                    // KC x RB (sym)
+  int* midx = reinterpret_cast<int*>(S2 + (sym ? KC * RB : 0));
   const int c = leaves[blockIdx.x];
   const uint32_t b = cbegin[c], n = csize[c];
   const int q = ip.q, tid = threadIdx.x;
@@ -266,9 +283,9 @@ __global__ void far_grad_kernel(const int32_t* __restrict__ leaves,
   T* df = D + tid * 24;
   for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
     const bool valid = i0 + tid < n;
-    T yv[RB];
+    T yv[RB], xv[RB];
 #pragma unroll
-    for (int r = 0; r < RB; ++r) yv[r] = T(0);
+    for (int r = 0; r < RB; ++r) yv[r] = xv[r] = T(0);
     if (valid) {
       const Pt4<T> p = pts[b + i0 + tid];
       const T pc[3] = {p.x, p.y, p.z};
@@ -280,10 +297,16 @@ __global__ void far_grad_kernel(const int32_t* __restrict__ leaves,
           df[d * 8] = T(0);
         }
       }
-      const T* tv = tval + (size_t)(b + i0 + tid) * ld;
+      const T* tv = tval + (size_t)(b + i0 + tid) * ld + ofs.y;
 #pragma unroll
       for (int r = 0; r < RB; ++r)
         if (r < rcount) yv[r] = (T)((double)tv[r] * colscale[r]);
+      if (sym) {
+        const T* tv2 = tval2 + (size_t)(b + i0 + tid) * ld + ofs.w;
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+          if (r < rcount) xv[r] = (T)((double)tv2[r] * colscale[r]);
+      }
     }
     T gx = T(0), gy = T(0), gz = T(0);
     for (int k0 = 0; k0 < q; k0 += KC) {
@@ -291,7 +314,9 @@ __global__ void far_grad_kernel(const int32_t* __restrict__ leaves,
       __syncthreads();
       for (int e = tid; e < cnt * RB; e += blockDim.x) {
         const int k = e / RB, r = e % RB;
-        S[e] = (r < rcount) ? U[((size_t)c * q + k0 + k) * ld + r] : T(0);
+        const size_t row = ((size_t)c * q + k0 + k) * ld;
+        S[e] = (r < rcount) ? U[row + ofs.x + r] : T(0);
+        if (sym) S2[e] = (r < rcount) ? U2[row + ofs.z + r] : T(0);
       }
       __syncthreads();
       if (valid) {
@@ -299,6 +324,10 @@ __global__ void far_grad_kernel(const int32_t* __restrict__ leaves,
           T h = T(0);
 #pragma unroll
           for (int r = 0; r < RB; ++r) h += S[k * RB + r] * yv[r];
+          if (sym) {
+#pragma unroll
+            for (int r = 0; r < RB; ++r) h += S2[k * RB + r] * xv[r];
+          }
           const int kk = k0 + k;
           const int m0 = midx[kk * 3], m1 = midx[kk * 3 + 1], m2 = midx[kk * 3 + 2];
           const T f0 = f[m0], f1 = f[8 + m1], f2 = f[16 + m2];
@@ -401,6 +430,21 @@ __global__ void scale_copy_kernel(int64_t n, int R, const T* __restrict__ x, dou
     const int64_t i = e % n;
     const int r = (int)(e / n);
     y[i * syi + (int64_t)r * syr] = (T)(a * (double)x[e]);
+  }
+}
+
+// out (n x 2R, column-major, leading dimension n) = [x | y] from two
+// strided n x R inputs
+template <typename T>
+__global__ void pack_pair_kernel(int64_t n, int R, const T* __restrict__ x, int64_t sxi,
+                                 int64_t sxr, const T* __restrict__ y, int64_t syi, int64_t syr,
+                                 T* __restrict__ out) {
+  const int64_t total = n * (int64_t)R * 2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % n;
+    const int c = (int)(e / n);
+    out[e] = c < R ? x[i * sxi + (int64_t)c * sxr] : y[i * syi + (int64_t)(c - R) * syr];
   }
 }
 

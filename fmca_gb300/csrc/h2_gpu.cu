@@ -1017,6 +1017,7 @@ struct MatvecState {
   const unsigned int* cmax = nullptr;  // column maxima of the scaled path, or null
   int ld = 0, rb = 0, nch = 0;
   bool fp64 = false;
+  int cofs = 0;  // first column of this product's right-hand sides in the buffers
 };
 
 template <typename T>
@@ -2031,44 +2032,49 @@ __global__ void set_scalar_kernel(double* out, int idx, double v) {
 
 // tval2 / sval2 given: the symmetric form (both sides of the adjoint from one
 // evaluation per pair; one point cloud)
+// ofs: column offsets of tval, sval, tval2, sval2 in their rows
 template <typename T, int RB>
 cudaError_t launch_near_grad(const GroupList& gl, const Pt4<T>* tgt, const Pt4<T>* src,
                              const T* tval, const T* sval, int ld, const double* cs,
                              int rcount, const KParams<T>& kp, double scale, double* G,
                              int* errf, cudaStream_t st, const T* tval2 = nullptr,
-                             const T* sval2 = nullptr) {
+                             const T* sval2 = nullptr, int4 ofs = {0, 0, 0, 0}) {
   if (gl.ngroups == 0) return cudaSuccess;
   constexpr int TS = TileSize<T>::value;
   const bool sym = tval2 && sval2;
+  const bool two = sym && sval2 != sval;
   const size_t smem =
-      128 + (size_t)kStages * TS * (sizeof(Pt4<T>) + (sym ? 2 : 1) * (size_t)ld * sizeof(T));
+      128 + (size_t)kStages * TS * (sizeof(Pt4<T>) + (two ? 2 : 1) * (size_t)ld * sizeof(T));
   const int threads = std::max(32, (gl.maxcount + 31) / 32 * 32);
   if (sym) {
     auto kern = near_grad_kernel<T, RB, TS, kStages, true>;
     ensure_smem(kern, smem);
     kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
-                                            rcount, kp, scale, G, errf, tval2, sval2);
+                                            rcount, kp, scale, G, errf, tval2, sval2, ofs);
   } else {
     auto kern = near_grad_kernel<T, RB, TS, kStages, false>;
     ensure_smem(kern, smem);
     kern<<<gl.ngroups, threads, smem, st>>>(gl.groups, gl.ivl, tgt, src, tval, sval, ld, cs,
-                                            rcount, kp, scale, G, errf, nullptr, nullptr);
+                                            rcount, kp, scale, G, errf, nullptr, nullptr, ofs);
   }
   return cudaGetLastError();
 }
 
+// U2 / tval2 given: both sides of the adjoint in one pass; ofs: column
+// offsets of U, tval, U2, tval2 in their rows
 template <typename T, int RB>
 cudaError_t launch_far_grad(const Plan& plan, DevPlan* dp, DevSet<T>& S, const T* U,
                             const T* tval, int ld, const double* cs, int rcount,
-                            double scale, double* G, cudaStream_t st) {
+                            double scale, double* G, cudaStream_t st, const T* U2 = nullptr,
+                            const T* tval2 = nullptr, int4 ofs = {0, 0, 0, 0}) {
   if (!dp->nleaves_r) return cudaSuccess;
   auto kern = far_grad_kernel<T, RB>;
-  const size_t smem =
-      (128 * 48 + 64 * RB) * sizeof(T) + (size_t)plan.interp.q * 3 * sizeof(int);
+  const size_t smem = (128 * 48 + (U2 ? 2 : 1) * 64 * RB) * sizeof(T) +
+                      (size_t)plan.interp.q * 3 * sizeof(int);
   ensure_smem(kern, smem);
   kern<<<dp->nleaves_r, 128, smem, st>>>(dp->leaves_r, dp->cbegin_r, dp->csize_r, S.bbmin_r,
                                          S.bbext_r, S.pts_r, U, tval, ld, cs, rcount,
-                                         dp->midx, S.ip, scale, G);
+                                         dp->midx, S.ip, scale, G, U2, tval2, ofs);
   return cudaGetLastError();
 }
 
@@ -2081,6 +2087,9 @@ int grad_terms(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
   const int64_t nr = plan.rows.n, nc = plan.cols.n;
   const size_t Cr = plan.rows.nclusters();
   const int ld = A.ld, rb = A.rb;
+  // the two sides (x: A, y: B) may share buffers at different column offsets
+  const int4 nofs = {B.cofs, A.cofs, A.cofs, B.cofs};  // near: y_t, x_s, x_t, y_s
+  const int4 fofs = {A.cofs, B.cofs, B.cofs, A.cofs};  // far: U_x, y_t, U_y, x_t
   for (int ch = 0; ch < A.nch; ++ch) {
     const int rcount = std::min(rb, nrhs - ch * rb);
     const T* xa = static_cast<const T*>(A.xc) + (size_t)ch * nc * ld;
@@ -2088,37 +2097,31 @@ int grad_terms(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
     const T* ua = static_cast<const T*>(A.s) + (size_t)ch * Cr * q * ld;
     const T* ub = static_cast<const T*>(B.s) + (size_t)ch * Cr * q * ld;
     const double* csc = cs + ch * rb;
+    // one point cloud (the adjoint refuses point gradients otherwise): both
+    // sides, y_t x_s and x_t y_s, in one pass over the dense pairs and one
+    // over the row leaves
     cudaError_t e = cudaSuccess;
     switch (rb) {
       case 1:
-        // one point cloud (the adjoint refuses point gradients otherwise):
-        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 1>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                   scale, G, dp->err_flag, st, xa, yb);
+                                   scale, G, dp->err_flag, st, xa, yb, nofs);
         if (e == cudaSuccess)
-          e = launch_far_grad<T, 1>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
-        if (e == cudaSuccess)
-          e = launch_far_grad<T, 1>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+          e = launch_far_grad<T, 1>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st, ub, xa,
+                                    fofs);
         break;
       case 8:
-        // one point cloud (the adjoint refuses point gradients otherwise):
-        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 8>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                   scale, G, dp->err_flag, st, xa, yb);
+                                   scale, G, dp->err_flag, st, xa, yb, nofs);
         if (e == cudaSuccess)
-          e = launch_far_grad<T, 8>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
-        if (e == cudaSuccess)
-          e = launch_far_grad<T, 8>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+          e = launch_far_grad<T, 8>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st, ub, xa,
+                                    fofs);
         break;
       default:
-        // one point cloud (the adjoint refuses point gradients otherwise):
-        // both sides, y_t x_s and x_t y_s, in one pass over the dense pairs
         e = launch_near_grad<T, 32>(dp->near, S.pts_r, S.pts_c, yb, xa, ld, csc, rcount, kp,
-                                   scale, G, dp->err_flag, st, xa, yb);
+                                    scale, G, dp->err_flag, st, xa, yb, nofs);
         if (e == cudaSuccess)
-          e = launch_far_grad<T, 32>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st);
-        if (e == cudaSuccess)
-          e = launch_far_grad<T, 32>(plan, dp, S, ub, xa, ld, csc, rcount, scale, G, st);
+          e = launch_far_grad<T, 32>(plan, dp, S, ua, yb, ld, csc, rcount, scale, G, st, ub,
+                                     xa, fofs);
         break;
     }
     FMCA_CK(e);
@@ -2129,13 +2132,21 @@ int grad_terms(const Plan& plan, DevPlan* dp, DevSet<T>& S, const KernelDesc& k,
 struct AdjointWorkspace {
   void *wsA, *wsB;
   size_t mv;
-  void* z;  // dtype of the inputs
+  void* z;   // dtype of the inputs, n x 2 nrhs
+  void* xy;  // [x | y] for the joint product K [x | y] (n x 2 nrhs), dtype
   double *G, *partial, *colscale, *scal;
 };
 
+// K x and K y run as one product of 2 nrhs columns when those fit one
+// 32-column chunk (every kernel value then serves both)
+bool adjoint_joint(int nrhs) { return 2 * nrhs <= 32; }
+
 size_t adjoint_layout(const Plan& plan, int precision, int nrhs, void* base,
                       AdjointWorkspace* w) {
-  const size_t mv = align_up(workspace_bytes(plan, precision, nrhs));
+  size_t mvb = workspace_bytes(plan, precision, nrhs);
+  if (adjoint_joint(nrhs)) mvb = std::max(mvb, workspace_bytes(plan, precision, 2 * nrhs));
+  const size_t mv = align_up(mvb);
+  const size_t n = std::max<size_t>(plan.rows.n, plan.cols.n);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     void* p = base ? static_cast<char*>(base) + off : nullptr;
@@ -2146,7 +2157,8 @@ size_t adjoint_layout(const Plan& plan, int precision, int nrhs, void* base,
   t.mv = mv;
   t.wsA = take(mv);
   t.wsB = take(mv);
-  t.z = take(sizeof(double) * std::max<size_t>(plan.rows.n, plan.cols.n) * nrhs);
+  t.z = take(sizeof(double) * n * 2 * nrhs);
+  t.xy = adjoint_joint(nrhs) ? take(sizeof(double) * n * 2 * nrhs) : nullptr;
   t.G = (double*)take(sizeof(double) * 4 * std::max<size_t>(plan.rows.n, plan.cols.n));
   t.partial = (double*)take(sizeof(double) * kDotBlocks);
   t.colscale = (double*)take(sizeof(double) * nrhs);
@@ -2192,9 +2204,30 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)dp->sms * 32));
   };
   MatvecState A, B;
-  // z = K x with unit variance; f = sigma2 * y . z, df/dsigma2 = y . z
-  FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, nrhs, x, sxi, sxr, w.z, w.wsA, w.mv,
-                        st, err, &A));
+  // with point gradients or K y on one point cloud and few right-hand
+  // sides, K x and K y come from one product of [x | y]: its first nrhs
+  // columns are the x side (state A), the others the y side (state B)
+  const bool joint = (dX || Ky) && plan.same_tree && adjoint_joint(nrhs);
+  if (joint) {
+    if (dtype == FMCA_DTYPE_F64)
+      pack_pair_kernel<double><<<blocks(nr * 2 * nrhs), nthr, 0, st>>>(
+          nr, nrhs, static_cast<const double*>(x), sxi, sxr, static_cast<const double*>(y), syi,
+          syr, static_cast<double*>(w.xy));
+    else
+      pack_pair_kernel<float><<<blocks(nr * 2 * nrhs), nthr, 0, st>>>(
+          nr, nrhs, static_cast<const float*>(x), sxi, sxr, static_cast<const float*>(y), syi,
+          syr, static_cast<float*>(w.xy));
+    FMCA_CK(cudaGetLastError());
+    FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, 2 * nrhs, w.xy, 1, nr, w.z, w.wsA,
+                          w.mv, st, err, &A));
+    B = A;
+    B.cofs = nrhs;
+  } else {
+    // z = K x with unit variance
+    FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, nrhs, x, sxi, sxr, w.z, w.wsA, w.mv,
+                          st, err, &A));
+  }
+  // f = sigma2 * y . K x, df/dsigma2 = y . K x
   FMCA_CK(launch_dot(dtype, nr, nrhs, y, syi, syr, w.z, w.partial, 1.0, w.scal, 0, st));
   if (values) {
     scalar_axpy_kernel<<<1, 32, 0, st>>>(w.scal, 0, k.sigma2, values, 0);
@@ -2210,6 +2243,18 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
           nr, nrhs, static_cast<const float*>(w.z), k.sigma2, static_cast<float*>(Kx), syi,
           syr);
   }
+  // K y of the joint product, before z is reused below
+  if (joint && Ky) {
+    const size_t zofs = (size_t)nr * nrhs * (dtype == FMCA_DTYPE_F64 ? 8 : 4);
+    const void* zy = static_cast<const char*>(w.z) + zofs;
+    if (dtype == FMCA_DTYPE_F64)
+      scale_copy_kernel<double><<<blocks(nc * nrhs), nthr, 0, st>>>(
+          nc, nrhs, static_cast<const double*>(zy), k.sigma2, static_cast<double*>(Ky), sxi,
+          sxr);
+    else
+      scale_copy_kernel<float><<<blocks(nc * nrhs), nthr, 0, st>>>(
+          nc, nrhs, static_cast<const float*>(zy), k.sigma2, static_cast<float*>(Ky), sxi, sxr);
+  }
   // df/dl = sigma2 * y . H2[dk/dl] x
   if (values) {
     if (base_kernel) {
@@ -2223,7 +2268,7 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
       set_scalar_kernel<<<1, 32, 0, st>>>(values, 1, std::nan(""));
     }
   }
-  if (dX || Ky) {
+  if ((dX || Ky) && !joint) {
     // the y-side product (K is symmetric for one point cloud)
     FMCA_TRY(matvec_state(plan, dp, k1, precision, dtype, nrhs, y, syi, syr, w.z, w.wsB, w.mv,
                           st, err, &B));
@@ -2240,7 +2285,8 @@ int adjoint(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, i
   }
   if (dX) {
     FMCA_CK(cudaMemsetAsync(w.G, 0, sizeof(double) * 4 * nr, st));
-    colscale_kernel<<<1, 256, 0, st>>>(nrhs, A.cmax, B.cmax, w.colscale);
+    colscale_kernel<<<1, 256, 0, st>>>(nrhs, A.cmax ? A.cmax + A.cofs : nullptr,
+                                       B.cmax ? B.cmax + B.cofs : nullptr, w.colscale);
     if (A.fp64)
       FMCA_TRY(grad_terms<double>(plan, dp, dp->d, k1, A, B, nrhs, w.colscale, k.sigma2, w.G,
                                   st, err));
