@@ -73,6 +73,16 @@ def test_assembled_size_counts_the_blocks(p, leaf, n):
         assert H.assembled_bytes(prec) == expected_bytes(H, prec)
 
 
+def test_assembled_size_of_a_batched_plan():
+    # a forest of clouds: the groups of every cloud, in one store
+    rng = np.random.default_rng(12)
+    clouds = [uniform_cloud(int(n), 3, seed=i) for i, n in enumerate(rng.integers(300, 2500, 4))]
+    B = H2Matrix.batched(CovarianceKernel("MATERN32", 0.3), clouds, 3, 0.8)
+    singles = [H2Matrix(CovarianceKernel("MATERN32", 0.3), P, P, 3, 0.8) for P in clouds]
+    for prec in ("fp64", "fp32"):
+        assert B.assembled_bytes(prec) == sum(S.assembled_bytes(prec) for S in singles)
+
+
 def test_assembled_size_of_two_clouds():
     Pr = sphere_cloud(1500, seed=1)
     Pc = sphere_cloud(2200, seed=2)
