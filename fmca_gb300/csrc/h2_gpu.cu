@@ -1263,8 +1263,14 @@ struct TcChunk {
   TcWorkspace w;
   cudaStream_t st;
 
+  // The leaf passes accumulate only the chunk's rcount columns (1, 8 or 32
+  // per thread): every later reader of t and s (moment scaling, transfers,
+  // gradient terms) and of yfar (scatter) takes rcount columns too
   cudaError_t leafmom() {
-    cudaError_t e = launch_leafmom<float, kTcRhs>(dp, *S, xc, kTcRhs, 0, rcount, t, st);
+    cudaError_t e =
+        rcount <= 1   ? launch_leafmom<float, 1>(dp, *S, xc, kTcRhs, 0, rcount, t, st)
+        : rcount <= 8 ? launch_leafmom<float, 8>(dp, *S, xc, kTcRhs, 0, rcount, t, st)
+                      : launch_leafmom<float, kTcRhs>(dp, *S, xc, kTcRhs, 0, rcount, t, st);
     if (e != cudaSuccess) return e;
     dp->launches += dp->nleaves_c ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFMOM, st);
@@ -1336,7 +1342,10 @@ struct TcChunk {
     return cudaGetLastError();
   }
   cudaError_t leafgather() {
-    cudaError_t e = launch_leafgather<float, kTcRhs>(dp, *S, s, kTcRhs, 0, rcount, yfar, st);
+    cudaError_t e =
+        rcount <= 1   ? launch_leafgather<float, 1>(dp, *S, s, kTcRhs, 0, rcount, yfar, st)
+        : rcount <= 8 ? launch_leafgather<float, 8>(dp, *S, s, kTcRhs, 0, rcount, yfar, st)
+                      : launch_leafgather<float, kTcRhs>(dp, *S, s, kTcRhs, 0, rcount, yfar, st);
     if (e != cudaSuccess) return e;
     dp->launches += dp->nleaves_r ? 1 : 0;
     dp->mark(FMCA_STAGE_LEAFGATHER, st);
