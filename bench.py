@@ -271,6 +271,16 @@ def run_c3(args, torch, dev):
     for _ in range(args.warmup):
         g.launch()
     ms_graph = _events_ms(torch, g.launch, args.steps)
+    # stage times of the batched product (CUDA events between the stages of
+    # ordinary launches, averaged over the timed steps)
+    B.set_profiling(True)
+    stage_tot = None
+    for _ in range(args.steps):
+        B.matvec(X, Y)
+        st, _ = B.profile()
+        stage_tot = st if stage_tot is None else {k: stage_tot[k] + st[k] for k in st}
+    B.set_profiling(False)
+    stage_ms = {k: v / args.steps for k, v in stage_tot.items()}
     singles = [H2Matrix(cov, P, P, 3, 0.8, precision="mixed") for P in clouds]
     xs = [X[B.offsets[i]:B.offsets[i + 1]] for i in range(64)]
     ys = [torch.empty_like(x) for x in xs]
@@ -301,6 +311,7 @@ def run_c3(args, torch, dev):
         "per_instance": {"value": N * R / (ms_each * 1e-3), "ms_per_step": ms_each,
                          "launch": "64 plans, one matvec each, back to back"},
         "speedup_graph_vs_per_instance": ms_each / ms_graph,
+        "stage_ms": stage_ms,
         "max_rel_diff_batched_vs_single": err,
         "max_rel_err_vs_fp64_oracle": {"value": err_or, "clouds": [int(clouds[i].shape[1])
                                                                   for i in small]},

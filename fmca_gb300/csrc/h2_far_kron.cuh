@@ -33,8 +33,8 @@ template <typename T, int DIM, int P, int RW>
 __global__ void __launch_bounds__(256)
     far_kron_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                     const Pt4<T>* __restrict__ nodes_r, const Pt4<T>* __restrict__ nodes_c,
-                    const int* __restrict__ midx_g, T e, const T* __restrict__ t,
-                    T* __restrict__ s, int ldv, int rofs, int rcount) {
+                    const int* __restrict__ midx_g, T e, const T* __restrict__ t, int ldt,
+                    int tofs, T* __restrict__ s, int lds, int sofs, int rcount) {
   constexpr int Q = DIM == 1 ? P : DIM == 2 ? P * P : P * P * P;
   constexpr int NC = Q / P;
   constexpr int SL = 32 / RW;          // source clusters per step
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int slot = lane / RW, col = lane % RW;
   const bool live = col < rcount;
-  const int r = rofs + col;
+  const int r = tofs + col;
   for (int k = threadIdx.x; k < Q; k += blockDim.x) {
     int pos = 0;
 #pragma unroll
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int q = t0 + nw * u;
-        v[u] = (q < Q && live && sc >= 0) ? t[((size_t)sc * Q + sidx[q]) * ldv + r] : T(0);
+        v[u] = (q < Q && live && sc >= 0) ? t[((size_t)sc * Q + sidx[q]) * ldt + r] : T(0);
       }
 #pragma unroll
       for (int u = 0; u < U; ++u)
@@ -154,10 +154,183 @@ __global__ void __launch_bounds__(256)
       T sum = T(0);
 #pragma unroll
       for (int j = 0; j < SL; ++j) sum += Z[q * 32 + j * RW + c];
-      s[((size_t)g.tbegin + sidx[q]) * ldv + rofs + c] = sum;
+      s[((size_t)g.tbegin + sidx[q]) * lds + sofs + c] = sum;
+    }
+  }
+}
+
+// The same far field in FP32 for grids of Q <= 64 nodes: one warp per far
+// group, no barrier but __syncwarp.  Each lane holds one right-hand side
+// (r = lane % RW) of one source cluster (slot lane / RW, SL = 32 / RW
+// clusters per step) as Q registers: every index of the contractions is a
+// compile-time constant once the loops are unrolled, so the DIM
+// contractions run in place on the registers, fibre by fibre, and the last
+// one is added into the lane's column of the accumulator Z in shared
+// memory.  Lanes of unused columns load a used one (their sums are never
+// read); slots past the group's last source cluster load its first one and
+// get zero factors.  At the end the slots' columns of Z are added.
+// Every source cluster's coefficients are read once per admissible block
+// (about 50 times): the columns should fill the rows of t (ldt = the
+// columns in use), so that t stays in L2 for the re-reads.
+// shared: sidx, soff [Q4] ints, sb [DP4] ints, xt [DP4], Z [Q][32],
+// xs [SL][DP], ef [SL][NFS] floats, scls [SL] ints
+template <int DIM, int P>
+struct KronShape {
+  static constexpr int Q = DIM == 2 ? P * P : P * P * P;
+  static constexpr int DP = DIM * P;      // 1-D nodes of all dimensions
+  static constexpr int NF = DIM * P * P;  // factor entries per source cluster
+  static constexpr int NFS = NF | 1;      // odd slot stride: slots on distinct banks
+  static constexpr int Q4 = (Q + 3) / 4 * 4;
+  static constexpr int DP4 = (DP + 3) / 4 * 4;
+  // shared-memory bytes for RW columns per slot
+  static constexpr size_t smem_bytes(int rw) {
+    return sizeof(int) * (2 * Q4 + DP4) +
+           sizeof(float) * (DP4 + Q * 32 + (32 / rw) * (DP + NFS)) + sizeof(int) * (32 / rw);
+  }
+  // stride of digit d in tensor order (digit 0 most significant)
+  static constexpr int stride(int d) { return d == DIM - 1 ? 1 : (d == DIM - 2 ? P : P * P); }
+};
+
+template <int DIM, int P, int RW>
+__global__ void __launch_bounds__(32)
+    far_kron_reg_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
+                        const Pt4<float>* __restrict__ nodes_r,
+                        const Pt4<float>* __restrict__ nodes_c, const int* __restrict__ midx_g,
+                        float e, const float* __restrict__ t, int ldt, int tofs,
+                        float* __restrict__ s, int lds, int sofs, int rcount) {
+  using S = KronShape<DIM, P>;
+  constexpr int Q = S::Q, DP = S::DP, NF = S::NF, NFS = S::NFS;
+  constexpr int SL = 32 / RW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* sidx = reinterpret_cast<int*>(smem_raw);  // tensor position -> storage index
+  int* soff = sidx + S::Q4;                      // sidx * ldt
+  int* sb = soff + S::Q4;  // [DIM][P] storage index of the node with digit d = b, others 0
+  float* xt = reinterpret_cast<float*>(sb + S::DP4);  // [DIM][P] target node coordinates
+  float* Z = xt + S::DP4;                             // [Q][32]
+  float* xs = Z + Q * 32;                             // [SL][DIM][P] source node coordinates
+  float* ef = xs + SL * DP;                           // [SL][NFS] factors [d][a][b]
+  int* scls = reinterpret_cast<int*>(ef + SL * NFS);  // [SL] clusters of the step
+  const KGroup g = groups[blockIdx.x];
+  const int lane = threadIdx.x;
+  const int slot = lane / RW, col = lane % RW;
+  auto coord = [](const Pt4<float>& p, int d) { return d == 0 ? p.x : (d == 1 ? p.y : p.z); };
+  for (int k = lane; k < Q; k += 32) {
+    int pos = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) pos = pos * P + midx_g[k * 3 + d];
+    sidx[pos] = k;
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) Z[q * 32 + lane] = 0.f;
+  __syncwarp();
+  for (int q = lane; q < Q; q += 32) soff[q] = sidx[q] * ldt;
+  for (int i = lane; i < DP; i += 32) {
+    const int d = i / P, b = i - d * P;
+    const int k = sidx[b * S::stride(d)];
+    sb[i] = k;
+    xt[i] = coord(nodes_r[g.tbegin + k], d);
+  }
+  __syncwarp();
+  // the walk over the group's source clusters (uniform over the warp):
+  // interval iv, next cluster cur of it
+  int iv = g.ivl_begin;
+  uint32_t cur = 0, cend = 0;
+  if (iv < g.ivl_end) {
+    cur = ivl[2 * iv] / Q;
+    cend = ivl[2 * iv + 1] / Q;
+  }
+  auto next_cluster = [&]() -> int {
+    while (iv < g.ivl_end && cur >= cend) {
+      if (++iv < g.ivl_end) {
+        cur = ivl[2 * iv] / Q;
+        cend = ivl[2 * iv + 1] / Q;
+      }
+    }
+    return iv < g.ivl_end ? (int)cur++ : -1;
+  };
+  const int cc = tofs + (col < rcount ? col : rcount - 1);
+  while (true) {
+    int sc = -1, sc0 = -1;
+#pragma unroll
+    for (int j = 0; j < SL; ++j) {
+      const int c = next_cluster();
+      if (j == 0) sc0 = c;
+      if (j == slot) sc = c;
+    }
+    if (sc0 < 0) break;
+    // this lane's column of its source cluster's coefficients; the loads
+    // are issued before the factors are computed
+    float x[Q];
+    {
+      const float* tc = t + (size_t)(sc < 0 ? sc0 : sc) * Q * ldt + cc;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) x[q] = __ldg(tc + soff[q]);
+    }
+    __syncwarp();  // the previous step is done with scls, xs and ef
+    if (col == 0) scls[slot] = sc;
+    __syncwarp();
+    for (int i = lane; i < SL * DP; i += 32) {
+      const int j = i / DP, f = i - j * DP;
+      const int sj = scls[j];
+      xs[i] = coord(nodes_c[(size_t)(sj < 0 ? sc0 : sj) * Q + sb[f]], f / P);
+    }
+    __syncwarp();
+    // factor rows (slot j, dimension d, target node a), P entries each
+    for (int i = lane; i < SL * DP; i += 32) {
+      const int j = i / DP, f = i - j * DP, d = f / P;
+      const bool used = scls[j] >= 0;
+      const float xa = xt[f];
+      const float* xr = xs + j * DP + d * P;
+      float* er = ef + j * NFS + f * P;
+#pragma unroll
+      for (int b = 0; b < P; ++b) {
+        const float dv = xa - xr[b];
+        er[b] = used ? ex2_approx(dv * dv * e) : 0.f;
+      }
+    }
+    __syncwarp();
+    const float* efs = ef + slot * NFS;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      constexpr int NC = Q / P;
+      const int stride = S::stride(d);
+      float f[P][P];
+#pragma unroll
+      for (int a = 0; a < P; ++a)
+#pragma unroll
+        for (int b = 0; b < P; ++b) f[a][b] = efs[(d * P + a) * P + b];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const int base = (c / stride) * stride * P + c % stride;
+        float v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) v[j] = x[base + j * stride];
+#pragma unroll
+        for (int a = 0; a < P; ++a) {
+          const int o = base + a * stride;
+          float acc = d == DIM - 1 ? Z[o * 32 + lane] : 0.f;
+#pragma unroll
+          for (int j = 0; j < P; ++j) acc = fmaf(f[a][j], v[j], acc);
+          if (d == DIM - 1)
+            Z[o * 32 + lane] = acc;
+          else
+            x[o] = acc;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < Q * RW; i += 32) {
+    const int q = i / RW, c = i - q * RW;
+    if (c < rcount) {
+      float sum = 0.f;
+#pragma unroll
+      for (int j = 0; j < SL; ++j) sum += Z[q * 32 + j * RW + c];
+      s[((size_t)g.tbegin + sidx[q]) * lds + sofs + c] = sum;
     }
   }
 }
 
 }  // namespace gpu
 }  // namespace fmca
+

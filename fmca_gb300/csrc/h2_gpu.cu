@@ -833,12 +833,13 @@ bool far_kron_ok(const DevPlan* dp, const DevSet<T>& S, int type, int rcount) {
 }
 template <typename T>
 bool launch_far_kron(const DevPlan* dp, const DevSet<T>& S, const KParams<T>& kp, const T* t,
-                     T* s, int ld, int rofs, int rcount, cudaStream_t st, cudaError_t* err) {
+                     int ldt, int tofs, T* s, int lds, int sofs, int rcount, cudaStream_t st,
+                     cudaError_t* err) {
   if (!far_kron_ok(dp, S, kp.type, rcount)) return false;
   const T e = sizeof(T) == 4 ? kp.e2 : T(-0.5) / (kp.l * kp.l);
   *err = launch_far_kron_kernel<T>(S.ip.dim, S.ip.p1, dp->far.groups, dp->far.ngroups,
-                                   dp->far.ivl, S.nodes_r, S.nodes_c, dp->midx, e, t, s, ld,
-                                   rofs, rcount, st);
+                                   dp->far.ivl, S.nodes_r, S.nodes_c, dp->midx, e, t, ldt, tofs,
+                                   s, lds, sofs, rcount, st);
   return true;
 }
 
@@ -941,7 +942,7 @@ cudaError_t run_tree_stages(const Plan& plan, DevPlan* dp, DevSet<T>& S,
     e = launch_kstream<T>(RB, dp->far.groups, dp->far.ngroups, dp->far.maxcount, dp->far.ivl,
                           as->far_off, static_cast<const T*>(as->far), w.t, ld, w.s, rofs,
                           rcount, kp.wait_ns, kp.stall, dp->err_flag, st);
-  else if (!launch_far_kron<T>(dp, S, kp, w.t, w.s, ld, rofs, rcount, st, &e))
+  else if (!launch_far_kron<T>(dp, S, kp, w.t, ld, rofs, w.s, ld, rofs, rcount, st, &e))
     e = launch_ksum<T>(RB, dp->far, S.nodes_r, S.nodes_c, w.t, ld, w.s, rofs, rcount, kp, 0,
                        dp->err_flag, st);
   if (e != cudaSuccess) return e;
@@ -1298,7 +1299,21 @@ struct TcChunk {
     // the Gaussian's far field as Kronecker products (FP32 CUDA cores on the
     // unscaled moments), when the grid is one it is compiled for
     cudaError_t ek = cudaSuccess;
-    if (cfg.far_kron && launch_far_kron<float>(dp, *S, kp, t, s, kTcRhs, 0, rcount, st, &ek)) {
+    if (cfg.far_kron && far_kron_ok(dp, *S, kp.type, rcount)) {
+      // up to 8 columns in use: the moments are read from a compact copy
+      // (in the idle FP16 value buffer), rows of 1 or 8 values instead of
+      // 32, which stays in L2 for the re-reads of each source cluster
+      const int rb = rhs_block(rcount);
+      const float* tk = t;
+      if (rb < kTcRhs) {
+        float* tc = reinterpret_cast<float*>(w.tv);
+        ek = launch_compact_columns(t, kTcRhs, tc, rb, (int64_t)Cc * q, rcount, st);
+        if (ek != cudaSuccess) return ek;
+        ++dp->launches;
+        tk = tc;
+      }
+      launch_far_kron<float>(dp, *S, kp, tk, rb < kTcRhs ? rb : kTcRhs, 0, s, kTcRhs, 0, rcount,
+                             st, &ek);
       ++dp->launches;
       if (ek != cudaSuccess) return ek;
       dp->mark(FMCA_STAGE_FAR, st);

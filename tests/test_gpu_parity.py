@@ -308,3 +308,23 @@ def test_gaussian_far_field_as_kronecker_products(cuda_device, prec, dim, p):
         y2 = H.matvec(x).cpu().numpy()
         H.check_device_error()
         assert rel_err(y2, Y_ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+@pytest.mark.parametrize("R", [1, 5, 20, 40])
+@pytest.mark.parametrize("dim,p", [(3, 3), (2, 4)])
+def test_gaussian_kronecker_column_counts(cuda_device, prec, R, dim, p):
+    # the Kronecker far field holds 1, 8 or 32 right-hand sides per source
+    # cluster (32, 4 or 1 clusters per warp step), some of them unused; 40
+    # takes two launches, the second from column 32
+    import torch
+    n = 9000
+    P = uniform_cloud(n, dim, seed=70 + 10 * dim + R)
+    X = np.random.default_rng(R).standard_normal((n, R))
+    O = oracle.OraclePlan(P, None, p, 0.8, 0)
+    assert O.n_far > 0
+    Y_ref, _ = O.action(3, 0.3, X)
+    H = H2Matrix(CovarianceKernel("GAUSSIAN", 0.3), P, P, p, 0.8, precision=prec)
+    y = H.matvec(torch.tensor(X, device=cuda_device)).cpu().numpy()
+    H.check_device_error()
+    assert rel_err(y, Y_ref) < TOL[prec]
