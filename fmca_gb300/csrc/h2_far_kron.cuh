@@ -1,6 +1,6 @@
-// Far field of the GAUSSIAN kernel as Kronecker products.  The kernel below
-// is instantiated only in h2_far_kron.cu, a translation unit of its own, so
-// that its instantiations compile in parallel with h2_gpu.cu.
+// Far field of the GAUSSIAN kernel as Kronecker products.  The kernels below
+// are instantiated only in h2_far_kron.cu, a translation unit of its own, so
+// that their instantiations compile in parallel with h2_gpu.cu.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -823,9 +823,10 @@ void launch_transfer(int nb, const int32_t* list, const int32_t* son0,
 }
 
 // The far field of the GAUSSIAN kernel on tensor-product nodes as Kronecker
-// products (far_kron_kernel), for the grids it is instantiated for: 2-D with
-// 3..8 nodes per dimension, 3-D with 3..6.  false: not applicable (another
-// kernel, total degree, other grids); the caller runs the dense kernel sum.
+// products (far_kron_reg_kernel, far_kron_kernel), for the grids they are
+// instantiated for: 2-D with 3..8 nodes per dimension, 3-D with 3..6.
+// false: not applicable (another kernel, total degree, other grids); the
+// caller runs the dense kernel sum.
 template <typename T>
 bool far_kron_ok(const DevPlan* dp, const DevSet<T>& S, int type, int rcount) {
   return type == FMCA_KERNEL_GAUSSIAN && S.ip.kind == kInterpTensor && rcount <= 32 &&
