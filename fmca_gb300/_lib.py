@@ -59,7 +59,7 @@ EXPORTED = [
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
              "small_r_tensor", "near_halves", "near_persist", "far_persist", "tune_us",
-             "tunings", "far_kron"]
+             "tunings", "far_kron", "near_pack"]
 STAGES = ["gather", "leafmom", "m2m", "far", "l2l", "leafgather", "near", "scatter"]
 
 

@@ -90,7 +90,10 @@ void cloud_centre(const Plan& plan, float ctr[3]) {
 struct GroupList {
   KGroup* groups = nullptr;
   uint32_t* ivl = nullptr;
-  uint32_t* imask = nullptr;  // per interval: target halves it serves (paired grid lists)
+  // per interval: target halves it serves (paired grid lists), or the leaves
+  // it serves (packed near lists)
+  uint32_t* imask = nullptr;
+  uint32_t* split = nullptr;  // packed near lists: rows of a group's first leaf
   int ngroups = 0;
   int maxcount = 0;
 };
@@ -122,6 +125,9 @@ struct TuneCfg {
   // tensor-core path, GAUSSIAN on tensor-product nodes: the far field as
   // Kronecker products on the CUDA cores (1) or the tensor-core kernel sum (0)
   int far_kron = 1;
+  // near field with one half: target rows of up to two leaves per group
+  // over the union of their sources (1), or one leaf per group (0)
+  int near_pack = 0;
   int tuned = 0;      // 1 if the autotuner chose these values
   float tune_ms = 0;  // time the tuning took
   static TuneCfg defaults(int sms) {
@@ -180,6 +186,7 @@ struct DevPlan {
   std::vector<int> l2l_ptr;
   GroupList far, near;  // chunked to kGroupCap targets (near: also the tensor-core list)
   GroupList near_h1;    // near field chunked to kTcGroupCap targets (one target half)
+  GroupList near_pk;    // near field, one target half, rows of up to two leaves per group
   float* gexp = nullptr;  // per far group and target half: the moment exponent E
   GroupList far_tc;     // chunked to kTcGroupCap targets
   GroupList far_grid2;  // tensor grids: sibling row clusters paired as two target halves
@@ -285,6 +292,183 @@ int upload_groups(DevPlan* dp, const HostGroups& hg, GroupList* gl,
   gl->ngroups = (int)hg.groups.size();
   gl->maxcount = hg.maxcount;
   return FMCA_OK;
+}
+
+// Packed near groups for the tensor-core kernel sum with one target half:
+// the rows of consecutive row leaves back to back in groups of up to
+// kTcGroupCap targets, at most two leaves per group.  A group of two leaves
+// runs over the union of their source intervals, split into disjoint pieces
+// that carry the leaves they serve (imask bit 0: the first leaf, bit 1: the
+// second); split[g] = rows of the first leaf.  A leaf joins the group of the
+// previous one only if it adds at most half of that leaf's source points
+// (the leaves of different clouds of a batched plan have disjoint sources,
+// so they never share a group).  false: no packed list (it would not save a
+// tenth of the groups, or a check of the result failed).
+bool build_near_packed(const Plan& plan, int unpacked_groups, HostGroups* hg,
+                       std::vector<uint32_t>* split) {
+  using Iv = std::pair<uint32_t, uint32_t>;
+  const Pattern& P = plan.pat;
+  const size_t L = plan.row_leaves.size();
+  const uint32_t cap = kTcGroupCap;
+  if (L == 0) return false;
+  std::vector<std::vector<Iv>> lists(L);
+  for (size_t l = 0; l < L; ++l) {
+    for (int k = P.near_ptr[l]; k < P.near_ptr[l + 1]; ++k)
+      lists[l].push_back({P.near_ivl[2 * k], P.near_ivl[2 * k + 1]});
+    std::sort(lists[l].begin(), lists[l].end());
+    for (size_t i = 0; i < lists[l].size(); ++i) {  // sorted, disjoint, non-empty
+      if (lists[l][i].first >= lists[l][i].second || lists[l][i].second > plan.cols.n)
+        return false;
+      if (i && lists[l][i].first < lists[l][i - 1].second) return false;
+    }
+  }
+  auto points = [](const std::vector<Iv>& v) {
+    uint64_t s = 0;
+    for (const Iv& p : v) s += p.second - p.first;
+    return s;
+  };
+  // pieces of the union of a and b with the bits of the lists covering them
+  auto merge = [](const std::vector<Iv>& a, const std::vector<Iv>& b, std::vector<Iv>* out,
+                  std::vector<uint32_t>* bits) {
+    std::vector<uint32_t> x;
+    for (const Iv& p : a) {
+      x.push_back(p.first);
+      x.push_back(p.second);
+    }
+    for (const Iv& p : b) {
+      x.push_back(p.first);
+      x.push_back(p.second);
+    }
+    std::sort(x.begin(), x.end());
+    x.erase(std::unique(x.begin(), x.end()), x.end());
+    size_t ia = 0, ib = 0;
+    for (size_t i = 0; i + 1 < x.size(); ++i) {
+      const uint32_t x0 = x[i], x1 = x[i + 1];
+      while (ia < a.size() && a[ia].second <= x0) ++ia;
+      while (ib < b.size() && b[ib].second <= x0) ++ib;
+      const uint32_t bt = (ia < a.size() && a[ia].first <= x0 ? 1u : 0u) |
+                          (ib < b.size() && b[ib].first <= x0 ? 2u : 0u);
+      if (!bt) continue;
+      if (!out->empty() && out->back().second == x0 && bits->back() == bt)
+        out->back().second = x1;
+      else {
+        out->push_back({x0, x1});
+        bits->push_back(bt);
+      }
+    }
+  };
+  std::vector<size_t> ord(L);
+  for (size_t l = 0; l < L; ++l) ord[l] = l;
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+    return plan.rows.begin[plan.row_leaves[a]] < plan.rows.begin[plan.row_leaves[b]];
+  });
+  // the open group: leaf la from row tb (ra rows), then leaf lb (rb rows)
+  size_t la = 0, lb = 0;
+  uint32_t tb = 0, ra = 0, rb = 0;
+  int nseg = 0;
+  auto flush = [&]() {
+    if (!nseg) return;
+    const int ib = (int)(hg->ivl.size() / 2);
+    std::vector<Iv> pcs;
+    std::vector<uint32_t> bits;
+    if (nseg == 1) {
+      pcs = lists[la];
+      bits.assign(pcs.size(), 1u);
+    } else {
+      merge(lists[la], lists[lb], &pcs, &bits);
+    }
+    for (size_t i = 0; i < pcs.size(); ++i) {
+      hg->ivl.push_back(pcs[i].first);
+      hg->ivl.push_back(pcs[i].second);
+      hg->imask.push_back(bits[i]);
+    }
+    KGroup g;
+    g.tbegin = tb;
+    g.tcount = ra + rb;
+    g.ivl_begin = ib;
+    g.ivl_end = (int)(hg->ivl.size() / 2);
+    hg->groups.push_back(g);
+    hg->maxcount = std::max<int>(hg->maxcount, (int)g.tcount);
+    split->push_back(ra);
+    nseg = 0;
+    ra = rb = 0;
+  };
+  for (size_t oi = 0; oi < L; ++oi) {
+    const size_t l = ord[oi];
+    const int c = plan.row_leaves[l];
+    uint32_t row = plan.rows.begin[c], left = plan.rows.size[c];
+    while (left > 0) {
+      if (nseg == 1) {  // join the open group, or close it
+        std::vector<Iv> pcs;
+        std::vector<uint32_t> bits;
+        merge(lists[la], lists[l], &pcs, &bits);
+        uint64_t added = 0;
+        for (size_t i = 0; i < pcs.size(); ++i)
+          if (bits[i] == 2u) added += pcs[i].second - pcs[i].first;
+        if (2 * added > points(lists[la])) flush();
+      } else if (nseg == 2) {
+        flush();
+      }
+      const uint32_t take = std::min(left, cap - (ra + rb));
+      if (nseg == 0) {
+        la = l;
+        tb = row;
+        ra = take;
+        nseg = 1;
+      } else {
+        lb = l;
+        rb = take;
+        nseg = 2;
+      }
+      row += take;
+      left -= take;
+      if (ra + rb == cap) flush();
+    }
+  }
+  flush();
+  if ((int64_t)hg->groups.size() * 10 > (int64_t)unpacked_groups * 9) return false;
+  // checks: every row once, in order; pieces sorted, disjoint, inside the
+  // columns, with the points of each leaf's own list
+  uint64_t rows = 0;
+  for (size_t l = 0; l < L; ++l) rows += plan.rows.size[plan.row_leaves[l]];
+  uint64_t seen = 0;
+  for (size_t g = 0; g < hg->groups.size(); ++g) {
+    const KGroup& G = hg->groups[g];
+    if (G.tcount == 0 || G.tcount > cap || (*split)[g] == 0 || (*split)[g] > G.tcount ||
+        G.ivl_begin > G.ivl_end)
+      return false;
+    uint32_t prev = 0;
+    for (int k = G.ivl_begin; k < G.ivl_end; ++k) {
+      const uint32_t b = hg->ivl[2 * k], e = hg->ivl[2 * k + 1], m = hg->imask[k];
+      if (b >= e || e > plan.cols.n || (k > G.ivl_begin && b < prev) || m == 0u || m > 3u ||
+          ((*split)[g] == G.tcount && m != 1u))
+        return false;
+      prev = e;
+    }
+    seen += G.tcount;
+  }
+  if (seen != rows) return false;
+  // most work first, split permuted alongside
+  std::vector<uint64_t> work(hg->groups.size());
+  for (size_t i = 0; i < hg->groups.size(); ++i) {
+    uint64_t s = 0;
+    for (int k = hg->groups[i].ivl_begin; k < hg->groups[i].ivl_end; ++k)
+      s += hg->ivl[2 * k + 1] - hg->ivl[2 * k];
+    work[i] = s;
+  }
+  std::vector<size_t> order(hg->groups.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return work[a] > work[b]; });
+  std::vector<KGroup> g2(order.size());
+  std::vector<uint32_t> s2(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    g2[i] = hg->groups[order[i]];
+    s2[i] = (*split)[order[i]];
+  }
+  hg->groups.swap(g2);
+  split->swap(s2);
+  return true;
 }
 
 template <typename T>
@@ -497,6 +681,14 @@ int upload_common(const Plan& plan, DevPlan* dp, std::string* err) {
     }
     sort_groups(&hg);
     FMCA_TRY(upload_groups(dp, hg, pass == 0 ? &dp->near : &dp->near_h1, err));
+  }
+  {
+    HostGroups hg;
+    std::vector<uint32_t> split;
+    if (build_near_packed(plan, dp->near_h1.ngroups, &hg, &split)) {
+      FMCA_TRY(upload_groups(dp, hg, &dp->near_pk, err));
+      FMCA_TRY(to_device(dp, split.data(), split.size(), &dp->near_pk.split, err));
+    }
   }
   {
     void* p = nullptr;
@@ -1166,16 +1358,18 @@ cudaError_t launch_um_v(const GroupList& gl, const Pt4<float>* tgt, const float4
                         const __half* vals, float* out, int rcount,
                         const KParams<float>& kp, int q, int* errf, cudaStream_t st,
                         const UmCfg& uc, float* gexp, int sms) {
-  if (uc.persist)
+  if (uc.persist) {
+    if (gl.split) return cudaErrorInvalidValue;  // packed lists: one CTA per group only
     return launch_um_persistent(KT, H, REL, GRID, gl.groups, gl.ngroups, gl.ivl, gl.imask, tgt,
                                 pairs, vals, out, rcount, kp, q, errf, gexp, uc.nst, uc.F, sms,
                                 st);
+  }
   auto kern = ksum_um_kernel<KT, H, REL, GRID>;
   const size_t smem = um_smem_bytes(H, kUmMaxStages);
   ensure_smem(kern, smem);
   kern<<<gl.ngroups, kUmThreads, um_smem_bytes(H, uc.nst), st>>>(
       gl.groups, gl.ivl, tgt, pairs, vals, out, kTcRhs, rcount, kp, q, errf, gl.imask, uc.nst,
-      uc.F);
+      uc.F, gl.split);
   return cudaGetLastError();
 }
 
@@ -1368,9 +1562,11 @@ struct TcChunk {
     return cudaGetLastError();
   }
   // near field: groups of up to 256 targets as two halves of 128, or of up
-  // to 128 targets as one half (halves = 1)
-  cudaError_t near(const UmCfg& uc, int halves) {
-    const GroupList& gl = halves == 1 ? dp->near_h1 : dp->near;
+  // to 128 targets as one half (halves = 1), one leaf per group or (pack,
+  // one CTA per group) the rows of up to two leaves
+  cudaError_t near(const UmCfg& uc, int halves, int pack = 0) {
+    const bool pk = pack && halves == 1 && !uc.persist && dp->near_pk.ngroups > 0;
+    const GroupList& gl = pk ? dp->near_pk : halves == 1 ? dp->near_h1 : dp->near;
     cudaError_t e =
         halves == 1
             ? launch_um<1>(gl, S->pts_r, w.pairs_c, xv, ynear, rcount, kp, 0, dp->err_flag, st,
@@ -1477,7 +1673,7 @@ int matvec_tc(const Plan& plan, DevPlan* dp, DevSet<float>& S, const KernelDesc&
     FMCA_CK(c.far(dp->cfg));
     FMCA_CK(c.l2l(dp->cfg.tr));
     FMCA_CK(c.leafgather());
-    FMCA_CK(c.near(dp->cfg.near, dp->cfg.near_halves));
+    FMCA_CK(c.near(dp->cfg.near, dp->cfg.near_halves, dp->cfg.near_pack));
   }
   if (dtype == FMCA_DTYPE_F64)
     scatter_scaled_kernel<double><<<blocks(nr * nrhs), nthr, 0, st>>>(
@@ -1639,29 +1835,35 @@ int tune(const Plan& plan, DevPlan* dp, const KernelDesc& k, int precision, int 
         tc_ws_layout(plan, nrhs, ws ? ws : dp->ws, &w);
         TcChunk c = tc_chunk(plan, dp, dp->f, w, tc_kparams(dp->f, k, dp->opts), nrhs, 0, st);
         float bt = -1.f;
+        // one half: also the groups of two leaves' rows (packed)
+        const int max_pack = dp->near_pk.ngroups > 0 ? 1 : 0;
         for (int halves = 2; halves >= 1 && status == FMCA_OK; --halves)
           for (int nst = halves == 2 ? 4 : 5; nst <= kUmMaxStages && status == FMCA_OK; ++nst)
-            for (int F = 1; F <= (halves == 2 ? kUmMaxUnit : 2); ++F) {
-              const UmCfg uc{nst, F};
-              const float ms = timed([&]() { return ok_cuda(c.near(uc, halves)); });
-              if (ms < 0.f) {
-                status = FMCA_ERR_CUDA;
-                break;
+            for (int F = 1; F <= (halves == 2 ? kUmMaxUnit : 2) && status == FMCA_OK; ++F)
+              for (int pack = 0; pack <= (halves == 1 ? max_pack : 0); ++pack) {
+                const UmCfg uc{nst, F};
+                const float ms = timed([&]() { return ok_cuda(c.near(uc, halves, pack)); });
+                if (ms < 0.f) {
+                  status = FMCA_ERR_CUDA;
+                  break;
+                }
+                if (bt < 0.f || ms < bt) {
+                  bt = ms;
+                  best.near = uc;
+                  best.near_halves = halves;
+                  best.near_pack = pack;
+                }
               }
-              if (bt < 0.f || ms < bt) {
-                bt = ms;
-                best.near = uc;
-                best.near_halves = halves;
-              }
-            }
-        if (status == FMCA_OK) {  // the fastest shape as a persistent launch
+        if (status == FMCA_OK) {  // the fastest shape as a persistent launch (one leaf per group)
           UmCfg uc = best.near;
           uc.persist = 1;
           const float ms = timed([&]() { return ok_cuda(c.near(uc, best.near_halves)); });
-          if (ms < 0.f)
+          if (ms < 0.f) {
             status = FMCA_ERR_CUDA;
-          else if (ms < bt)
+          } else if (ms < bt) {
             best.near = uc;
+            best.near_pack = 0;
+          }
         }
         bt = -1.f;
         // the Gaussian's Kronecker far field first (the default where it
@@ -1972,6 +2174,7 @@ void tuned_config(DevPlan* dp, int precision, int type, int nrhs, int32_t* out) 
   out[FMCA_TUNE_FAR_PERSIST] = c.far_grid.persist | c.far_nodes.persist;
   out[FMCA_TUNE_US] = (int32_t)(c.tune_ms * 1000.f);
   out[FMCA_TUNE_FAR_KRON] = c.far_kron;
+  out[FMCA_TUNE_NEAR_PACK] = c.near_pack;
   (void)pairs;
 }
 
@@ -1989,9 +2192,15 @@ int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32
       (in[FMCA_TUNE_NEAR_PERSIST] != 0 && in[FMCA_TUNE_NEAR_PERSIST] != 1) ||
       (in[FMCA_TUNE_FAR_PERSIST] != 0 && in[FMCA_TUNE_FAR_PERSIST] != 1) ||
       (in[FMCA_TUNE_FAR_KRON] != 0 && in[FMCA_TUNE_FAR_KRON] != 1) ||
+      (in[FMCA_TUNE_NEAR_PACK] != 0 && in[FMCA_TUNE_NEAR_PACK] != 1) ||
       in[FMCA_TUNE_WIDE_BELOW] < 0 || in[FMCA_TUNE_SLICE_BELOW] < 0) {
     *err = "launch shapes out of range (stages 2..7, units 1..min(3, stages), flags 0/1, "
            "halves 1/2, thresholds >= 0)";
+    return FMCA_ERR_INVALID_ARGUMENT;
+  }
+  if (in[FMCA_TUNE_NEAR_PACK] && dp->near_pk.ngroups == 0) {
+    *err = "near_pack: this plan has no packed near groups (they would not save a tenth of "
+           "the groups of one leaf each)";
     return FMCA_ERR_INVALID_ARGUMENT;
   }
   TuneCfg c = TuneCfg::defaults(dp->sms);
@@ -2005,6 +2214,7 @@ int set_tuned_config(DevPlan* dp, int precision, int type, int nrhs, const int32
   c.tr = TrCfg{in[FMCA_TUNE_WIDE_BELOW], in[FMCA_TUNE_SLICE_BELOW]};
   c.small_tc = in[FMCA_TUNE_SMALL_R_TENSOR];
   c.far_kron = in[FMCA_TUNE_FAR_KRON];
+  c.near_pack = in[FMCA_TUNE_NEAR_PACK];
   c.tuned = 1;
   std::lock_guard<std::mutex> lock(dp->mu);
   dp->tuned[tune_key(precision, type, nrhs)] = c;

@@ -291,13 +291,18 @@ __device__ __forceinline__ uint32_t row_bits(uint32_t vb, uint32_t ve, uint32_t 
 // made the far field 5 % and the near field 2 % faster, and the far field's
 // rounding error 1.5x larger (5e-7 relative at n = 1e6, measured against
 // FP64). Both are chosen per plan by the autotuner when it is enabled.
+// split (point sources, one half; null otherwise): the group's targets are
+// rows of up to two leaves, rows [0, split[g]) of the first and the rest of
+// the second, over the union of the leaves' source intervals; imask[i] holds
+// the leaves interval i serves (bit 0: the first, bit 1: the second), the
+// producer posts one row mask per leaf and every target takes its leaf's.
 template <int KT, int H, bool REL, bool GRID>
 __global__ void __launch_bounds__(kUmThreads, 1)
     ksum_um_kernel(const KGroup* __restrict__ groups, const uint32_t* __restrict__ ivl,
                    const Pt4<float>* __restrict__ tgt, const float4* __restrict__ pairs,
                    const __half* __restrict__ vals, float* __restrict__ out, int ldo, int rcount,
                    KParams<float> kp, int q, int* err, const uint32_t* __restrict__ imask,
-                   int nst, int F) {
+                   int nst, int F, const uint32_t* __restrict__ split) {
   const int NST = nst;
   constexpr int NSETS = kUmSets, NEVAL = 4 * NSETS;
   constexpr int NT = 128 * H;  // targets of a group
@@ -334,10 +339,18 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   uint64_t* never = done + 2;  // nothing arrives (the stalled-wait test hook)
   static_assert(8 * (2 * kUmMaxStages + 2 * NPS + 4 + 2 + 2 + 1) <= 512, "barrier area");
   static_assert(528 + 16 * kUmMaxStages <= 640, "stage masks");
+  static_assert(640 + (int)sizeof(float) * NEVAL * H <= 768 &&
+                    768 + 16 * kUmMaxStages <= kUmHeader,
+                "second-leaf masks after the exponent maxima");
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + 512);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 516);
   uint32_t* masks = reinterpret_cast<uint32_t*>(smem_raw + 528);  // [kUmMaxStages][4]
   float* ered = reinterpret_cast<float*>(smem_raw + 640);          // [NEVAL][H]
+  // row masks of the second leaf of packed groups [kUmMaxStages][4]
+  uint32_t* masks2 = reinterpret_cast<uint32_t*>(smem_raw + 768);
+  // packed groups of two leaves (point sources, one half only)
+  constexpr bool PKOK = H == 1 && !REL && !GRID;
+  const bool pk = PKOK && split != nullptr;
   unsigned char* stages = smem_raw + kUmHeader;
   float* tot = reinterpret_cast<float*>(stages + (size_t)NST * kUmStageBytes);
 
@@ -430,6 +443,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         // the stage barrier before its copies, and the final arrival (after
         // the row mask is written) lets the phase complete
         uint32_t row = 0, m0 = 0u, m1 = 0u, m2 = 0u, m3 = 0u;
+        uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;  // second leaf (packed groups)
         while (row < (uint32_t)kUmTile && pi < g.ivl_end) {
           const uint32_t b = ivl[2 * pi], e = ivl[2 * pi + 1];
           const uint32_t a0 = pos != 0xffffffffu ? pos : (b & ~7u);
@@ -443,10 +457,21 @@ __global__ void __launch_bounds__(kUmThreads, 1)
             // rows [vb, ve) hold sources of the interval
             const uint32_t vb = max(b, a0) - a0 + row;
             const uint32_t ve = e > a0 ? min(e, a0 + take) - a0 + row : vb;
-            m0 |= row_bits(vb, ve, 0);
-            m1 |= row_bits(vb, ve, 32);
-            m2 |= row_bits(vb, ve, 64);
-            m3 |= row_bits(vb, ve, 96);
+            const uint32_t r0 = row_bits(vb, ve, 0), r1 = row_bits(vb, ve, 32);
+            const uint32_t r2 = row_bits(vb, ve, 64), r3 = row_bits(vb, ve, 96);
+            const uint32_t sv = pk ? imask[pi] : 1u;  // leaves the interval serves
+            if (sv & 1u) {
+              m0 |= r0;
+              m1 |= r1;
+              m2 |= r2;
+              m3 |= r3;
+            }
+            if (sv & 2u) {
+              n0 |= r0;
+              n1 |= r1;
+              n2 |= r2;
+              n3 |= r3;
+            }
           }
           row += take;
           if (a0 + take >= ae) {
@@ -460,6 +485,12 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         masks[stage * 4 + 1] = m1;
         masks[stage * 4 + 2] = m2;
         masks[stage * 4 + 3] = m3;
+        if (pk) {
+          masks2[stage * 4 + 0] = n0;
+          masks2[stage * 4 + 1] = n1;
+          masks2[stage * 4 + 2] = n2;
+          masks2[stage * 4 + 3] = n3;
+        }
         mbar_arrive1(&full[stage]);
         ++issued;
       }
@@ -534,9 +565,10 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int ew = warp - 3, set = ew >> 2;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
     const int row = (warp & 3) * 32 + lane;
+    // packed groups: this target belongs to the second leaf
+    const bool second = pk && (uint32_t)row >= split[blockIdx.x];
     float2 tx[H], ty[H], tz[H], tn[H];
     um_targets<H, DOT>(tgt, g, row, HS, kp, tx, ty, tz, tn);
-    // largest moment exponent E of the group's source clusters
     // largest moment exponent E of the group's source clusters, per target
     // half (Eh: over the intervals that serve the half) and overall (E)
     float E = 0.f, Eh[H];
@@ -646,14 +678,23 @@ __global__ void __launch_bounds__(kUmThreads, 1)
 #pragma unroll
         for (int cc = 0; cc < 2; ++cc) {
           const int kk = 2 * set + cc;
-          const uint32_t m16 = (masks[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
+          uint32_t m16 = (masks[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
+          bool full16 = m16 == 0xffffu, none16 = m16 == 0u;
+          if constexpr (PKOK) {
+            if (pk) {  // the target's own leaf's mask; the paths by vote
+              if (second)
+                m16 = (masks2[stage * 4 + (kk >> 1)] >> ((kk & 1) * 16)) & 0xffffu;
+              full16 = __all_sync(0xffffffffu, m16 == 0xffffu);
+              none16 = __all_sync(0xffffffffu, m16 == 0u);
+            }
+          }
           uint32_t hi[H][8], lo[H][8];
-          if (m16 == 0xffffu) {
+          if (full16) {
             if constexpr (DOT)
               um_eval_chunk_dot<KT, H, false>(R4 + kk * 16, m16, tx, ty, tz, tn, kp, hi, lo);
             else
               um_eval_chunk<KT, H, false, REL>(R4 + kk * 16, m16, tx, ty, tz, E, kp, hi, lo);
-          } else if (m16 == 0u) {
+          } else if (none16) {
 #pragma unroll
             for (int h = 0; h < H; ++h)
 #pragma unroll

@@ -448,15 +448,18 @@ enum {
   FMCA_TUNE_TUNINGS = 15,         /* tuning runs on this plan so far */
   FMCA_TUNE_FAR_KRON = 16,        /* GAUSSIAN on tensor-product nodes, mixed precision:
                                      1 far field as Kronecker products, 0 kernel sums */
-  FMCA_TUNE_COUNT = 17
+  FMCA_TUNE_NEAR_PACK = 17,       /* near field with 1 x 128 targets, one CTA per group:
+                                     1 rows of up to two leaves per group, 0 one leaf */
+  FMCA_TUNE_COUNT = 18
 };
 /* The launch shapes a matvec of this key uses now: the tuned ones, or the
    defaults (FMCA_TUNE_TUNED = 0). */
 fmca_status fmca_plan_tuned_config(fmca_plan* plan, int precision, int kernel_type, int nrhs,
                                    int32_t out[FMCA_TUNE_COUNT]);
 /* Sets the launch shapes of a key as if the autotuner had chosen them
-   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_FAR_PERSIST and
-   FMCA_TUNE_FAR_KRON of cfg; the others are ignored): for reusing shapes tuned earlier, for instance in another
+   (entries FMCA_TUNE_NEAR_STAGES .. FMCA_TUNE_FAR_PERSIST, FMCA_TUNE_FAR_KRON
+   and FMCA_TUNE_NEAR_PACK of cfg; the others are ignored): for reusing
+   shapes tuned earlier, for instance in another
    process on the same plan.  The plan must be resident on the current
    device (after one matvec).  Out-of-range shapes give
    FMCA_ERR_INVALID_ARGUMENT. */
