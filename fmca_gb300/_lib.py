@@ -54,7 +54,7 @@ EXPORTED = [
     "fmca_plan_set_wait_limit", "fmca_plan_set_stalled_wait", "fmca_plan_set_autotune",
     "fmca_plan_tuned_config", "fmca_plan_create_gpu", "fmca_plan_set_tuned_config",
     "fmca_plan_assembled_size", "fmca_plan_assemble", "fmca_matvec_assembled",
-    "fmca_plan_release_assembled",
+    "fmca_plan_release_assembled", "fmca_plan_near_packed",
 ]
 TUNE_KEYS = ["tuned", "near_stages", "near_unit", "far_pairs", "far_grid_stages",
              "far_grid_unit", "far_node_stages", "far_node_unit", "wide_below", "slice_below",
@@ -110,6 +110,8 @@ def load() -> C.CDLL:
     lib.fmca_plan_permutation.argtypes = [vp, i32, C.POINTER(C.c_uint32)]
     lib.fmca_plan_clusters.argtypes = [vp, i32, C.POINTER(C.c_int32), dp]
     lib.fmca_plan_blocks.argtypes = [vp, i32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.fmca_plan_near_packed.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     lib.fmca_matvec_workspace_size.argtypes = [vp, i32, i32, C.POINTER(C.c_size_t)]
     lib.fmca_matvec.argtypes = [vp, C.POINTER(KernelDesc), i32, i32, i32, i32,
                                 vp, i64, i64, vp, i64, i64, vp, C.c_size_t, vp]

@@ -29,10 +29,10 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
               "-Xptxas", "-O3"] + ARCH
 
-HOST_SOURCES = ["h2_plan.cpp", "plan_io.cpp", "c_api.cpp"]
+HOST_SOURCES = ["h2_plan.cpp", "plan_io.cpp", "near_pack.cpp", "c_api.cpp"]
 CUDA_SOURCES = ["h2_gpu.cu", "h2_static_scratch.cu", "h2_tree_gpu.cu", "h2_umma_persistent.cu",
                 "h2_assembled.cu", "h2_far_kron.cu"]
-HEADERS = ["h2_plan.h", "plan_io.h", "h2_gpu.h", "compensated_sum.h", "h2_gpu_kernels.cuh", "h2_tc_kernels.cuh", "h2_umma_kernels.cuh", "umma.cuh",
+HEADERS = ["h2_plan.h", "plan_io.h", "near_pack.h", "h2_gpu.h", "compensated_sum.h", "h2_gpu_kernels.cuh", "h2_tc_kernels.cuh", "h2_umma_kernels.cuh", "umma.cuh",
            "h2_umma_persistent.cuh", "h2_umma_persistent.h",
            "h2_adjoint_kernels.cuh", "c_api_internal.h", "h2_assembled.h",
            "h2_assembled_kernels.cuh", "h2_far_kron.h", "h2_far_kron.cuh"]

@@ -15,6 +15,7 @@
 #include "../../include/fmca_gb300.h"
 #include "c_api_internal.h"
 #include "plan_io.h"
+#include "near_pack.h"
 #include "h2_gpu.h"
 #include "h2_plan.h"
 
@@ -412,6 +413,37 @@ fmca_status fmca_plan_blocks(const fmca_plan* p, int kind, int32_t* rows,
   const auto& c = kind == 0 ? p->plan.pat.far_col : p->plan.pat.near_col;
   std::memcpy(rows, r.data(), sizeof(int32_t) * r.size());
   std::memcpy(cols, c.data(), sizeof(int32_t) * c.size());
+  return ok();
+}
+
+fmca_status fmca_plan_near_packed(const fmca_plan* p, int64_t* ngroups, int64_t* nintervals,
+                                  uint32_t* groups, uint32_t* intervals) {
+  if (!p || !ngroups || !nintervals) return fail(FMCA_ERR_INVALID_ARGUMENT, "NULL argument");
+  try {
+    fmca::PackedNear pk;
+    fmca::build_near_packed(p->plan, 128, &pk);
+    const int64_t ng = (int64_t)pk.ngroups(), ni = (int64_t)pk.imask.size();
+    if (groups && intervals) {
+      if (*ngroups < ng || *nintervals < ni)
+        return fail(FMCA_ERR_INVALID_ARGUMENT, "arrays smaller than the counts");
+      for (int64_t g = 0; g < ng; ++g) {
+        groups[5 * g + 0] = pk.tbegin[g];
+        groups[5 * g + 1] = pk.tcount[g];
+        groups[5 * g + 2] = (uint32_t)pk.ivl_begin[g];
+        groups[5 * g + 3] = (uint32_t)pk.ivl_end[g];
+        groups[5 * g + 4] = pk.split[g];
+      }
+      for (int64_t i = 0; i < ni; ++i) {
+        intervals[3 * i + 0] = pk.ivl[2 * i];
+        intervals[3 * i + 1] = pk.ivl[2 * i + 1];
+        intervals[3 * i + 2] = pk.imask[i];
+      }
+    }
+    *ngroups = ng;
+    *nintervals = ni;
+  } catch (const std::exception& e) {
+    return fail(FMCA_ERR_INTERNAL, e.what());
+  }
   return ok();
 }
 

@@ -280,6 +280,24 @@ class H2Matrix:
                                            c.ctypes.data_as(C.POINTER(C.c_int32))))
         return r, c
 
+    def near_packed(self):
+        """(groups, intervals) of the packed near field (fmca_plan_near_packed):
+        groups[g] = (first target, targets, first interval, end interval,
+        targets of the first leaf), intervals[i] = (first source, end source,
+        leaves served: bit 0 the first, bit 1 the second); cluster order.
+        Empty arrays where the plan has no packed groups."""
+        ng, ni = C.c_int64(0), C.c_int64(0)
+        lib = _lib.load()
+        check(lib.fmca_plan_near_packed(self._h, C.byref(ng), C.byref(ni), None, None))
+        groups = np.zeros((ng.value, 5), dtype=np.uint32)
+        ivl = np.zeros((ni.value, 3), dtype=np.uint32)
+        if ng.value:
+            check(lib.fmca_plan_near_packed(
+                self._h, C.byref(ng), C.byref(ni),
+                groups.ctypes.data_as(C.POINTER(C.c_uint32)),
+                ivl.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return groups, ivl
+
     def action(self, rhs, precision: Optional[str] = None, out=None):
         """y = K_H2 rhs in natural order (pyH2Matrix::action).
 

@@ -253,6 +253,20 @@ fmca_status fmca_plan_load(const char* path, fmca_plan** out);
    in the order the pattern recursion produced them. */
 fmca_status fmca_plan_blocks(const fmca_plan* plan, int kind, int32_t* rows,
                              int32_t* cols);
+/* The packed near groups of the tensor-core kernel sum with one target half
+   (an autotuner choice, FMCA_TUNE_NEAR_PACK): the rows of up to two
+   consecutive row leaves per group of up to 128 targets, over the union of
+   the leaves' source intervals.  Pass NULL groups and intervals for the
+   counts (both 0 where the plan has no packed groups: they would not save a
+   tenth of the groups of one leaf each); then groups receives ngroups x 5
+   values (first target, targets, first interval, end interval, targets of
+   the group's first leaf) in launch order, and intervals nintervals x 3
+   (first source, end source, leaves served: bit 0 the group's first leaf,
+   bit 1 its second), targets and sources in cluster order.  The groups
+   cover the dense blocks of H2MatrixBase.h:143-146 (every pair of a row
+   leaf and a point of its dense blocks) once. */
+fmca_status fmca_plan_near_packed(const fmca_plan* plan, int64_t* ngroups, int64_t* nintervals,
+                                  uint32_t* groups, uint32_t* intervals);
 
 /* Device memory the plan holds now, in bytes: its uploaded data (lists,
    points, nodes, transfers), the workspace it owns (allocated or grown by
