@@ -31,7 +31,6 @@ bool build_near_packed(const Plan& plan, uint32_t cap, PackedNear* out) {
   };
   std::vector<G> groups;
   std::vector<uint32_t> ivl, imask, splits;
-  std::vector<uint32_t>* split = &splits;
   std::vector<std::vector<Iv>> lists(L);
   for (size_t l = 0; l < L; ++l) {
     for (int k = P.near_ptr[l]; k < P.near_ptr[l + 1]; ++k)
@@ -104,7 +103,7 @@ bool build_near_packed(const Plan& plan, uint32_t cap, PackedNear* out) {
       imask.push_back(bits[i]);
     }
     groups.push_back(G{tb, ra + rb, ib, (int32_t)(ivl.size() / 2)});
-    split->push_back(ra);
+    splits.push_back(ra);
     nseg = 0;
     ra = rb = 0;
   };
@@ -142,21 +141,22 @@ bool build_near_packed(const Plan& plan, uint32_t cap, PackedNear* out) {
   }
   flush();
   if ((int64_t)groups.size() * 10 > unpacked_groups * 9) return false;
-  // checks: every row once, in order; pieces sorted, disjoint, inside the
-  // columns, with the points of each leaf's own list
+  // checks: the groups hold as many rows as the leaves, at most cap each;
+  // every group's pieces sorted, disjoint and inside the columns, flags 1..3
+  // (1 only in groups of one leaf)
   uint64_t rows = 0;
   for (size_t l = 0; l < L; ++l) rows += plan.rows.size[plan.row_leaves[l]];
   uint64_t seen = 0;
   for (size_t g = 0; g < groups.size(); ++g) {
     const G& gr = groups[g];
-    if (gr.tcount == 0 || gr.tcount > cap || (*split)[g] == 0 || (*split)[g] > gr.tcount ||
+    if (gr.tcount == 0 || gr.tcount > cap || splits[g] == 0 || splits[g] > gr.tcount ||
         gr.ivl_begin > gr.ivl_end)
       return false;
     uint32_t prev = 0;
     for (int k = gr.ivl_begin; k < gr.ivl_end; ++k) {
       const uint32_t b = ivl[2 * k], e = ivl[2 * k + 1], m = imask[k];
       if (b >= e || e > plan.cols.n || (k > gr.ivl_begin && b < prev) || m == 0u || m > 3u ||
-          ((*split)[g] == gr.tcount && m != 1u))
+          (splits[g] == gr.tcount && m != 1u))
         return false;
       prev = e;
     }
