@@ -147,3 +147,34 @@ def test_header_compiles_as_c_and_links(tmp_path):
     P = np.random.default_rng(0).random((3, 10))  # any plan: the nodes do not depend on points
     H = H2Matrix(CovarianceKernel("MATERN32", 0.5), P, P, 4, 0.8, interpolator="total_degree")
     assert float(out[5]) == H.interpolation_nodes()[0][0, 0]
+
+
+def test_tune_indices_match_the_binding():
+    # the FMCA_TUNE_* indices of the header and the binding's key order
+    txt = open(os.path.join(ROOT, "include", "fmca_gb300.h")).read()
+    idx = {m.group(1).lower(): int(m.group(2))
+           for m in re.finditer(r"\bFMCA_TUNE_([A-Z0-9_]+)\s*=\s*(\d+)", txt)}
+    count = idx.pop("count")
+    assert count == len(_lib.TUNE_KEYS) == len(idx)
+    for key, i in idx.items():
+        assert _lib.TUNE_KEYS[i] == {"us": "tune_us"}.get(key, key), key
+
+
+def test_near_packed_argument_checks():
+    lib = _lib.load()
+    ng, ni = C.c_int64(0), C.c_int64(0)
+    assert lib.fmca_plan_near_packed(None, C.byref(ng), C.byref(ni), None, None) == 1
+    P = np.random.default_rng(16).random((2, 20000))
+    H = H2Matrix(CovarianceKernel("MATERN32", 0.3), P, P, 3, 0.8)
+    assert lib.fmca_plan_near_packed(H.handle, None, C.byref(ni), None, None) == 1
+    assert lib.fmca_plan_near_packed(H.handle, C.byref(ng), C.byref(ni), None, None) == 0
+    assert ng.value > 0 and ni.value > 0
+    # arrays shorter than the counts are refused
+    g = np.zeros((ng.value, 5), dtype=np.uint32)
+    v = np.zeros((ni.value, 3), dtype=np.uint32)
+    short = C.c_int64(ng.value - 1)
+    assert lib.fmca_plan_near_packed(
+        H.handle, C.byref(short), C.byref(ni), g.ctypes.data_as(C.POINTER(C.c_uint32)),
+        v.ctypes.data_as(C.POINTER(C.c_uint32))) == 1
+    groups, ivl = H.near_packed()
+    assert groups.shape == (ng.value, 5) and ivl.shape == (ni.value, 3)
